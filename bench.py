@@ -1,0 +1,344 @@
+"""Benchmark: one SR step of the VMC hot path at N=32, M=64, K=2 (FP64).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--chains C]
+
+A step is one full stochastic-reconfiguration step of code/rbm.cc:564-719:
+128 Metropolis chains x 200 samples (64 burn-in sweeps), local energies,
+log-derivatives, moments, the matrix-free MINRES-QLP solve (rtol 1e-9) and
+the weight update, on the trapped-ion chain J_ij = |i-j|^-1.2 (max |J| = 1),
+h = 0.595, with seeded real N(0, 0.01^2) weights (synthetic data; the
+schedule lambda 40 -> 1 (x0.9 per step) and lr 0.1 -> 0.01 (x0.99) of the
+reference README continues across warm-up and timed steps).
+
+Metric: MC samples per second over whole SR steps (samples x steps / time),
+the unit of the reference's published logs; SR steps/s is reported beside it.
+`value` is device time (CUDA events on the library's stream) with all inputs
+resident in HBM; `e2e` is the same metric through the C ABI with host
+buffers: the weights go host->device and e_mat + weights come back every
+step. The O matrix (0.88 GB) is larger than L2, so no L2 flush is needed.
+
+--impl reference times the reference algorithm on the host cores: the
+reference itself cannot be compiled (no Eigen3 / libmatio here or on the GPU
+host), so its C++ restatement in oracle/ (matrix-free S·v recomputing every
+log-derivative each MINRES-QLP iteration, OpenMP over chains) runs instead,
+on a bounded sample of the workload: one chain per host core, 200 samples each.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, M, K, H = 32, 64, 2, 0.595
+SAMPLES, BURN, RTOL, MAXIT = 200, 64, 1e-9, 100000
+REGLAM0, REGLAM_DECAY, REGLAM_CUT = 40.0, 0.9, 1.0
+LR0, LR_DECAY, LR_CUT = 0.1, 0.99, 0.01
+SEED = 20240601
+
+
+def schedule(t):
+    return max(LR0 * LR_DECAY ** t, LR_CUT), max(REGLAM0 * REGLAM_DECAY ** t, REGLAM_CUT)
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 throughput of this GPU (cuBLAS DGEMM, best of 5)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(chains, steps_done):
+    """Reference algorithm (oracle restatement) on the host cores, one bounded step."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers
+    import nqes_gb300 as pkg
+    cores = os.cpu_count() or 1
+    orc = helpers.Oracle(N, M, K, pkg.synthetic_j(N), H)
+    orc.set_weights(*pkg.synthetic_weights(N, M, K, 0.01, SEED))
+    lr, reglam = schedule(steps_done)
+    t0 = time.perf_counter()
+    _, info = orc.sr_step(SEED + steps_done * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT,
+                          store_o=False, threads=cores)
+    dt = time.perf_counter() - t0
+    return {"value": chains * SAMPLES / dt, "unit": "MC samples/s", "cores": cores, "kind": "port",
+            "sample": f"1 SR step, {chains} chains x {SAMPLES} samples (burn-in {BURN}), matrix-free S.v, "
+                      f"{int(info['iters'])} MINRES-QLP iterations, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import helpers
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    cores = os.cpu_count() or 1
+    chains = cores
+    orc = helpers.Oracle(N, M, K, pkg.synthetic_j(N), H)
+    orc.set_weights(*pkg.synthetic_weights(N, M, K, 0.01, SEED))
+    times, iters = [], []
+    for t in range(args.warmup + args.steps):
+        lr, reglam = schedule(t)
+        t0 = time.perf_counter()
+        _, info = orc.sr_step(SEED + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT, store_o=False,
+                              threads=cores)
+        dt = time.perf_counter() - t0
+        if t >= args.warmup:
+            times.append(dt)
+            iters.append(info["iters"])
+    tot = sum(times)
+    value = args.steps * chains * SAMPLES / tot
+    out = {
+        "impl": "reference", "metric": "MC samples/s (whole SR step) at N32 M64 K2", "value": value,
+        "unit": "MC samples/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "SR step, trapped-ion N=32 M=64 K=2 h=0.595, J=|i-j|^-1.2", "chains": chains,
+                   "samples_per_chain": SAMPLES, "burn_in": BURN, "minres_rtol": RTOL,
+                   "schedule": "lambda 40->1 x0.9, lr 0.1->0.01 x0.99", "parallelism": f"{cores} host threads"},
+        "sr_steps_per_s": args.steps / tot, "minres_iters_mean": float(np.mean(iters)),
+        "cpu_baseline": {"value": value, "unit": "MC samples/s", "cores": cores, "kind": "port",
+                         "sample": f"{chains} chains (one per core) x {SAMPLES} samples per step; the reference "
+                                   f"binary needs Eigen3/libmatio, absent here, so its oracle restatement runs"},
+        "e2e": {"value": value, "unit": "MC samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    import __graft_entry__ as ge
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    pkg = ge.load_package()
+    chains = args.chains
+    J = pkg.synthetic_j(N)
+    a0, b0, w0 = pkg.synthetic_weights(N, M, K, 0.01, SEED + rank)
+    ctx = pkg.Context(N, M, K, J, H, device=local)
+    ctx.set_weights(a0, b0, w0)
+    ns = chains * SAMPLES
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-resident steps ----
+    infos = []
+    for t in range(args.warmup):
+        lr, reglam = schedule(t)
+        ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+    clocks = ClockSampler(local)
+    barrier()
+    clocks.start()
+    t_wall0 = time.perf_counter()
+    for t in range(args.warmup, args.warmup + args.steps):
+        lr, reglam = schedule(t)
+        _, info = ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        infos.append(info)
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    dev_ms = sum(i["ms_total"] for i in infos)
+    if world > 1:
+        tt = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    value = world * args.steps * ns / (dev_ms * 1e-3)
+
+    # ---- per-kernel timing for the roofline (same data, same stream) ----
+    kern = {}
+    for name, kid in [("sample", pkg.KERNEL_SAMPLE), ("sv_rows", pkg.KERNEL_SV_ROWS), ("sv_cols", pkg.KERNEL_SV_COLS),
+                      ("moments", pkg.KERNEL_MOMENTS)]:
+        ms, by = ctx.time_kernel(kid, reps=3 if kid == pkg.KERNEL_SAMPLE else 10)
+        kern[name] = {"avg_ms": ms, "bytes": by}
+    bodies = [(i["kernel_launches"] - 9) // 6 for i in infos]
+    share = {
+        "sample": kern["sample"]["avg_ms"],
+        "sv_rows": kern["sv_rows"]["avg_ms"] * float(np.mean(bodies)),
+        "sv_cols": kern["sv_cols"]["avg_ms"] * float(np.mean(bodies)),
+    }
+    dom = max(share, key=share.get)
+    hbm, hbm_src = measured_peaks()
+    ach = kern[dom]["bytes"] / (kern[dom]["avg_ms"] * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dom)
+    fp64_tf = fp64_peak_tflops(torch)
+    # algorithmic FLOPs of the S·v passes: one FMA per stored real log-derivative
+    sv_flops = 2.0 * ns * ctx.P * (4 if infos[-1]["arith"] == pkg.ARITH_COMPLEX else 1)
+
+    # ---- end to end through the C ABI with host buffers ----
+    a_h, b_h, w_h = ctx.get_weights()
+    h2d = a_h.nbytes + b_h.nbytes + w_h.nbytes
+    d2h = K * K * 16 + h2d
+    barrier()
+    t0 = time.perf_counter()
+    t_base = args.warmup + args.steps
+    for t in range(t_base, t_base + args.steps):
+        lr, reglam = schedule(t)
+        ctx.set_weights(a_h, b_h, w_h)
+        ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        a_h, b_h, w_h = ctx.get_weights()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = world * args.steps * ns / e2e_s
+
+    out = {
+        "metric": "MC samples/s (whole SR step) at N32 M64 K2",
+        "value": value,
+        "unit": "MC samples/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "SR step, trapped-ion N=32 M=64 K=2 h=0.595, J=|i-j|^-1.2, real N(0,0.01^2) weights",
+                   "chains": chains, "samples_per_chain": SAMPLES, "burn_in": BURN, "minres_rtol": RTOL,
+                   "schedule": "lambda 40->1 x0.9, lr 0.1->0.01 x0.99",
+                   "l2": "inputs larger than L2 (O is %.2f GB)" % (ns * ctx.P * 8 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "sr_steps_per_s": args.steps / (dev_ms * 1e-3) * world,
+        "wall_sr_steps_per_s": args.steps / t_wall,
+        "minres_iters_mean": float(np.mean([i["minres_iters"] for i in infos])),
+        "accept_rate": float(np.mean([i["accepted"] / i["proposals"] for i in infos])),
+        "gpu_launches": int(sum(i["kernel_launches"] for i in infos)),
+        "kernels": kern,
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                     "frac": ach / hbm, "traffic": traffic, "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "fp64": {"achieved_tflops": (sv_flops / (kern[dom]["avg_ms"] * 1e-3) / 1e12)
+                              if dom.startswith("sv") else None,
+                              "peak_tflops_dgemm": fp64_tf}},
+        "e2e": {"value": e2e, "unit": "MC samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+    }
+    if clk:
+        out["clocks"] = clk
+    if rank == 0 and world == 1 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, args.warmup)
+    if rank == 0:
+        print(json.dumps(out))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chains", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

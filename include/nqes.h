@@ -1,0 +1,147 @@
+/*
+ * nqes.h — C ABI of the GB300 (sm_103a) VMC / stochastic-reconfiguration
+ * library for K multi-RBM excited states (libnqes.so).
+ *
+ * The reference (cl91/nqes-trapped-ion) has no plugin or FFI: its hot path is
+ * the function seam inside code/rbm.cc that its executable drives. Each entry
+ * point below replaces one such seam; the comment names it (file:line).
+ *
+ * Conventions
+ *   - Every call returns int status: NQES_OK (0) or a negative NQES_ERR_*;
+ *     nqes_last_error(ctx) then describes the failure. No C++ exception
+ *     crosses this boundary.
+ *   - Complex arrays are interleaved (re, im) doubles (C99 double _Complex /
+ *     std::complex<double> layout).
+ *   - Weights use the reference layout (code/rbm.cc:121-132):
+ *       a: K×N, b: K×M, w: K×N×M with w[(k*N+i)*M+j], all row-major.
+ *   - A spin configuration is ceil(N/64) uint64 words, bit i set = spin i
+ *     down (sigma_i = -1), as std::bitset in code/rbm.cc:77-83.
+ *   - Parameter vectors (log-derivatives, forces, solutions) have length
+ *     P = K*(N+M+N*M) in the layout [k][a_i | b_j | w_{i*M+j}]
+ *     (code/rbm.cc:199-239).
+ *   - The caller owns every host buffer; the context owns device memory.
+ *     One host thread per context; a context is bound to one device and one
+ *     CUDA stream. All results are computed on the GPU; there is no CPU path.
+ */
+#ifndef NQES_H
+#define NQES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NQES_OK 0
+#define NQES_ERR_CUDA (-1)       /* CUDA runtime error, or no CUDA device */
+#define NQES_ERR_OOM (-2)        /* device allocation failed */
+#define NQES_ERR_NONFINITE (-3)  /* non-finite amplitude ratio, energy, derivative or solver scalar */
+#define NQES_ERR_TIMEOUT (-4)    /* a bounded device-side wait ran out */
+#define NQES_ERR_INVALID (-5)    /* invalid argument or shape */
+#define NQES_ERR_STATE (-6)      /* call out of order (e.g. no sampled step yet) */
+
+/* Arithmetic of the device path (nqes_set_option NQES_OPT_ARITH). */
+#define NQES_ARITH_AUTO 0     /* real if every weight has zero imaginary part, else complex */
+#define NQES_ARITH_COMPLEX 1  /* always complex (the reference's own arithmetic) */
+#define NQES_ARITH_REAL 2     /* real; rejected when a weight has a non-zero imaginary part */
+
+/* Options (nqes_set_option). */
+#define NQES_OPT_ARITH 1             /* NQES_ARITH_* (default AUTO) */
+#define NQES_OPT_THREADS_PER_BLOCK 2 /* sampler threads per RBM column block: 32, 64, 128 or 0 = autotune */
+#define NQES_OPT_MINRES_CAP 3        /* device-side MINRES-QLP iteration cap (default 100000) */
+
+typedef struct nqes_ctx nqes_ctx;
+
+/* Result of one SR step. */
+typedef struct nqes_step_info {
+    int minres_flag;             /* MINRES-QLP exit flag, code/minresqlp.h:14-54 */
+    int arith;                   /* NQES_ARITH_REAL or NQES_ARITH_COMPLEX actually used */
+    uint64_t minres_iters;       /* iterations as the reference counts them */
+    uint64_t qlp_iters;
+    double relres, anorm, acond, xnorm;
+    uint64_t accepted;           /* accepted proposals, all chains, burn-in included */
+    uint64_t proposals;          /* chains * (burn_in + m) * K * N */
+    int warnings;                /* bit 1: device-side MINRES cap reached */
+    double eloc_re, eloc_im;     /* mean local energy (trace of e_mat) */
+    double ms_total;             /* device time of the step, CUDA events */
+    uint64_t kernel_launches;    /* kernels this step launched (graph nodes run, loop bodies counted) */
+} nqes_step_info;
+
+/* Kernels nqes_time_kernel can time in isolation. */
+#define NQES_KERNEL_SAMPLE 1   /* the sampler: one CTA per chain, whole chains */
+#define NQES_KERNEL_SV_ROWS 2  /* u = O v over the stored log-derivatives */
+#define NQES_KERNEL_SV_COLS 3  /* y = O^H u over the stored log-derivatives */
+#define NQES_KERNEL_MOMENTS 4  /* o, <|O|^2>, <E conj O> column reductions */
+
+/* Create a context for N spins, M hidden units, K states on CUDA `device`,
+ * for H = sum_{i!=j} J_ij sz_i sz_j - h sum_i sx_i with the diagonal term
+ * evaluated as 2 sum_{i>j} J[i*N+j] s_i s_j (lower triangle of the row-major
+ * N×N J).  Replaces the compile-time shape, the compiled-in J (JMAT_INC) and
+ * the `hamiltonian` callable of code/rbm.cc:1011-1062, 1273-1313.
+ * Limits: 1 <= K <= 4, 1 <= N <= 128, 1 <= M <= 512. */
+int nqes_create(int n_spins, int n_hidden, int n_states, const double *J, double h, int device, nqes_ctx **out);
+int nqes_destroy(nqes_ctx *ctx);
+/* Description of the last failure on ctx (or of the last failed nqes_create
+ * when ctx is NULL). Valid until the next call on the same context. */
+const char *nqes_last_error(const nqes_ctx *ctx);
+int nqes_set_option(nqes_ctx *ctx, int option, int64_t value);
+
+/* Weights, reference layout, complex interleaved.  Replaces the in-memory
+ * MultiRBM of code/rbm.cc:127-132 (load_rbm / dump_rbm read and write it). */
+int nqes_set_weights(nqes_ctx *ctx, const double *a, const double *b, const double *w);
+int nqes_get_weights(nqes_ctx *ctx, double *a, double *b, double *w);
+/* Reference initialisation: init_multi_rbm with pcg64(seed - 1) and
+ * std::normal_distribution<double>, code/rbm.cc:241-270, 1127, 1146-1147. */
+int nqes_init_weights(nqes_ctx *ctx, uint64_t seed);
+
+/* One SR step: sample, local energies, log-derivatives, moments, matrix-free
+ * MINRES-QLP solve of (S + reglam diag S) x = f, and w -= lr x.
+ * Replaces monte_carlo(rbm, seed, ncpus, m, burn_in, lr, reglam, rtol, maxit,
+ * hamiltonian), code/rbm.cc:564-719 (chain c uses pcg64(seed + c), so pass
+ * seed + iter*chains as code/rbm.cc:1179 does).  e_mat receives the K×K
+ * complex matrix the reference returns (e_mat / Ns, not yet divided by N). */
+int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int samples_per_chain, int burn_in, double lr,
+                 double reglam, double rtol, uint64_t maxit, double *e_mat, nqes_step_info *info);
+
+/* Correlation functions x, z (N×K) and xx, zz (N*N×K), row-major
+ * [row][state], unsorted: res(i,k) = Re diag(V^-1 <Phi^-1 F_i> V)_k for the
+ * K×K eigenvector matrix V (evecs, row-major complex).  Replaces the four
+ * correlation_fcn passes of code/rbm.cc:730-771, 1206-1217, which share one
+ * seed and therefore one set of chains. */
+int nqes_correlations(nqes_ctx *ctx, uint64_t seed, int chains, int samples_per_chain, int burn_in,
+                      const double *evecs, double *x, double *z, double *xx, double *zz);
+
+/* ---- inspection (parity tests and diagnostics) ---- */
+
+/* Phi (K×K complex, row-major, unscaled), tanh(theta) (M×K² complex,
+ * column k*K+kk), E = Phi^-1 H Phi (K×K complex) and O (P complex) at `count`
+ * given configurations (count × K × ceil(N/64) words); any output may be
+ * NULL.  The same device code the sampler runs per sample (state_fcn,
+ * ising_like_hamiltonian, deriv: code/rbm.cc:146-171, 1042-1062, 199-239). */
+int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi, double *tanh_theta, double *E,
+                  double *O);
+/* Per-sample records of the last SR step: configurations (Ns × K × words),
+ * local energies tr E (Ns complex) and E matrices (Ns × K² complex). */
+int nqes_get_samples(nqes_ctx *ctx, uint64_t *configs, double *eloc, double *E);
+/* Accepted proposals per chain (chains entries) of the last SR step. */
+int nqes_get_accepts(nqes_ctx *ctx, uint64_t *accepted);
+/* Rows [first, first+count) of the last step's O (count × P complex). */
+int nqes_get_O(nqes_ctx *ctx, int first, int count, double *O);
+/* Moments of the last step: o = <O>, skk = reglam(<|O|^2>-|o|^2), f (P complex each). */
+int nqes_get_moments(nqes_ctx *ctx, double *o, double *skk, double *f);
+/* Solution x of the last step's MINRES-QLP solve (P complex). */
+int nqes_get_solution(nqes_ctx *ctx, double *x);
+/* out = S v with the last step's samples and moments (P complex). */
+int nqes_apply_S(nqes_ctx *ctx, const double *v, double *out);
+/* Average device time (ms, CUDA events on the context's stream) of `reps`
+ * back-to-back launches of one kernel (NQES_KERNEL_*) on the last step's
+ * shapes and data, and the algorithmic bytes one launch moves (inputs read +
+ * outputs written once). For benchmarks; re-running the sampler overwrites
+ * the last step's samples with the same values (same seed). */
+int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double *algorithmic_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NQES_H */

@@ -1,0 +1,261 @@
+"""Python host mirror of libnqes (include/nqes.h) over ctypes.
+
+The reference drives its hot path through three functions of code/rbm.cc:
+monte_carlo (one SR step, 564-719), correlation_fcn (730-771) and the weight
+state (load_rbm / dump_rbm / init_multi_rbm). `Context` exposes the same
+operations with the same argument meanings: `sr_step` takes the per-step seed
+(seed + iter*chains, code/rbm.cc:1179), chains, samples per chain, burn-in,
+learning rate, lambda, MINRES-QLP rtol and maxit, updates the weights in place
+and returns the K×K matrix e_mat / Ns.
+
+Everything runs in the CUDA library; this module only moves arrays. If the
+library has not been built, `load_library` raises instead of falling back.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libnqes.so")
+
+OK = 0
+ERR_CUDA, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_INVALID, ERR_STATE = -1, -2, -3, -4, -5, -6
+ARITH_AUTO, ARITH_COMPLEX, ARITH_REAL = 0, 1, 2
+OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP = 1, 2, 3
+
+EXPORTS = [
+    "nqes_create", "nqes_destroy", "nqes_last_error", "nqes_set_option", "nqes_set_weights", "nqes_get_weights",
+    "nqes_init_weights", "nqes_sr_step", "nqes_correlations", "nqes_evaluate", "nqes_get_samples",
+    "nqes_get_accepts", "nqes_get_O", "nqes_get_moments", "nqes_get_solution", "nqes_apply_S", "nqes_time_kernel",
+]
+KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
+
+
+class NqesError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"libnqes error {status}: {message}")
+        self.status = status
+
+
+class StepInfo(ctypes.Structure):
+    _fields_ = [
+        ("minres_flag", ctypes.c_int), ("arith", ctypes.c_int),
+        ("minres_iters", ctypes.c_uint64), ("qlp_iters", ctypes.c_uint64),
+        ("relres", ctypes.c_double), ("anorm", ctypes.c_double), ("acond", ctypes.c_double),
+        ("xnorm", ctypes.c_double), ("accepted", ctypes.c_uint64), ("proposals", ctypes.c_uint64),
+        ("warnings", ctypes.c_int), ("eloc_re", ctypes.c_double), ("eloc_im", ctypes.c_double),
+        ("ms_total", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+_LIB = None
+_dp = ctypes.POINTER(ctypes.c_double)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def load_library(path=None):
+    """Load libnqes.so; raises when it is missing (there is no CPU path)."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(p)
+    vp, i, d, u64, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64, ctypes.c_int64
+    sigs = {
+        "nqes_create": (i, [i, i, i, _dp, d, i, ctypes.POINTER(vp)]),
+        "nqes_destroy": (i, [vp]),
+        "nqes_last_error": (ctypes.c_char_p, [vp]),
+        "nqes_set_option": (i, [vp, i, i64]),
+        "nqes_set_weights": (i, [vp, _dp, _dp, _dp]),
+        "nqes_get_weights": (i, [vp, _dp, _dp, _dp]),
+        "nqes_init_weights": (i, [vp, u64]),
+        "nqes_sr_step": (i, [vp, u64, i, i, i, d, d, d, u64, _dp, ctypes.POINTER(StepInfo)]),
+        "nqes_correlations": (i, [vp, u64, i, i, i, _dp, _dp, _dp, _dp, _dp]),
+        "nqes_evaluate": (i, [vp, _u64p, i, _dp, _dp, _dp, _dp]),
+        "nqes_get_samples": (i, [vp, _u64p, _dp, _dp]),
+        "nqes_get_accepts": (i, [vp, _u64p]),
+        "nqes_get_O": (i, [vp, i, i, _dp]),
+        "nqes_get_moments": (i, [vp, _dp, _dp, _dp]),
+        "nqes_get_solution": (i, [vp, _dp]),
+        "nqes_apply_S": (i, [vp, _dp, _dp]),
+        "nqes_time_kernel": (i, [vp, i, i, _dp, _dp]),
+    }
+    for name, (res, args) in sigs.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def _cp(a):
+    """complex128 array -> pointer to its interleaved doubles (None passes NULL)."""
+    if a is None:
+        return None
+    return a.view(np.float64).ctypes.data_as(_dp)
+
+
+def synthetic_j(n, alpha=1.2):
+    """Power-law chain coupling J_ij = |i-j|^-alpha (i != j), zero diagonal, max |J| = 1."""
+    i = np.arange(n)
+    d = np.abs(i[:, None] - i[None, :]).astype(float)
+    with np.errstate(divide="ignore"):
+        J = np.where(d > 0, d ** (-alpha), 0.0)
+    return J / np.max(np.abs(J)) if n > 1 else J
+
+
+def synthetic_weights(n, m, k, sigma=0.01, seed=0, real=True):
+    """Seeded N(0, sigma^2) weights in the reference layout (complex128, zero imaginary part when real)."""
+    rng = np.random.default_rng(seed)
+
+    def draw(shape):
+        z = rng.normal(0.0, sigma, size=shape)
+        if not real:
+            z = z + 1j * rng.normal(0.0, sigma, size=shape)
+        return np.ascontiguousarray(z, dtype=np.complex128)
+
+    return draw((k, n)), draw((k, m)), draw((k, n, m))
+
+
+class Context:
+    """One solve (N spins, M hidden units, K states) resident on one GPU."""
+
+    def __init__(self, n_spins, n_hidden, n_states, J, h, device=0, lib=None):
+        self.lib = lib or load_library()
+        self.N, self.M, self.K = int(n_spins), int(n_hidden), int(n_states)
+        self.L = self.N + self.M + self.N * self.M
+        self.P = self.K * self.L
+        self.NW = (self.N + 63) // 64
+        Jc = np.ascontiguousarray(J, dtype=np.float64)
+        if Jc.shape != (self.N, self.N):
+            raise ValueError("J must be N x N")
+        h_ = ctypes.c_void_p()
+        st = self.lib.nqes_create(self.N, self.M, self.K, Jc.ctypes.data_as(_dp), float(h), int(device),
+                                  ctypes.byref(h_))
+        if st != OK:
+            raise NqesError(st, self.lib.nqes_last_error(None).decode())
+        self._h = h_
+        self.chains = 0
+
+    def _check(self, st):
+        if st != OK:
+            raise NqesError(st, self.lib.nqes_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.nqes_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_option(self, option, value):
+        self._check(self.lib.nqes_set_option(self._h, option, int(value)))
+
+    def set_weights(self, a, b, w):
+        a = np.ascontiguousarray(a, np.complex128).reshape(self.K, self.N)
+        b = np.ascontiguousarray(b, np.complex128).reshape(self.K, self.M)
+        w = np.ascontiguousarray(w, np.complex128).reshape(self.K, self.N, self.M)
+        self._check(self.lib.nqes_set_weights(self._h, _cp(a), _cp(b), _cp(w)))
+
+    def get_weights(self):
+        a = np.zeros((self.K, self.N), np.complex128)
+        b = np.zeros((self.K, self.M), np.complex128)
+        w = np.zeros((self.K, self.N, self.M), np.complex128)
+        self._check(self.lib.nqes_get_weights(self._h, _cp(a), _cp(b), _cp(w)))
+        return a, b, w
+
+    def init_weights(self, seed):
+        self._check(self.lib.nqes_init_weights(self._h, int(seed)))
+
+    def sr_step(self, seed, chains, samples_per_chain, burn_in, lr, reglam, rtol, maxit):
+        emat = np.zeros((self.K, self.K), np.complex128)
+        info = StepInfo()
+        self._check(self.lib.nqes_sr_step(self._h, int(seed), int(chains), int(samples_per_chain), int(burn_in),
+                                          float(lr), float(reglam), float(rtol), int(maxit), _cp(emat),
+                                          ctypes.byref(info)))
+        self.chains = int(chains)
+        self.ns = int(chains) * int(samples_per_chain)
+        return emat, info.as_dict()
+
+    def correlations(self, seed, chains, samples_per_chain, burn_in, evecs):
+        N, K = self.N, self.K
+        ev = np.ascontiguousarray(evecs, np.complex128)
+        x = np.zeros((N, K))
+        z = np.zeros((N, K))
+        xx = np.zeros((N * N, K))
+        zz = np.zeros((N * N, K))
+        p = lambda arr: arr.ctypes.data_as(_dp)
+        self._check(self.lib.nqes_correlations(self._h, int(seed), int(chains), int(samples_per_chain),
+                                               int(burn_in), _cp(ev), p(x), p(z), p(xx), p(zz)))
+        return x, z, xx, zz
+
+    def evaluate(self, configs):
+        cfg = np.ascontiguousarray(configs, np.uint64).reshape(-1, self.K, self.NW)
+        n = cfg.shape[0]
+        K, M = self.K, self.M
+        phi = np.zeros((n, K, K), np.complex128)
+        th = np.zeros((n, M, K * K), np.complex128)
+        E = np.zeros((n, K, K), np.complex128)
+        O = np.zeros((n, self.P), np.complex128)
+        self._check(self.lib.nqes_evaluate(self._h, cfg.ctypes.data_as(_u64p), n, _cp(phi), _cp(th), _cp(E),
+                                           _cp(O)))
+        return phi, th, E, O
+
+    def get_samples(self):
+        spins = np.zeros((self.ns, self.K, self.NW), np.uint64)
+        eloc = np.zeros(self.ns, np.complex128)
+        E = np.zeros((self.ns, self.K, self.K), np.complex128)
+        self._check(self.lib.nqes_get_samples(self._h, spins.ctypes.data_as(_u64p), _cp(eloc), _cp(E)))
+        return spins, eloc, E
+
+    def get_accepts(self):
+        acc = np.zeros(self.chains, np.uint64)
+        self._check(self.lib.nqes_get_accepts(self._h, acc.ctypes.data_as(_u64p)))
+        return acc
+
+    def get_O(self, first, count):
+        O = np.zeros((count, self.P), np.complex128)
+        self._check(self.lib.nqes_get_O(self._h, int(first), int(count), _cp(O)))
+        return O
+
+    def get_moments(self):
+        o = np.zeros(self.P, np.complex128)
+        s = np.zeros(self.P, np.complex128)
+        f = np.zeros(self.P, np.complex128)
+        self._check(self.lib.nqes_get_moments(self._h, _cp(o), _cp(s), _cp(f)))
+        return o, s, f
+
+    def get_solution(self):
+        x = np.zeros(self.P, np.complex128)
+        self._check(self.lib.nqes_get_solution(self._h, _cp(x)))
+        return x
+
+    def time_kernel(self, kernel, reps=5):
+        """(average ms, algorithmic bytes per launch) of one kernel on the last step's data."""
+        ms = ctypes.c_double()
+        by = ctypes.c_double()
+        self._check(self.lib.nqes_time_kernel(self._h, int(kernel), int(reps), ctypes.byref(ms), ctypes.byref(by)))
+        return ms.value, by.value
+
+    def apply_S(self, v):
+        v = np.ascontiguousarray(v, np.complex128)
+        out = np.zeros(self.P, np.complex128)
+        self._check(self.lib.nqes_apply_S(self._h, _cp(v), _cp(out)))
+        return out

@@ -1,0 +1,430 @@
+// Metropolis sampler, local energy and log-derivative emission — one CTA per
+// Markov chain, the whole chain (start configuration, burn-in, m samples) in
+// one launch. This is the GPU form of code/rbm.cc:561-632 (the chain loop of
+// monte_carlo): init_multi_spin (98-119), state_fcn (146-171),
+// monte_carlo_step (530-552), ising_like_hamiltonian + trapped_ion_model
+// (1011-1062) and deriv (199-239).
+//
+// Thread layout. A chain's CTA has T = K * TK threads (TK a multiple of 32):
+// column block kk (RBM kk) owns threads [kk*TK, (kk+1)*TK), and thread jl of
+// the block owns hidden units j = jl, jl + TK, ... of that RBM. For a proposal
+// (k, i) every thread forms its factors
+//     f_j = cosh(2 w_ij) - sigma_i tanh(theta_j^{(k,kk)}) sinh(2 w_ij)
+// (= cosh(theta_j - 2 sigma_i w_ij) / cosh(theta_j), the factor of
+// flip_state_fcn, code/rbm.cc:182-187) from per-step tables, and the block
+// multiplies them by warp shuffles and one shared-memory step. Warp 0 turns
+// the K products into the new row k of Phi, its determinant and the
+// Metropolis decision; on acceptance every thread updates its tanh(theta)
+// entries with the same factor it already holds.
+//
+// On GB300 an FP64 warp instruction occupies the issuing warp for ~64 cycles
+// whether one lane or 32 are active, so the kernel keeps the per-proposal
+// FP64 instruction count per warp small rather than minimising lane work.
+//
+// Rows of Phi are kept scaled by exact powers of two. Every quantity the
+// reference derives from Phi (the ratio |det Phi'|^2/|det Phi|^2, Phi^-1 H Phi
+// and the log-derivatives) is invariant under row scaling, and power-of-two
+// scaling is exact, so this changes no result while keeping Phi in range.
+#include "nqes_internal.h"
+#include "pcg64.cuh"
+
+namespace nqes {
+
+namespace {
+
+constexpr int kUMax = 4;     // hidden units per thread in a column block
+constexpr int kMaxSpinWords = 8;  // K <= 4 configurations of <= 128 spins
+
+__device__ __forceinline__ double ldg(const double *p) { return __ldg(p); }
+__device__ __forceinline__ cplx ldg(const cplx *p) {
+    double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    return cplx{v.x, v.y};
+}
+__device__ __forceinline__ bool spin_down(const uint64_t *s, int i) { return (s[i >> 6] >> (i & 63)) & 1ULL; }
+template <class S> __device__ __forceinline__ S neg_if(S v, bool n) { return n ? -v : v; }
+template <class S> __device__ __forceinline__ S wt(const cplx &z);
+template <> __device__ __forceinline__ double wt<double>(const cplx &z) { return z.re; }
+template <> __device__ __forceinline__ cplx wt<cplx>(const cplx &z) { return z; }
+
+// Multiply v by 2^-e where e is v's binary exponent when it leaves [-256, 256].
+template <class S> __device__ __forceinline__ void renorm(S &v, int &e) {
+    int x = expo(v);
+    if (x > 256 || x < -256) {
+        v = scale2(v, -x);
+        e += x;
+    }
+}
+
+template <class S> struct Smem {
+    S *tnh, *phi, *pinv, *red, *rat, *bsig, *Bm, *Dm, *pm;
+    double *jk;
+    int *pe, *rowe, *flag;
+    uint64_t *spin;
+};
+
+__host__ __device__ inline size_t smem_bytes(int N, int M, int K, size_t ssz) {
+    size_t KK = size_t(K) * K;
+    size_t nS = KK * M + 2 * KK + 32 + 2 * KK * N + 2 * KK + KK + 32;
+    return nS * ssz + 8 * 4 + 8 * kMaxSpinWords + 4 * (32 + 4 + 4);
+}
+
+template <class S> __device__ inline Smem<S> carve(unsigned char *base, int N, int M, int K) {
+    Smem<S> s;
+    const int KK = K * K;
+    S *p = reinterpret_cast<S *>(base);
+    s.tnh = p; p += KK * M;
+    s.phi = p; p += KK;
+    s.pinv = p; p += KK;
+    s.red = p; p += 32;
+    s.rat = p; p += KK * N;
+    s.bsig = p; p += KK * N;
+    s.Bm = p; p += KK;
+    s.Dm = p; p += KK;
+    s.pm = p; p += KK + 32;  // (mantissa of Phi entries during init) + per-warp scratch
+    double *d = reinterpret_cast<double *>(p);
+    s.jk = d; d += 4;
+    s.spin = reinterpret_cast<uint64_t *>(d);
+    int *ip = reinterpret_cast<int *>(s.spin + kMaxSpinWords);
+    s.pe = ip; ip += 32;
+    s.rowe = ip; ip += 4;
+    s.flag = ip;
+    return s;
+}
+
+// Phi and tanh(theta) from scratch for the current configuration
+// (code/rbm.cc:146-171), with Phi's rows rescaled by powers of two.
+template <class S>
+__device__ void init_state(const SampleArgs<S> &A, Smem<S> &sm) {
+    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K;
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
+    for (int q = 0; q < KK; q++) {
+        const int k = q / K, kk = q - k * K;
+        const uint64_t *sk = sm.spin + k * NW;
+        S prod = one<S>();
+        int pe = 0;
+        for (int j = tid; j < M; j += T) {
+            S th = wt<S>(A.b[kk * M + j]);
+            const cplx *wc = A.w + size_t(kk) * N * M + j;
+            for (int i = 0; i < N; i++) {
+                S wij = wt<S>(wc[size_t(i) * M]);
+                th = spin_down(sk, i) ? th - wij : th + wij;
+            }
+            sm.tnh[q * M + j] = ctanh_(th);
+            prod = prod * ccosh_(th);
+            renorm(prod, pe);
+        }
+        // exp(sum_i sigma_i a_i) from thread 0
+        if (tid == 0) {
+            S sa = zero<S>();
+            for (int i = 0; i < N; i++) {
+                S ai = wt<S>(A.a[kk * N + i]);
+                sa = spin_down(sk, i) ? sa - ai : sa + ai;
+            }
+            prod = prod * cexp_(sa);
+            renorm(prod, pe);
+        }
+        // block product of (mantissa, exponent)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            S p2 = shfl_xor(prod, o);
+            int e2 = __shfl_xor_sync(0xffffffffu, pe, o);
+            prod = prod * p2;
+            pe += e2;
+            renorm(prod, pe);
+        }
+        if (lane == 0) {
+            sm.red[warp] = prod;
+            sm.pe[warp] = pe;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            S p = sm.red[0];
+            int e = sm.pe[0];
+            for (int w2 = 1; w2 < nwarp; w2++) {
+                p = p * sm.red[w2];
+                e += sm.pe[w2];
+                renorm(p, e);
+            }
+            sm.pm[q] = p;
+            sm.pe[32 - 1 - q] = e;  // exponents kept at the top of the scratch
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        for (int k = 0; k < K; k++) {
+            int emax = -100000;
+            for (int kk = 0; kk < K; kk++) {
+                const int q = k * K + kk;
+                if (!is_zero(sm.pm[q])) emax = max(emax, sm.pe[31 - q] + expo(sm.pm[q]));
+            }
+            if (emax == -100000) emax = 0;
+            for (int kk = 0; kk < K; kk++) {
+                const int q = k * K + kk;
+                sm.phi[q] = scale2(sm.pm[q], sm.pe[31 - q] - emax);
+            }
+            sm.rowe[k] = emax;
+        }
+    }
+    __syncthreads();
+}
+
+template <class S>
+__global__ void __launch_bounds__(512) k_sample(const SampleArgs<S> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K, L = A.sh.L;
+    const size_t P = size_t(A.sh.P);
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
+    const int TK = A.tk, WK = TK >> 5;
+    const int my_kk = tid / TK, my_jl = tid - my_kk * TK;
+    const int U = (M + TK - 1) / TK;
+    const int c = blockIdx.x;
+    Smem<S> sm = carve<S>(smem_raw, N, M, K);
+
+    Pcg64 rng{0, 0};
+    if (A.cfg) {
+        for (int t = tid; t < K * NW; t += T) sm.spin[t] = A.cfg[size_t(c) * K * NW + t];
+    } else if (tid == 0) {
+        // init_multi_spin: K·N Bernoulli draws, k-major (code/rbm.cc:98-119).
+        rng = pcg_seed(A.sp->seed + uint64_t(c));
+        for (int t = 0; t < K * NW; t++) sm.spin[t] = 0;
+        for (int k = 0; k < K; k++)
+            for (int i = 0; i < N; i++)
+                if (pcg_bernoulli_half(rng)) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
+    }
+    __syncthreads();
+    init_state(A, sm);
+
+    S detv = zero<S>();
+    double detn = 0.0;
+    unsigned long long nacc = 0;
+    const int total = A.cfg ? 1 : A.burn + A.m;
+    for (int sw = 0; sw < total; sw++) {
+        if (!A.cfg) {
+            // ---- one sweep: proposals k outer, i inner (code/rbm.cc:536-551) ----
+            if (tid == 0) {
+                detv = small_det(sm.phi, K);
+                detn = norm2(detv);
+            }
+            for (int k = 0; k < K; k++) {
+                S *trow = sm.tnh + (k * K + my_kk) * M;
+                for (int i = 0; i < N; i++) {
+                    const bool down = spin_down(sm.spin + k * NW, i);
+                    const S *crow = A.tab.ch + (size_t(my_kk) * N + i) * M;
+                    const S *srow = A.tab.sh + (size_t(my_kk) * N + i) * M;
+                    S f[kUMax], tq[kUMax], cq[kUMax], sq[kUMax];
+                    S prod = one<S>();
+#pragma unroll
+                    for (int q = 0; q < kUMax; q++) {
+                        const int j = my_jl + q * TK;
+                        if (q < U && j < M) {
+                            tq[q] = trow[j];
+                            cq[q] = ldg(crow + j);
+                            sq[q] = ldg(srow + j);
+                            // f = cosh(ws) - tanh * sinh(ws), ws = 2 sigma w
+                            f[q] = mad(neg_if(tq[q], !down), sq[q], cq[q]);
+                            prod = prod * f[q];
+                        }
+                    }
+                    prod = warp_prod(prod);
+                    if (lane == 0) sm.red[warp] = prod;
+                    __syncthreads();
+                    if (tid == 0) {
+                        S row[4], tmp[16];
+                        for (int t = 0; t < KK; t++) tmp[t] = sm.phi[t];
+                        for (int kk = 0; kk < K; kk++) {
+                            S r = sm.red[kk * WK];
+                            for (int w2 = 1; w2 < WK; w2++) r = r * sm.red[kk * WK + w2];
+                            r = r * ldg((down ? A.tab.edn : A.tab.eup) + kk * N + i);
+                            row[kk] = sm.phi[k * K + kk] * r;
+                            tmp[k * K + kk] = row[kk];
+                        }
+                        const S dp = small_det(tmp, K);
+                        const double np = norm2(dp);
+                        const double u = pcg_uniform(rng);
+                        // Accept iff u <= min(1, |det Phi'|^2 / |det Phi|^2), with
+                        // probability one when det Phi == 0 (code/rbm.cc:541-543),
+                        // evaluated as u |det Phi|^2 <= |det Phi'|^2.
+                        const bool acc = is_zero(detv) || u * detn <= np;
+                        if (acc) {
+                            int ex = -100000;
+                            for (int kk = 0; kk < K; kk++) ex = max(ex, expo(row[kk]));
+                            const bool rs = ex > 256 || ex < -256;
+                            for (int kk = 0; kk < K; kk++) sm.phi[k * K + kk] = rs ? scale2(row[kk], -ex) : row[kk];
+                            detv = rs ? scale2(dp, -ex) : dp;
+                            detn = norm2(detv);
+                            if (rs) sm.rowe[k] += ex;
+                            sm.spin[k * NW + (i >> 6)] ^= 1ULL << (i & 63);
+                            nacc++;
+                        }
+                        sm.flag[0] = acc;
+                    }
+                    __syncthreads();
+                    if (sm.flag[0]) {
+#pragma unroll
+                        for (int q = 0; q < kUMax; q++) {
+                            const int j = my_jl + q * TK;
+                            if (q < U && j < M) {
+                                // tanh' = (tanh cosh(ws) - sinh(ws)) / f  (code/rbm.cc:185)
+                                trow[j] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * inv(f[q]);
+                            }
+                        }
+                    }
+                }
+            }
+            if (sw < A.burn) continue;
+        }
+        // ---- sample: local energy and log-derivatives ----
+        const size_t s = A.cfg ? size_t(c) : size_t(c) * A.m + (sw - A.burn);
+        if (tid == 0) {
+            if (!small_inv(sm.phi, sm.pinv, K)) {
+                atomicOr(A.err, kErrSingular);
+                for (int t = 0; t < KK; t++) sm.pinv[t] = zero<S>();
+            }
+        }
+        __syncthreads();
+        if (warp < K) {
+            // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031)
+            const uint64_t *sk = sm.spin + warp * NW;
+            double acc = 0.0;
+            for (int i = 1 + lane; i < N; i += 32) {
+                const bool si = spin_down(sk, i);
+                const double *Jr = A.J + size_t(i) * N;
+                for (int j = 0; j < i; j++) {
+                    const double p = Jr[j];
+                    acc += (si ^ spin_down(sk, j)) ? -p : p;
+                }
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) sm.jk[warp] = 2.0 * acc;
+        }
+        // Ratios Phi(flip i in row k)[k][kk] / Phi[k][kk] for every (k, kk, i),
+        // the N single-flip terms of the transverse field (code/rbm.cc:1050-1058).
+        for (int it = tid; it < KK * N; it += T) {
+            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const bool down = spin_down(sm.spin + k * NW, i);
+            const S *crow = A.tab.ch + (size_t(kk) * N + i) * M;
+            const S *srow = A.tab.sh + (size_t(kk) * N + i) * M;
+            const S *trow = sm.tnh + q * M;
+            S p = one<S>();
+            for (int j = 0; j < M; j++) p = p * mad(neg_if(trow[j], !down), ldg(srow + j), ldg(crow + j));
+            sm.rat[it] = p * ldg((down ? A.tab.edn : A.tab.eup) + kk * N + i);
+            // B(kk->k) sigma^{(kk)}_i for the a and w derivatives, where
+            // B(kk->k) = (Phi^-1)[k][kk] Phi[kk][k] (closed form of the
+            // determinants in code/rbm.cc:211-236).
+            const S B = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
+            sm.bsig[it] = spin_down(sm.spin + kk * NW, i) ? -B : B;
+        }
+        __syncthreads();
+        for (int q = warp; q < KK; q += nwarp) {
+            S acc = zero<S>();
+            for (int i = lane; i < N; i += 32) acc = acc + sm.rat[q * N + i];
+            acc = warp_sum(acc);
+            if (lane == 0) sm.Dm[q] = one<S>() * sm.jk[q / K] - A.h * acc;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            // E = Phi^-1 (D o Phi)  (code/rbm.cc:1046-1061)
+            bool ok = true;
+            for (int r = 0; r < K; r++)
+                for (int cc = 0; cc < K; cc++) {
+                    S e = zero<S>();
+                    for (int t = 0; t < K; t++) e = mad(sm.pinv[r * K + t], sm.Dm[t * K + cc] * sm.phi[t * K + cc], e);
+                    ok = ok && finite(e);
+                    A.E[s * KK + r * K + cc] = to_c(e);
+                }
+            for (int k = 0; k < K; k++)
+                for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
+            if (!ok) atomicOr(A.err, kErrNonFinite);
+        }
+        for (int t = tid; t < K * NW; t += T) A.spins[s * K * NW + t] = sm.spin[t];
+        if (A.cfg && A.phi_out) {
+            for (int t = tid; t < KK; t += T) A.phi_out[s * KK + t] = to_c(scale2(sm.phi[t], sm.rowe[t / K]));
+            for (int t = tid; t < KK * M; t += T) {
+                const int q = t / M, j = t - q * M;
+                A.tanh_out[s * KK * M + size_t(j) * KK + q] = to_c(sm.tnh[t]);
+            }
+        }
+        __syncthreads();
+        // O row, layout [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239):
+        //   O_{k,a_i}  = sum_kk B(kk->k) sigma^{(kk)}_i
+        //   O_{k,b_j}  = sum_kk B(kk->k) tanh theta_j^{(kk,k)}
+        //   O_{k,w_ij} = sum_kk B(kk->k) sigma^{(kk)}_i tanh theta_j^{(kk,k)}
+        S *orow = A.O + s * P;
+        for (int k = 0; k < K; k++) {
+            S *ok = orow + size_t(k) * L;
+            for (int p = tid; p < L; p += T) {
+                S v = zero<S>();
+                if (p < N) {
+                    for (int kk = 0; kk < K; kk++) v = v + sm.bsig[(k * K + kk) * N + p];
+                } else if (p < N + M) {
+                    const int j = p - N;
+                    for (int kk = 0; kk < K; kk++) v = mad(sm.Bm[k * K + kk], sm.tnh[(kk * K + k) * M + j], v);
+                } else {
+                    const int q = p - N - M, i = q / M, j = q - i * M;
+                    for (int kk = 0; kk < K; kk++)
+                        v = mad(sm.bsig[(k * K + kk) * N + i], sm.tnh[(kk * K + k) * M + j], v);
+                }
+                ok[p] = v;
+            }
+        }
+        // (No barrier needed here: the next sweep's first shared write follows a
+        // __syncthreads that every thread reaches only after its O stores.)
+    }
+    if (tid == 0 && !A.cfg) A.accepted[c] = nacc;
+}
+
+// Per-step tables from the weights: cosh(2w), sinh(2w), exp(-2a), exp(2a).
+template <class S>
+__global__ void k_tables(Shape sh, const cplx *a, const cplx *w, S *ch, S *shh, S *eup, S *edn) {
+    const size_t nw = size_t(sh.K) * sh.N * sh.M;
+    for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < nw; t += size_t(gridDim.x) * blockDim.x) {
+        const S w2 = wt<S>(w[t]) * 2.0;
+        ch[t] = ccosh_(w2);
+        shh[t] = csinh_(w2);
+        if (t < size_t(sh.K) * sh.N) {
+            const S a2 = wt<S>(a[t]) * 2.0;
+            eup[t] = cexp_(-a2);
+            edn[t] = cexp_(a2);
+        }
+    }
+}
+
+}  // namespace
+
+size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith) {
+    (void)threads;
+    return smem_bytes(sh.N, sh.M, sh.K, complex_arith ? sizeof(cplx) : sizeof(double));
+}
+
+// Sets the sampler's dynamic shared-memory limit; call outside stream capture.
+template <class S> cudaError_t prepare_sample(const Shape &sh) {
+    const size_t smem = smem_bytes(sh.N, sh.M, sh.K, sizeof(S));
+    return cudaFuncSetAttribute(k_sample<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+}
+
+template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st) {
+    const size_t smem = smem_bytes(a.sh.N, a.sh.M, a.sh.K, sizeof(S));
+    k_sample<S><<<a.chains, threads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template cudaError_t prepare_sample<double>(const Shape &);
+template cudaError_t prepare_sample<cplx>(const Shape &);
+
+template <class S>
+cudaError_t launch_tables(const Shape &sh, const cplx *a, const cplx *w, S *ch, S *shh, S *eup, S *edn,
+                          cudaStream_t st) {
+    const size_t nw = size_t(sh.K) * sh.N * sh.M;
+    int blocks = int(std::min<size_t>((nw + 255) / 256, 4096));
+    k_tables<S><<<blocks, 256, 0, st>>>(sh, a, w, ch, shh, eup, edn);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_sample<double>(const SampleArgs<double> &, int, cudaStream_t);
+template cudaError_t launch_sample<cplx>(const SampleArgs<cplx> &, int, cudaStream_t);
+template cudaError_t launch_tables<double>(const Shape &, const cplx *, const cplx *, double *, double *, double *,
+                                           double *, cudaStream_t);
+template cudaError_t launch_tables<cplx>(const Shape &, const cplx *, const cplx *, cplx *, cplx *, cplx *, cplx *,
+                                         cudaStream_t);
+
+}  // namespace nqes

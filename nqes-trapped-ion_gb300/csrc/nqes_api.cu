@@ -1,0 +1,836 @@
+// Host side of libnqes: the C ABI of include/nqes.h.
+//
+// One SR step (code/rbm.cc:564-719) is one CUDA graph launch:
+//   [clear error word] -> tables(w) -> sampler (one CTA per chain) ->
+//   moments -> MINRES-QLP init -> while (running) { S·v rows, S·v cols,
+//   Lanczos a, Lanczos b, QLP scalars, QLP vectors } -> w -= lr x
+// The while loop is a graph conditional node whose condition the QLP scalar
+// kernel sets, so the Krylov solve runs without host round trips. Per-step
+// scalars (seed, lr, reglam, rtol, maxit) live in device memory and are
+// rewritten before each launch; the graph is rebuilt only when the chain
+// count, samples per chain, burn-in, arithmetic or thread shape change.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/nqes.h"
+#include "nqes_internal.h"
+#include "pcg64.cuh"
+
+using namespace nqes;
+
+struct nqes_ctx {
+    Shape sh{};
+    int device = 0;
+    cudaStream_t st = nullptr;
+    double h = 0;
+    int arith_opt = NQES_ARITH_AUTO;
+    int tk_opt = 0;
+    uint64_t minres_cap = 100000;
+    bool weights_real = true;
+    std::string err;
+
+    cplx *a = nullptr, *b = nullptr, *w = nullptr;
+    double *J = nullptr;
+    void *tab = nullptr;  // ch, sh (K·N·M each), eup, edn (K·N each), sized for complex
+    StepParams *sp = nullptr, *sp_host = nullptr;
+    QlpState *qs = nullptr, *qs_host = nullptr;
+    int *err_d = nullptr, *err_host = nullptr;
+    cplx *emat_d = nullptr, *eloc_d = nullptr, *emat_host = nullptr;
+
+    // per-shape step buffers
+    int chains = 0, m = 0, arith = 0;
+    size_t Ns = 0;
+    void *O = nullptr;
+    cplx *E = nullptr;
+    uint64_t *spins = nullptr;
+    unsigned long long *accepted = nullptr;
+    void *u = nullptr, *ypart = nullptr, *vecs = nullptr, *ovpart = nullptr;
+    double *part = nullptr;
+    int rchunks = 1;
+
+    cudaGraphExec_t exec = nullptr;
+    int g_chains = -1, g_m = -1, g_burn = -1, g_arith = -1, g_tk = -1;
+    bool have_step = false;
+    int last_burn = 0, last_tk = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+static std::string g_create_error;
+
+#define NQES_CUDA(call)                                                                                   \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) {                                                                          \
+            ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                                \
+            return e_ == cudaErrorMemoryAllocation ? NQES_ERR_OOM : NQES_ERR_CUDA;                        \
+        }                                                                                                 \
+    } while (0)
+
+namespace {
+
+template <class T> int dalloc(nqes_ctx *ctx, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), count * sizeof(T));
+    if (e != cudaSuccess) {
+        ctx->err = "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes: " + cudaGetErrorString(e);
+        return NQES_ERR_OOM;
+    }
+    return NQES_OK;
+}
+template <class T> void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+size_t ssize(int arith) { return arith == NQES_ARITH_COMPLEX ? sizeof(cplx) : sizeof(double); }
+
+void free_step_buffers(nqes_ctx *ctx) {
+    dfree(ctx->O);
+    dfree(ctx->E);
+    dfree(ctx->spins);
+    dfree(ctx->accepted);
+    dfree(ctx->u);
+    dfree(ctx->ypart);
+    dfree(ctx->vecs);
+    dfree(ctx->ovpart);
+    dfree(ctx->part);
+    if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
+    ctx->exec = nullptr;
+    ctx->g_chains = -1;
+    ctx->chains = ctx->m = 0;
+    ctx->Ns = 0;
+    ctx->have_step = false;
+}
+
+int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
+    if (ctx->chains == chains && ctx->m == m && ctx->arith == arith && ctx->O) return NQES_OK;
+    free_step_buffers(ctx);
+    const Shape &sh = ctx->sh;
+    const size_t Ns = size_t(chains) * m, P = size_t(sh.P), ss = ssize(arith);
+    const int nb = int((P + 255) / 256);
+    const int ctiles = nb;
+    ctx->rchunks = std::max(1, std::min(32, int((Ns + 255) / 256)));
+    ctx->rchunks = std::max(1, std::min(ctx->rchunks, std::max(1, 600 / std::max(1, ctiles))));
+    int rc;
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * ss))) return rc;
+    if ((rc = dalloc(ctx, &ctx->E, Ns * sh.K * sh.K))) return rc;
+    if ((rc = dalloc(ctx, &ctx->spins, Ns * sh.K * sh.NW))) return rc;
+    if ((rc = dalloc(ctx, &ctx->accepted, size_t(chains)))) return rc;
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->u), Ns * ss))) return rc;
+    // ypart doubles as scratch for the moment partials: 3 × rchunks × P scalars
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ypart), 3 * size_t(ctx->rchunks) * P * ss)))
+        return rc;
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->vecs), 14 * P * ss))) return rc;
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ovpart), size_t(kPartStride) * ss))) return rc;
+    if ((rc = dalloc(ctx, &ctx->part, size_t(3 * kPartStride)))) return rc;
+    ctx->chains = chains;
+    ctx->m = m;
+    ctx->arith = arith;
+    ctx->Ns = Ns;
+    return NQES_OK;
+}
+
+template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
+    SolveBufs<S> B{};
+    const size_t P = ctx->sh.P;
+    B.sh = ctx->sh;
+    B.Ns = int(ctx->Ns);
+    B.O = static_cast<const S *>(ctx->O);
+    B.E = ctx->E;
+    S *vec = static_cast<S *>(ctx->vecs);
+    B.o = vec + 0 * P;
+    B.skk = vec + 1 * P;
+    B.f = vec + 2 * P;
+    B.r1 = vec + 3 * P;
+    B.r2 = vec + 4 * P;
+    B.r3 = vec + 5 * P;
+    B.v = vec + 6 * P;
+    B.vn = vec + 7 * P;
+    B.w = vec + 8 * P;
+    B.wl = vec + 9 * P;
+    B.wl2 = vec + 10 * P;
+    B.x = vec + 11 * P;
+    B.xl2 = vec + 12 * P;
+    B.u = static_cast<S *>(ctx->u);
+    B.ypart = static_cast<S *>(ctx->ypart);
+    B.rchunks = ctx->rchunks;
+    B.part = ctx->part;
+    B.ovpart = static_cast<S *>(ctx->ovpart);
+    B.qs = ctx->qs;
+    B.sp = ctx->sp;
+    B.emat = ctx->emat_d;
+    B.eloc = ctx->eloc_d;
+    B.err = ctx->err_d;
+    B.use_cond = 0;
+    return B;
+}
+
+template <class S> Tables<S> tables(nqes_ctx *ctx) {
+    const size_t nw = size_t(ctx->sh.K) * ctx->sh.N * ctx->sh.M, na = size_t(ctx->sh.K) * ctx->sh.N;
+    S *t = static_cast<S *>(ctx->tab);
+    return Tables<S>{t, t + nw, t + 2 * nw, t + 2 * nw + na};
+}
+
+template <class S> SampleArgs<S> sample_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
+    SampleArgs<S> A{};
+    A.sh = ctx->sh;
+    A.chains = chains;
+    A.m = m;
+    A.burn = burn;
+    A.tk = tk;
+    A.sp = ctx->sp;
+    A.tab = tables<S>(ctx);
+    A.a = ctx->a;
+    A.b = ctx->b;
+    A.w = ctx->w;
+    A.J = ctx->J;
+    A.h = ctx->h;
+    A.O = static_cast<S *>(ctx->O);
+    A.E = ctx->E;
+    A.spins = ctx->spins;
+    A.accepted = ctx->accepted;
+    A.err = ctx->err_d;
+    return A;
+}
+
+template <class S> cudaError_t launch_tables_ctx(nqes_ctx *ctx) {
+    Tables<S> t = tables<S>(ctx);
+    return launch_tables<S>(ctx->sh, ctx->a, ctx->w, const_cast<S *>(t.ch), const_cast<S *>(t.sh),
+                            const_cast<S *>(t.eup), const_cast<S *>(t.edn), ctx->st);
+}
+
+// Threads per RBM column block: enough that each thread holds at most four
+// hidden units, more when there are few chains to spread over the SMs.
+int choose_tk(nqes_ctx *ctx, int chains) {
+    const int M = ctx->sh.M, K = ctx->sh.K;
+    int tmin = std::max(32, ((M + 3) / 4 + 31) / 32 * 32);
+    int tk;
+    if (ctx->tk_opt) {
+        tk = std::max(tmin, ctx->tk_opt);
+    } else {
+        int dev_sms = 152;
+        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        tk = chains <= dev_sms ? std::min(128, (M + 31) / 32 * 32) : tmin;
+        tk = std::max(tk, tmin);
+    }
+    while (K * tk > 512) tk -= 32;
+    return tk;
+}
+
+template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
+    if (ctx->exec) {
+        cudaGraphExecDestroy(ctx->exec);
+        ctx->exec = nullptr;
+    }
+    SampleArgs<S> A = sample_args<S>(ctx, chains, m, burn, tk);
+    SolveBufs<S> B = solve_bufs<S>(ctx);
+    const int threads = ctx->sh.K * tk;
+    {
+        // the sampler's dynamic shared memory attribute must be set before capture
+        const size_t smem = sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
+        if (smem > 227 * 1024) {
+            ctx->err = "shape needs " + std::to_string(smem) + " bytes of shared memory per chain";
+            return NQES_ERR_INVALID;
+        }
+        NQES_CUDA(prepare_sample<S>(ctx->sh));
+    }
+    cudaGraph_t g = nullptr, gA = nullptr, gC = nullptr;
+    NQES_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond;
+    // Default value 1 on every launch: the body runs at least once, and its
+    // scalar kernel writes 0 as soon as the solve has finished (or was
+    // never needed), so the loop always ends.
+    NQES_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
+
+    NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->st);
+    cudaError_t le = launch_tables_ctx<S>(ctx);
+    if (le == cudaSuccess) le = launch_sample<S>(A, threads, ctx->st);
+    if (le == cudaSuccess) le = launch_moments<S>(B, ctx->st);
+    if (le == cudaSuccess) le = launch_minres_init<S>(B, ctx->st);
+    cudaError_t ce = cudaStreamEndCapture(ctx->st, &gA);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        ctx->err = std::string("capture of the sampling segment: ") +
+                   cudaGetErrorString(le != cudaSuccess ? le : ce);
+        cudaGraphDestroy(g);
+        return NQES_ERR_CUDA;
+    }
+    cudaGraphNode_t nA, nW, nC;
+    NQES_CUDA(cudaGraphAddChildGraphNode(&nA, g, nullptr, 0, gA));
+    cudaGraphNodeParams cp{};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    NQES_CUDA(cudaGraphAddNode(&nW, g, &nA, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    B.cond = cond;
+    B.use_cond = 1;
+    NQES_CUDA(cudaStreamBeginCaptureToGraph(ctx->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    le = launch_minres_iter<S>(B, ctx->st);
+    ce = cudaStreamEndCapture(ctx->st, &body);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        ctx->err = std::string("capture of the MINRES-QLP body: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
+        cudaGraphDestroy(g);
+        cudaGraphDestroy(gA);
+        return NQES_ERR_CUDA;
+    }
+    NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    le = launch_update<S>(ctx->sh, ctx->sp, B.x, ctx->a, ctx->b, ctx->w, ctx->st);
+    ce = cudaStreamEndCapture(ctx->st, &gC);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        ctx->err = std::string("capture of the update: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
+        return NQES_ERR_CUDA;
+    }
+    NQES_CUDA(cudaGraphAddChildGraphNode(&nC, g, &nW, 1, gC));
+    NQES_CUDA(cudaGraphInstantiate(&ctx->exec, g, 0));
+    cudaGraphDestroy(gA);
+    cudaGraphDestroy(gC);
+    cudaGraphDestroy(g);
+    ctx->g_chains = chains;
+    ctx->g_m = m;
+    ctx->g_burn = burn;
+    ctx->g_arith = ctx->arith;
+    ctx->g_tk = tk;
+    return NQES_OK;
+}
+
+bool host_weights_real(const double *a, const double *b, const double *w, const Shape &sh) {
+    auto check = [](const double *p, size_t n) {
+        for (size_t t = 0; t < n; t++)
+            if (p[2 * t + 1] != 0.0) return false;
+        return true;
+    };
+    return check(a, size_t(sh.K) * sh.N) && check(b, size_t(sh.K) * sh.M) && check(w, size_t(sh.K) * sh.N * sh.M);
+}
+
+int resolve_arith(nqes_ctx *ctx) {
+    if (ctx->arith_opt == NQES_ARITH_COMPLEX) return NQES_ARITH_COMPLEX;
+    if (ctx->arith_opt == NQES_ARITH_REAL) return NQES_ARITH_REAL;
+    return ctx->weights_real ? NQES_ARITH_REAL : NQES_ARITH_COMPLEX;
+}
+
+// Copy an S-typed device array to interleaved complex host memory.
+int copy_out_c(nqes_ctx *ctx, const void *src, size_t n, double *dst) {
+    if (ctx->arith == NQES_ARITH_COMPLEX) {
+        NQES_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(cplx), cudaMemcpyDeviceToHost, ctx->st));
+        NQES_CUDA(cudaStreamSynchronize(ctx->st));
+    } else {
+        std::vector<double> tmp(n);
+        NQES_CUDA(cudaMemcpyAsync(tmp.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+        NQES_CUDA(cudaStreamSynchronize(ctx->st));
+        for (size_t t = 0; t < n; t++) {
+            dst[2 * t] = tmp[t];
+            dst[2 * t + 1] = 0.0;
+        }
+    }
+    return NQES_OK;
+}
+
+template <class S> int sr_step_t(nqes_ctx *ctx, int chains, int m, int burn) {
+    const int tk = choose_tk(ctx, chains);
+    if (!ctx->exec || ctx->g_chains != chains || ctx->g_m != m || ctx->g_burn != burn || ctx->g_arith != ctx->arith ||
+        ctx->g_tk != tk) {
+        int rc = build_graph<S>(ctx, chains, m, burn, tk);
+        if (rc) return rc;
+    }
+    ctx->last_tk = tk;
+    NQES_CUDA(cudaMemcpyAsync(ctx->sp, ctx->sp_host, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->st));
+    NQES_CUDA(cudaEventRecord(ctx->ev0, ctx->st));
+    NQES_CUDA(cudaGraphLaunch(ctx->exec, ctx->st));
+    NQES_CUDA(cudaEventRecord(ctx->ev1, ctx->st));
+    return NQES_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *nqes_last_error(const nqes_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes_ctx **out) {
+    if (!out) {
+        g_create_error = "out is NULL";
+        return NQES_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (K < 1 || K > 4 || N < 1 || N > 128 || M < 1 || M > 512 || !J) {
+        g_create_error = "shape out of range (1<=K<=4, 1<=N<=128, 1<=M<=512) or J is NULL";
+        return NQES_ERR_INVALID;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+        g_create_error = "no CUDA device " + std::to_string(device);
+        return NQES_ERR_CUDA;
+    }
+    nqes_ctx *ctx = new nqes_ctx();
+    ctx->device = device;
+    ctx->h = h;
+    ctx->sh = Shape{N, M, K, N + M + N * M, K * (N + M + N * M), (N + 63) / 64};
+    auto fail = [&](int rc) {
+        g_create_error = ctx->err;
+        nqes_destroy(ctx);
+        return rc;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) {
+        ctx->err = "cudaSetDevice failed";
+        return fail(NQES_ERR_CUDA);
+    }
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) {
+        ctx->err = "cudaStreamCreate failed";
+        return fail(NQES_ERR_CUDA);
+    }
+    cudaEventCreate(&ctx->ev0);
+    cudaEventCreate(&ctx->ev1);
+    const size_t nw = size_t(K) * N * M, na = size_t(K) * N;
+    int rc;
+    if ((rc = dalloc(ctx, &ctx->a, na)) || (rc = dalloc(ctx, &ctx->b, size_t(K) * M)) ||
+        (rc = dalloc(ctx, &ctx->w, nw)) || (rc = dalloc(ctx, &ctx->J, size_t(N) * N)) ||
+        (rc = dalloc(ctx, reinterpret_cast<cplx **>(&ctx->tab), 2 * nw + 2 * na)) ||
+        (rc = dalloc(ctx, &ctx->sp, 1)) || (rc = dalloc(ctx, &ctx->qs, 1)) || (rc = dalloc(ctx, &ctx->err_d, 1)) ||
+        (rc = dalloc(ctx, &ctx->emat_d, 16)) || (rc = dalloc(ctx, &ctx->eloc_d, 1)))
+        return fail(rc);
+    if (cudaMallocHost(&ctx->sp_host, sizeof(StepParams)) != cudaSuccess ||
+        cudaMallocHost(&ctx->qs_host, sizeof(QlpState)) != cudaSuccess ||
+        cudaMallocHost(&ctx->err_host, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost(&ctx->emat_host, 17 * sizeof(cplx)) != cudaSuccess) {
+        ctx->err = "cudaMallocHost failed";
+        return fail(NQES_ERR_OOM);
+    }
+    if (cudaMemcpy(ctx->J, J, sizeof(double) * N * N, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(ctx->a, 0, sizeof(cplx) * na) != cudaSuccess ||
+        cudaMemset(ctx->b, 0, sizeof(cplx) * K * M) != cudaSuccess ||
+        cudaMemset(ctx->w, 0, sizeof(cplx) * nw) != cudaSuccess) {
+        ctx->err = "initial copies failed";
+        return fail(NQES_ERR_CUDA);
+    }
+    *out = ctx;
+    return NQES_OK;
+}
+
+int nqes_destroy(nqes_ctx *ctx) {
+    if (!ctx) return NQES_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    free_step_buffers(ctx);
+    dfree(ctx->a);
+    dfree(ctx->b);
+    dfree(ctx->w);
+    dfree(ctx->J);
+    dfree(ctx->tab);
+    dfree(ctx->sp);
+    dfree(ctx->qs);
+    dfree(ctx->err_d);
+    dfree(ctx->emat_d);
+    dfree(ctx->eloc_d);
+    if (ctx->sp_host) cudaFreeHost(ctx->sp_host);
+    if (ctx->qs_host) cudaFreeHost(ctx->qs_host);
+    if (ctx->err_host) cudaFreeHost(ctx->err_host);
+    if (ctx->emat_host) cudaFreeHost(ctx->emat_host);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return NQES_OK;
+}
+
+int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
+    if (!ctx) return NQES_ERR_INVALID;
+    switch (option) {
+    case NQES_OPT_ARITH:
+        if (value < 0 || value > 2) {
+            ctx->err = "arith must be AUTO, COMPLEX or REAL";
+            return NQES_ERR_INVALID;
+        }
+        if (value == NQES_ARITH_REAL && !ctx->weights_real) {
+            ctx->err = "weights have non-zero imaginary parts; real arithmetic refused";
+            return NQES_ERR_INVALID;
+        }
+        ctx->arith_opt = int(value);
+        return NQES_OK;
+    case NQES_OPT_THREADS_PER_BLOCK:
+        if (value != 0 && value != 32 && value != 64 && value != 96 && value != 128) {
+            ctx->err = "threads per column block must be 0 (auto), 32, 64, 96 or 128";
+            return NQES_ERR_INVALID;
+        }
+        ctx->tk_opt = int(value);
+        return NQES_OK;
+    case NQES_OPT_MINRES_CAP:
+        if (value < 1) {
+            ctx->err = "MINRES cap must be positive";
+            return NQES_ERR_INVALID;
+        }
+        ctx->minres_cap = uint64_t(value);
+        return NQES_OK;
+    default:
+        ctx->err = "unknown option " + std::to_string(option);
+        return NQES_ERR_INVALID;
+    }
+}
+
+int nqes_set_weights(nqes_ctx *ctx, const double *a, const double *b, const double *w) {
+    if (!ctx || !a || !b || !w) return NQES_ERR_INVALID;
+    const Shape &sh = ctx->sh;
+    const bool real = host_weights_real(a, b, w, sh);
+    if (ctx->arith_opt == NQES_ARITH_REAL && !real) {
+        ctx->err = "weights have non-zero imaginary parts but arithmetic is forced REAL";
+        return NQES_ERR_INVALID;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    NQES_CUDA(cudaMemcpyAsync(ctx->a, a, sizeof(cplx) * sh.K * sh.N, cudaMemcpyHostToDevice, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->b, b, sizeof(cplx) * sh.K * sh.M, cudaMemcpyHostToDevice, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->w, w, sizeof(cplx) * sh.K * sh.N * sh.M, cudaMemcpyHostToDevice, ctx->st));
+    NQES_CUDA(cudaStreamSynchronize(ctx->st));
+    ctx->weights_real = real;
+    return NQES_OK;
+}
+
+int nqes_get_weights(nqes_ctx *ctx, double *a, double *b, double *w) {
+    if (!ctx || !a || !b || !w) return NQES_ERR_INVALID;
+    const Shape &sh = ctx->sh;
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    NQES_CUDA(cudaMemcpyAsync(a, ctx->a, sizeof(cplx) * sh.K * sh.N, cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(b, ctx->b, sizeof(cplx) * sh.K * sh.M, cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(w, ctx->w, sizeof(cplx) * sh.K * sh.N * sh.M, cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaStreamSynchronize(ctx->st));
+    return NQES_OK;
+}
+
+int nqes_init_weights(nqes_ctx *ctx, uint64_t seed) {
+    if (!ctx) return NQES_ERR_INVALID;
+    // pcg64 as a UniformRandomBitGenerator for libstdc++'s normal_distribution.
+    struct Urbg {
+        using result_type = uint64_t;
+        Pcg64 g;
+        static constexpr uint64_t min() { return 0; }
+        static constexpr uint64_t max() { return ~uint64_t(0); }
+        uint64_t operator()() { return pcg_next(g); }
+    } rg{pcg_seed(seed - 1)};
+    const Shape &sh = ctx->sh;
+    std::normal_distribution<double> nd;
+    std::vector<double> a(2 * sh.K * sh.N), b(2 * sh.K * sh.M), w(2 * size_t(sh.K) * sh.N * sh.M);
+    auto draw = [&](double *dst, double scale) {
+        const double re = nd(rg), im = nd(rg);  // braced-init order of code/rbm.cc:248
+        dst[0] = re / scale;
+        dst[1] = im / scale;
+    };
+    for (int k = 0; k < sh.K; k++) {
+        for (int i = 0; i < sh.N; i++) draw(&a[2 * (k * sh.N + i)], std::sqrt(double(sh.N)));
+        for (int j = 0; j < sh.M; j++) draw(&b[2 * (k * sh.M + j)], std::sqrt(double(sh.M)));
+        for (int i = 0; i < sh.N; i++)
+            for (int j = 0; j < sh.M; j++)
+                draw(&w[2 * ((size_t(k) * sh.N + i) * sh.M + j)], std::sqrt(double(sh.N * sh.M)));
+    }
+    return nqes_set_weights(ctx, a.data(), b.data(), w.data());
+}
+
+int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, double lr, double reglam, double rtol,
+                 uint64_t maxit, double *e_mat, nqes_step_info *info) {
+    if (!ctx) return NQES_ERR_INVALID;
+    if (chains < 1 || m < 1 || burn < 0 || !std::isfinite(lr) || !std::isfinite(reglam) || !(rtol >= 0)) {
+        ctx->err = "invalid SR step arguments (chains >= 1, m >= 1, burn_in >= 0, finite lr/reglam, rtol >= 0)";
+        return NQES_ERR_INVALID;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const int arith = resolve_arith(ctx);
+    int rc = ensure_step_buffers(ctx, chains, m, arith);
+    if (rc) return rc;
+    StepParams &p = *ctx->sp_host;
+    p.seed = seed;
+    p.lr = lr;
+    p.reglam = reglam;
+    p.rtol = rtol;
+    p.maxit = std::min<uint64_t>(maxit, ctx->minres_cap);
+    rc = arith == NQES_ARITH_COMPLEX ? sr_step_t<cplx>(ctx, chains, m, burn) : sr_step_t<double>(ctx, chains, m, burn);
+    if (rc) return rc;
+    NQES_CUDA(cudaMemcpyAsync(ctx->emat_host, ctx->emat_d, sizeof(cplx) * ctx->sh.K * ctx->sh.K,
+                              cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->emat_host + 16, ctx->eloc_d, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->qs_host, ctx->qs, sizeof(QlpState), cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->err_host, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    NQES_CUDA(cudaStreamSynchronize(ctx->st));
+    ctx->have_step = true;
+    ctx->last_burn = burn;
+    if (e_mat) std::memcpy(e_mat, ctx->emat_host, sizeof(cplx) * ctx->sh.K * ctx->sh.K);
+    const QlpState &q = *ctx->qs_host;
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->minres_flag = q.flag;
+        info->arith = arith;
+        info->minres_iters = q.iters;
+        info->qlp_iters = q.qlp_iters;
+        info->relres = q.relres;
+        info->anorm = q.anorm;
+        info->acond = q.acond;
+        info->xnorm = q.xnorm;
+        info->proposals = uint64_t(chains) * (burn + m) * ctx->sh.K * ctx->sh.N;
+        info->eloc_re = ctx->emat_host[16].re;
+        info->eloc_im = ctx->emat_host[16].im;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        info->ms_total = ms;
+        std::vector<unsigned long long> acc(chains);
+        NQES_CUDA(cudaMemcpy(acc.data(), ctx->accepted, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
+        for (auto x : acc) info->accepted += x;
+        if (q.flag == 8 && q.iters >= ctx->minres_cap && maxit > ctx->minres_cap) info->warnings |= 1;
+        // tables, sampler, 3 moment kernels, 3 MINRES-QLP init kernels, update,
+        // and 6 kernels per execution of the loop body
+        info->kernel_launches = 9 + 6 * q.bodies;
+    }
+    const int e = *ctx->err_host;
+    if (e & (kErrNonFinite | kErrMinresNonFinite)) {
+        ctx->err = "non-finite value during the SR step (error bits " + std::to_string(e) + ")";
+        return NQES_ERR_NONFINITE;
+    }
+    if (e & kErrSingular) {
+        ctx->err = "a sample was taken at a singular Phi";
+        return NQES_ERR_NONFINITE;
+    }
+    return NQES_OK;
+}
+
+int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi, double *tanh_theta, double *E,
+                  double *O) {
+    if (!ctx || !configs || count < 1) return NQES_ERR_INVALID;
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const Shape &sh = ctx->sh;
+    const int arith = resolve_arith(ctx);
+    const size_t KK = size_t(sh.K) * sh.K, ss = ssize(arith), words = size_t(count) * sh.K * sh.NW;
+    uint64_t *cfg = nullptr, *sp = nullptr;
+    cplx *dphi = nullptr, *dth = nullptr, *dE = nullptr;
+    unsigned char *dO = nullptr;
+    int rc;
+    if ((rc = dalloc(ctx, &cfg, words)) || (rc = dalloc(ctx, &sp, words)) || (rc = dalloc(ctx, &dphi, count * KK)) ||
+        (rc = dalloc(ctx, &dth, count * KK * sh.M)) || (rc = dalloc(ctx, &dE, count * KK)) ||
+        (rc = dalloc(ctx, &dO, size_t(count) * sh.P * ss))) {
+        dfree(cfg); dfree(sp); dfree(dphi); dfree(dth); dfree(dE); dfree(dO);
+        return rc;
+    }
+    int status = NQES_OK;
+    auto run = [&]() -> int {
+        NQES_CUDA(cudaMemcpy(cfg, configs, words * 8, cudaMemcpyHostToDevice));
+        NQES_CUDA(cudaMemset(ctx->err_d, 0, sizeof(int)));
+        const int tk = choose_tk(ctx, count);
+        if (arith == NQES_ARITH_COMPLEX) {
+            NQES_CUDA(prepare_sample<cplx>(sh));
+            NQES_CUDA(launch_tables_ctx<cplx>(ctx));
+            SampleArgs<cplx> A = sample_args<cplx>(ctx, count, 1, 0, tk);
+            A.O = reinterpret_cast<cplx *>(dO);
+            A.E = dE;
+            A.spins = sp;
+            A.cfg = cfg;
+            A.phi_out = dphi;
+            A.tanh_out = dth;
+            NQES_CUDA(launch_sample<cplx>(A, sh.K * tk, ctx->st));
+        } else {
+            NQES_CUDA(prepare_sample<double>(sh));
+            NQES_CUDA(launch_tables_ctx<double>(ctx));
+            SampleArgs<double> A = sample_args<double>(ctx, count, 1, 0, tk);
+            A.O = reinterpret_cast<double *>(dO);
+            A.E = dE;
+            A.spins = sp;
+            A.cfg = cfg;
+            A.phi_out = dphi;
+            A.tanh_out = dth;
+            NQES_CUDA(launch_sample<double>(A, sh.K * tk, ctx->st));
+        }
+        NQES_CUDA(cudaStreamSynchronize(ctx->st));
+        if (phi) NQES_CUDA(cudaMemcpy(phi, dphi, count * KK * sizeof(cplx), cudaMemcpyDeviceToHost));
+        if (tanh_theta) NQES_CUDA(cudaMemcpy(tanh_theta, dth, count * KK * sh.M * sizeof(cplx), cudaMemcpyDeviceToHost));
+        if (E) NQES_CUDA(cudaMemcpy(E, dE, count * KK * sizeof(cplx), cudaMemcpyDeviceToHost));
+        if (O) {
+            const int saved = ctx->arith;
+            ctx->arith = arith;
+            int r = copy_out_c(ctx, dO, size_t(count) * sh.P, O);
+            ctx->arith = saved;
+            if (r) return r;
+        }
+        int e = 0;
+        NQES_CUDA(cudaMemcpy(&e, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) {
+            ctx->err = "evaluation flagged error bits " + std::to_string(e);
+            return NQES_ERR_NONFINITE;
+        }
+        return NQES_OK;
+    };
+    status = run();
+    dfree(cfg); dfree(sp); dfree(dphi); dfree(dth); dfree(dE); dfree(dO);
+    return status;
+}
+
+int nqes_get_samples(nqes_ctx *ctx, uint64_t *configs, double *eloc, double *E) {
+    if (!ctx) return NQES_ERR_INVALID;
+    if (!ctx->have_step) {
+        ctx->err = "no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const size_t KK = size_t(ctx->sh.K) * ctx->sh.K;
+    if (configs)
+        NQES_CUDA(cudaMemcpy(configs, ctx->spins, ctx->Ns * ctx->sh.K * ctx->sh.NW * 8, cudaMemcpyDeviceToHost));
+    if (eloc || E) {
+        std::vector<cplx> e(ctx->Ns * KK);
+        NQES_CUDA(cudaMemcpy(e.data(), ctx->E, e.size() * sizeof(cplx), cudaMemcpyDeviceToHost));
+        if (E) std::memcpy(E, e.data(), e.size() * sizeof(cplx));
+        if (eloc)
+            for (size_t s = 0; s < ctx->Ns; s++) {
+                cplx t{0, 0};
+                for (int k = 0; k < ctx->sh.K; k++) t += e[s * KK + k * ctx->sh.K + k];
+                eloc[2 * s] = t.re;
+                eloc[2 * s + 1] = t.im;
+            }
+    }
+    return NQES_OK;
+}
+
+int nqes_get_accepts(nqes_ctx *ctx, uint64_t *accepted) {
+    if (!ctx || !accepted) return NQES_ERR_INVALID;
+    if (!ctx->have_step) {
+        ctx->err = "no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaMemcpy(accepted, ctx->accepted, sizeof(uint64_t) * ctx->chains, cudaMemcpyDeviceToHost));
+    return NQES_OK;
+}
+
+int nqes_get_O(nqes_ctx *ctx, int first, int count, double *O) {
+    if (!ctx || !O || first < 0 || count < 1) return NQES_ERR_INVALID;
+    if (!ctx->have_step || size_t(first) + count > ctx->Ns) {
+        ctx->err = "rows out of range or no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const size_t P = ctx->sh.P;
+    const unsigned char *src = static_cast<const unsigned char *>(ctx->O) + size_t(first) * P * ssize(ctx->arith);
+    return copy_out_c(ctx, src, size_t(count) * P, O);
+}
+
+int nqes_get_moments(nqes_ctx *ctx, double *o, double *skk, double *f) {
+    if (!ctx) return NQES_ERR_INVALID;
+    if (!ctx->have_step) {
+        ctx->err = "no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const size_t P = ctx->sh.P, ss = ssize(ctx->arith);
+    const unsigned char *v = static_cast<const unsigned char *>(ctx->vecs);
+    int rc;
+    if (o && (rc = copy_out_c(ctx, v + 0 * P * ss, P, o))) return rc;
+    if (skk && (rc = copy_out_c(ctx, v + 1 * P * ss, P, skk))) return rc;
+    if (f && (rc = copy_out_c(ctx, v + 2 * P * ss, P, f))) return rc;
+    return NQES_OK;
+}
+
+int nqes_get_solution(nqes_ctx *ctx, double *x) {
+    if (!ctx || !x) return NQES_ERR_INVALID;
+    if (!ctx->have_step) {
+        ctx->err = "no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const size_t P = ctx->sh.P, ss = ssize(ctx->arith);
+    return copy_out_c(ctx, static_cast<const unsigned char *>(ctx->vecs) + 11 * P * ss, P, x);
+}
+
+int nqes_apply_S(nqes_ctx *ctx, const double *v, double *out) {
+    if (!ctx || !v || !out) return NQES_ERR_INVALID;
+    if (!ctx->have_step) {
+        ctx->err = "no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const size_t P = ctx->sh.P, ss = ssize(ctx->arith);
+    unsigned char *dv = nullptr, *dout = nullptr;
+    int rc;
+    if ((rc = dalloc(ctx, &dv, P * ss)) || (rc = dalloc(ctx, &dout, P * ss))) {
+        dfree(dv);
+        return rc;
+    }
+    auto run = [&]() -> int {
+        if (ctx->arith == NQES_ARITH_COMPLEX) {
+            NQES_CUDA(cudaMemcpy(dv, v, P * sizeof(cplx), cudaMemcpyHostToDevice));
+            SolveBufs<cplx> B = solve_bufs<cplx>(ctx);
+            NQES_CUDA(launch_apply_S<cplx>(B, reinterpret_cast<cplx *>(dv), reinterpret_cast<cplx *>(dout), ctx->st));
+        } else {
+            std::vector<double> tmp(P);
+            for (size_t t = 0; t < P; t++) tmp[t] = v[2 * t];
+            NQES_CUDA(cudaMemcpy(dv, tmp.data(), P * sizeof(double), cudaMemcpyHostToDevice));
+            SolveBufs<double> B = solve_bufs<double>(ctx);
+            NQES_CUDA(launch_apply_S<double>(B, reinterpret_cast<double *>(dv), reinterpret_cast<double *>(dout),
+                                             ctx->st));
+        }
+        NQES_CUDA(cudaStreamSynchronize(ctx->st));
+        return copy_out_c(ctx, dout, P, out);
+    };
+    rc = run();
+    dfree(dv);
+    dfree(dout);
+    return rc;
+}
+
+}  // extern "C"
+
+namespace {
+template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double *bytes) {
+    SolveBufs<S> B = solve_bufs<S>(ctx);
+    const size_t Ns = ctx->Ns, P = ctx->sh.P, ss = sizeof(S), KK = size_t(ctx->sh.K) * ctx->sh.K;
+    auto launch = [&]() -> cudaError_t {
+        switch (kernel) {
+        case NQES_KERNEL_SAMPLE: {
+            SampleArgs<S> A = sample_args<S>(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
+            return launch_sample<S>(A, ctx->sh.K * ctx->last_tk, ctx->st);
+        }
+        case NQES_KERNEL_SV_ROWS: return launch_sv_rows_only<S>(B, ctx->st);
+        case NQES_KERNEL_SV_COLS: return launch_sv_cols_only<S>(B, ctx->st);
+        default: return launch_moment_part_only<S>(B, ctx->st);
+        }
+    };
+    switch (kernel) {
+    case NQES_KERNEL_SAMPLE: *bytes = double(Ns) * (P * ss + KK * sizeof(cplx) + ctx->sh.K * ctx->sh.NW * 8); break;
+    case NQES_KERNEL_SV_ROWS: *bytes = double(Ns) * P * ss + double(P) * ss + double(Ns) * ss; break;
+    case NQES_KERNEL_SV_COLS: *bytes = double(Ns) * P * ss + double(Ns) * ss + double(ctx->rchunks) * P * ss; break;
+    default: *bytes = double(Ns) * P * ss + double(Ns) * KK * sizeof(cplx) + 3.0 * ctx->rchunks * P * ss; break;
+    }
+    if (kernel == NQES_KERNEL_SAMPLE) NQES_CUDA(prepare_sample<S>(ctx->sh));
+    NQES_CUDA(launch());  // warm-up
+    NQES_CUDA(cudaStreamSynchronize(ctx->st));
+    NQES_CUDA(cudaEventRecord(ctx->ev0, ctx->st));
+    for (int r = 0; r < reps; r++) NQES_CUDA(launch());
+    NQES_CUDA(cudaEventRecord(ctx->ev1, ctx->st));
+    NQES_CUDA(cudaEventSynchronize(ctx->ev1));
+    float ms = 0;
+    NQES_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    *avg_ms = double(ms) / reps;
+    return NQES_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double *algorithmic_bytes) {
+    if (!ctx || !avg_ms || !algorithmic_bytes || reps < 1 || kernel < NQES_KERNEL_SAMPLE ||
+        kernel > NQES_KERNEL_MOMENTS)
+        return NQES_ERR_INVALID;
+    if (!ctx->have_step) {
+        ctx->err = "no SR step has run";
+        return NQES_ERR_STATE;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    return ctx->arith == NQES_ARITH_COMPLEX ? time_kernel_t<cplx>(ctx, kernel, reps, avg_ms, algorithmic_bytes)
+                                            : time_kernel_t<double>(ctx, kernel, reps, avg_ms, algorithmic_bytes);
+}
+
+int nqes_correlations(nqes_ctx *ctx, uint64_t, int, int, int, const double *, double *, double *, double *,
+                      double *) {
+    if (!ctx) return NQES_ERR_INVALID;
+    ctx->err = "correlations are not built yet";
+    return NQES_ERR_STATE;
+}
+
+}  // extern "C"

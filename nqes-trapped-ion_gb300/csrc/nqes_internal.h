@@ -1,0 +1,126 @@
+// Internal interfaces between the host orchestration (nqes_api.cu) and the
+// kernel translation units. Not part of the public C ABI.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "nqes_math.cuh"
+
+namespace nqes {
+
+// Per-SR-step scalars. Lives in device memory so that one captured CUDA graph
+// serves every step: the host rewrites it before each launch.
+struct StepParams {
+    uint64_t seed;      // chain c uses pcg64(seed + c)
+    double lr;          // learning rate for w -= lr * x
+    double reglam;      // lambda of S + lambda diag(S)
+    double rtol;        // MINRES-QLP relative tolerance
+    uint64_t maxit;     // MINRES-QLP iteration limit (already capped)
+};
+
+// Device tables derived from the weights at the start of every SR step.
+// Layouts: ch/sh [kk][i][j] = cosh(2 w), sinh(2 w); eup/edn [kk][i] =
+// exp(-2 a) (flip of an up spin) and exp(+2 a) (flip of a down spin).
+template <class S> struct Tables {
+    const S *ch, *sh, *eup, *edn;
+};
+
+struct Shape {
+    int N, M, K, L, P, NW;
+};
+
+template <class S> struct SampleArgs {
+    Shape sh;
+    int chains, m, burn;
+    int tk;                     // threads per RBM column block (multiple of 32)
+    const StepParams *sp;
+    Tables<S> tab;
+    const cplx *a, *b, *w;      // weights, reference layout
+    const double *J;            // N×N row-major
+    double h;
+    S *O;                       // Ns × P log-derivatives (row s = c*m + t)
+    cplx *E;                    // Ns × K² local-energy matrices
+    uint64_t *spins;            // Ns × K × NW configurations
+    unsigned long long *accepted;  // per chain
+    int *err;                   // error bits (see kErr*)
+    // Evaluation mode (configs given, no sampling): when cfg != nullptr the
+    // kernel evaluates Phi / tanh(theta) / E / O at cfg[c] for c < chains.
+    const uint64_t *cfg;
+    cplx *phi_out, *tanh_out;   // chains × K², chains × M × K² (optional)
+};
+
+enum : int {
+    kErrNonFinite = 1,      // a non-finite amplitude ratio, energy or derivative
+    kErrSingular = 2,       // a sample was taken at a singular Phi
+    kErrMinresNonFinite = 4,
+    kErrMinresCap = 8,      // MINRES-QLP stopped at the device-side iteration cap
+};
+
+size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith);
+template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st);
+template <class S> cudaError_t launch_tables(const Shape &sh, const cplx *a, const cplx *w, S *ch, S *shh, S *eup,
+                                             S *edn, cudaStream_t st);
+
+// ---- moments, S·v, MINRES-QLP ----
+
+// Device-resident MINRES-QLP scalar state (double-buffered by the host
+// schedule; see kernels_solve.cu).
+struct QlpState {
+    // recurrence scalars (code/minresqlp.h:128-138 names)
+    double beta, tau, taul, phi, betan, gmin, gminl;
+    double cs, sn, cr1, sr1, cr2, sr2, dltan, eplnn;
+    double gama, gamal, gamal2, eta, etal, etal2;
+    double vepln, veplnl, veplnl2, ul3, ul2, ul, u;
+    double gama_qlp, gamal_qlp, vepln_qlp, u_qlp, ul_qlp;
+    double rnorm, xnorm, xl2norm, axnorm, anorm, acond, relres, beta1;
+    // per-iteration values consumed by the vector kernel
+    double alfa, epln, dlta_qlp, gama_tmp, gamal3, veplnl2_v, etal_v;
+    double w_gamal_qlp, w_vepln_qlp, w_gama_qlp, w_ul_qlp, w_u_qlp;
+    double cr2_v, sr2_v;   // P_{k-2,k} rotation as of the vector update
+    unsigned long long iters, qlp_iters, cap, iters_snapshot;
+    unsigned long long bodies;  // executions of the loop body (for launch counts)
+    int flag;
+    int mode;         // 0: no update, 1: MINRES update, 2: QLP update, 3: x = b/alfa
+    int qlp_first;    // QLP update is the first one (rebuild w's)
+    int running;
+};
+
+// Reduction partial buffers: one slot per 256-element vector block. P <= 4 *
+// (128 + 512 + 128*512) gives at most 1034 blocks; three regions of this
+// stride live in SolveBufs::part (alfa, |r3|^2, |b|^2) and one in ovpart.
+constexpr int kPartStride = 2048;
+
+template <class S> cudaError_t prepare_sample(const Shape &sh);
+
+template <class S> struct SolveBufs {
+    Shape sh;
+    int Ns;
+    const S *O;
+    const cplx *E;       // per-sample E matrices (for eloc and e_mat)
+    S *o, *skk, *f;      // moments (P)
+    S *u;                // Ns: O v
+    S *ypart;            // rchunks × P partial O^H u
+    int rchunks;
+    S *r1, *r2, *r3, *v, *vn, *w, *wl, *wl2, *x, *xl2;
+    double *part;        // reduction partials (>= 2 * 1024)
+    S *ovpart;           // partial o·v
+    QlpState *qs;
+    const StepParams *sp;
+    cplx *emat;          // K² mean E (unnormalised by N)
+    cplx *eloc;          // mean trace
+    int *err;
+    cudaGraphConditionalHandle cond;
+    int use_cond;
+};
+
+template <class S> cudaError_t launch_moments(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &b, const S *v, S *out, cudaStream_t st);
+template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_update(const Shape &sh, const StepParams *sp, const S *x, cplx *a, cplx *b,
+                                             cplx *w, cudaStream_t st);
+
+}  // namespace nqes

@@ -1,0 +1,207 @@
+// Scalar arithmetic shared by every kernel of the library.
+//
+// Kernels are written once over a scalar type S that is either `double`
+// (real arithmetic: all weights, J and h real, so every amplitude, ratio,
+// local energy and log-derivative is real) or `cplx` (complex arithmetic, the
+// general case of code/rbm.cc:25-26). With real inputs the complex algebra of
+// the reference stays exactly real, so the real instantiation computes the
+// same quantities with a quarter of the FP64 work.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace nqes {
+
+struct __align__(16) cplx {
+    double re, im;
+};
+
+__host__ __device__ __forceinline__ cplx mk(double r, double i) { return cplx{r, i}; }
+__host__ __device__ __forceinline__ cplx operator+(cplx a, cplx b) { return {a.re + b.re, a.im + b.im}; }
+__host__ __device__ __forceinline__ cplx operator-(cplx a, cplx b) { return {a.re - b.re, a.im - b.im}; }
+__host__ __device__ __forceinline__ cplx operator-(cplx a) { return {-a.re, -a.im}; }
+__host__ __device__ __forceinline__ cplx operator*(cplx a, cplx b) {
+    return {fma(a.re, b.re, -a.im * b.im), fma(a.re, b.im, a.im * b.re)};
+}
+__host__ __device__ __forceinline__ cplx operator*(cplx a, double s) { return {a.re * s, a.im * s}; }
+__host__ __device__ __forceinline__ cplx operator*(double s, cplx a) { return {a.re * s, a.im * s}; }
+__host__ __device__ __forceinline__ cplx operator/(cplx a, double s) { return {a.re / s, a.im / s}; }
+__host__ __device__ __forceinline__ cplx &operator+=(cplx &a, cplx b) { a = a + b; return a; }
+__host__ __device__ __forceinline__ cplx &operator-=(cplx &a, cplx b) { a = a - b; return a; }
+__host__ __device__ __forceinline__ cplx &operator*=(cplx &a, cplx b) { a = a * b; return a; }
+__host__ __device__ __forceinline__ bool operator==(cplx a, cplx b) { return a.re == b.re && a.im == b.im; }
+
+// Scalar-type traits: one name per operation for both real and complex S.
+__host__ __device__ __forceinline__ double re(double x) { return x; }
+__host__ __device__ __forceinline__ double re(cplx x) { return x.re; }
+__host__ __device__ __forceinline__ double im(double) { return 0.0; }
+__host__ __device__ __forceinline__ double im(cplx x) { return x.im; }
+__host__ __device__ __forceinline__ double conj(double x) { return x; }
+__host__ __device__ __forceinline__ cplx conj(cplx x) { return {x.re, -x.im}; }
+__host__ __device__ __forceinline__ double norm2(double x) { return x * x; }
+__host__ __device__ __forceinline__ double norm2(cplx x) { return fma(x.re, x.re, x.im * x.im); }
+template <class S> __host__ __device__ __forceinline__ S one();
+template <> __host__ __device__ __forceinline__ double one<double>() { return 1.0; }
+template <> __host__ __device__ __forceinline__ cplx one<cplx>() { return {1.0, 0.0}; }
+template <class S> __host__ __device__ __forceinline__ S zero();
+template <> __host__ __device__ __forceinline__ double zero<double>() { return 0.0; }
+template <> __host__ __device__ __forceinline__ cplx zero<cplx>() { return {0.0, 0.0}; }
+template <class S> __host__ __device__ __forceinline__ S from_c(cplx z);
+template <> __host__ __device__ __forceinline__ double from_c<double>(cplx z) { return z.re; }
+template <> __host__ __device__ __forceinline__ cplx from_c<cplx>(cplx z) { return z; }
+__host__ __device__ __forceinline__ cplx to_c(double x) { return {x, 0.0}; }
+__host__ __device__ __forceinline__ cplx to_c(cplx x) { return x; }
+// a*b + c
+__host__ __device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+__host__ __device__ __forceinline__ cplx mad(cplx a, cplx b, cplx c) {
+    return {fma(a.re, b.re, fma(-a.im, b.im, c.re)), fma(a.re, b.im, fma(a.im, b.re, c.im))};
+}
+// conj(a)*b + c
+__host__ __device__ __forceinline__ double cmad(double a, double b, double c) { return fma(a, b, c); }
+__host__ __device__ __forceinline__ cplx cmad(cplx a, cplx b, cplx c) {
+    return {fma(a.re, b.re, fma(a.im, b.im, c.re)), fma(a.re, b.im, fma(-a.im, b.re, c.im))};
+}
+__host__ __device__ __forceinline__ double inv(double x) { return 1.0 / x; }
+__host__ __device__ __forceinline__ cplx inv(cplx x) {
+    double d = 1.0 / fma(x.re, x.re, x.im * x.im);
+    return {x.re * d, -x.im * d};
+}
+__host__ __device__ __forceinline__ bool finite(double x) { return isfinite(x); }
+__host__ __device__ __forceinline__ bool finite(cplx x) { return isfinite(x.re) && isfinite(x.im); }
+__host__ __device__ __forceinline__ bool is_zero(double x) { return x == 0.0; }
+__host__ __device__ __forceinline__ bool is_zero(cplx x) { return x.re == 0.0 && x.im == 0.0; }
+
+// Elementary functions.
+__device__ __forceinline__ double cexp_(double x) { return exp(x); }
+__device__ __forceinline__ cplx cexp_(cplx z) {
+    double e = exp(z.re), s, c;
+    sincos(z.im, &s, &c);
+    return {e * c, e * s};
+}
+__device__ __forceinline__ double ccosh_(double x) { return cosh(x); }
+__device__ __forceinline__ cplx ccosh_(cplx z) {
+    double s, c;
+    sincos(z.im, &s, &c);
+    return {cosh(z.re) * c, sinh(z.re) * s};
+}
+__device__ __forceinline__ double csinh_(double x) { return sinh(x); }
+__device__ __forceinline__ cplx csinh_(cplx z) {
+    double s, c;
+    sincos(z.im, &s, &c);
+    return {sinh(z.re) * c, cosh(z.re) * s};
+}
+__device__ __forceinline__ double ctanh_(double x) { return tanh(x); }
+// tanh(x+iy) = (sinh 2x + i sin 2y) / (cosh 2x + cos 2y), with the large-|x|
+// limit taken explicitly so that no inf/inf arises.
+__device__ __forceinline__ cplx ctanh_(cplx z) {
+    if (fabs(z.re) > 20.0) {
+        double s, c;
+        sincos(2.0 * z.im, &s, &c);
+        double e = exp(-2.0 * fabs(z.re));
+        return {copysign(1.0, z.re), 2.0 * s * e};
+    }
+    double s, c;
+    sincos(2.0 * z.im, &s, &c);
+    double d = cosh(2.0 * z.re) + c;
+    return {sinh(2.0 * z.re) / d, s / d};
+}
+
+// Exact power-of-two scaling (used to keep rows of Phi in range without
+// changing any ratio): x * 2^e for real and complex.
+__device__ __forceinline__ double scale2(double x, int e) { return ldexp(x, e); }
+__device__ __forceinline__ cplx scale2(cplx x, int e) { return {ldexp(x.re, e), ldexp(x.im, e)}; }
+// Binary exponent of the larger component (0 for zero), from the bit pattern.
+__device__ __forceinline__ int expo(double x) {
+    int hi = __double2hiint(x);
+    int e = (hi >> 20) & 0x7ff;
+    return e == 0 ? -1023 : e - 1023;
+}
+__device__ __forceinline__ int expo(cplx x) { return max(expo(x.re), expo(x.im)); }
+
+// Warp-level reductions.
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ cplx shfl_xor(cplx v, int m) {
+    return {__shfl_xor_sync(0xffffffffu, v.re, m), __shfl_xor_sync(0xffffffffu, v.im, m)};
+}
+template <class S> __device__ __forceinline__ S warp_sum(S v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v = v + shfl_xor(v, m);
+    return v;
+}
+template <class S> __device__ __forceinline__ S warp_prod(S v) {
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) v = v * shfl_xor(v, m);
+    return v;
+}
+
+// Small K×K (K <= 4) row-major matrix helpers, run by one thread.
+template <class S> __host__ __device__ inline S small_det(const S *m, int K) {
+    if (K == 1) return m[0];
+    if (K == 2) return m[0] * m[3] - m[2] * m[1];
+    if (K == 3) {
+        auto h3 = [&](int a, int b, int c) {
+            return m[a * 3] * (m[b * 3 + 1] * m[c * 3 + 2] - m[b * 3 + 2] * m[c * 3 + 1]);
+        };
+        return h3(0, 1, 2) - h3(1, 0, 2) + h3(2, 0, 1);
+    }
+    // K == 4: Laplace expansion along the first column.
+    S d = zero<S>();
+    for (int r = 0; r < 4; r++) {
+        int rr[3], t = 0;
+        for (int q = 0; q < 4; q++)
+            if (q != r) rr[t++] = q;
+        auto e = [&](int a, int c) { return m[rr[a] * 4 + c]; };
+        S minor = e(0, 1) * (e(1, 2) * e(2, 3) - e(1, 3) * e(2, 2)) - e(1, 1) * (e(0, 2) * e(2, 3) - e(0, 3) * e(2, 2)) +
+                  e(2, 1) * (e(0, 2) * e(1, 3) - e(0, 3) * e(1, 2));
+        S term = m[r * 4] * minor;
+        d = (r & 1) ? d - term : d + term;
+    }
+    return d;
+}
+
+// Inverse by Gauss-Jordan with partial pivoting; false when singular.
+template <class S> __host__ __device__ inline bool small_inv(const S *m, S *out, int K) {
+    S a[16];
+    for (int t = 0; t < K * K; t++) {
+        a[t] = m[t];
+        out[t] = zero<S>();
+    }
+    for (int t = 0; t < K; t++) out[t * K + t] = one<S>();
+    for (int c = 0; c < K; c++) {
+        int p = c;
+        double best = norm2(a[c * K + c]);
+        for (int r = c + 1; r < K; r++) {
+            double v = norm2(a[r * K + c]);
+            if (v > best) {
+                best = v;
+                p = r;
+            }
+        }
+        if (best == 0.0) return false;
+        if (p != c)
+            for (int j = 0; j < K; j++) {
+                S t1 = a[p * K + j];
+                a[p * K + j] = a[c * K + j];
+                a[c * K + j] = t1;
+                S t2 = out[p * K + j];
+                out[p * K + j] = out[c * K + j];
+                out[c * K + j] = t2;
+            }
+        S piv = inv(a[c * K + c]);
+        for (int j = 0; j < K; j++) {
+            a[c * K + j] = a[c * K + j] * piv;
+            out[c * K + j] = out[c * K + j] * piv;
+        }
+        for (int r = 0; r < K; r++) {
+            if (r == c) continue;
+            S f = a[r * K + c];
+            for (int j = 0; j < K; j++) {
+                a[r * K + j] = a[r * K + j] - f * a[c * K + j];
+                out[r * K + j] = out[r * K + j] - f * out[c * K + j];
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace nqes

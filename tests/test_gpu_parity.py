@@ -1,0 +1,168 @@
+"""GPU parity of libnqes against the CPU oracle (restatement of code/rbm.cc).
+
+Tolerances (FP64): amplitudes, tanh(theta), local energies, log-derivatives,
+moments and S·v agree to 1e-11 relative (the oracle multiplies factors in the
+reference's sequential order, the GPU in a tree; both are FP64). Random
+draws, start configurations and every sampled spin configuration are
+bit-exact, and so are per-chain accept counts. MINRES-QLP solutions agree to
+the solver tolerance scale (1e-7 relative at rtol 1e-9)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import helpers
+from helpers import GOLDEN, Oracle, cfg_words, cplx_arr, synthetic_j
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    ge._load_build_module().build_library()
+    return ge.load_package()
+
+
+def rel_err(a, b):
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def make_pair(pkg, N, M, K, h, scale, seed, real):
+    J = synthetic_j(N)
+    a, b, w = helpers.random_weights(N, M, K, scale, seed, real=real)
+    ctx = pkg.Context(N, M, K, J, h)
+    ctx.set_weights(a, b, w)
+    orc = Oracle(N, M, K, J, h)
+    orc.set_weights(a, b, w)
+    return ctx, orc
+
+
+def test_evaluate_matches_definitions_and_oracle(pkg):
+    with open(os.path.join(GOLDEN, "physics_golden.json")) as f:
+        phys = json.load(f)
+    for case in phys["cases"]:
+        N, M, K = case["N"], case["M"], case["K"]
+        J = np.array(case["J"]).reshape(N, N)
+        ctx = pkg.Context(N, M, K, J, case["h"])
+        ctx.set_weights(cplx_arr(case["a"]).reshape(K, N), cplx_arr(case["b"]).reshape(K, M),
+                        cplx_arr(case["w"]).reshape(K, N, M))
+        cfgs = np.stack([cfg_words(c["cfg"], N) for c in case["configs"]])
+        phi, th, E, O = ctx.evaluate(cfgs)
+        orc = Oracle(N, M, K, J, case["h"])
+        orc.set_weights(*ctx.get_weights())
+        for t, c in enumerate(case["configs"]):
+            assert rel_err(phi[t], cplx_arr(c["phi"]).reshape(K, K)) < 1e-11
+            assert rel_err(E[t], cplx_arr(c["E"]).reshape(K, K)) < 1e-10
+            assert rel_err(O[t][::c["O_stride"]], cplx_arr(c["O"])) < 1e-10
+            ophi, oth = orc.state(cfgs[t])
+            assert rel_err(th[t], oth) < 1e-11
+            oE, oO = orc.local(cfgs[t])
+            assert rel_err(E[t], oE) < 1e-11
+            assert rel_err(O[t], oO) < 1e-11
+        ctx.close()
+
+
+@pytest.mark.parametrize("N,M,K,real", [(6, 12, 2, False), (8, 16, 2, True), (5, 10, 1, False), (4, 8, 3, False),
+                                        (8, 16, 4, True), (66, 66, 2, True)])
+def test_sr_step_parity(pkg, N, M, K, real):
+    # Shapes keep 2^N well above K: when two rows of a chain land on the same
+    # configuration through different flip histories, det Phi is rounding
+    # noise and the reference's accept decisions depend on the last bit of its
+    # own arithmetic, which no independent implementation reproduces.
+    ctx, orc = make_pair(pkg, N, M, K, 0.595, 0.1 if N < 20 else 0.02, 7 + N + K, real)
+    chains, m, burn = 6, 12, 5
+    if N > 20:
+        chains, m, burn = 3, 4, 2
+    args = (9000 + N, chains, m, burn, 0.1, 2.0, 1e-9, 1000)
+    e_g, info = ctx.sr_step(*args)
+    e_o, oinfo = orc.sr_step(*args)
+    ns = chains * m
+    sg, elg, Eg = ctx.get_samples()
+    so, elo, Eo = orc.samples(ns)
+    assert np.array_equal(sg, so), "sampled configurations differ"
+    assert info["accepted"] == oinfo["accepted"]
+    assert rel_err(Eg, Eo) < 1e-11
+    assert rel_err(e_g, e_o) < 1e-11
+    og, sk_g, fg = ctx.get_moments()
+    oo, sk_o, fo = orc.moments()
+    assert rel_err(og, oo) < 1e-11
+    assert rel_err(sk_g, sk_o) < 1e-10
+    assert rel_err(fg, fo) < 1e-10
+    # O rows (stored by the GPU) against the oracle's determinant form
+    for s in [0, ns // 2, ns - 1]:
+        assert rel_err(ctx.get_O(s, 1)[0], orc.sample_deriv(s)) < 1e-11
+    # S·v on a random vector
+    rng = np.random.default_rng(1)
+    v = rng.normal(size=ctx.P) + (0 if real else 1j) * rng.normal(size=ctx.P)
+    assert rel_err(ctx.apply_S(v), orc.apply_S(v)) < 1e-11
+    # Solver: both stop on the reference's criteria; the GPU solution meets the
+    # MINRES-QLP relative-residual bound when checked with the oracle's S.
+    assert info["minres_flag"] == int(oinfo["flag"])
+    it_g, it_o = int(info["minres_iters"]), int(oinfo["iters"])
+    assert abs(it_g - it_o) <= max(2, it_o // 10), (it_g, it_o)
+    x = ctx.get_solution()
+    r = np.linalg.norm(orc.apply_S(x) - fo)
+    assert r <= 10 * 1e-9 * (info["anorm"] * np.linalg.norm(x) + np.linalg.norm(fo)), r
+    ag, bg, wg = ctx.get_weights()
+    ao, bo, wo = orc.get_weights()
+    assert rel_err(np.concatenate([ag.ravel(), bg.ravel(), wg.ravel()]),
+                   np.concatenate([ao.ravel(), bo.ravel(), wo.ravel()])) < 1e-4
+    ctx.close()
+
+
+def test_consecutive_steps_and_reproducibility(pkg):
+    """Three SR steps reuse one CUDA graph; a second context reproduces them bit for bit."""
+    N, M, K = 8, 16, 2
+    outs = []
+    for rep in range(2):
+        ctx, orc = make_pair(pkg, N, M, K, 0.595, 0.05, 3, True)
+        es = []
+        for it in range(3):
+            e, info = ctx.sr_step(100 + it * 16, 16, 20, 8, 0.1, 5.0 * 0.9 ** it, 1e-9, 2000)
+            es.append(e)
+            if rep == 0:
+                eo, _ = orc.sr_step(100 + it * 16, 16, 20, 8, 0.1, 5.0 * 0.9 ** it, 1e-9, 2000)
+                assert rel_err(e, eo) < 1e-7  # weights differ at the rtol scale after step 1
+        outs.append((np.array(es), ctx.get_weights()))
+        ctx.close()
+    assert np.array_equal(outs[0][0], outs[1][0])
+    for x, y in zip(outs[0][1], outs[1][1]):
+        assert np.array_equal(x, y)
+
+
+def test_nonfinite_weights_report_error(pkg):
+    N, M, K = 4, 8, 2
+    ctx = pkg.Context(N, M, K, synthetic_j(N), 1.0)
+    a, b, w = helpers.random_weights(N, M, K, 0.1, 1, real=True)
+    w[0, 0, 0] = np.nan
+    ctx.set_weights(a, b, w)
+    with pytest.raises(pkg.NqesError) as e:
+        ctx.sr_step(1, 4, 4, 2, 0.1, 1.0, 1e-9, 100)
+    assert e.value.status == pkg.ERR_NONFINITE
+    ctx.close()
+
+
+def test_training_reaches_exact_diagonalisation(pkg):
+    """N=8, K=2, h=1: SR training (lambda 40 -> 5, lr 0.1) brings the two lowest
+    energies per site to exact diagonalisation within the variational error of
+    an M=2N RBM (1% of |E|), averaged over the last 10 steps."""
+    with open(os.path.join(GOLDEN, "ed_golden.json")) as f:
+        ed = [c for c in json.load(f)["cases"] if c["N"] == 8 and c["h"] == 1.0][0]
+    want = np.array(ed["evals_per_site"][:2])
+    N, M, K = 8, 16, 2
+    ctx = pkg.Context(N, M, K, synthetic_j(N), ed["h"])
+    ctx.set_weights(*helpers.random_weights(N, M, K, 0.05, 11, real=True))
+    lr, reglam, hist = 0.1, 40.0, []
+    chains, m = 256, 200
+    for it in range(150):
+        e, info = ctx.sr_step(5000 + it * chains, chains, m, 32, max(lr, 0.01), max(reglam, 5.0), 1e-9, 5000)
+        lr *= 0.99
+        reglam *= 0.9
+        hist.append(np.sort(np.linalg.eigvals(e / N).real))
+    final = np.mean(hist[-10:], axis=0)
+    print("final", final, "ED", want)
+    assert np.all(final >= want - 2e-3), (final, want)          # variational (up to noise)
+    assert np.all(np.abs(final - want) < 0.01 * np.abs(want)), (final, want)
+    ctx.close()
