@@ -28,6 +28,7 @@ EXPORTS = [
     "nqes_create", "nqes_destroy", "nqes_last_error", "nqes_set_option", "nqes_set_weights", "nqes_get_weights",
     "nqes_init_weights", "nqes_sr_step", "nqes_correlations", "nqes_evaluate", "nqes_get_samples",
     "nqes_get_accepts", "nqes_get_O", "nqes_get_moments", "nqes_get_solution", "nqes_apply_S", "nqes_time_kernel",
+    "nqes_apply_S_static",
 ]
 KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
 
@@ -85,6 +86,7 @@ def load_library(path=None):
         "nqes_get_solution": (i, [vp, _dp]),
         "nqes_apply_S": (i, [vp, _dp, _dp]),
         "nqes_time_kernel": (i, [vp, i, i, _dp, _dp]),
+        "nqes_apply_S_static": (i, [vp, vp, vp, vp, vp, i64, i64, i, vp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)

@@ -62,6 +62,11 @@ struct nqes_ctx {
 
 static std::string g_create_error;
 
+// Error text for calls that have no context (reported by nqes_last_error(NULL)).
+namespace nqes {
+void set_global_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace nqes
+
 #define NQES_CUDA(call)                                                                                   \
     do {                                                                                                  \
         cudaError_t e_ = (call);                                                                          \
