@@ -5,21 +5,25 @@
 // monte_carlo_step (530-552), ising_like_hamiltonian + trapped_ion_model
 // (1011-1062) and deriv (199-239).
 //
-// Thread layout. A chain's CTA has T = K * TK threads (TK a multiple of 32):
-// column block kk (RBM kk) owns threads [kk*TK, (kk+1)*TK), and thread jl of
-// the block owns hidden units j = jl, jl + TK, ... of that RBM. For a proposal
-// (k, i) every thread forms its factors
+// Thread layout. A chain's CTA has K*TK "unit" threads (TK a multiple of 32)
+// and one "decision" warp. Column block kk (RBM kk) owns unit threads
+// [kk*TK, (kk+1)*TK); thread jl of the block owns hidden units j = jl,
+// jl + TK, ... of that RBM. For a proposal (k, i) every unit thread forms
 //     f_j = cosh(2 w_ij) - sigma_i tanh(theta_j^{(k,kk)}) sinh(2 w_ij)
 // (= cosh(theta_j - 2 sigma_i w_ij) / cosh(theta_j), the factor of
-// flip_state_fcn, code/rbm.cc:182-187) from per-step tables, and the block
-// multiplies them by warp shuffles and one shared-memory step. Warp 0 turns
-// the K products into the new row k of Phi, its determinant and the
-// Metropolis decision; on acceptance every thread updates its tanh(theta)
-// entries with the same factor it already holds.
+// flip_state_fcn, code/rbm.cc:182-187) from per-step tables, the block
+// multiplies them by warp shuffles, and each thread already computes the
+// updated tanh(theta_j) it would store if the flip is accepted
+// (code/rbm.cc:185). Meanwhile the decision warp turns the K products into the
+// new determinant by a Laplace expansion along row k,
+//     det Phi' = sum_kk r_kk * g_kk,   g_kk = Phi[k][kk] * cofactor(k, kk),
+// whose cofactors do not depend on row k and so are computed once per row and
+// sweep, and applies the reference's acceptance test (code/rbm.cc:541-543).
 //
 // On GB300 an FP64 warp instruction occupies the issuing warp for ~64 cycles
-// whether one lane or 32 are active, so the kernel keeps the per-proposal
-// FP64 instruction count per warp small rather than minimising lane work.
+// whether one lane or 32 are active, so the kernel keeps the FP64 instruction
+// count on the proposal's critical path (reduction, then decision) small and
+// moves the tanh update off it.
 //
 // Rows of Phi are kept scaled by exact powers of two. Every quantity the
 // reference derives from Phi (the ratio |det Phi'|^2/|det Phi|^2, Phi^-1 H Phi
@@ -32,8 +36,9 @@ namespace nqes {
 
 namespace {
 
-constexpr int kUMax = 4;     // hidden units per thread in a column block
+constexpr int kUMax = 8;          // hidden units per unit thread
 constexpr int kMaxSpinWords = 8;  // K <= 4 configurations of <= 128 spins
+constexpr int kMaxThreads = 288;  // K*TK <= 256 unit threads + the decision warp
 
 __device__ __forceinline__ double ldg(const double *p) { return __ldg(p); }
 __device__ __forceinline__ cplx ldg(const cplx *p) {
@@ -45,6 +50,15 @@ template <class S> __device__ __forceinline__ S neg_if(S v, bool n) { return n ?
 template <class S> __device__ __forceinline__ S wt(const cplx &z);
 template <> __device__ __forceinline__ double wt<double>(const cplx &z) { return z.re; }
 template <> __device__ __forceinline__ cplx wt<cplx>(const cplx &z) { return z; }
+__device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
+__device__ __forceinline__ cplx rcp(cplx x) {
+    const double d = __drcp_rn(fma(x.re, x.re, x.im * x.im));
+    return {x.re * d, -x.im * d};
+}
+__device__ __forceinline__ double shfl0(double v) { return __shfl_sync(0xffffffffu, v, 0); }
+__device__ __forceinline__ cplx shfl0(cplx v) {
+    return {__shfl_sync(0xffffffffu, v.re, 0), __shfl_sync(0xffffffffu, v.im, 0)};
+}
 
 // Multiply v by 2^-e where e is v's binary exponent when it leaves [-256, 256].
 template <class S> __device__ __forceinline__ void renorm(S &v, int &e) {
@@ -53,6 +67,20 @@ template <class S> __device__ __forceinline__ void renorm(S &v, int &e) {
         v = scale2(v, -x);
         e += x;
     }
+}
+
+// Signed cofactor (-1)^{r+c} det(Phi without row r and column c), K <= 4.
+template <class S> __device__ S cofactor(const S *m, int K, int r, int c) {
+    if (K == 1) return one<S>();
+    S sub[9];
+    int t = 0;
+    for (int a = 0; a < K; a++) {
+        if (a == r) continue;
+        for (int b = 0; b < K; b++)
+            if (b != c) sub[t++] = m[a * K + b];
+    }
+    const S d = small_det(sub, K - 1);
+    return ((r + c) & 1) ? -d : d;
 }
 
 template <class S> struct Smem {
@@ -168,113 +196,192 @@ __device__ void init_state(const SampleArgs<S> &A, Smem<S> &sm) {
     __syncthreads();
 }
 
-template <class S>
-__global__ void __launch_bounds__(512) k_sample(const SampleArgs<S> A) {
+template <class S, int UMAX>
+__global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K, L = A.sh.L;
     const size_t P = size_t(A.sh.P);
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int TK = A.tk, WK = TK >> 5;
-    const int my_kk = tid / TK, my_jl = tid - my_kk * TK;
+    const int nunit = K * TK;
+    const bool is_unit = tid < nunit;
+    const bool is_dec = warp == (nunit >> 5);
+    const int my_kk = is_unit ? tid / TK : 0, my_jl = is_unit ? tid - my_kk * TK : 0;
     const int U = (M + TK - 1) / TK;
     const int c = blockIdx.x;
     Smem<S> sm = carve<S>(smem_raw, N, M, K);
 
+    // The decision warp owns the chain's pcg64 stream; all its lanes advance
+    // identical copies so that every lane holds each draw.
     Pcg64 rng{0, 0};
     if (A.cfg) {
         for (int t = tid; t < K * NW; t += T) sm.spin[t] = A.cfg[size_t(c) * K * NW + t];
-    } else if (tid == 0) {
+    } else if (is_dec) {
         // init_multi_spin: K·N Bernoulli draws, k-major (code/rbm.cc:98-119).
         rng = pcg_seed(A.sp->seed + uint64_t(c));
-        for (int t = 0; t < K * NW; t++) sm.spin[t] = 0;
+        if (lane == 0)
+            for (int t = 0; t < K * NW; t++) sm.spin[t] = 0;
+        __syncwarp();
         for (int k = 0; k < K; k++)
-            for (int i = 0; i < N; i++)
-                if (pcg_bernoulli_half(rng)) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
+            for (int i = 0; i < N; i++) {
+                const bool d = pcg_bernoulli_half(rng);
+                if (d && lane == 0) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
+            }
     }
     __syncthreads();
     init_state(A, sm);
 
-    S detv = zero<S>();
-    double detn = 0.0;
+    // decision-warp state
+    S det = zero<S>(), g = zero<S>(), phik = zero<S>(), eg = zero<S>();
+    double detn = 0.0, u_next = 0.0;
     unsigned long long nacc = 0;
+    if (is_dec && !A.cfg) u_next = pcg_uniform(rng);
+
     const int total = A.cfg ? 1 : A.burn + A.m;
     for (int sw = 0; sw < total; sw++) {
         if (!A.cfg) {
             // ---- one sweep: proposals k outer, i inner (code/rbm.cc:536-551) ----
-            if (tid == 0) {
-                detv = small_det(sm.phi, K);
-                detn = norm2(detv);
+            if (is_dec) {
+                det = small_det(sm.phi, K);  // recomputed at every sweep, as code/rbm.cc:533
+                detn = norm2(det);
             }
             for (int k = 0; k < K; k++) {
+                if (is_dec && lane < K) {
+                    phik = sm.phi[k * K + lane];
+                    g = phik * cofactor(sm.phi, K, k, lane);
+                }
                 S *trow = sm.tnh + (k * K + my_kk) * M;
+                // pending bookkeeping of the previous accepted proposal (decision warp)
+                bool pend = false;
+                int pend_i = 0;
+                S pend_r = one<S>(), pend_ea = one<S>(), ea = one<S>();
                 for (int i = 0; i < N; i++) {
                     const bool down = spin_down(sm.spin + k * NW, i);
-                    const S *crow = A.tab.ch + (size_t(my_kk) * N + i) * M;
-                    const S *srow = A.tab.sh + (size_t(my_kk) * N + i) * M;
-                    S f[kUMax], tq[kUMax], cq[kUMax], sq[kUMax];
-                    S prod = one<S>();
+                    S tn[UMAX], tq[UMAX], cq[UMAX], sq[UMAX], fq[UMAX];
+                    double ud = 0.0;
+                    if (is_unit) {
+                        const S *crow = A.tab.ch + (size_t(my_kk) * N + i) * M;
+                        const S *srow = A.tab.sh + (size_t(my_kk) * N + i) * M;
+                        S prod = one<S>();
 #pragma unroll
-                    for (int q = 0; q < kUMax; q++) {
-                        const int j = my_jl + q * TK;
-                        if (q < U && j < M) {
-                            tq[q] = trow[j];
-                            cq[q] = ldg(crow + j);
-                            sq[q] = ldg(srow + j);
-                            // f = cosh(ws) - tanh * sinh(ws), ws = 2 sigma w
-                            f[q] = mad(neg_if(tq[q], !down), sq[q], cq[q]);
-                            prod = prod * f[q];
+                        for (int q = 0; q < UMAX; q++) {
+                            const int j = my_jl + q * TK;
+                            if (j < M) {
+                                tq[q] = trow[j];
+                                cq[q] = ldg(crow + j);
+                                sq[q] = ldg(srow + j);
+                                // f = cosh(ws) - tanh * sinh(ws), ws = 2 sigma w
+                                fq[q] = mad(neg_if(tq[q], !down), sq[q], cq[q]);
+                                prod = q == 0 ? fq[q] : prod * fq[q];
+                            }
                         }
+                        prod = warp_prod(prod);
+                        if (lane == 0) sm.red[warp] = prod;
+                        // tanh' = (tanh cosh(ws) - sinh(ws)) / f, ready for an accept;
+                        // computed after the product is published, off the critical path
+#pragma unroll
+                        for (int q = 0; q < UMAX; q++) {
+                            const int j = my_jl + q * TK;
+                            if (j < M) tn[q] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * rcp(fq[q]);
+                        }
+                    } else if (is_dec) {
+                        // finish the previous proposal's bookkeeping, then prepare
+                        // e^{-2 sigma a} g and u |det Phi|^2 for this one
+                        if (pend) {
+                            if (lane < K) {
+                                phik = phik * (pend_r * pend_ea);
+                                sm.phi[k * K + lane] = phik;
+                            }
+                            int ex = lane < K ? expo(phik) : -100000;
+                            ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 1));
+                            ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 2));
+                            ex = __shfl_sync(0xffffffffu, ex, 0);
+                            if (ex > 256 || ex < -256) {
+                                phik = scale2(phik, -ex);
+                                g = scale2(g, -ex);
+                                det = scale2(det, -ex);
+                                detn = norm2(det);
+                                if (lane < K) sm.phi[k * K + lane] = phik;
+                                if (lane == 0) sm.rowe[k] += ex;
+                            }
+                            if (lane == 0) sm.spin[k * NW + (pend_i >> 6)] ^= 1ULL << (pend_i & 63);
+                            pend = false;
+                        }
+                        if (lane < K) {
+                            ea = ldg((down ? A.tab.edn : A.tab.eup) + lane * N + i);
+                            eg = ea * g;
+                        }
+                        ud = u_next * detn;
                     }
-                    prod = warp_prod(prod);
-                    if (lane == 0) sm.red[warp] = prod;
                     __syncthreads();
-                    if (tid == 0) {
-                        S row[4], tmp[16];
-                        for (int t = 0; t < KK; t++) tmp[t] = sm.phi[t];
-                        for (int kk = 0; kk < K; kk++) {
-                            S r = sm.red[kk * WK];
-                            for (int w2 = 1; w2 < WK; w2++) r = r * sm.red[kk * WK + w2];
-                            r = r * ldg((down ? A.tab.edn : A.tab.eup) + kk * N + i);
-                            row[kk] = sm.phi[k * K + kk] * r;
-                            tmp[k * K + kk] = row[kk];
+                    if (is_dec) {
+                        S x = zero<S>(), r = one<S>();
+                        if (lane < K) {
+                            r = sm.red[lane * WK];
+                            for (int w2 = 1; w2 < WK; w2++) r = r * sm.red[lane * WK + w2];
+                            x = r * eg;
                         }
-                        const S dp = small_det(tmp, K);
-                        const double np = norm2(dp);
-                        const double u = pcg_uniform(rng);
+                        // det Phi' = sum over lanes 0..K-1 (K <= 4)
+                        S s = x + shfl_xor(x, 1);
+                        s = s + shfl_xor(s, 2);
+                        s = shfl0(s);
+                        const double np = norm2(s);
                         // Accept iff u <= min(1, |det Phi'|^2 / |det Phi|^2), with
                         // probability one when det Phi == 0 (code/rbm.cc:541-543),
                         // evaluated as u |det Phi|^2 <= |det Phi'|^2.
-                        const bool acc = is_zero(detv) || u * detn <= np;
+                        const bool acc = is_zero(det) || ud <= np;
+                        if (lane == 0) sm.flag[0] = acc;
                         if (acc) {
-                            int ex = -100000;
-                            for (int kk = 0; kk < K; kk++) ex = max(ex, expo(row[kk]));
-                            const bool rs = ex > 256 || ex < -256;
-                            for (int kk = 0; kk < K; kk++) sm.phi[k * K + kk] = rs ? scale2(row[kk], -ex) : row[kk];
-                            detv = rs ? scale2(dp, -ex) : dp;
-                            detn = norm2(detv);
-                            if (rs) sm.rowe[k] += ex;
-                            sm.spin[k * NW + (i >> 6)] ^= 1ULL << (i & 63);
+                            // Row k of Phi is multiplied by r = ratio * e^{-2 sigma a}
+                            // once the unit warps are released (pending above).
+                            if (lane < K) {
+                                g = x;
+                                pend_r = r;
+                                pend_ea = ea;
+                            }
+                            det = s;
+                            detn = np;
+                            pend = true;
+                            pend_i = i;
                             nacc++;
                         }
-                        sm.flag[0] = acc;
+                        u_next = pcg_uniform(rng);  // the next proposal's draw
                     }
                     __syncthreads();
-                    if (sm.flag[0]) {
+                    if (is_unit && sm.flag[0]) {
 #pragma unroll
-                        for (int q = 0; q < kUMax; q++) {
+                        for (int q = 0; q < UMAX; q++) {
                             const int j = my_jl + q * TK;
-                            if (q < U && j < M) {
-                                // tanh' = (tanh cosh(ws) - sinh(ws)) / f  (code/rbm.cc:185)
-                                trow[j] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * inv(f[q]);
-                            }
+                            if (j < M) trow[j] = tn[q];
                         }
                     }
                 }
+                // complete the row's last accepted proposal before the next row
+                if (is_dec && pend) {
+                    if (lane < K) {
+                        phik = phik * (pend_r * pend_ea);
+                        sm.phi[k * K + lane] = phik;
+                    }
+                    int ex = lane < K ? expo(phik) : -100000;
+                    ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 1));
+                    ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 2));
+                    ex = __shfl_sync(0xffffffffu, ex, 0);
+                    if (ex > 256 || ex < -256) {
+                        phik = scale2(phik, -ex);
+                        det = scale2(det, -ex);
+                        detn = norm2(det);
+                        if (lane < K) sm.phi[k * K + lane] = phik;
+                        if (lane == 0) sm.rowe[k] += ex;
+                    }
+                    if (lane == 0) sm.spin[k * NW + (pend_i >> 6)] ^= 1ULL << (pend_i & 63);
+                }
+                __syncthreads();
             }
             if (sw < A.burn) continue;
         }
         // ---- sample: local energy and log-derivatives ----
         const size_t s = A.cfg ? size_t(c) : size_t(c) * A.m + (sw - A.burn);
+        __syncthreads();
         if (tid == 0) {
             if (!small_inv(sm.phi, sm.pinv, K)) {
                 atomicOr(A.err, kErrSingular);
@@ -367,10 +474,9 @@ __global__ void __launch_bounds__(512) k_sample(const SampleArgs<S> A) {
                 ok[p] = v;
             }
         }
-        // (No barrier needed here: the next sweep's first shared write follows a
-        // __syncthreads that every thread reaches only after its O stores.)
+        __syncthreads();
     }
-    if (tid == 0 && !A.cfg) A.accepted[c] = nacc;
+    if (is_dec && lane == 0 && !A.cfg) A.accepted[c] = nacc;
 }
 
 // Per-step tables from the weights: cosh(2w), sinh(2w), exp(-2a), exp(2a).
@@ -396,15 +502,32 @@ size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith) {
     return smem_bytes(sh.N, sh.M, sh.K, complex_arith ? sizeof(cplx) : sizeof(double));
 }
 
+int sample_threads(int K, int tk) { return K * tk + 32; }
+
 // Sets the sampler's dynamic shared-memory limit; call outside stream capture.
 template <class S> cudaError_t prepare_sample(const Shape &sh) {
-    const size_t smem = smem_bytes(sh.N, sh.M, sh.K, sizeof(S));
-    return cudaFuncSetAttribute(k_sample<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const int smem = int(smem_bytes(sh.N, sh.M, sh.K, sizeof(S)));
+    cudaError_t e = cudaFuncSetAttribute(k_sample<S, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample<S, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample<S, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample<S, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    return e;
 }
 
+// Launch with the smallest compiled units-per-thread bound that covers M/TK.
 template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st) {
     const size_t smem = smem_bytes(a.sh.N, a.sh.M, a.sh.K, sizeof(S));
-    k_sample<S><<<a.chains, threads, smem, st>>>(a);
+    const int U = (a.sh.M + a.tk - 1) / a.tk;
+    if (threads != sample_threads(a.sh.K, a.tk) || threads > kMaxThreads || U > kUMax || a.tk % 32)
+        return cudaErrorInvalidConfiguration;
+    if (U <= 1)
+        k_sample<S, 1><<<a.chains, threads, smem, st>>>(a);
+    else if (U <= 2)
+        k_sample<S, 2><<<a.chains, threads, smem, st>>>(a);
+    else if (U <= 4)
+        k_sample<S, 4><<<a.chains, threads, smem, st>>>(a);
+    else
+        k_sample<S, 8><<<a.chains, threads, smem, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -210,22 +210,22 @@ template <class S> cudaError_t launch_tables_ctx(nqes_ctx *ctx) {
                             const_cast<S *>(t.eup), const_cast<S *>(t.edn), ctx->st);
 }
 
-// Threads per RBM column block: enough that each thread holds at most four
-// hidden units, more when there are few chains to spread over the SMs.
+// Threads per RBM column block (TK): at most eight hidden units per thread,
+// K*TK <= 256 unit threads; wide blocks when there are few chains to spread
+// over the SMs (latency), narrow ones when chains fill the GPU (throughput).
 int choose_tk(nqes_ctx *ctx, int chains) {
     const int M = ctx->sh.M, K = ctx->sh.K;
-    int tmin = std::max(32, ((M + 3) / 4 + 31) / 32 * 32);
+    const int tmin = std::max(32, ((M + 7) / 8 + 31) / 32 * 32);
+    const int tmax = std::max(32, 256 / K / 32 * 32);
     int tk;
     if (ctx->tk_opt) {
-        tk = std::max(tmin, ctx->tk_opt);
+        tk = ctx->tk_opt;
     } else {
         int dev_sms = 152;
         cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
         tk = chains <= dev_sms ? std::min(128, (M + 31) / 32 * 32) : tmin;
-        tk = std::max(tk, tmin);
     }
-    while (K * tk > 512) tk -= 32;
-    return tk;
+    return std::min(std::max(tk, tmin), tmax);
 }
 
 template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
@@ -235,7 +235,7 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     }
     SampleArgs<S> A = sample_args<S>(ctx, chains, m, burn, tk);
     SolveBufs<S> B = solve_bufs<S>(ctx);
-    const int threads = ctx->sh.K * tk;
+    const int threads = sample_threads(ctx->sh.K, tk);
     {
         // the sampler's dynamic shared memory attribute must be set before capture
         const size_t smem = sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
@@ -632,7 +632,7 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
             A.cfg = cfg;
             A.phi_out = dphi;
             A.tanh_out = dth;
-            NQES_CUDA(launch_sample<cplx>(A, sh.K * tk, ctx->st));
+            NQES_CUDA(launch_sample<cplx>(A, sample_threads(sh.K, tk), ctx->st));
         } else {
             NQES_CUDA(prepare_sample<double>(sh));
             NQES_CUDA(launch_tables_ctx<double>(ctx));
@@ -643,7 +643,7 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
             A.cfg = cfg;
             A.phi_out = dphi;
             A.tanh_out = dth;
-            NQES_CUDA(launch_sample<double>(A, sh.K * tk, ctx->st));
+            NQES_CUDA(launch_sample<double>(A, sample_threads(sh.K, tk), ctx->st));
         }
         NQES_CUDA(cudaStreamSynchronize(ctx->st));
         if (phi) NQES_CUDA(cudaMemcpy(phi, dphi, count * KK * sizeof(cplx), cudaMemcpyDeviceToHost));
@@ -789,7 +789,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
         switch (kernel) {
         case NQES_KERNEL_SAMPLE: {
             SampleArgs<S> A = sample_args<S>(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
-            return launch_sample<S>(A, ctx->sh.K * ctx->last_tk, ctx->st);
+            return launch_sample<S>(A, sample_threads(ctx->sh.K, ctx->last_tk), ctx->st);
         }
         case NQES_KERNEL_SV_ROWS: return launch_sv_rows_only<S>(B, ctx->st);
         case NQES_KERNEL_SV_COLS: return launch_sv_cols_only<S>(B, ctx->st);

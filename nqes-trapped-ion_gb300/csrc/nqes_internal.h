@@ -57,6 +57,7 @@ enum : int {
 };
 
 size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith);
+int sample_threads(int K, int tk);  // K*tk unit threads + one decision warp
 template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st);
 template <class S> cudaError_t launch_tables(const Shape &sh, const cplx *a, const cplx *w, S *ch, S *shh, S *eup,
                                              S *edn, cudaStream_t st);
