@@ -69,9 +69,66 @@ def build_library(verbose=False):
     return lib
 
 
+
+
+# ---- drop-in executables ----
+CLI = os.path.join(PKG, "cli")
+BINDIR = os.path.join(PKG, "bin")
+CLI_SOURCES = ["cmdline.cc", "matv5.cc"]
+CLI_HEADERS = ["cmdline.h", "matv5.h", "small_eig.h"]
+# The reference's build list (code/build.sh:28) plus the K=4 precision shape.
+DEFAULT_SHAPES = [(8, 16, 2), (8, 32, 2), (16, 32, 2), (16, 64, 2), (32, 64, 2), (32, 128, 2), (64, 128, 2),
+                  (64, 256, 2), (128, 256, 2), (64, 128, 4)]
+
+
+def _gxx():
+    return shutil.which("g++") or "g++"
+
+
+def _cli_object(src):
+    obj = os.path.join(OBJDIR, "cli_" + os.path.splitext(src)[0] + ".o")
+    deps = [os.path.join(CLI, src)] + [os.path.join(CLI, h) for h in CLI_HEADERS]
+    if _stale(obj, deps):
+        r = subprocess.run([_gxx(), "-std=c++20", "-O2", "-fPIC", "-c", os.path.join(CLI, src), "-o", obj],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed on {src}:\n{r.stderr}")
+    return obj
+
+
+def _cli_binary(shape, objs, lib):
+    n, m, k = shape
+    name = f"rbm-matfree-N{n}-M{m}-K{k}-opt"
+    out = os.path.join(BINDIR, name)
+    deps = [os.path.join(CLI, "rbm_main.cc"), lib, os.path.join(INCLUDE, "nqes.h")] + objs + \
+        [os.path.join(CLI, h) for h in CLI_HEADERS]
+    if _stale(out, deps):
+        cmd = [_gxx(), "-std=c++20", "-O2", f"-DNUM_SPINS={n}", f"-DNUM_HIDDEN_UNITS={m}", f"-DNUM_EIGENSTATES={k}",
+               "-I", INCLUDE, "-I", CLI, os.path.join(CLI, "rbm_main.cc"), *objs, "-L", LIBDIR, "-lnqes",
+               "-Wl,-rpath,$ORIGIN/../lib", "-o", out]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"g++ failed on {name}:\n{r.stderr}")
+    if n <= 16:  # the reference names its N <= 16 builds without "matfree"
+        alias = os.path.join(BINDIR, f"rbm-N{n}-M{m}-K{k}-opt")
+        if not os.path.exists(alias):
+            os.symlink(name, alias)
+    return out
+
+
+def build_cli(shapes=None):
+    """Builds rbm-matfree-N{N}-M{M}-K{K}-opt for each (N, M, K)."""
+    lib = build_library()
+    os.makedirs(BINDIR, exist_ok=True)
+    objs = [_cli_object(s) for s in CLI_SOURCES]
+    with cf.ThreadPoolExecutor(max_workers=8) as ex:
+        return list(ex.map(lambda sh: _cli_binary(sh, objs, lib), shapes or DEFAULT_SHAPES))
+
+
 def main():
-    lib = build_library(verbose="--verbose" in sys.argv)
-    print(lib)
+    print(build_library(verbose="--verbose" in sys.argv))
+    for b in build_cli():
+        print(b)
 
 
 if __name__ == "__main__":

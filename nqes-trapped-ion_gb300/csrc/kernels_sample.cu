@@ -5,25 +5,28 @@
 // monte_carlo_step (530-552), ising_like_hamiltonian + trapped_ion_model
 // (1011-1062) and deriv (199-239).
 //
-// Thread layout. A chain's CTA has K*TK "unit" threads (TK a multiple of 32)
-// and one "decision" warp. Column block kk (RBM kk) owns unit threads
-// [kk*TK, (kk+1)*TK); thread jl of the block owns hidden units j = jl,
-// jl + TK, ... of that RBM. For a proposal (k, i) every unit thread forms
+// Thread layout. A chain's CTA has K*TK threads (TK a multiple of 32). Column
+// block kk (RBM kk) owns threads [kk*TK, (kk+1)*TK); thread jl of the block
+// owns hidden units j = jl, jl + TK, ... of that RBM. For a proposal (k, i)
+// every thread forms
 //     f_j = cosh(2 w_ij) - sigma_i tanh(theta_j^{(k,kk)}) sinh(2 w_ij)
 // (= cosh(theta_j - 2 sigma_i w_ij) / cosh(theta_j), the factor of
-// flip_state_fcn, code/rbm.cc:182-187) from per-step tables, the block
-// multiplies them by warp shuffles, and each thread already computes the
-// updated tanh(theta_j) it would store if the flip is accepted
-// (code/rbm.cc:185). Meanwhile the decision warp turns the K products into the
-// new determinant by a Laplace expansion along row k,
+// flip_state_fcn, code/rbm.cc:182-187) from per-step tables, and each warp
+// multiplies its factors by shuffles. After one barrier every warp reads the
+// K products and takes the accept decision itself, turning them into the new
+// determinant by a Laplace expansion along row k,
 //     det Phi' = sum_kk r_kk * g_kk,   g_kk = Phi[k][kk] * cofactor(k, kk),
 // whose cofactors do not depend on row k and so are computed once per row and
-// sweep, and applies the reference's acceptance test (code/rbm.cc:541-543).
+// sweep; then the reference's acceptance test (code/rbm.cc:541-543) and, on
+// acceptance, the tanh update of the thread's own units (code/rbm.cc:185).
+// All warps hold identical copies of the random stream and of the decision
+// state, so a proposal costs one barrier.
 //
 // On GB300 an FP64 warp instruction occupies the issuing warp for ~64 cycles
-// whether one lane or 32 are active, so the kernel keeps the FP64 instruction
-// count on the proposal's critical path (reduction, then decision) small and
-// moves the tanh update off it.
+// whether one lane or 32 are active, so the kernel minimises the FP64
+// instruction count on a proposal's critical path (factor, reduction,
+// decision) rather than lane work; replicating the decision in every warp
+// costs no more time than running it in one.
 //
 // Rows of Phi are kept scaled by exact powers of two. Every quantity the
 // reference derives from Phi (the ratio |det Phi'|^2/|det Phi|^2, Phi^-1 H Phi
@@ -38,7 +41,7 @@ namespace {
 
 constexpr int kUMax = 8;          // hidden units per unit thread
 constexpr int kMaxSpinWords = 8;  // K <= 4 configurations of <= 128 spins
-constexpr int kMaxThreads = 288;  // K*TK <= 256 unit threads + the decision warp
+constexpr int kMaxThreads = 256;  // K*TK threads
 
 __device__ __forceinline__ double ldg(const double *p) { return __ldg(p); }
 __device__ __forceinline__ cplx ldg(const cplx *p) {
@@ -196,6 +199,80 @@ __device__ void init_state(const SampleArgs<S> &A, Smem<S> &sm) {
     __syncthreads();
 }
 
+// Correlation-function contributions of one sample (code/rbm.cc:730-826): for
+// every site i the K×K matrices Phi^-1 F_i with F_i = Phi(flip i in every row)
+// (sigma^x_i) and F_i = diag(sigma_i) Phi (sigma^z_i), and for every pair
+// (i, j) Phi(flip i and j) (sigma^x_i sigma^x_j) and diag(sigma_i sigma_j) Phi
+// (sigma^z_i sigma^z_j), accumulated into the chain's slice of A.corr.
+// Single-flip ratios come from sm.rat (the local-energy terms); pair ratios
+// use cosh(d_i + d_j) - tanh(theta) sinh(d_i + d_j) with d = 2 sigma w.
+template <class S> __device__ void corr_sample(const SampleArgs<S> &A, Smem<S> &sm, int c) {
+    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K;
+    const int T = blockDim.x, tid = threadIdx.x;
+    S *acc = A.corr + size_t(c) * A.corr_stride;
+    S *ax = acc, *az = ax + size_t(N) * KK, *axx = az + size_t(N) * KK, *azz = axx + size_t(N) * N * KK;
+    S *R = A.corr_scratch + size_t(c) * N * N * KK;
+    for (int i = tid; i < N; i += T) {
+        for (int r = 0; r < K; r++)
+            for (int cc = 0; cc < K; cc++) {
+                S mx = zero<S>(), mz = zero<S>();
+                for (int t = 0; t < K; t++) {
+                    const S pt = sm.phi[t * K + cc];
+                    mx = mad(sm.pinv[r * K + t], pt * sm.rat[(t * K + cc) * N + i], mx);
+                    mz = mad(sm.pinv[r * K + t], spin_down(sm.spin + t * NW, i) ? -pt : pt, mz);
+                }
+                ax[i * KK + r * K + cc] = ax[i * KK + r * K + cc] + mx;
+                az[i * KK + r * K + cc] = az[i * KK + r * K + cc] + mz;
+            }
+    }
+    // pair ratios R[(i*N+j)*KK + k*K+kk], i < j
+    for (int it = tid; it < N * N * KK; it += T) {
+        const int q = it % KK, ij = it / KK, i = ij / N, j = ij - i * N;
+        if (i >= j) continue;
+        const int k = q / K, kk = q - k * K;
+        const bool di = spin_down(sm.spin + k * NW, i), dj = spin_down(sm.spin + k * NW, j);
+        const S *ci = A.tab.ch + (size_t(kk) * N + i) * M, *si = A.tab.sh + (size_t(kk) * N + i) * M;
+        const S *cj = A.tab.ch + (size_t(kk) * N + j) * M, *sj = A.tab.sh + (size_t(kk) * N + j) * M;
+        const S *tr = sm.tnh + q * M;
+        S p = one<S>();
+        for (int l = 0; l < M; l++) {
+            const S Ci = ldg(ci + l), Cj = ldg(cj + l);
+            const S Si = neg_if(ldg(si + l), di), Sj = neg_if(ldg(sj + l), dj);  // sinh(d) = sigma S
+            const S chs = mad(Ci, Cj, Si * Sj);
+            const S shs = mad(Si, Cj, Ci * Sj);
+            p = p * mad(-tr[l], shs, chs);
+        }
+        p = p * ldg((di ? A.tab.edn : A.tab.eup) + kk * N + i) * ldg((dj ? A.tab.edn : A.tab.eup) + kk * N + j);
+        R[size_t(ij) * KK + q] = p;
+    }
+    __syncthreads();
+    for (int ij = tid; ij < N * N; ij += T) {
+        const int i = ij / N, j = ij - i * N;
+        if (i > j) continue;
+        for (int r = 0; r < K; r++)
+            for (int cc = 0; cc < K; cc++) {
+                S mxx = zero<S>(), mzz = zero<S>();
+                if (i == j) {  // flipping i twice, and sigma_i^2 = 1: the identity
+                    mxx = mzz = (r == cc) ? one<S>() : zero<S>();
+                } else {
+                    for (int t = 0; t < K; t++) {
+                        const S pt = sm.phi[t * K + cc];
+                        mxx = mad(sm.pinv[r * K + t], pt * R[size_t(ij) * KK + t * K + cc], mxx);
+                        const bool flip = spin_down(sm.spin + t * NW, i) ^ spin_down(sm.spin + t * NW, j);
+                        mzz = mad(sm.pinv[r * K + t], flip ? -pt : pt, mzz);
+                    }
+                }
+                const size_t e1 = size_t(i * N + j) * KK + r * K + cc, e2 = size_t(j * N + i) * KK + r * K + cc;
+                axx[e1] = axx[e1] + mxx;
+                azz[e1] = azz[e1] + mzz;
+                if (i != j) {
+                    axx[e2] = axx[e2] + mxx;
+                    azz[e2] = azz[e2] + mzz;
+                }
+            }
+    }
+}
+
 template <class S, int UMAX>
 __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -203,177 +280,123 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
     const size_t P = size_t(A.sh.P);
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int TK = A.tk, WK = TK >> 5;
-    const int nunit = K * TK;
-    const bool is_unit = tid < nunit;
-    const bool is_dec = warp == (nunit >> 5);
-    const int my_kk = is_unit ? tid / TK : 0, my_jl = is_unit ? tid - my_kk * TK : 0;
-    const int U = (M + TK - 1) / TK;
+    const int my_kk = tid / TK, my_jl = tid - (tid / TK) * TK;
     const int c = blockIdx.x;
     Smem<S> sm = carve<S>(smem_raw, N, M, K);
 
-    // The decision warp owns the chain's pcg64 stream; all its lanes advance
-    // identical copies so that every lane holds each draw.
+    // Every thread advances an identical copy of the chain's pcg64 stream, so
+    // each warp holds every draw and takes every accept decision itself.
     Pcg64 rng{0, 0};
     if (A.cfg) {
         for (int t = tid; t < K * NW; t += T) sm.spin[t] = A.cfg[size_t(c) * K * NW + t];
-    } else if (is_dec) {
+    } else {
         // init_multi_spin: K·N Bernoulli draws, k-major (code/rbm.cc:98-119).
         rng = pcg_seed(A.sp->seed + uint64_t(c));
-        if (lane == 0)
+        if (tid == 0)
             for (int t = 0; t < K * NW; t++) sm.spin[t] = 0;
-        __syncwarp();
+        __syncthreads();
         for (int k = 0; k < K; k++)
             for (int i = 0; i < N; i++) {
                 const bool d = pcg_bernoulli_half(rng);
-                if (d && lane == 0) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
+                if (d && tid == 0) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
             }
     }
     __syncthreads();
     init_state(A, sm);
 
-    // decision-warp state
-    S det = zero<S>(), g = zero<S>(), phik = zero<S>(), eg = zero<S>();
-    double detn = 0.0, u_next = 0.0;
+    // Decision state, identical in every warp: det Phi, |det Phi|^2 and, in
+    // lanes kk < K, the current row's Phi[k][kk] and g_kk = Phi[k][kk] cof(k, kk).
+    S det = zero<S>(), g = zero<S>(), phik = zero<S>();
+    double detn = 0.0;
     unsigned long long nacc = 0;
-    if (is_dec && !A.cfg) u_next = pcg_uniform(rng);
+    const bool writer = tid == 0;  // the one thread that commits shared state
 
     const int total = A.cfg ? 1 : A.burn + A.m;
     for (int sw = 0; sw < total; sw++) {
         if (!A.cfg) {
             // ---- one sweep: proposals k outer, i inner (code/rbm.cc:536-551) ----
-            if (is_dec) {
-                det = small_det(sm.phi, K);  // recomputed at every sweep, as code/rbm.cc:533
-                detn = norm2(det);
-            }
+            det = small_det(sm.phi, K);  // recomputed at every sweep, as code/rbm.cc:533
+            detn = norm2(det);
             for (int k = 0; k < K; k++) {
-                if (is_dec && lane < K) {
+                if (lane < K) {
                     phik = sm.phi[k * K + lane];
                     g = phik * cofactor(sm.phi, K, k, lane);
                 }
                 S *trow = sm.tnh + (k * K + my_kk) * M;
-                // pending bookkeeping of the previous accepted proposal (decision warp)
-                bool pend = false;
-                int pend_i = 0;
-                S pend_r = one<S>(), pend_ea = one<S>(), ea = one<S>();
                 for (int i = 0; i < N; i++) {
+                    const int par = (i & 1) * 16;  // reduction slots alternate between proposals
                     const bool down = spin_down(sm.spin + k * NW, i);
-                    S tn[UMAX], tq[UMAX], cq[UMAX], sq[UMAX], fq[UMAX];
-                    double ud = 0.0;
-                    if (is_unit) {
-                        const S *crow = A.tab.ch + (size_t(my_kk) * N + i) * M;
-                        const S *srow = A.tab.sh + (size_t(my_kk) * N + i) * M;
-                        S prod = one<S>();
+                    const S *crow = A.tab.ch + (size_t(my_kk) * N + i) * M;
+                    const S *srow = A.tab.sh + (size_t(my_kk) * N + i) * M;
+                    S tq[UMAX], cq[UMAX], sq[UMAX], fq[UMAX];
+                    S prod = one<S>();
 #pragma unroll
-                        for (int q = 0; q < UMAX; q++) {
-                            const int j = my_jl + q * TK;
-                            if (j < M) {
-                                tq[q] = trow[j];
-                                cq[q] = ldg(crow + j);
-                                sq[q] = ldg(srow + j);
-                                // f = cosh(ws) - tanh * sinh(ws), ws = 2 sigma w
-                                fq[q] = mad(neg_if(tq[q], !down), sq[q], cq[q]);
-                                prod = q == 0 ? fq[q] : prod * fq[q];
-                            }
-                        }
-                        prod = warp_prod(prod);
-                        if (lane == 0) sm.red[warp] = prod;
-                        // tanh' = (tanh cosh(ws) - sinh(ws)) / f, ready for an accept;
-                        // computed after the product is published, off the critical path
-#pragma unroll
-                        for (int q = 0; q < UMAX; q++) {
-                            const int j = my_jl + q * TK;
-                            if (j < M) tn[q] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * rcp(fq[q]);
-                        }
-                    } else if (is_dec) {
-                        // finish the previous proposal's bookkeeping, then prepare
-                        // e^{-2 sigma a} g and u |det Phi|^2 for this one
-                        if (pend) {
-                            if (lane < K) {
-                                phik = phik * (pend_r * pend_ea);
-                                sm.phi[k * K + lane] = phik;
-                            }
-                            int ex = lane < K ? expo(phik) : -100000;
-                            ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 1));
-                            ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 2));
-                            ex = __shfl_sync(0xffffffffu, ex, 0);
-                            if (ex > 256 || ex < -256) {
-                                phik = scale2(phik, -ex);
-                                g = scale2(g, -ex);
-                                det = scale2(det, -ex);
-                                detn = norm2(det);
-                                if (lane < K) sm.phi[k * K + lane] = phik;
-                                if (lane == 0) sm.rowe[k] += ex;
-                            }
-                            if (lane == 0) sm.spin[k * NW + (pend_i >> 6)] ^= 1ULL << (pend_i & 63);
-                            pend = false;
-                        }
-                        if (lane < K) {
-                            ea = ldg((down ? A.tab.edn : A.tab.eup) + lane * N + i);
-                            eg = ea * g;
-                        }
-                        ud = u_next * detn;
-                    }
-                    __syncthreads();
-                    if (is_dec) {
-                        S x = zero<S>(), r = one<S>();
-                        if (lane < K) {
-                            r = sm.red[lane * WK];
-                            for (int w2 = 1; w2 < WK; w2++) r = r * sm.red[lane * WK + w2];
-                            x = r * eg;
-                        }
-                        // det Phi' = sum over lanes 0..K-1 (K <= 4)
-                        S s = x + shfl_xor(x, 1);
-                        s = s + shfl_xor(s, 2);
-                        s = shfl0(s);
-                        const double np = norm2(s);
-                        // Accept iff u <= min(1, |det Phi'|^2 / |det Phi|^2), with
-                        // probability one when det Phi == 0 (code/rbm.cc:541-543),
-                        // evaluated as u |det Phi|^2 <= |det Phi'|^2.
-                        const bool acc = is_zero(det) || ud <= np;
-                        if (lane == 0) sm.flag[0] = acc;
-                        if (acc) {
-                            // Row k of Phi is multiplied by r = ratio * e^{-2 sigma a}
-                            // once the unit warps are released (pending above).
-                            if (lane < K) {
-                                g = x;
-                                pend_r = r;
-                                pend_ea = ea;
-                            }
-                            det = s;
-                            detn = np;
-                            pend = true;
-                            pend_i = i;
-                            nacc++;
-                        }
-                        u_next = pcg_uniform(rng);  // the next proposal's draw
-                    }
-                    __syncthreads();
-                    if (is_unit && sm.flag[0]) {
-#pragma unroll
-                        for (int q = 0; q < UMAX; q++) {
-                            const int j = my_jl + q * TK;
-                            if (j < M) trow[j] = tn[q];
+                    for (int q = 0; q < UMAX; q++) {
+                        const int j = my_jl + q * TK;
+                        if (j < M) {
+                            tq[q] = trow[j];
+                            cq[q] = ldg(crow + j);
+                            sq[q] = ldg(srow + j);
+                            // f = cosh(ws) - tanh * sinh(ws), ws = 2 sigma w
+                            fq[q] = mad(neg_if(tq[q], !down), sq[q], cq[q]);
+                            prod = q == 0 ? fq[q] : prod * fq[q];
                         }
                     }
-                }
-                // complete the row's last accepted proposal before the next row
-                if (is_dec && pend) {
+                    prod = warp_prod(prod);
+                    if (lane == 0) sm.red[par + warp] = prod;
+                    // e^{-2 sigma_i a_i} g_kk and u |det Phi|^2 while the other warps finish
+                    S ea = one<S>(), eg = zero<S>();
                     if (lane < K) {
-                        phik = phik * (pend_r * pend_ea);
-                        sm.phi[k * K + lane] = phik;
+                        ea = ldg((down ? A.tab.edn : A.tab.eup) + lane * N + i);
+                        eg = ea * g;
                     }
-                    int ex = lane < K ? expo(phik) : -100000;
-                    ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 1));
-                    ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 2));
-                    ex = __shfl_sync(0xffffffffu, ex, 0);
-                    if (ex > 256 || ex < -256) {
-                        phik = scale2(phik, -ex);
-                        det = scale2(det, -ex);
-                        detn = norm2(det);
-                        if (lane < K) sm.phi[k * K + lane] = phik;
-                        if (lane == 0) sm.rowe[k] += ex;
+                    const double ud = pcg_uniform(rng) * detn;
+                    __syncthreads();
+                    // det Phi' = sum_kk r_kk e^{-2 sigma a} g_kk over lanes 0..K-1 (K <= 4)
+                    S x = zero<S>(), r = one<S>();
+                    if (lane < K) {
+                        r = sm.red[par + lane * WK];
+                        for (int w2 = 1; w2 < WK; w2++) r = r * sm.red[par + lane * WK + w2];
+                        x = r * eg;
                     }
-                    if (lane == 0) sm.spin[k * NW + (pend_i >> 6)] ^= 1ULL << (pend_i & 63);
+                    S s = x + shfl_xor(x, 1);
+                    s = s + shfl_xor(s, 2);
+                    s = shfl0(s);
+                    const double np = norm2(s);
+                    // Accept iff u <= min(1, |det Phi'|^2 / |det Phi|^2), with
+                    // probability one when det Phi == 0 (code/rbm.cc:541-543),
+                    // evaluated as u |det Phi|^2 <= |det Phi'|^2.
+                    const bool acc = is_zero(det) || ud <= np;
+                    if (acc) {
+                        // tanh' = (tanh cosh(ws) - sinh(ws)) / f  (code/rbm.cc:185)
+#pragma unroll
+                        for (int q = 0; q < UMAX; q++) {
+                            const int j = my_jl + q * TK;
+                            if (j < M) trow[j] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * rcp(fq[q]);
+                        }
+                        if (lane < K) {
+                            g = x;
+                            phik = phik * (r * ea);
+                        }
+                        det = s;
+                        detn = np;
+                        int ex = lane < K ? expo(phik) : -100000;
+                        ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 1));
+                        ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, 2));
+                        ex = __shfl_sync(0xffffffffu, ex, 0);
+                        if (ex > 256 || ex < -256) {
+                            phik = scale2(phik, -ex);
+                            g = scale2(g, -ex);
+                            det = scale2(det, -ex);
+                            detn = norm2(det);
+                            if (writer) sm.rowe[k] += ex;
+                        }
+                        if (warp == 0 && lane < K) sm.phi[k * K + lane] = phik;
+                        // Other warps may already read bit i+1 of this word: the
+                        // read sees bit i+1 unchanged before or after the flip.
+                        if (writer) sm.spin[k * NW + (i >> 6)] ^= 1ULL << (i & 63);
+                        nacc++;
+                    }
                 }
                 __syncthreads();
             }
@@ -422,6 +445,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
             sm.bsig[it] = spin_down(sm.spin + kk * NW, i) ? -B : B;
         }
         __syncthreads();
+        if (A.corr) {  // correlation pass: observables instead of E and O
+            corr_sample(A, sm, c);
+            __syncthreads();
+            continue;
+        }
         for (int q = warp; q < KK; q += nwarp) {
             S acc = zero<S>();
             for (int i = lane; i < N; i += 32) acc = acc + sm.rat[q * N + i];
@@ -476,7 +504,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
         }
         __syncthreads();
     }
-    if (is_dec && lane == 0 && !A.cfg) A.accepted[c] = nacc;
+    if (writer && !A.cfg && A.accepted) A.accepted[c] = nacc;
 }
 
 // Per-step tables from the weights: cosh(2w), sinh(2w), exp(-2a), exp(2a).
@@ -502,7 +530,7 @@ size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith) {
     return smem_bytes(sh.N, sh.M, sh.K, complex_arith ? sizeof(cplx) : sizeof(double));
 }
 
-int sample_threads(int K, int tk) { return K * tk + 32; }
+int sample_threads(int K, int tk) { return K * tk; }
 
 // Sets the sampler's dynamic shared-memory limit; call outside stream capture.
 template <class S> cudaError_t prepare_sample(const Shape &sh) {
@@ -533,6 +561,23 @@ template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads
 
 template cudaError_t prepare_sample<double>(const Shape &);
 template cudaError_t prepare_sample<cplx>(const Shape &);
+
+// out[e] = sum over chains of acc[chain][e], in chain order.
+template <class S> __global__ void k_corr_reduce(const S *acc, int chains, size_t stride, S *out) {
+    for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < stride; e += size_t(gridDim.x) * blockDim.x) {
+        S s = zero<S>();
+        for (int c = 0; c < chains; c++) s = s + acc[size_t(c) * stride + e];
+        out[e] = s;
+    }
+}
+
+template <class S> cudaError_t launch_corr_reduce(const S *acc, int chains, size_t stride, S *out, cudaStream_t st) {
+    const int blocks = int(std::min<size_t>((stride + 255) / 256, 1024));
+    k_corr_reduce<S><<<blocks, 256, 0, st>>>(acc, chains, stride, out);
+    return cudaGetLastError();
+}
+template cudaError_t launch_corr_reduce<double>(const double *, int, size_t, double *, cudaStream_t);
+template cudaError_t launch_corr_reduce<cplx>(const cplx *, int, size_t, cplx *, cudaStream_t);
 
 template <class S>
 cudaError_t launch_tables(const Shape &sh, const cplx *a, const cplx *w, S *ch, S *shh, S *eup, S *edn,

@@ -831,11 +831,101 @@ int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double
                                             : time_kernel_t<double>(ctx, kernel, reps, avg_ms, algorithmic_bytes);
 }
 
-int nqes_correlations(nqes_ctx *ctx, uint64_t, int, int, int, const double *, double *, double *, double *,
-                      double *) {
-    if (!ctx) return NQES_ERR_INVALID;
-    ctx->err = "correlations are not built yet";
-    return NQES_ERR_STATE;
+}  // extern "C"
+
+namespace {
+template <class S>
+int correlations_t(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, const cplx *evecs, double *x, double *z,
+                   double *xx, double *zz) {
+    const Shape &sh = ctx->sh;
+    const int N = sh.N, K = sh.K, KK = K * K;
+    const size_t stride = 2 * size_t(N) * KK + 2 * size_t(N) * N * KK;
+    S *acc = nullptr, *scratch = nullptr, *out = nullptr;
+    uint64_t *spins = nullptr;
+    int rc;
+    if ((rc = dalloc(ctx, &acc, size_t(chains) * stride)) ||
+        (rc = dalloc(ctx, &scratch, size_t(chains) * N * N * KK)) || (rc = dalloc(ctx, &out, stride)) ||
+        (rc = dalloc(ctx, &spins, size_t(chains) * m * K * sh.NW))) {
+        dfree(acc); dfree(scratch); dfree(out); dfree(spins);
+        return rc;
+    }
+    auto run = [&]() -> int {
+        StepParams p{};
+        p.seed = seed;
+        NQES_CUDA(cudaMemcpyAsync(ctx->sp, &p, sizeof(p), cudaMemcpyHostToDevice, ctx->st));
+        NQES_CUDA(cudaMemsetAsync(acc, 0, sizeof(S) * chains * stride, ctx->st));
+        NQES_CUDA(cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->st));
+        NQES_CUDA(prepare_sample<S>(sh));
+        NQES_CUDA(launch_tables_ctx<S>(ctx));
+        const int tk = choose_tk(ctx, chains);
+        SampleArgs<S> A = sample_args<S>(ctx, chains, m, burn, tk);
+        A.O = nullptr;
+        A.E = nullptr;
+        A.spins = spins;
+        A.accepted = nullptr;
+        A.corr = acc;
+        A.corr_scratch = scratch;
+        A.corr_stride = stride;
+        NQES_CUDA(launch_sample<S>(A, sample_threads(K, tk), ctx->st));
+        NQES_CUDA(launch_corr_reduce<S>(acc, chains, stride, out, ctx->st));
+        std::vector<S> h(stride);
+        NQES_CUDA(cudaMemcpyAsync(h.data(), out, sizeof(S) * stride, cudaMemcpyDeviceToHost, ctx->st));
+        int e = 0;
+        NQES_CUDA(cudaMemcpyAsync(&e, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+        NQES_CUDA(cudaStreamSynchronize(ctx->st));
+        // res(i, k) = Re diag(V^-1 (sum_i / Ns) V)_k  (code/rbm.cc:761-769)
+        cplx vinv[16];
+        if (!small_inv(evecs, vinv, K)) {
+            ctx->err = "eigenvector matrix is singular";
+            return NQES_ERR_INVALID;
+        }
+        const double ns = double(chains) * m;
+        auto finish = [&](size_t off, size_t rows, double *dst) {
+            for (size_t r = 0; r < rows; r++) {
+                cplx mat[16], t1[16];
+                for (int q = 0; q < KK; q++) mat[q] = to_c(h[off + r * KK + q]) * (1.0 / ns);
+                for (int a = 0; a < K; a++)
+                    for (int b = 0; b < K; b++) {
+                        cplx s{0, 0};
+                        for (int t = 0; t < K; t++) s += vinv[a * K + t] * mat[t * K + b];
+                        t1[a * K + b] = s;
+                    }
+                for (int k = 0; k < K; k++) {
+                    cplx s{0, 0};
+                    for (int t = 0; t < K; t++) s += t1[k * K + t] * evecs[t * K + k];
+                    dst[r * K + k] = s.re;
+                }
+            }
+        };
+        finish(0, N, x);
+        finish(size_t(N) * KK, N, z);
+        finish(2 * size_t(N) * KK, size_t(N) * N, xx);
+        finish(2 * size_t(N) * KK + size_t(N) * N * KK, size_t(N) * N, zz);
+        if (e & (kErrNonFinite | kErrSingular)) {
+            ctx->err = "non-finite value or singular Phi in the correlation pass (error bits " + std::to_string(e) + ")";
+            return NQES_ERR_NONFINITE;
+        }
+        return NQES_OK;
+    };
+    rc = run();
+    dfree(acc); dfree(scratch); dfree(out); dfree(spins);
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int nqes_correlations(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, const double *evecs, double *x,
+                      double *z, double *xx, double *zz) {
+    if (!ctx || !evecs || !x || !z || !xx || !zz || chains < 1 || m < 1 || burn < 0) {
+        if (ctx) ctx->err = "invalid correlation arguments";
+        return NQES_ERR_INVALID;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const int arith = resolve_arith(ctx);
+    const cplx *V = reinterpret_cast<const cplx *>(evecs);
+    return arith == NQES_ARITH_COMPLEX ? correlations_t<cplx>(ctx, seed, chains, m, burn, V, x, z, xx, zz)
+                                       : correlations_t<double>(ctx, seed, chains, m, burn, V, x, z, xx, zz);
 }
 
 }  // extern "C"

@@ -47,7 +47,14 @@ template <class S> struct SampleArgs {
     // kernel evaluates Phi / tanh(theta) / E / O at cfg[c] for c < chains.
     const uint64_t *cfg;
     cplx *phi_out, *tanh_out;   // chains × K², chains × M × K² (optional)
+    // Correlation mode (corr != nullptr): per-chain sums of the x, z, xx, zz
+    // observables instead of E and O; layout per chain [x N×K²][z N×K²]
+    // [xx N×N×K²][zz N×N×K²] (corr_stride scalars), scratch N×N×K² per chain.
+    S *corr, *corr_scratch;
+    size_t corr_stride;
 };
+
+template <class S> cudaError_t launch_corr_reduce(const S *acc, int chains, size_t stride, S *out, cudaStream_t st);
 
 enum : int {
     kErrNonFinite = 1,      // a non-finite amplitude ratio, energy or derivative
@@ -57,7 +64,7 @@ enum : int {
 };
 
 size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith);
-int sample_threads(int K, int tk);  // K*tk unit threads + one decision warp
+int sample_threads(int K, int tk);  // K*tk threads per chain
 template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st);
 template <class S> cudaError_t launch_tables(const Shape &sh, const cplx *a, const cplx *w, S *ch, S *shh, S *eup,
                                              S *edn, cudaStream_t st);

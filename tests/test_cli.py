@@ -1,0 +1,143 @@
+"""The drop-in executable rbm-matfree-N{N}-M{M}-K{K}-opt.
+
+CPU tests: the command-line surface of the reference (code/rbm.cc:900-961
+through code/argparse.h) — help, missing/invalid arguments (exit 255),
+-c 0 (exit 1), unknown options — and the MAT v5 reader/writer against scipy.
+GPU test: a short run whose printed energies, dumped weights and correlation
+file agree with the CPU oracle driven through the same schedule."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import helpers
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+BIN = os.path.join(ROOT, "nqes-trapped-ion_gb300", "bin")
+
+
+@pytest.fixture(scope="module")
+def exe():
+    ge._load_build_module().build_cli([(8, 16, 2)])
+    return os.path.join(BIN, "rbm-matfree-N8-M16-K2-opt")
+
+
+def run(cmd, **kw):
+    return subprocess.run(cmd, capture_output=True, text=True, timeout=600, **kw)
+
+
+def test_help_lists_the_reference_options(exe):
+    r = run([exe, "-?"])
+    assert r.returncode == 0
+    assert r.stdout.startswith("This program computes the lowest 2 energy eigenstates")
+    for key in ["--model", "-n,--niters", "-m,--mc-steps-percpu", "-c,--ncpus", "--burn-in-steps", "--tol",
+                "--reglam-init", "--reglam-cutoff", "--minres-rtol", "--correlation-data", "--dump-rbm",
+                "--throw-fperror", "--load-rbm"]:
+        assert key in r.stdout, key
+
+
+def test_missing_and_invalid_arguments(exe):
+    r = run([exe, "--model", "trappedion", "-h", "1", "-n", "2", "-m", "3"])
+    assert r.returncode == 255
+    assert r.stderr.strip() == "Argument missing: -c,--ncpus (Specify the number of CPU cores to use.)"
+    r = run([exe, "--model", "nope", "-h", "1", "-n", "2", "-m", "3", "-c", "1", "--correlation-data", "x.mat"])
+    assert r.returncode == 255
+    assert "enum is only accepting [ising, periodicising, hs, xxz, longrange, trappedion]" in r.stderr
+    r = run([exe, "--model", "TRAPPEDION", "-h", "abc", "-n", "2", "-m", "3", "-c", "1", "--correlation-data", "x"])
+    assert r.returncode == 255 and r.stderr.startswith('Invalid argument, could not convert "abc" for -h')
+
+
+def test_zero_chains_and_unknown_option(exe):
+    r = run([exe, "--model", "trappedion", "-h", "1", "-n", "2", "-m", "3", "-c", "0", "--correlation-data", "x",
+             "--bogus", "1"])
+    assert r.returncode == 1
+    assert "unrecognised commandline argument: bogus" in r.stderr
+    assert "Number of CPU cores cannot be zero." in r.stderr
+
+
+@pytest.fixture(scope="module")
+def mat_driver(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("drv") / "mat_driver")
+    cli = os.path.join(ROOT, "nqes-trapped-ion_gb300", "cli")
+    subprocess.run(["g++", "-std=c++20", "-O1", "-I", cli, os.path.join(ROOT, "tests", "mat_driver.cc"),
+                    os.path.join(cli, "matv5.cc"), "-o", out], check=True)
+    return out
+
+
+def test_mat_reader_reads_scipy_files(mat_driver, tmp_path):
+    sio = pytest.importorskip("scipy.io")
+    rng = np.random.default_rng(0)
+    a = rng.normal(size=(2, 5)) + 1j * rng.normal(size=(2, 5))
+    w = rng.normal(size=(2, 5, 3)) + 1j * rng.normal(size=(2, 5, 3))
+    J = rng.normal(size=(4, 4))
+    f = str(tmp_path / "w.mat")
+    sio.savemat(f, {"a": a, "w": w, "J": J, "N": 4})
+    out = run([mat_driver, "read", f]).stdout.strip().split("\n")
+    got = {ln.split()[0]: ln.split()[1:] for ln in out}
+    for name, arr in [("a", a), ("w", w), ("J", J)]:
+        fields = got[name]
+        cpx, rank = int(fields[0]), int(fields[1])
+        dims = tuple(int(d) for d in fields[2:2 + rank])
+        vals = np.array([float(v) for v in fields[2 + rank:]])
+        assert dims == arr.shape and cpx == int(np.iscomplexobj(arr))
+        flat = arr.ravel(order="F")
+        want = np.stack([flat.real, flat.imag], -1).ravel() if cpx else flat
+        assert np.array_equal(vals, want)
+    assert [float(v) for v in got["N"][4:]] == [4.0]
+
+
+def test_mat_writer_is_read_by_scipy(mat_driver, tmp_path):
+    sio = pytest.importorskip("scipy.io")
+    f = str(tmp_path / "o.mat")
+    assert run([mat_driver, "write", f]).returncode == 0
+    d = sio.loadmat(f)
+    want_a = (np.arange(6) + 0.25 - 1j * (np.arange(6) + 0.5)).reshape(2, 3, order="F")
+    assert np.array_equal(d["a"], want_a)
+    assert np.array_equal(d["xx"], (np.arange(8) * 1.5).reshape(2, 2, 2, order="F"))
+
+
+@pytest.mark.gpu
+def test_executable_matches_oracle_schedule(exe, tmp_path):
+    sio = pytest.importorskip("scipy.io")
+    N, M, K, h = 8, 16, 2, 0.595
+    seed, chains, m, burn, niters = 31, 8, 25, 8, 4
+    w0 = helpers.random_weights(N, M, K, 0.05, 2, real=False)
+    wfile = str(tmp_path / "w0.mat")
+    sio.savemat(wfile, {"a": w0[0], "b": w0[1], "w": w0[2]})
+    corr = str(tmp_path / "corr.mat")
+    prefix = str(tmp_path / "out")
+    args = [exe, "--model", "trappedion", "-h", str(h), "-n", str(niters), "-m", str(m), "-c", str(chains),
+            "--burn-in-steps", str(burn), "--seed", str(seed), "--load-rbm", wfile, "--reglam-init", "5",
+            "--minres-rtol", "1e-9", "--tol", "1e-12", "--correlation-data", corr, "--dump-rbm", prefix]
+    r = run(args)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().split("\n")
+    assert lines[0] == f"Random seed is {seed}"
+    got = np.array([[float(v) for v in ln.split()] for ln in lines[1:1 + niters]])
+    # oracle through the same schedule (code/rbm.cc:1178-1196)
+    orc = helpers.Oracle(N, M, K, helpers.synthetic_j(N), h)
+    orc.set_weights(*w0)
+    lr, reglam = 0.1, 5.0
+    want = []
+    for it in range(niters):
+        e, _ = orc.sr_step(seed + it * chains, chains, m, burn, max(lr, 0.01), max(reglam, 0.001), 1e-9, 2 ** 63)
+        e = e / N
+        lr *= 0.99
+        reglam *= 0.9
+        want.append(np.sort(np.linalg.eigvals(e).real))
+    want = np.array(want)
+    assert np.allclose(got, want, rtol=0, atol=2e-5), (got, want)  # printed with 6 significant digits
+    d = sio.loadmat(prefix + f"N{N}M{M}K{K}.mat")
+    ao, bo, wo = orc.get_weights()
+    assert np.max(np.abs(d["w"] - wo)) <= 1e-5 * np.max(np.abs(wo))
+    # correlations with the oracle's own eigenvectors of the last e_mat, sorted by eigenvalue
+    ev, V = np.linalg.eig(e)
+    order = np.argsort(ev.real)
+    x, z, xx, zz = orc.correlations(seed + niters * chains, chains, m, burn, V)
+    c = sio.loadmat(corr)
+    assert np.allclose(c["x"], x[:, order], atol=1e-6)
+    assert np.allclose(c["z"], z[:, order], atol=1e-6)
+    assert np.allclose(c["xx"], xx[:, order].reshape(N, N, K), atol=1e-6)
+    assert np.allclose(c["zz"], zz[:, order].reshape(N, N, K), atol=1e-6)

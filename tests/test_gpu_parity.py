@@ -166,3 +166,17 @@ def test_training_reaches_exact_diagonalisation(pkg):
     assert np.all(final >= want - 2e-3), (final, want)          # variational (up to noise)
     assert np.all(np.abs(final - want) < 0.01 * np.abs(want)), (final, want)
     ctx.close()
+
+
+@pytest.mark.parametrize("N,M,K,real", [(6, 12, 2, False), (8, 16, 2, True), (5, 10, 3, False)])
+def test_correlations_match_oracle(pkg, N, M, K, real):
+    """x, z, xx, zz from one correlation pass (code/rbm.cc:730-826): same chains
+    as the reference's four passes with one seed, results within 1e-10."""
+    ctx, orc = make_pair(pkg, N, M, K, 0.8, 0.15, 40 + N, real)
+    rng = np.random.default_rng(N)
+    V = rng.normal(size=(K, K)) + 1j * rng.normal(size=(K, K))
+    got = ctx.correlations(77, 6, 15, 5, V)
+    want = orc.correlations(77, 6, 15, 5, V)
+    for g, w in zip(got, want):
+        assert np.max(np.abs(g - w)) <= 1e-10 * max(1.0, np.max(np.abs(w)))
+    ctx.close()
