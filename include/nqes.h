@@ -50,6 +50,24 @@ extern "C" {
 #define NQES_OPT_ARITH 1             /* NQES_ARITH_* (default AUTO) */
 #define NQES_OPT_THREADS_PER_BLOCK 2 /* sampler threads per RBM column block: 32, 64, 128 or 0 = autotune */
 #define NQES_OPT_MINRES_CAP 3        /* device-side MINRES-QLP iteration cap (default 100000) */
+#define NQES_OPT_PRECISION 4         /* NQES_PRECISION_* (default FP64) */
+#define NQES_OPT_REJECT_FILTER 5     /* 1: FP32 rejection filter in the FP64 real sampler; 0 (default): off.
+                                      * The filter skips the FP64 work of proposals that a rigorous
+                                      * FP32 bound proves rejected, in sweeps that follow a sweep with
+                                      * under 50% acceptance; results are bit-identical either way. */
+#define NQES_OPT_MIXED_EXACT 6       /* 1: MIXED takes every accept decision by its exact FP64 path
+                                      * (verification of that path); 0 (default): only when the FP32
+                                      * bound cannot decide. */
+
+/* Precision of the SR step (nqes_set_option NQES_OPT_PRECISION).
+ * FP64: every quantity in FP64, as the reference.
+ * MIXED (real weights only): factors, ratio products and accept decisions
+ *   in FP32 with a certified error bound and an exact FP64 decision whenever
+ *   the bound cannot decide, so the Markov chains are the FP64 chains;
+ *   theta, Phi, local-energy sums, moments, MINRES-QLP and the update in FP64;
+ *   log-derivatives stored in FP32 and the two O passes of S·v in FP32. */
+#define NQES_PRECISION_FP64 0
+#define NQES_PRECISION_MIXED 1
 
 typedef struct nqes_ctx nqes_ctx;
 
@@ -66,6 +84,8 @@ typedef struct nqes_step_info {
     double eloc_re, eloc_im;     /* mean local energy (trace of e_mat) */
     double ms_total;             /* device time of the step, CUDA events */
     uint64_t kernel_launches;    /* kernels this step launched (graph nodes run, loop bodies counted) */
+    int precision;               /* NQES_PRECISION_* used */
+    uint64_t exact_decisions;    /* MIXED: accept decisions the FP32 bound left to the exact FP64 path */
 } nqes_step_info;
 
 /* Kernels nqes_time_kernel can time in isolation. */

@@ -22,7 +22,9 @@ LIB_PATH = os.path.join(PKG_DIR, "lib", "libnqes.so")
 OK = 0
 ERR_CUDA, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_INVALID, ERR_STATE = -1, -2, -3, -4, -5, -6
 ARITH_AUTO, ARITH_COMPLEX, ARITH_REAL = 0, 1, 2
-OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP = 1, 2, 3
+OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP, OPT_PRECISION = 1, 2, 3, 4
+OPT_REJECT_FILTER, OPT_MIXED_EXACT = 5, 6
+PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 EXPORTS = [
     "nqes_create", "nqes_destroy", "nqes_last_error", "nqes_set_option", "nqes_set_weights", "nqes_get_weights",
@@ -47,6 +49,7 @@ class StepInfo(ctypes.Structure):
         ("xnorm", ctypes.c_double), ("accepted", ctypes.c_uint64), ("proposals", ctypes.c_uint64),
         ("warnings", ctypes.c_int), ("eloc_re", ctypes.c_double), ("eloc_im", ctypes.c_double),
         ("ms_total", ctypes.c_double), ("kernel_launches", ctypes.c_uint64),
+        ("precision", ctypes.c_int), ("exact_decisions", ctypes.c_uint64),
     ]
 
     def as_dict(self):

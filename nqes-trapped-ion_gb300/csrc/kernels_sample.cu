@@ -32,6 +32,8 @@
 // reference derives from Phi (the ratio |det Phi'|^2/|det Phi|^2, Phi^-1 H Phi
 // and the log-derivatives) is invariant under row scaling, and power-of-two
 // scaling is exact, so this changes no result while keeping Phi in range.
+#include <type_traits>
+
 #include "nqes_internal.h"
 #include "pcg64.cuh"
 
@@ -91,12 +93,13 @@ template <class S> struct Smem {
     double *jk;
     int *pe, *rowe, *flag;
     uint64_t *spin;
+    float *t32, *red32, *rbd32;  // rejection filter: FP32 tanh(theta), per-warp products and bounds
 };
 
 __host__ __device__ inline size_t smem_bytes(int N, int M, int K, size_t ssz) {
     size_t KK = size_t(K) * K;
     size_t nS = KK * M + 2 * KK + 32 + 2 * KK * N + 2 * KK + KK + 32;
-    return nS * ssz + 8 * 4 + 8 * kMaxSpinWords + 4 * (32 + 4 + 4);
+    return nS * ssz + 8 * 4 + 8 * kMaxSpinWords + 4 * (32 + 4 + 4) + 4 * (KK * M + 64);
 }
 
 template <class S> __device__ inline Smem<S> carve(unsigned char *base, int N, int M, int K) {
@@ -118,7 +121,11 @@ template <class S> __device__ inline Smem<S> carve(unsigned char *base, int N, i
     int *ip = reinterpret_cast<int *>(s.spin + kMaxSpinWords);
     s.pe = ip; ip += 32;
     s.rowe = ip; ip += 4;
-    s.flag = ip;
+    s.flag = ip; ip += 4;
+    float *fp = reinterpret_cast<float *>(ip);
+    s.t32 = fp; fp += KK * M;
+    s.red32 = fp; fp += 32;
+    s.rbd32 = fp;
     return s;
 }
 
@@ -273,8 +280,32 @@ template <class S> __device__ void corr_sample(const SampleArgs<S> &A, Smem<S> &
     }
 }
 
-template <class S, int UMAX>
-__global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
+// Rejection filter (FILT, real arithmetic). Most proposals are rejected, and a
+// rejection changes no state, so the FP64 work of a proposal is needed only
+// when it might be accepted. Each proposal is first evaluated in FP32 from
+// FP32 roundings of the FP64 tables and of tanh(theta), with a rigorous bound
+// on its distance from the FP64 value:
+//   factor f = c - sigma t s: c, s, t and the fma each rounded once, so
+//     |f32 - f| <= (2 cond + 1) u |f|,  cond = (|c| + |t s|) / |f|;
+//   product r of the M factors: sum of the factors' bounds plus one rounding
+//     per product, beta = u (3 sum cond + 2M + 16) with slack for the FP64
+//     value's own rounding;
+//   x_kk = r e^{-2 sigma a} g_kk and det' = sum_kk x_kk: four more roundings
+//     per term and K for the sum, |det'32 - det'64| <= 1.02 sum beta |x| +
+//     (8 + K) u sum |x| (1.02 turns bounds relative to the FP64 values into
+//     bounds relative to the computed ones while beta < 0.01).
+// When (|det'32| + bound)^2 < u |det|^2 with a margin for the roundings of
+// the comparison itself, the FP64 test u |det|^2 <= |det'|^2 fails for
+// certain and the proposal is rejected without FP64 work. Every other
+// proposal runs the FP64 code unchanged, so the chains, Phi, tanh(theta) and
+// all results are bit-identical to the unfiltered kernel. The filter's
+// determinant and g_kk are FP32 copies scaled by 2^-expo(det) so that
+// |det|^2 stays within FP32 range; det == 0, non-finite values, FP32 over-
+// or underflow and large bounds all fall through to FP64.
+constexpr float kU32 = 5.9604645e-8f;  // FP32 unit roundoff 2^-24
+
+template <class S, int UMAX, bool FILT>
+__global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K, L = A.sh.L;
     const size_t P = size_t(A.sh.P);
@@ -309,6 +340,23 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
     S det = zero<S>(), g = zero<S>(), phik = zero<S>();
     double detn = 0.0;
     unsigned long long nacc = 0;
+    // Filter copies, identical in every thread: g_kk / 2^e and (det / 2^e)^2, e = expo(det).
+    float g32[4] = {0.f, 0.f, 0.f, 0.f}, dn32 = 0.f;
+    auto filt_setup = [&]() {
+        if constexpr (FILT) {
+            const int e = is_zero(det) ? 0 : expo(det);
+            const double ds = scale2(det, -e);
+            dn32 = float(ds * ds);
+#pragma unroll
+            for (int kk = 0; kk < 4; kk++)
+                if (kk < K) g32[kk] = float(scale2(__shfl_sync(0xffffffffu, g, kk), -e));
+        }
+    };
+    // The filter pays when most proposals are rejected: a sweep runs it when
+    // the chain's previous sweep accepted fewer than half of its proposals
+    // (a count every thread holds, so the choice is uniform in the CTA).
+    bool filt_next = FILT;
+    unsigned long long nacc_sweep = 0;
     const bool writer = tid == 0;  // the one thread that commits shared state
 
     const int total = A.cfg ? 1 : A.burn + A.m;
@@ -317,11 +365,20 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
             // ---- one sweep: proposals k outer, i inner (code/rbm.cc:536-551) ----
             det = small_det(sm.phi, K);  // recomputed at every sweep, as code/rbm.cc:533
             detn = norm2(det);
+            const bool use_f = filt_next;
+            if constexpr (FILT) {
+                if (use_f) {
+                    for (int t = tid; t < KK * M; t += T) sm.t32[t] = float(sm.tnh[t]);
+                    __syncthreads();
+                }
+                nacc_sweep = nacc;
+            }
             for (int k = 0; k < K; k++) {
                 if (lane < K) {
                     phik = sm.phi[k * K + lane];
                     g = phik * cofactor(sm.phi, K, k, lane);
                 }
+                if (use_f) filt_setup();
                 S *trow = sm.tnh + (k * K + my_kk) * M;
                 for (int i = 0; i < N; i++) {
                     const int par = (i & 1) * 16;  // reduction slots alternate between proposals
@@ -329,14 +386,78 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
                     const S *crow = A.tab.ch + (size_t(my_kk) * N + i) * M;
                     const S *srow = A.tab.sh + (size_t(my_kk) * N + i) * M;
                     S tq[UMAX], cq[UMAX], sq[UMAX], fq[UMAX];
+                    uint64_t draw = 0;
+                    bool loaded = false;
+                    if (FILT && use_f) {
+                        // ---- FP32 stage: certain rejections skip the FP64 stage ----
+                        loaded = true;
+                        const float *c32 = A.c32 + (size_t(my_kk) * N + i) * M;
+                        const float *s32 = A.s32 + (size_t(my_kk) * N + i) * M;
+                        const float *t32 = sm.t32 + (k * K + my_kk) * M;
+                        float p32 = 1.f, eb = 0.f;
+#pragma unroll
+                        for (int q = 0; q < UMAX; q++) {
+                            const int j = my_jl + q * TK;
+                            if (j < M) {
+                                const float t = t32[j], cc = __ldg(c32 + j), ss = __ldg(s32 + j);
+                                const float f = fmaf(down ? t : -t, ss, cc);
+                                p32 *= f;
+                                eb = fmaf(fabsf(cc) + fabsf(t * ss), __frcp_rn(fabsf(f)), eb);
+                                // operands of the FP64 stage, loaded while the filter runs
+                                tq[q] = trow[j];
+                                cq[q] = ldg(crow + j);
+                                sq[q] = ldg(srow + j);
+                            }
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) {
+                            p32 *= __shfl_xor_sync(0xffffffffu, p32, o);
+                            eb += __shfl_xor_sync(0xffffffffu, eb, o);
+                        }
+                        if (lane == 0) {
+                            sm.red32[par + warp] = p32;
+                            sm.rbd32[par + warp] = eb;
+                        }
+                        float ea32[4];
+#pragma unroll
+                        for (int kk = 0; kk < 4; kk++)
+                            ea32[kk] = kk < K ? __ldg((down ? A.ed32 : A.eu32) + kk * N + i) : 0.f;
+                        draw = pcg_next(rng);
+                        const float ud32 = __ull2float_rn(draw) * 0x1p-64f * dn32;
+                        __syncthreads();
+                        float sx = 0.f, sab = 0.f, eterm = 0.f, bmax = 0.f;
+#pragma unroll
+                        for (int kk = 0; kk < 4; kk++) {
+                            if (kk < K) {
+                                float r = sm.red32[par + kk * WK], e2 = sm.rbd32[par + kk * WK];
+                                for (int w2 = 1; w2 < WK; w2++) {
+                                    r *= sm.red32[par + kk * WK + w2];
+                                    e2 += sm.rbd32[par + kk * WK + w2];
+                                }
+                                const float beta = kU32 * (3.f * e2 + 2.f * float(M) + 16.f);
+                                const float xx = r * ea32[kk] * g32[kk];
+                                sx += xx;
+                                sab += fabsf(xx);
+                                eterm = fmaf(beta, fabsf(xx), eterm);
+                                bmax = fmaxf(bmax, beta);
+                            }
+                        }
+                        const float hi = fabsf(sx) + 1.02f * eterm + (8.f + float(K)) * kU32 * sab;
+                        if (bmax < 0.01f && ud32 > 1e-30f && ud32 < 1e30f &&
+                            hi * hi * (1.f + 4.f * kU32) < ud32 * (1.f - 8.f * kU32))
+                            continue;  // rejected: no state changes (same in every thread)
+                    }
+                    // ---- FP64 stage (the whole proposal when unfiltered) ----
                     S prod = one<S>();
 #pragma unroll
                     for (int q = 0; q < UMAX; q++) {
                         const int j = my_jl + q * TK;
                         if (j < M) {
-                            tq[q] = trow[j];
-                            cq[q] = ldg(crow + j);
-                            sq[q] = ldg(srow + j);
+                            if (!loaded) {
+                                tq[q] = trow[j];
+                                cq[q] = ldg(crow + j);
+                                sq[q] = ldg(srow + j);
+                            }
                             // f = cosh(ws) - tanh * sinh(ws), ws = 2 sigma w
                             fq[q] = mad(neg_if(tq[q], !down), sq[q], cq[q]);
                             prod = q == 0 ? fq[q] : prod * fq[q];
@@ -350,7 +471,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
                         ea = ldg((down ? A.tab.edn : A.tab.eup) + lane * N + i);
                         eg = ea * g;
                     }
-                    const double ud = pcg_uniform(rng) * detn;
+                    const double ud = (loaded ? pcg_u01(draw) : pcg_uniform(rng)) * detn;
                     __syncthreads();
                     // det Phi' = sum_kk r_kk e^{-2 sigma a} g_kk over lanes 0..K-1 (K <= 4)
                     S x = zero<S>(), r = one<S>();
@@ -372,7 +493,11 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
 #pragma unroll
                         for (int q = 0; q < UMAX; q++) {
                             const int j = my_jl + q * TK;
-                            if (j < M) trow[j] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * rcp(fq[q]);
+                            if (j < M) {
+                                trow[j] = mad(tq[q], cq[q], neg_if(sq[q], !down)) * rcp(fq[q]);
+                                if constexpr (FILT)
+                                    if (use_f) sm.t32[(k * K + my_kk) * M + j] = float(trow[j]);
+                            }
                         }
                         if (lane < K) {
                             g = x;
@@ -391,6 +516,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
                             detn = norm2(det);
                             if (writer) sm.rowe[k] += ex;
                         }
+                        if (use_f) filt_setup();
                         if (warp == 0 && lane < K) sm.phi[k * K + lane] = phik;
                         // Other warps may already read bit i+1 of this word: the
                         // read sees bit i+1 unchanged before or after the flip.
@@ -400,6 +526,7 @@ __global__ void __launch_bounds__(kMaxThreads) k_sample(const SampleArgs<S> A) {
                 }
                 __syncthreads();
             }
+            if constexpr (FILT) filt_next = (nacc - nacc_sweep) * 2 < (unsigned long long)(K * N);
             if (sw < A.burn) continue;
         }
         // ---- sample: local energy and log-derivatives ----
@@ -533,29 +660,50 @@ size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith) {
 int sample_threads(int K, int tk) { return K * tk; }
 
 // Sets the sampler's dynamic shared-memory limit; call outside stream capture.
-template <class S> cudaError_t prepare_sample(const Shape &sh) {
-    const int smem = int(smem_bytes(sh.N, sh.M, sh.K, sizeof(S)));
-    cudaError_t e = cudaFuncSetAttribute(k_sample<S, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample<S, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample<S, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample<S, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+template <class S, bool FILT> cudaError_t prepare_variants(int smem) {
+    cudaError_t e = cudaFuncSetAttribute(k_sample<S, 1, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_sample<S, 2, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_sample<S, 4, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_sample<S, 8, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     return e;
 }
 
-// Launch with the smallest compiled units-per-thread bound that covers M/TK.
+template <class S> cudaError_t prepare_sample(const Shape &sh) {
+    const int smem = int(smem_bytes(sh.N, sh.M, sh.K, sizeof(S)));
+    cudaError_t e = prepare_variants<S, false>(smem);
+    if constexpr (std::is_same<S, double>::value)
+        if (e == cudaSuccess) e = prepare_variants<S, true>(smem);
+    return e;
+}
+
+template <class S, bool FILT> void launch_variant(const SampleArgs<S> &a, int U, int threads, size_t smem, cudaStream_t st) {
+    if (U <= 1)
+        k_sample<S, 1, FILT><<<a.chains, threads, smem, st>>>(a);
+    else if (U <= 2)
+        k_sample<S, 2, FILT><<<a.chains, threads, smem, st>>>(a);
+    else if (U <= 4)
+        k_sample<S, 4, FILT><<<a.chains, threads, smem, st>>>(a);
+    else
+        k_sample<S, 8, FILT><<<a.chains, threads, smem, st>>>(a);
+}
+
+// Launch with the smallest compiled units-per-thread bound that covers M/TK;
+// the rejection filter runs when the FP32 tables are given (real arithmetic).
 template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st) {
     const size_t smem = smem_bytes(a.sh.N, a.sh.M, a.sh.K, sizeof(S));
     const int U = (a.sh.M + a.tk - 1) / a.tk;
     if (threads != sample_threads(a.sh.K, a.tk) || threads > kMaxThreads || U > kUMax || a.tk % 32)
         return cudaErrorInvalidConfiguration;
-    if (U <= 1)
-        k_sample<S, 1><<<a.chains, threads, smem, st>>>(a);
-    else if (U <= 2)
-        k_sample<S, 2><<<a.chains, threads, smem, st>>>(a);
-    else if (U <= 4)
-        k_sample<S, 4><<<a.chains, threads, smem, st>>>(a);
-    else
-        k_sample<S, 8><<<a.chains, threads, smem, st>>>(a);
+    bool filt = false;
+    if constexpr (std::is_same<S, double>::value) filt = a.c32 && a.s32 && a.eu32 && a.ed32;
+    if (filt) {
+        if constexpr (std::is_same<S, double>::value) launch_variant<S, true>(a, U, threads, smem, st);
+    } else {
+        launch_variant<S, false>(a, U, threads, smem, st);
+    }
     return cudaGetLastError();
 }
 

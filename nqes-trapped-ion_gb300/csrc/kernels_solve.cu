@@ -16,6 +16,7 @@
 //   * the update w -= lr x of code/rbm.cc:699-717.
 // All sums use a fixed order, so results are reproducible run to run.
 #include <cmath>
+#include <type_traits>
 
 #include "nqes_internal.h"
 
@@ -88,8 +89,8 @@ __global__ void k_emat(int Ns, int K, const cplx *E, cplx *emat, cplx *eloc) {
 }
 
 // Partial column sums over a chunk of rows: o, |O|^2 and E_loc conj(O).
-template <class S>
-__global__ void k_moment_part(int Ns, int P, int K, int rchunks, const S *O, const cplx *E, S *po, double *ps2,
+template <class S, class TO>
+__global__ void k_moment_part(int Ns, int P, int K, int rchunks, const TO *O, const cplx *E, S *po, double *ps2,
                               S *pf) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = blockIdx.y;
@@ -159,11 +160,48 @@ template <class S> __global__ void k_sv_cols(int Ns, int P, int rchunks, const S
     ypart[size_t(r) * P + p] = acc;
 }
 
+// FP32 passes of the mixed form: u = O v and partial O^T u with FP32 storage
+// and FP32 accumulation (real arithmetic).
+__global__ void k_sv_rows_f32(int Ns, int P, const float *O, const float *v, float *u) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= Ns) return;
+    const float *row = O + size_t(warp) * P;
+    float acc = 0.f;
+    for (int p = lane; p < P; p += 32) acc = fmaf(row[p], __ldg(v + p), acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) u[warp] = acc;
+}
+
+__global__ void k_sv_cols_f32(int Ns, int P, int rchunks, const float *O, const float *u, float *ypart) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.y;
+    if (p >= P) return;
+    const int s0 = int(int64_t(Ns) * r / rchunks), s1 = int(int64_t(Ns) * (r + 1) / rchunks);
+    float acc = 0.f;
+    for (int s = s0; s < s1; s++) acc = fmaf(O[size_t(s) * P + p], __ldg(u + s), acc);
+    ypart[size_t(r) * P + p] = acc;
+}
+
+__global__ void k_to_f32(int n, const double *x, float *y) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) y[t] = float(x[t]);
+}
+
+__device__ __forceinline__ void mirror_f32(float *v32, int p, double v) {
+    if (v32) v32[p] = float(v);
+}
+__device__ __forceinline__ void mirror_f32(float *, int, cplx) {}
+
 // out = ypart-sum / Ns + skk v - (o·v) conj(o), with o·v from per-block partials.
 template <class S>
 __device__ __forceinline__ S sv_epilogue(const SolveBufs<S> &B, int p, const S *v, S ov) {
     S y = zero<S>();
-    for (int r = 0; r < B.rchunks; r++) y = y + B.ypart[size_t(r) * B.sh.P + p];
+    if (B.O32) {
+        for (int r = 0; r < B.rchunks; r++) y = y + one<S>() * double(B.ypart32[size_t(r) * B.sh.P + p]);
+    } else {
+        for (int r = 0; r < B.rchunks; r++) y = y + B.ypart[size_t(r) * B.sh.P + p];
+    }
     y = y * (1.0 / double(B.Ns));
     y = mad(B.skk[p], v[p], y);
     y = y - ov * conj(B.o[p]);
@@ -251,6 +289,7 @@ template <class S> __global__ void k_minres_first_v(SolveBufs<S> B) {
     if (p < P) {
         const S v = B.r3[p] * (1.0 / beta);
         B.v[p] = v;
+        mirror_f32(B.v32, p, v);
         t = B.o[p] * v;
     }
     S s = block_sum_s(t, sh);
@@ -567,6 +606,7 @@ template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
         if (q.running) {
             const S vn = B.r3[p] * (1.0 / q.betan);
             B.v[p] = vn;
+            mirror_f32(B.v32, p, vn);
             ovt = B.o[p] * vn;
         }
     }
@@ -603,7 +643,11 @@ template <class S> cudaError_t launch_moments(const SolveBufs<S> &B, cudaStream_
     S *pf = B.ypart + size_t(B.rchunks) * P;
     double *ps2 = reinterpret_cast<double *>(B.ypart + size_t(2) * B.rchunks * P);
     dim3 g(nb, B.rchunks);
-    k_moment_part<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
+    if constexpr (std::is_same<S, double>::value) {
+        if (B.O32) k_moment_part<S, float><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O32, B.E, po, ps2, pf);
+    }
+    if (!B.O32)
+        k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
     k_moment_final<S><<<nb, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.sp, po, ps2, pf, B.eloc, B.o, B.skk, B.f,
                                                    B.err);
     return cudaGetLastError();
@@ -617,12 +661,20 @@ template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &B, cudaStr
     return cudaGetLastError();
 }
 
+// u = O v then the row-chunk partials of O^H u. In the mixed form v must
+// already be mirrored in B.v32.
 template <class S> static void launch_sv_passes(const SolveBufs<S> &B, const S *v, cudaStream_t st) {
     const int P = B.sh.P, nb = (P + kVecThreads - 1) / kVecThreads;
     const int rows_per_block = kVecThreads / 32;
-    k_sv_rows<S><<<(B.Ns + rows_per_block - 1) / rows_per_block, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u);
+    const int rb = (B.Ns + rows_per_block - 1) / rows_per_block;
     dim3 g(nb, B.rchunks);
-    k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart);
+    if (B.O32) {
+        k_sv_rows_f32<<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O32, B.v32, B.u32);
+        k_sv_cols_f32<<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O32, B.u32, B.ypart32);
+    } else {
+        k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u);
+        k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart);
+    }
 }
 
 template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &B, cudaStream_t st) {
@@ -637,14 +689,21 @@ template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &B, cudaStr
 
 template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &B, cudaStream_t st) {
     const int rows_per_block = kVecThreads / 32;
-    k_sv_rows<S><<<(B.Ns + rows_per_block - 1) / rows_per_block, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O, B.v, B.u);
+    const int rb = (B.Ns + rows_per_block - 1) / rows_per_block;
+    if (B.O32)
+        k_sv_rows_f32<<<rb, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O32, B.v32, B.u32);
+    else
+        k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O, B.v, B.u);
     return cudaGetLastError();
 }
 
 template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &B, cudaStream_t st) {
     const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
     dim3 g(nb, B.rchunks);
-    k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O, B.u, B.ypart);
+    if (B.O32)
+        k_sv_cols_f32<<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O32, B.u32, B.ypart32);
+    else
+        k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O, B.u, B.ypart);
     return cudaGetLastError();
 }
 
@@ -654,13 +713,18 @@ template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &B, cu
     S *pf = B.ypart + size_t(B.rchunks) * P;
     double *ps2 = reinterpret_cast<double *>(B.ypart + size_t(2) * B.rchunks * P);
     dim3 g(nb, B.rchunks);
-    k_moment_part<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
+    if constexpr (std::is_same<S, double>::value) {
+        if (B.O32) k_moment_part<S, float><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O32, B.E, po, ps2, pf);
+    }
+    if (!B.O32)
+        k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
     return cudaGetLastError();
 }
 
 template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &B, const S *v, S *out, cudaStream_t st) {
     const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
     k_ov_part<S><<<nb, kVecThreads, 0, st>>>(B.sh.P, B.o, v, B.ovpart);
+    if (B.O32) k_to_f32<<<nb, kVecThreads, 0, st>>>(B.sh.P, reinterpret_cast<const double *>(v), B.v32);
     launch_sv_passes(B, v, st);
     k_apply_out<S><<<nb, kVecThreads, 0, st>>>(B, v, out);
     return cudaGetLastError();

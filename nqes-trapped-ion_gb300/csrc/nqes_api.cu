@@ -15,6 +15,7 @@
 #include <cstring>
 #include <random>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/nqes.h"
@@ -29,8 +30,17 @@ struct nqes_ctx {
     cudaStream_t st = nullptr;
     double h = 0;
     int arith_opt = NQES_ARITH_AUTO;
+    int precision = NQES_PRECISION_FP64;
+    // mixed-precision tables: FP32 cosh/sinh(2w), exp(-+2a); FP64 real w, a, b
+    float *mch = nullptr, *msh = nullptr, *meup = nullptr, *medn = nullptr;
+    double *mw = nullptr, *ma = nullptr, *mb = nullptr;
+    unsigned long long *exact = nullptr;           // per chain
+    float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
+    int step_precision = NQES_PRECISION_FP64;      // precision of the allocated step buffers
     int tk_opt = 0;
     uint64_t minres_cap = 100000;
+    bool reject_filter = false;  // FP32 rejection filter in the FP64 real sampler (opt-in)
+    bool mixed_exact_all = false;  // MIXED: every decision through the exact FP64 path
     bool weights_real = true;
     std::string err;
 
@@ -54,7 +64,7 @@ struct nqes_ctx {
     int rchunks = 1;
 
     cudaGraphExec_t exec = nullptr;
-    int g_chains = -1, g_m = -1, g_burn = -1, g_arith = -1, g_tk = -1;
+    int g_chains = -1, g_m = -1, g_burn = -1, g_arith = -1, g_tk = -1, g_prec = -1;
     bool have_step = false;
     int last_burn = 0, last_tk = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -105,6 +115,10 @@ void free_step_buffers(nqes_ctx *ctx) {
     dfree(ctx->vecs);
     dfree(ctx->ovpart);
     dfree(ctx->part);
+    dfree(ctx->exact);
+    dfree(ctx->v32);
+    dfree(ctx->u32);
+    dfree(ctx->ypart32);
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
     ctx->exec = nullptr;
     ctx->g_chains = -1;
@@ -114,7 +128,9 @@ void free_step_buffers(nqes_ctx *ctx) {
 }
 
 int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
-    if (ctx->chains == chains && ctx->m == m && ctx->arith == arith && ctx->O) return NQES_OK;
+    if (ctx->chains == chains && ctx->m == m && ctx->arith == arith && ctx->step_precision == ctx->precision &&
+        ctx->O)
+        return NQES_OK;
     free_step_buffers(ctx);
     const Shape &sh = ctx->sh;
     const size_t Ns = size_t(chains) * m, P = size_t(sh.P), ss = ssize(arith);
@@ -123,7 +139,15 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     ctx->rchunks = std::max(1, std::min(32, int((Ns + 255) / 256)));
     ctx->rchunks = std::max(1, std::min(ctx->rchunks, std::max(1, 600 / std::max(1, ctiles))));
     int rc;
-    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * ss))) return rc;
+    const bool mixed = ctx->precision == NQES_PRECISION_MIXED;
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * (mixed ? sizeof(float) : ss))))
+        return rc;
+    if (mixed) {
+        if ((rc = dalloc(ctx, &ctx->exact, size_t(chains))) || (rc = dalloc(ctx, &ctx->v32, P)) ||
+            (rc = dalloc(ctx, &ctx->u32, Ns)) || (rc = dalloc(ctx, &ctx->ypart32, size_t(ctx->rchunks) * P)))
+            return rc;
+    }
+    ctx->step_precision = ctx->precision;
     if ((rc = dalloc(ctx, &ctx->E, Ns * sh.K * sh.K))) return rc;
     if ((rc = dalloc(ctx, &ctx->spins, Ns * sh.K * sh.NW))) return rc;
     if ((rc = dalloc(ctx, &ctx->accepted, size_t(chains)))) return rc;
@@ -173,7 +197,46 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     B.eloc = ctx->eloc_d;
     B.err = ctx->err_d;
     B.use_cond = 0;
+    if (ctx->step_precision == NQES_PRECISION_MIXED) {
+        B.O = nullptr;
+        B.O32 = static_cast<const float *>(ctx->O);
+        B.v32 = ctx->v32;
+        B.u32 = ctx->u32;
+        B.ypart32 = ctx->ypart32;
+    }
     return B;
+}
+
+MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
+    MixedArgs A{};
+    A.sh = ctx->sh;
+    A.chains = chains;
+    A.m = m;
+    A.burn = burn;
+    A.tk = tk;
+    A.sp = ctx->sp;
+    A.ch = ctx->mch;
+    A.sh32 = ctx->msh;
+    A.eup = ctx->meup;
+    A.edn = ctx->medn;
+    A.w64 = ctx->mw;
+    A.a64 = ctx->ma;
+    A.b64 = ctx->mb;
+    A.J = ctx->J;
+    A.h = ctx->h;
+    A.O = static_cast<float *>(ctx->O);
+    A.E = ctx->E;
+    A.spins = ctx->spins;
+    A.accepted = ctx->accepted;
+    A.exact = ctx->exact;
+    A.err = ctx->err_d;
+    A.exact_all = ctx->mixed_exact_all ? 1 : 0;
+    return A;
+}
+
+cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
+    return launch_tables_mixed(ctx->sh, ctx->a, ctx->b, ctx->w, ctx->mch, ctx->msh, ctx->meup, ctx->medn, ctx->mw,
+                               ctx->ma, ctx->mb, ctx->st);
 }
 
 template <class S> Tables<S> tables(nqes_ctx *ctx) {
@@ -201,13 +264,23 @@ template <class S> SampleArgs<S> sample_args(nqes_ctx *ctx, int chains, int m, i
     A.spins = ctx->spins;
     A.accepted = ctx->accepted;
     A.err = ctx->err_d;
+    if (std::is_same<S, double>::value && ctx->reject_filter) {
+        A.c32 = ctx->mch;
+        A.s32 = ctx->msh;
+        A.eu32 = ctx->meup;
+        A.ed32 = ctx->medn;
+    }
     return A;
 }
 
+// The sampler's per-step tables; with the rejection filter (real arithmetic)
+// also their FP32 roundings.
 template <class S> cudaError_t launch_tables_ctx(nqes_ctx *ctx) {
     Tables<S> t = tables<S>(ctx);
-    return launch_tables<S>(ctx->sh, ctx->a, ctx->w, const_cast<S *>(t.ch), const_cast<S *>(t.sh),
-                            const_cast<S *>(t.eup), const_cast<S *>(t.edn), ctx->st);
+    cudaError_t e = launch_tables<S>(ctx->sh, ctx->a, ctx->w, const_cast<S *>(t.ch), const_cast<S *>(t.sh),
+                                     const_cast<S *>(t.eup), const_cast<S *>(t.edn), ctx->st);
+    if (e == cudaSuccess && std::is_same<S, double>::value && ctx->reject_filter) e = launch_tables_mixed_ctx(ctx);
+    return e;
 }
 
 // Threads per RBM column block (TK): at most eight hidden units per thread,
@@ -238,12 +311,16 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     const int threads = sample_threads(ctx->sh.K, tk);
     {
         // the sampler's dynamic shared memory attribute must be set before capture
-        const size_t smem = sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
+        const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
+        const size_t smem = mixed ? mixed_smem_bytes(ctx->sh) : sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
         if (smem > 227 * 1024) {
             ctx->err = "shape needs " + std::to_string(smem) + " bytes of shared memory per chain";
             return NQES_ERR_INVALID;
         }
-        NQES_CUDA(prepare_sample<S>(ctx->sh));
+        if (mixed)
+            NQES_CUDA(prepare_sample_mixed(ctx->sh));
+        else
+            NQES_CUDA(prepare_sample<S>(ctx->sh));
     }
     cudaGraph_t g = nullptr, gA = nullptr, gC = nullptr;
     NQES_CUDA(cudaGraphCreate(&g, 0));
@@ -255,8 +332,14 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
 
     NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->st);
-    cudaError_t le = launch_tables_ctx<S>(ctx);
-    if (le == cudaSuccess) le = launch_sample<S>(A, threads, ctx->st);
+    cudaError_t le;
+    if (ctx->step_precision == NQES_PRECISION_MIXED) {
+        le = launch_tables_mixed_ctx(ctx);
+        if (le == cudaSuccess) le = launch_sample_mixed(mixed_args(ctx, chains, m, burn, tk), ctx->st);
+    } else {
+        le = launch_tables_ctx<S>(ctx);
+        if (le == cudaSuccess) le = launch_sample<S>(A, threads, ctx->st);
+    }
     if (le == cudaSuccess) le = launch_moments<S>(B, ctx->st);
     if (le == cudaSuccess) le = launch_minres_init<S>(B, ctx->st);
     cudaError_t ce = cudaStreamEndCapture(ctx->st, &gA);
@@ -303,6 +386,7 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     ctx->g_burn = burn;
     ctx->g_arith = ctx->arith;
     ctx->g_tk = tk;
+    ctx->g_prec = ctx->step_precision;
     return NQES_OK;
 }
 
@@ -341,7 +425,7 @@ int copy_out_c(nqes_ctx *ctx, const void *src, size_t n, double *dst) {
 template <class S> int sr_step_t(nqes_ctx *ctx, int chains, int m, int burn) {
     const int tk = choose_tk(ctx, chains);
     if (!ctx->exec || ctx->g_chains != chains || ctx->g_m != m || ctx->g_burn != burn || ctx->g_arith != ctx->arith ||
-        ctx->g_tk != tk) {
+        ctx->g_tk != tk || ctx->g_prec != ctx->step_precision) {
         int rc = build_graph<S>(ctx, chains, m, burn, tk);
         if (rc) return rc;
     }
@@ -399,7 +483,10 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
         (rc = dalloc(ctx, &ctx->w, nw)) || (rc = dalloc(ctx, &ctx->J, size_t(N) * N)) ||
         (rc = dalloc(ctx, reinterpret_cast<cplx **>(&ctx->tab), 2 * nw + 2 * na)) ||
         (rc = dalloc(ctx, &ctx->sp, 1)) || (rc = dalloc(ctx, &ctx->qs, 1)) || (rc = dalloc(ctx, &ctx->err_d, 1)) ||
-        (rc = dalloc(ctx, &ctx->emat_d, 16)) || (rc = dalloc(ctx, &ctx->eloc_d, 1)))
+        (rc = dalloc(ctx, &ctx->emat_d, 16)) || (rc = dalloc(ctx, &ctx->eloc_d, 1)) ||
+        (rc = dalloc(ctx, &ctx->mch, nw)) || (rc = dalloc(ctx, &ctx->msh, nw)) || (rc = dalloc(ctx, &ctx->meup, na)) ||
+        (rc = dalloc(ctx, &ctx->medn, na)) || (rc = dalloc(ctx, &ctx->mw, nw)) || (rc = dalloc(ctx, &ctx->ma, na)) ||
+        (rc = dalloc(ctx, &ctx->mb, size_t(K) * M)))
         return fail(rc);
     if (cudaMallocHost(&ctx->sp_host, sizeof(StepParams)) != cudaSuccess ||
         cudaMallocHost(&ctx->qs_host, sizeof(QlpState)) != cudaSuccess ||
@@ -429,6 +516,13 @@ int nqes_destroy(nqes_ctx *ctx) {
     dfree(ctx->w);
     dfree(ctx->J);
     dfree(ctx->tab);
+    dfree(ctx->mch);
+    dfree(ctx->msh);
+    dfree(ctx->meup);
+    dfree(ctx->medn);
+    dfree(ctx->mw);
+    dfree(ctx->ma);
+    dfree(ctx->mb);
     dfree(ctx->sp);
     dfree(ctx->qs);
     dfree(ctx->err_d);
@@ -472,6 +566,28 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
             return NQES_ERR_INVALID;
         }
         ctx->minres_cap = uint64_t(value);
+        return NQES_OK;
+    case NQES_OPT_PRECISION:
+        if (value != NQES_PRECISION_FP64 && value != NQES_PRECISION_MIXED) {
+            ctx->err = "precision must be NQES_PRECISION_FP64 or NQES_PRECISION_MIXED";
+            return NQES_ERR_INVALID;
+        }
+        ctx->precision = int(value);
+        return NQES_OK;
+    case NQES_OPT_REJECT_FILTER:
+    case NQES_OPT_MIXED_EXACT:
+        if (value != 0 && value != 1) {
+            ctx->err = "option value must be 0 or 1";
+            return NQES_ERR_INVALID;
+        }
+        if (option == NQES_OPT_REJECT_FILTER)
+            ctx->reject_filter = value == 1;
+        else
+            ctx->mixed_exact_all = value == 1;
+        if (ctx->exec) {  // the captured step bakes the sampler variant in
+            cudaGraphExecDestroy(ctx->exec);
+            ctx->exec = nullptr;
+        }
         return NQES_OK;
     default:
         ctx->err = "unknown option " + std::to_string(option);
@@ -544,6 +660,10 @@ int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, doub
     }
     NQES_CUDA(cudaSetDevice(ctx->device));
     const int arith = resolve_arith(ctx);
+    if (ctx->precision == NQES_PRECISION_MIXED && arith != NQES_ARITH_REAL) {
+        ctx->err = "mixed precision needs real weights (NQES_ARITH_REAL)";
+        return NQES_ERR_INVALID;
+    }
     int rc = ensure_step_buffers(ctx, chains, m, arith);
     if (rc) return rc;
     StepParams &p = *ctx->sp_host;
@@ -587,6 +707,12 @@ int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, doub
         // tables, sampler, 3 moment kernels, 3 MINRES-QLP init kernels, update,
         // and 6 kernels per execution of the loop body
         info->kernel_launches = 9 + 6 * q.bodies;
+        info->precision = ctx->step_precision;
+        if (ctx->step_precision == NQES_PRECISION_MIXED) {
+            std::vector<unsigned long long> ex(chains);
+            NQES_CUDA(cudaMemcpy(ex.data(), ctx->exact, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
+            for (auto x : ex) info->exact_decisions += x;
+        }
     }
     const int e = *ctx->err_host;
     if (e & (kErrNonFinite | kErrMinresNonFinite)) {
@@ -712,6 +838,16 @@ int nqes_get_O(nqes_ctx *ctx, int first, int count, double *O) {
     }
     NQES_CUDA(cudaSetDevice(ctx->device));
     const size_t P = ctx->sh.P;
+    if (ctx->step_precision == NQES_PRECISION_MIXED) {
+        std::vector<float> tmp(size_t(count) * P);
+        NQES_CUDA(cudaMemcpy(tmp.data(), static_cast<const float *>(ctx->O) + size_t(first) * P,
+                             tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        for (size_t t = 0; t < tmp.size(); t++) {
+            O[2 * t] = tmp[t];
+            O[2 * t + 1] = 0.0;
+        }
+        return NQES_OK;
+    }
     const unsigned char *src = static_cast<const unsigned char *>(ctx->O) + size_t(first) * P * ssize(ctx->arith);
     return copy_out_c(ctx, src, size_t(count) * P, O);
 }
@@ -788,6 +924,8 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
     auto launch = [&]() -> cudaError_t {
         switch (kernel) {
         case NQES_KERNEL_SAMPLE: {
+            if (ctx->step_precision == NQES_PRECISION_MIXED)
+                return launch_sample_mixed(mixed_args(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk), ctx->st);
             SampleArgs<S> A = sample_args<S>(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
             return launch_sample<S>(A, sample_threads(ctx->sh.K, ctx->last_tk), ctx->st);
         }
@@ -802,7 +940,18 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
     case NQES_KERNEL_SV_COLS: *bytes = double(Ns) * P * ss + double(Ns) * ss + double(ctx->rchunks) * P * ss; break;
     default: *bytes = double(Ns) * P * ss + double(Ns) * KK * sizeof(cplx) + 3.0 * ctx->rchunks * P * ss; break;
     }
-    if (kernel == NQES_KERNEL_SAMPLE) NQES_CUDA(prepare_sample<S>(ctx->sh));
+    const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
+    if (mixed && kernel != NQES_KERNEL_MOMENTS) {
+        // FP32 O: the sampler writes 4 bytes per entry, the S·v passes read 4
+        const double s32 = double(Ns) * P * (ss - sizeof(float));
+        *bytes -= s32;
+    }
+    if (kernel == NQES_KERNEL_SAMPLE) {
+        if (mixed)
+            NQES_CUDA(prepare_sample_mixed(ctx->sh));
+        else
+            NQES_CUDA(prepare_sample<S>(ctx->sh));
+    }
     NQES_CUDA(launch());  // warm-up
     NQES_CUDA(cudaStreamSynchronize(ctx->st));
     NQES_CUDA(cudaEventRecord(ctx->ev0, ctx->st));

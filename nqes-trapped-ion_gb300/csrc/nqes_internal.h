@@ -52,9 +52,37 @@ template <class S> struct SampleArgs {
     // [xx N×N×K²][zz N×N×K²] (corr_stride scalars), scratch N×N×K² per chain.
     S *corr, *corr_scratch;
     size_t corr_stride;
+    // Rejection filter (real arithmetic only; nullptr = off): FP32 roundings
+    // of the FP64 tables cosh(2w), sinh(2w), exp(-2a), exp(2a).
+    const float *c32, *s32, *eu32, *ed32;
 };
 
 template <class S> cudaError_t launch_corr_reduce(const S *acc, int chains, size_t stride, S *out, cudaStream_t st);
+
+// Mixed-precision sampler (real weights): FP32 factors, products and accept
+// decisions with a certified error bound, FP64 shadow of theta, exact FP64
+// Phi after every sweep, exact FP64 decision when the bound is inconclusive.
+struct MixedArgs {
+    Shape sh;
+    int chains, m, burn, tk;
+    const StepParams *sp;
+    const float *ch, *sh32, *eup, *edn;  // FP32 cosh(2w), sinh(2w) [kk][i][j]; exp(-2a), exp(2a) [kk][i]
+    const double *w64, *a64, *b64;       // real weights [kk][i][j], [kk][i], [kk][j]
+    const double *J;
+    double h;
+    float *O;                            // Ns × P log-derivatives in FP32
+    cplx *E;                             // Ns × K² local-energy matrices (FP64)
+    uint64_t *spins;
+    unsigned long long *accepted;        // per chain
+    unsigned long long *exact;           // per chain: decisions taken by the exact FP64 path
+    int *err;
+    int exact_all;                       // 1: every decision through the exact FP64 path (test hook)
+};
+size_t mixed_smem_bytes(const Shape &sh);
+cudaError_t prepare_sample_mixed(const Shape &sh);
+cudaError_t launch_sample_mixed(const MixedArgs &a, cudaStream_t st);
+cudaError_t launch_tables_mixed(const Shape &sh, const cplx *a, const cplx *b, const cplx *w, float *ch, float *sh32,
+                                float *eup, float *edn, double *w64, double *a64, double *b64, cudaStream_t st);
 
 enum : int {
     kErrNonFinite = 1,      // a non-finite amplitude ratio, energy or derivative
@@ -119,6 +147,11 @@ template <class S> struct SolveBufs {
     int *err;
     cudaGraphConditionalHandle cond;
     int use_cond;
+    // Mixed precision (real arithmetic only): O stored in FP32 and the two
+    // O passes of S·v in FP32 with FP32 accumulation; v is mirrored into v32
+    // by the kernels that produce it. Null in the FP64 form.
+    const float *O32;
+    float *v32, *u32, *ypart32;
 };
 
 template <class S> cudaError_t launch_moments(const SolveBufs<S> &b, cudaStream_t st);

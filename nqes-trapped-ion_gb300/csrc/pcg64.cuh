@@ -60,11 +60,12 @@ __host__ __device__ __forceinline__ uint64_t pcg_next(Pcg64 &g) {
     return (x >> rot) | (x << ((64u - rot) & 63u));
 }
 
-// libstdc++ generate_canonical<double, 53> on a 64-bit engine.
-__device__ __forceinline__ double pcg_uniform(Pcg64 &g) {
-    double u = __ull2double_rn(pcg_next(g)) * 0x1p-64;
+// libstdc++ generate_canonical<double, 53> of one 64-bit engine output.
+__device__ __forceinline__ double pcg_u01(uint64_t x) {
+    double u = __ull2double_rn(x) * 0x1p-64;
     return u >= 1.0 ? 0x1.fffffffffffffp-1 : u;
 }
+__device__ __forceinline__ double pcg_uniform(Pcg64 &g) { return pcg_u01(pcg_next(g)); }
 
 // bernoulli_distribution(0.5): true (spin down) iff u < 0.5.
 __device__ __forceinline__ bool pcg_bernoulli_half(Pcg64 &g) { return pcg_uniform(g) < 0.5; }

@@ -180,3 +180,76 @@ def test_correlations_match_oracle(pkg, N, M, K, real):
     for g, w in zip(got, want):
         assert np.max(np.abs(g - w)) <= 1e-10 * max(1.0, np.max(np.abs(w)))
     ctx.close()
+
+
+@pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 32, 20), (12, 24, 3, 8, 20)])
+def test_mixed_precision_keeps_fp64_chains(pkg, N, M, K, chains, m):
+    """MIXED: FP32 decisions with a certified bound and an exact FP64 fallback
+    give the FP64 chains bit for bit; energies within 1e-6 relative, FP32
+    log-derivatives within 1e-5, the updated weights within 1e-5 (the solve
+    runs its O passes in FP32)."""
+    J = synthetic_j(N)
+    w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 5 + N, real=True)
+    out = {}
+    for prec in (pkg.PRECISION_FP64, pkg.PRECISION_MIXED):
+        ctx = pkg.Context(N, M, K, J, 0.595)
+        ctx.set_weights(*w)
+        ctx.set_option(pkg.OPT_PRECISION, prec)
+        e, info = ctx.sr_step(4242, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
+        spins, eloc, E = ctx.get_samples()
+        out[prec] = dict(e=e, info=info, spins=spins, E=E, O=ctx.get_O(0, 4), acc=ctx.get_accepts(),
+                         mom=ctx.get_moments(), w=np.concatenate([x.ravel() for x in ctx.get_weights()]))
+        ctx.close()
+    f, x = out[0], out[1]
+    assert np.array_equal(f["spins"], x["spins"]), "mixed chains left the FP64 chains"
+    assert np.array_equal(f["acc"], x["acc"])
+    assert x["info"]["precision"] == 1
+    assert rel_err(x["E"], f["E"]) < 1e-5
+    assert rel_err(x["e"], f["e"]) < 1e-6
+    assert rel_err(x["O"], f["O"]) < 1e-5
+    assert rel_err(x["mom"][0], f["mom"][0]) < 1e-5
+    assert rel_err(x["w"], f["w"]) < 1e-5
+
+
+@pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 24, 20), (12, 24, 3, 8, 20),
+                                            (16, 300, 4, 4, 6), (20, 40, 1, 8, 10)])
+def test_reject_filter_is_bit_identical(pkg, N, M, K, chains, m):
+    """The FP32 rejection filter only skips FP64 work of proposals it proves
+    rejected: configurations, accept counts, E, O, moments, e_mat and the
+    updated weights are bit-identical with the filter on and off."""
+    J = synthetic_j(N)
+    w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 3 + N, real=True)
+    out = []
+    for filt in (0, 1):
+        ctx = pkg.Context(N, M, K, J, 0.595)
+        ctx.set_weights(*w)
+        ctx.set_option(pkg.OPT_REJECT_FILTER, filt)
+        e, info = ctx.sr_step(777, chains, m, 6, 0.1, 5.0, 1e-9, 2000)
+        spins, eloc, E = ctx.get_samples()
+        out.append(dict(e=e, spins=spins, E=E, O=ctx.get_O(0, chains * m), acc=ctx.get_accepts(),
+                        mom=ctx.get_moments(), w=np.concatenate([x.ravel() for x in ctx.get_weights()])))
+        ctx.close()
+    for key in out[0]:
+        for a, b in zip(out[0][key] if isinstance(out[0][key], tuple) else [out[0][key]],
+                        out[1][key] if isinstance(out[1][key], tuple) else [out[1][key]]):
+            assert np.array_equal(a, b), key
+
+
+@pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (12, 24, 3, 8, 20)])
+def test_mixed_exact_path_keeps_fp64_chains(pkg, N, M, K, chains, m):
+    """MIXED with every accept decision taken by its exact FP64 path follows
+    the FP64 chains."""
+    J = synthetic_j(N)
+    w = helpers.random_weights(N, M, K, 0.05, 5 + N, real=True)
+    spins = []
+    for prec in (pkg.PRECISION_FP64, pkg.PRECISION_MIXED):
+        ctx = pkg.Context(N, M, K, J, 0.595)
+        ctx.set_weights(*w)
+        ctx.set_option(pkg.OPT_PRECISION, prec)
+        ctx.set_option(pkg.OPT_MIXED_EXACT, 1)
+        e, info = ctx.sr_step(4242, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
+        spins.append(ctx.get_samples()[0])
+        if prec == pkg.PRECISION_MIXED:
+            assert info["exact_decisions"] > 0
+        ctx.close()
+    assert np.array_equal(spins[0], spins[1])
