@@ -158,7 +158,8 @@ int nqes_apply_S(nqes_ctx *ctx, const double *v, double *out);
  * back-to-back launches of one kernel (NQES_KERNEL_*) on the last step's
  * shapes and data, and the algorithmic bytes one launch moves (inputs read +
  * outputs written once). For benchmarks; re-running the sampler overwrites
- * the last step's samples with the same values (same seed). */
+ * the last step's samples (same seed, the current weights: after an SR step
+ * these are the updated ones, so the samples change). */
 int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double *algorithmic_bytes);
 
 /* ---- S·v without allocation ----

@@ -19,7 +19,8 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_solve.cu", "nqes_api.cu", "sv_static.cu"]
+SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_sample_warp.cu", "kernels_solve.cu",
+           "nqes_api.cu", "sv_static.cu"]
 HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

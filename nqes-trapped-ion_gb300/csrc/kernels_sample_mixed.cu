@@ -39,12 +39,6 @@ __device__ __forceinline__ int expo32(float x) {
     return b == 0 ? 0 : b - 127;
 }
 
-// log cosh x = |x| + log1p(exp(-2|x|)) - log 2, in FP64
-__device__ __forceinline__ double logcosh(double x) {
-    const double a = fabs(x);
-    return a + log1p(exp(-2.0 * a)) - 0.69314718055994530942;
-}
-
 struct MSmem {
     double *th, *phi, *pinv, *Dm, *jk, *lsum;
     float *t, *red, *rbd, *rat, *bsig, *Bm;
@@ -83,26 +77,62 @@ __device__ inline MSmem mcarve(unsigned char *base, int N, int M, int K) {
     return s;
 }
 
-// Exact Phi from theta (FP64): Phi[k][kk] = exp(sum_i sigma_i a_i + sum_j log cosh theta_j),
-// rows scaled by their largest entry. Block-wide; ends with a barrier.
-__device__ void resync_phi(const MixedArgs &A, MSmem &sm) {
-    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K;
+// log Phi[k][kk] up to a constant common to every entry, exactly in FP64:
+//   sum_i sigma_i a_i + sum_j log cosh theta_j
+//     = sum_i sigma_i a_i + sum_j |theta_j| + log prod_j (1 + e^{-2|theta_j|}) - M log 2,
+// one exp per hidden unit and one log per entry (each factor lies in (1, 2],
+// so the product stays in range for M <= 512). With a proposal (flip of spin i)
+// the same for the flipped configuration, theta'_j = theta_j - 2 sigma_i w_ij.
+// Warps kk < K write lsum[k*K + kk] (current) and lsum[16 + kk] (proposed).
+__device__ void row_logsums(const MixedArgs &A, MSmem &sm, int k, int i, bool with_new) {
+    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    for (int q = warp; q < KK; q += nwarp) {
-        const int k = q / K, kk = q - k * K;
-        double s = 0.0;
-        for (int j = lane; j < M; j += 32) s += logcosh(sm.th[q * M + j]);
-        for (int i = lane; i < N; i += 32) s += down_bit(sm.spin + k * NW, i) ? -A.a64[kk * N + i] : A.a64[kk * N + i];
-        s = warp_sum(s);
-        if (lane == 0) sm.lsum[q] = s;
+    const bool down = with_new && down_bit(sm.spin + k * NW, i);
+    for (int kk = warp; kk < K; kk += nwarp) {
+        const int q = k * K + kk;
+        double lin = 0.0, pr = 1.0, lin2 = 0.0, pr2 = 1.0;
+        for (int j = lane; j < M; j += 32) {
+            const double th = sm.th[q * M + j];
+            lin += fabs(th);
+            pr *= 1.0 + exp(-2.0 * fabs(th));
+            if (with_new) {
+                const double w = A.w64[(size_t(kk) * N + i) * M + j];
+                const double th2 = down ? th + 2.0 * w : th - 2.0 * w;
+                lin2 += fabs(th2);
+                pr2 *= 1.0 + exp(-2.0 * fabs(th2));
+            }
+        }
+        double as = 0.0;
+        for (int i2 = lane; i2 < N; i2 += 32) as += down_bit(sm.spin + k * NW, i2) ? -A.a64[kk * N + i2] : A.a64[kk * N + i2];
+        lin = warp_sum(lin);
+        as = warp_sum(as);
+        pr = warp_prod(pr);
+        if (with_new) {
+            lin2 = warp_sum(lin2);
+            pr2 = warp_prod(pr2);
+        }
+        if (lane == 0) {
+            sm.lsum[q] = as + lin + log(pr);
+            if (with_new) {
+                const double ai = A.a64[kk * N + i];
+                sm.lsum[16 + kk] = as + (down ? 2.0 * ai : -2.0 * ai) + lin2 + log(pr2);
+            }
+        }
     }
+}
+
+// Exact row k of Phi from theta (FP64), scaled by the row's largest entry.
+// Block-wide; starts and ends with a barrier (theta and the spins were just
+// written by other threads).
+__device__ void resync_row(const MixedArgs &A, MSmem &sm, int k) {
+    const int K = A.sh.K;
+    __syncthreads();
+    row_logsums(A, sm, k, 0, false);
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int k = 0; k < K; k++) {
-            double mx = -1e308;
-            for (int kk = 0; kk < K; kk++) mx = fmax(mx, sm.lsum[k * K + kk]);
-            for (int kk = 0; kk < K; kk++) sm.phi[k * K + kk] = exp(sm.lsum[k * K + kk] - mx);
-        }
+        double mx = -1e308;
+        for (int kk = 0; kk < K; kk++) mx = fmax(mx, sm.lsum[k * K + kk]);
+        for (int kk = 0; kk < K; kk++) sm.phi[k * K + kk] = exp(sm.lsum[k * K + kk] - mx);
     }
     __syncthreads();
 }
@@ -174,7 +204,7 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
         sm.t[u] = tanhf(float(th));
     }
     __syncthreads();
-    resync_phi(A, sm);
+    for (int k = 0; k < K; k++) resync_row(A, sm, k);
 
     // Decision state, identical in every warp. Lane kk < K holds the swept
     // row's Phi[k][kk] (phik) and g_kk = Phi[k][kk] cof(k, kk) in FP32, and
@@ -212,10 +242,12 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
         rho = 0.f;
     };
 
+    // Every row of Phi is exact (recomputed from theta) when its sweep starts:
+    // rows are recomputed at the end of every row that changed.
     const int total = A.burn + A.m;
     for (int sw = 0; sw < total; sw++) {
-        det_setup();  // Phi is exact here (recomputed from theta)
         for (int k = 0; k < K; k++) {
+            det_setup();
             row_setup(k);
             for (int i = 0; i < N; i++) {
                 const int par = (i & 1) * 16;
@@ -231,7 +263,7 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
                         const float t = sm.t[q * M + j], cc = __ldg(crow + j), ss = __ldg(srow + j);
                         const float f = fmaf(down ? t : -t, ss, cc);  // c - sigma t s
                         prod *= f;
-                        eb = fmaf(fabsf(cc) + fabsf(t * ss), __frcp_rn(fabsf(f)), eb);
+                        eb = fmaf(fabsf(cc) + 6.f * fabsf(t * ss), __frcp_rn(fabsf(f)), eb);
                     }
                 }
 #pragma unroll
@@ -259,10 +291,10 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
                     // |r - exact| <= beta |r|. Per factor f = c - sigma t s: c and s
                     // rounded once from FP64, t = tanhf(float(theta)) within 5 roundings
                     // (2 ulp, and the argument's rounding times theta sech^2 / tanh <= 1),
-                    // one rounding of the fma: (6 cond + 1) u; the reciprocal in cond
-                    // is itself rounded, covered by the constant term; then one
-                    // rounding per product, and the tables' own rounding.
-                    beta = kEps * (6.f * ebk + 2.f * float(M) + 16.f);
+                    // one rounding of the fma: ((|c| + 6 |t s|) / |f| + 1) u, summed
+                    // in ebk without the 1; then one rounding per product. The
+                    // constant covers the rounding of ebk itself and of the FP64 values.
+                    beta = kEps * (ebk + 2.f * float(M) + 16.f);
                     const float re = r * ea;
                     x = re * g32;
                     // drift of Phi: every Leibniz term of g takes one entry from each
@@ -283,48 +315,44 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
                 {
                     const float ad = fabsf(s), lo = ad - ed, hi = ad + ed;
                     const float dd = fabsf(det32), dlo = fmaxf(dd - edet, 0.f), dhi = dd + edet;
-                    const float su = u32 * (1.f + 8.f * kEps);
-                    const float sl = u32 * (1.f - 8.f * kEps);
+                    const float su = u32 * (1.f + 16.f * kEps);
+                    const float sl = u32 * (1.f - 16.f * kEps);
                     if (A.exact_all || !(dd > 1e-15f) || !(dd < 1e15f) || !(bmax < 0.01f)) {
                         // det == 0 (accepted, code/rbm.cc:542), squares outside the
                         // normal range or a loose bound: the exact path decides
                         exact_path = true;
-                    } else if (lo > 0.f && lo * lo * (1.f - 4.f * kEps) >= su * dhi * dhi) {
+                    } else if (lo > 0.f && lo * lo * (1.f - 16.f * kEps) >= su * dhi * dhi) {
                         acc = true;
-                    } else if (!(hi * hi * (1.f + 4.f * kEps) < sl * dlo * dlo)) {
+                    } else if (!(hi * hi * (1.f + 16.f * kEps) < sl * dlo * dlo)) {
                         exact_path = true;  // NaN lands here as well
                     }
                 }
                 if (exact_path) {
-                    // exact FP64 decision: Phi from theta, ratio from log cosh differences
-                    resync_phi(A, sm);
-                    for (int kk = warp; kk < K; kk += nwarp) {
-                        const int qq = k * K + kk;
-                        double lr = 0.0;
-                        for (int j = lane; j < M; j += 32) {
-                            const double th = sm.th[qq * M + j], w = A.w64[(size_t(kk) * N + i) * M + j];
-                            lr += logcosh(down ? th + 2.0 * w : th - 2.0 * w) - logcosh(th);
-                        }
-                        // log of the ratio: -2 sigma a_i plus the hidden units' log cosh differences
-                        lr = warp_sum(lr) + (down ? 2.0 * A.a64[kk * N + i] : -2.0 * A.a64[kk * N + i]);
-                        if (lane == 0) sm.lsum[16 + kk] = lr;
-                    }
+                    // Exact FP64 decision. The other rows of Phi are exact (recomputed
+                    // at their row's end); row k, current and proposed, from theta.
+                    row_logsums(A, sm, k, i, true);
                     __syncthreads();
-                    const double det_e = small_det(sm.phi, K);
-                    double xs = 0.0, rexact = 0.0;
+                    double xc = 0.0, xn = 0.0, pc = 0.0, pn = 0.0;
                     if (lane < K) {
+                        double mx = -1e308;
+                        for (int kk = 0; kk < K; kk++) mx = fmax(mx, sm.lsum[k * K + kk]);
                         double cof, cabs;
                         cofactors(sm.phi, K, k, lane, cof, cabs);
-                        rexact = exp(sm.lsum[16 + lane]);
-                        xs = rexact * sm.phi[k * K + lane] * cof;
+                        pc = exp(sm.lsum[k * K + lane] - mx);
+                        pn = exp(sm.lsum[16 + lane] - mx);
+                        xc = pc * cof;
+                        xn = pn * cof;
                     }
-                    double sx = xs + shfl_xor(xs, 1);
+                    double det_e = xc + shfl_xor(xc, 1);
+                    det_e = det_e + shfl_xor(det_e, 2);
+                    det_e = __shfl_sync(0xffffffffu, det_e, 0);
+                    double sx = xn + shfl_xor(xn, 1);
                     sx = sx + shfl_xor(sx, 2);
                     sx = __shfl_sync(0xffffffffu, sx, 0);
                     acc = det_e == 0.0 || pcg_u01(draw) * (det_e * det_e) <= sx * sx;
                     nexact++;
                     __syncthreads();  // every warp has read Phi before row k changes
-                    if (acc && warp == 0 && lane < K) sm.phi[k * K + lane] *= rexact;
+                    if (warp == 0 && lane < K) sm.phi[k * K + lane] = acc ? pn : pc;
                     __syncthreads();
                     // continue from the exact state
                     det_setup();
@@ -375,12 +403,12 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
                     nacc++;
                 }
             }
-            // the row's tracked entries back into Phi (its other rows' cofactors read them)
-            if (row_changed && warp == 0 && lane < K) sm.phi[k * K + lane] = double(phik);
-            __syncthreads();
+            // row k exact again before the next row's cofactors read it
+            if (row_changed)
+                resync_row(A, sm, k);
+            else
+                __syncthreads();
         }
-        // exact Phi after every sweep (bounds restart from zero drift)
-        resync_phi(A, sm);
         if (sw < A.burn) continue;
 
         // ---- sample: local energy (FP32 ratios, FP64 combination) and FP32 O ----

@@ -1,0 +1,663 @@
+// Mixed-precision sampler, decision-warp form (real weights, up to 16 hidden
+// units per lane). Same chains and same certified FP32 decisions as the
+// block form in kernels_sample_mixed.cu (code/rbm.cc:530-552 trajectories),
+// laid out for latency:
+//
+// One warp (warp 0 of the chain's CTA) runs every proposal of a row. Its
+// lanes form K groups of G lanes (G the largest power of two <= 32/K); lane
+// (kk, jl) owns hidden units j = jl*U .. jl*U+U-1 of RBM kk and keeps their
+// tanh(theta) and theta (as an FP32 pair, hi + lo) in registers for the whole
+// row. A proposal is U fused multiply-adds, a log2(G)-level shuffle tree
+// inside each group and K broadcasts; every lane then holds all K products
+// and takes the accept decision itself, so a proposal needs no CTA barrier
+// and no shared-memory round trip. An accepted flip adds -2 sigma w to the
+// lane's theta pairs (double-float addition) and recomputes tanh in FP32: no
+// FP64 instruction on the proposal path.
+//
+// At the end of a row that changed, the whole CTA (the other warps wait at a
+// barrier meanwhile) rebuilds that row's theta from the spins as double-float
+// sums of b and the +-w, recomputes tanh, and recomputes the row of Phi in
+// FP64 from log Phi = sum_i sigma_i a_i + sum_j |theta_j| +
+// log prod_j (1 + e^{-2|theta_j|}) (up to a constant), so every row of Phi is
+// exact (to ~1e-12 relative) whenever another row is swept. The FP32 bound
+// on a decision therefore only carries the drift of the current row.
+//
+// Decision bound (all in units of u = 2^-24), per factor f = c - sigma t s
+// with c, s rounded once from FP64 and t = tanhf(theta_hi) within 5 u |t|:
+// ((|c| + 6 |t s|) / |f| + 1) u; per product one rounding; so the row's ratio
+// r_kk has relative error beta_kk = u (sum_j (|c| + 6|t s|)/|f| + 2M + 16).
+// det Phi' = sum_kk r_kk e^{-2 sigma a} g_kk with g_kk = Phi[k][kk] cof(k, kk)
+// (cofactors exact, from the other rows): the bound adds four roundings per
+// term, the drift rho of row k (sum of the accepted ratios' bounds) and the
+// rounding of the sum. A decision the bound cannot make, or any value out of
+// FP32's normal range, goes to the exact path: row k's current and proposed
+// entries in FP64 from theta (log cosh sums as above) and the reference's
+// test u |det Phi|^2 <= |det Phi'|^2 in FP64.
+#include <algorithm>
+#include <cfloat>
+
+#include "nqes_internal.h"
+#include "pcg64.cuh"
+
+namespace nqes {
+
+namespace {
+
+constexpr float kU = 5.9604645e-8f;  // FP32 unit roundoff 2^-24
+constexpr int kMaxSpinWords = 8;
+
+__device__ __forceinline__ bool down_bit(const uint64_t *s, int i) { return (s[i >> 6] >> (i & 63)) & 1ULL; }
+__device__ __forceinline__ int expo32(float x) {
+    const int b = (__float_as_int(x) >> 23) & 0xff;
+    return b == 0 ? 0 : b - 127;
+}
+
+// (ah, al) += (bh, bl): double-float addition from two-sum (Knuth) and a
+// final fast two-sum; relative error a few 2^-48 of max(|a|, |b|).
+__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl) {
+    const float s = ah + bh;
+    const float bb = s - ah;
+    float e = (ah - (s - bb)) + (bh - bb);
+    e += al + bl;
+    const float h = s + e;
+    al = e - (h - s);
+    ah = h;
+}
+
+struct DSmem {
+    double *phi, *pinv, *Dm, *jk, *lsum;
+    float *th_hi, *th_lo, *t, *rat, *bsig, *Bm;
+    uint64_t *spin;
+    int *flag;
+};
+
+__host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K) {
+    const size_t KK = size_t(K) * K;
+    const size_t nd = 3 * KK + 4 + 32;
+    const size_t nf = 3 * KK * MP + 2 * KK * N + KK;
+    return nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 4 * 4;  // 16: alignment pad
+}
+
+__device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
+    const int KK = K * K;
+    DSmem s;
+    double *d = reinterpret_cast<double *>(base);
+    s.phi = d; d += KK;
+    s.pinv = d; d += KK;
+    s.Dm = d; d += KK;
+    s.jk = d; d += 4;
+    s.lsum = d; d += 32;
+    // float arrays start on a 16-byte boundary (vector loads of theta and tanh)
+    unsigned char *fb = reinterpret_cast<unsigned char *>(d);
+    fb += (16 - (reinterpret_cast<uintptr_t>(fb) & 15)) & 15;
+    float *f = reinterpret_cast<float *>(fb);
+    s.th_hi = f; f += KK * MP;
+    s.th_lo = f; f += KK * MP;
+    s.t = f; f += KK * MP;
+    s.rat = f; f += KK * N;
+    s.bsig = f; f += KK * N;
+    s.Bm = f; f += KK;
+    unsigned char *p = reinterpret_cast<unsigned char *>(f);
+    p += (8 - (reinterpret_cast<uintptr_t>(p) & 7)) & 7;
+    s.spin = reinterpret_cast<uint64_t *>(p);
+    s.flag = reinterpret_cast<int *>(s.spin + kMaxSpinWords);
+    return s;
+}
+
+// Cofactor of (r, c) and the sum of |Leibniz terms| of that minor, K <= 4.
+__device__ void cofactor_abs(const double *m, int K, int r, int c, double &cof, double &cabs) {
+    if (K == 1) {
+        cof = 1.0;
+        cabs = 1.0;
+        return;
+    }
+    double sub[9], sab[9];
+    int t = 0;
+    for (int a = 0; a < K; a++) {
+        if (a == r) continue;
+        for (int b = 0; b < K; b++)
+            if (b != c) {
+                sub[t] = m[a * K + b];
+                sab[t] = fabs(m[a * K + b]);
+                t++;
+            }
+    }
+    const double d = small_det(sub, K - 1);
+    double p;
+    if (K == 2) {
+        p = sab[0];
+    } else if (K == 3) {
+        p = sab[0] * sab[3] + sab[1] * sab[2];
+    } else {
+        p = sab[0] * (sab[4] * sab[8] + sab[5] * sab[7]) + sab[1] * (sab[3] * sab[8] + sab[5] * sab[6]) +
+            sab[2] * (sab[3] * sab[7] + sab[4] * sab[6]);
+    }
+    cof = ((r + c) & 1) ? -d : d;
+    cabs = p;
+}
+
+// Row k from the spins: theta (double-float sums of b and +-w), tanh(theta)
+// in FP32, and Phi[k][.] in FP64 scaled by the row's largest entry.
+// Block-wide; ends with a barrier.
+__device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
+    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, MP = A.MP;
+    const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
+    const uint64_t *sk = sm.spin + k * NW;
+    for (int idx = tid; idx < K * MP; idx += T) {
+        const int kk = idx / MP, j = idx - kk * MP, q = k * K + kk;
+        float h = 0.f, l = 0.f, t = 0.f;
+        if (j < M) {
+            h = A.bh[kk * MP + j];
+            l = A.bl[kk * MP + j];
+            for (int i = 0; i < N; i++) {
+                const size_t o = (size_t(kk) * N + i) * MP + j;
+                const float wh = A.whp[o], wl = A.wlp[o];
+                if (down_bit(sk, i))
+                    df_add(h, l, -wh, -wl);
+                else
+                    df_add(h, l, wh, wl);
+            }
+            t = tanhf(h);
+        }
+        sm.th_hi[q * MP + j] = h;
+        sm.th_lo[q * MP + j] = l;
+        sm.t[q * MP + j] = t;
+    }
+    __syncthreads();
+    for (int kk = warp; kk < K; kk += nwarp) {
+        const int q = k * K + kk;
+        double lin = 0.0, pr = 1.0, as = 0.0;
+        for (int j = lane; j < M; j += 32) {
+            const double th = double(sm.th_hi[q * MP + j]) + double(sm.th_lo[q * MP + j]);
+            lin += fabs(th);
+            pr *= 1.0 + exp(-2.0 * fabs(th));
+        }
+        for (int i = lane; i < N; i += 32) as += down_bit(sk, i) ? -A.a64[kk * N + i] : A.a64[kk * N + i];
+        lin = warp_sum(lin);
+        as = warp_sum(as);
+        pr = warp_prod(pr);
+        if (lane == 0) sm.lsum[q] = as + lin + log(pr);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double mx = -1e308;
+        for (int kk = 0; kk < K; kk++) mx = fmax(mx, sm.lsum[k * K + kk]);
+        for (int kk = 0; kk < K; kk++) sm.phi[k * K + kk] = exp(sm.lsum[k * K + kk] - mx);
+    }
+    __syncthreads();
+}
+
+// All proposals of row k, run by one warp. Returns whether the row changed.
+//
+// Error model of the FP32 proposal (u = 2^-24). tanh(theta) of the lane's
+// units is held in FP32 with an absolute error of at most Et (one bound per
+// RBM, the same in every lane): 5u after the row's rebuild (tanhf), and
+// after an accepted flip, whose update t' = (t c - sigma s) / f has
+// derivative dt'/dt = 1/f^2, Et' = Et max_j 1/f_j^2 + u (2 max_j cond_j + 5)
+// with cond_j = (c + |s|)/(c - |s|) >= (|c| + |t s|)/|f| (|t| <= 1). A factor
+// f_j = c - sigma t s then has relative error at most u (cond_j + 1) +
+// Et |s| / (c - |s|), and the product over the row's M factors (M - 1 + 16
+// roundings, the 16 also covering the FP64 tables' own rounding)
+//   beta = u (sum_j cond_j + 2M + 16) + Et sum_j |s_j| / (c_j - |s_j|).
+// The per-(kk, i) sums and maxima come from a table built with the weights.
+template <int K, int U>
+__device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsigned long long &nacc,
+                        unsigned long long &nexact) {
+    constexpr int G = K == 1 ? 32 : (K == 2 ? 16 : 8);
+    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
+    const int lane = threadIdx.x & 31;
+    const int gkk = lane / G, gjl = lane % G;
+    const bool active = gkk < K;
+    const int kkl = active ? gkk : 0;  // idle lanes (K = 3) read RBM 0's tables and contribute factor 1
+    const int q = k * K + kkl, base = gjl * U;
+
+    float t[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) t[u] = sm.t[q * MP + base + u];
+    bool live[U];  // unit inside the RBM (not padding) and lane in a group
+#pragma unroll
+    for (int u = 0; u < U; u++) live[u] = active && base + u < M;
+    uint64_t sk[2] = {sm.spin[k * NW], NW > 1 ? sm.spin[k * NW + 1] : 0ULL};
+
+    // Decision state, identical in every lane: exact cofactors of row k (the
+    // other rows are exact), the row's entries, g and det with error bounds.
+    double cofd[K], cabsd[K];
+    float phik[K], g[K], gabs[K], Et[K];
+    float det32, edet, rho = 0.f;
+    {
+        double det = 0.0, perm = 0.0;
+#pragma unroll
+        for (int kk = 0; kk < K; kk++) {
+            cofactor_abs(sm.phi, K, k, kk, cofd[kk], cabsd[kk]);
+            const double p = sm.phi[k * K + kk];
+            phik[kk] = float(p);
+            g[kk] = float(p * cofd[kk]);
+            gabs[kk] = float(fabs(p) * cabsd[kk]);
+            det += p * cofd[kk];
+            perm += fabs(p) * cabsd[kk];
+            Et[kk] = 5.f * kU;
+        }
+        det32 = float(det);
+        edet = 4.f * kU * fabsf(det32) + float(perm * 0x1p-50);
+    }
+    bool changed = false;
+
+    for (int i = 0; i < N; i++) {
+        const bool down = (sk[i >> 6] >> (i & 63)) & 1ULL;
+        const size_t row = (size_t(kkl) * N + i) * MP + base;
+        float cq[U], sq[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            cq[u] = __ldg(A.cp + row + u);
+            sq[u] = __ldg(A.spp + row + u);
+        }
+        float ea[K];
+        float4 bd[K];
+#pragma unroll
+        for (int kk = 0; kk < K; kk++) {
+            ea[kk] = __ldg((down ? A.edn : A.eup) + kk * N + i);
+            bd[kk] = __ldg(reinterpret_cast<const float4 *>(A.bnd) + kk * N + i);
+        }
+        const uint64_t draw = pcg_next(rng);
+        const float u32 = __ull2float_rn(draw) * 0x1p-64f;
+
+        // factors f = c - sigma t s and their product within the lane's group
+        float f[U], prod = 1.f;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            f[u] = fmaf(down ? t[u] : -t[u], sq[u], cq[u]);
+            if (live[u]) prod *= f[u];
+        }
+#pragma unroll
+        for (int o = G >> 1; o > 0; o >>= 1) prod *= __shfl_xor_sync(0xffffffffu, prod, o);
+        float x[K], rr[K], s = 0.f, ed = 0.f, bmax = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < K; kk++) {
+            rr[kk] = __shfl_sync(0xffffffffu, prod, kk * G);
+            const float beta = fmaf(Et[kk], bd[kk].y, bd[kk].x);
+            const float re = rr[kk] * ea[kk];
+            x[kk] = re * g[kk];
+            s += x[kk];
+            ed += fabsf(re) * ((beta + 3.f * kU) * fabsf(g[kk]) + 1.02f * rho * gabs[kk]) + 3.f * kU * fabsf(x[kk]);
+            bmax = fmaxf(bmax, beta);
+        }
+        ed = ed * 1.01f + 4.f * kU * fabsf(s);
+
+        bool acc = false, exact_path = false;
+        {
+            const float ad = fabsf(s), lo = ad - ed, hi = ad + ed;
+            const float dd = fabsf(det32), dlo = fmaxf(dd - edet, 0.f), dhi = dd + edet;
+            const float su = u32 * (1.f + 16.f * kU), sl = u32 * (1.f - 16.f * kU);
+            if (A.exact_all || !(dd > 1e-15f) || !(dd < 1e15f) || !(bmax < 0.01f))
+                exact_path = true;  // det == 0 (accepted, code/rbm.cc:542), range, loose bound
+            else if (lo > 0.f && lo * lo * (1.f - 16.f * kU) >= su * dhi * dhi)
+                acc = true;
+            else if (!(hi * hi * (1.f + 16.f * kU) < sl * dlo * dlo))
+                exact_path = true;  // NaN lands here as well
+        }
+        if (exact_path) {
+            // Row k current and proposed, in FP64: theta of the lane's units from
+            // the spins (double-float sums of b and +-w), then the log cosh sums.
+            double lin = 0.0, pr = 1.0, lin2 = 0.0, pr2 = 1.0;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (live[u]) {
+                    const int j = base + u;
+                    float h = A.bh[kkl * MP + j], l = A.bl[kkl * MP + j];
+                    for (int i2 = 0; i2 < N; i2++) {
+                        const size_t o = (size_t(kkl) * N + i2) * MP + j;
+                        const float wh = A.whp[o], wl = A.wlp[o];
+                        if ((sk[i2 >> 6] >> (i2 & 63)) & 1ULL)
+                            df_add(h, l, -wh, -wl);
+                        else
+                            df_add(h, l, wh, wl);
+                    }
+                    const double tt = double(h) + double(l);
+                    const double w = A.w64[(size_t(kkl) * N + i) * M + j];
+                    const double t2 = down ? tt + 2.0 * w : tt - 2.0 * w;
+                    lin += fabs(tt);
+                    pr *= 1.0 + exp(-2.0 * fabs(tt));
+                    lin2 += fabs(t2);
+                    pr2 *= 1.0 + exp(-2.0 * fabs(t2));
+                }
+            }
+#pragma unroll
+            for (int o = G >> 1; o > 0; o >>= 1) {
+                lin += __shfl_xor_sync(0xffffffffu, lin, o);
+                lin2 += __shfl_xor_sync(0xffffffffu, lin2, o);
+                pr *= __shfl_xor_sync(0xffffffffu, pr, o);
+                pr2 *= __shfl_xor_sync(0xffffffffu, pr2, o);
+            }
+            double Lc[K], Ln[K], mx = -1e308;
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) {
+                double as = 0.0;
+                for (int i2 = lane; i2 < N; i2 += 32) {
+                    const double ai = A.a64[kk * N + i2];
+                    as += ((sk[i2 >> 6] >> (i2 & 63)) & 1ULL) ? -ai : ai;
+                }
+                as = warp_sum(as);
+                const double l1 = __shfl_sync(0xffffffffu, lin, kk * G);
+                const double l2 = __shfl_sync(0xffffffffu, lin2, kk * G);
+                const double p1 = __shfl_sync(0xffffffffu, pr, kk * G);
+                const double p2 = __shfl_sync(0xffffffffu, pr2, kk * G);
+                const double ai = A.a64[kk * N + i];
+                Lc[kk] = as + l1 + log(p1);
+                Ln[kk] = as + (down ? 2.0 * ai : -2.0 * ai) + l2 + log(p2);
+                mx = fmax(mx, Lc[kk]);
+            }
+            double pc[K], pn[K], det_e = 0.0, sx = 0.0;
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) {
+                pc[kk] = exp(Lc[kk] - mx);
+                pn[kk] = exp(Ln[kk] - mx);
+                det_e += pc[kk] * cofd[kk];
+                sx += pn[kk] * cofd[kk];
+            }
+            acc = det_e == 0.0 || pcg_u01(draw) * (det_e * det_e) <= sx * sx;
+            nexact++;
+            // continue from the exact row
+            double perm = 0.0;
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) {
+                const double p = acc ? pn[kk] : pc[kk];
+                phik[kk] = float(p);
+                g[kk] = float(p * cofd[kk]);
+                gabs[kk] = float(fabs(p) * cabsd[kk]);
+                perm += fabs(p) * cabsd[kk];
+            }
+            det32 = float(acc ? sx : det_e);
+            edet = 4.f * kU * fabsf(det32) + float(perm * 0x1p-50);
+            rho = 0.f;
+        }
+        if (acc) {
+            // tanh' = (t c - sigma s) / f (code/rbm.cc:185) in FP32, and its bound
+#pragma unroll
+            for (int u = 0; u < U; u++) t[u] = __fdividef(fmaf(t[u], cq[u], down ? sq[u] : -sq[u]), f[u]);
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) Et[kk] = fmaf(Et[kk] * (1.f + 4.f * kU), bd[kk].z, bd[kk].w);
+            if (!exact_path) {
+                // row k times r e^{-2 sigma a}: g_kk becomes x_kk (cofactors exclude row k)
+#pragma unroll
+                for (int kk = 0; kk < K; kk++) {
+                    const float re = rr[kk] * ea[kk];
+                    phik[kk] *= re;
+                    g[kk] = x[kk];
+                    gabs[kk] *= fabsf(re);
+                }
+                det32 = s;
+                edet = ed;
+                rho += bmax + 4.f * kU;
+            }
+            // keep the row's largest entry near 1 (exact power-of-two scaling)
+            int ex = -100000;
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) ex = max(ex, expo32(phik[kk]));
+            if (ex > 20 || ex < -20) {
+                const float sc = ldexpf(1.f, -ex);
+#pragma unroll
+                for (int kk = 0; kk < K; kk++) {
+                    phik[kk] *= sc;
+                    g[kk] *= sc;
+                    gabs[kk] *= sc;
+                }
+                det32 *= sc;
+                edet *= sc;
+            }
+            sk[i >> 6] ^= 1ULL << (i & 63);
+            changed = true;
+            nacc++;
+        }
+    }
+    if (lane == 0) {
+        sm.spin[k * NW] = sk[0];
+        if (NW > 1) sm.spin[k * NW + 1] = sk[1];
+    }
+    return changed;
+}
+
+template <int K_, int U>
+__global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int K = K_, KK = K * K;
+    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, L = A.sh.L, MP = A.MP;
+    const size_t P = size_t(A.sh.P);
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
+    const int c = blockIdx.x;
+    DSmem sm = dcarve(smem_raw, N, MP, K);
+    const bool writer = tid == 0;
+
+    // init_multi_spin (code/rbm.cc:98-119): every thread advances the stream;
+    // warp 0 keeps it for the proposals.
+    Pcg64 rng = pcg_seed(A.sp->seed + uint64_t(c));
+    if (writer)
+        for (int t = 0; t < K * NW; t++) sm.spin[t] = 0;
+    __syncthreads();
+    for (int k = 0; k < K; k++)
+        for (int i = 0; i < N; i++) {
+            const bool d = pcg_bernoulli_half(rng);
+            if (d && writer) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
+        }
+    __syncthreads();
+    for (int k = 0; k < K; k++) rebuild_row(A, sm, k);
+
+    unsigned long long nacc = 0, nexact = 0;
+    int rowctr = 0;
+    const int total = A.burn + A.m;
+    for (int sw = 0; sw < total; sw++) {
+        for (int k = 0; k < K; k++, rowctr++) {
+            if (warp == 0) {
+                const bool ch = run_row<K_, U>(A, sm, k, rng, nacc, nexact);
+                if (lane == 0) sm.flag[rowctr & 1] = ch ? 1 : 0;
+            }
+            __syncthreads();
+            if (sm.flag[rowctr & 1]) rebuild_row(A, sm, k);  // uniform after the barrier
+        }
+        if (sw < A.burn) continue;
+
+        // ---- sample: local energy (FP32 ratios, FP64 combination) and FP32 O ----
+        const size_t s = size_t(c) * A.m + (sw - A.burn);
+        if (writer) {
+            double pinv[16];
+            if (!small_inv(sm.phi, pinv, K)) {
+                atomicOr(A.err, kErrSingular);
+                for (int t = 0; t < KK; t++) pinv[t] = 0.0;
+            }
+            for (int t = 0; t < KK; t++) sm.pinv[t] = pinv[t];
+        }
+        __syncthreads();
+        for (int k = warp; k < K; k += nwarp) {
+            const uint64_t *sk = sm.spin + k * NW;
+            double acc = 0.0;
+            for (int i = 1 + lane; i < N; i += 32) {
+                const bool si = down_bit(sk, i);
+                const double *Jr = A.J + size_t(i) * N;
+                for (int j = 0; j < i; j++) acc += (si ^ down_bit(sk, j)) ? -Jr[j] : Jr[j];
+            }
+            acc = warp_sum(acc);
+            if (lane == 0) sm.jk[k] = 2.0 * acc;
+        }
+        for (int it = tid; it < KK * N; it += T) {
+            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const bool down = down_bit(sm.spin + k * NW, i);
+            const float *crow = A.cp + (size_t(kk) * N + i) * MP;
+            const float *srow = A.spp + (size_t(kk) * N + i) * MP;
+            const float *trow = sm.t + q * MP;
+            float p = 1.f;
+            for (int j = 0; j < M; j++) p *= fmaf(down ? trow[j] : -trow[j], __ldg(srow + j), __ldg(crow + j));
+            sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
+            const float B = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
+            sm.bsig[it] = down_bit(sm.spin + kk * NW, i) ? -B : B;
+        }
+        __syncthreads();
+        for (int q = warp; q < KK; q += nwarp) {
+            float acc = 0.f;
+            for (int i = lane; i < N; i += 32) acc += sm.rat[q * N + i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) sm.Dm[q] = sm.jk[q / K] - A.h * double(acc);
+        }
+        __syncthreads();
+        if (writer) {
+            bool ok = true;
+            for (int r = 0; r < K; r++)
+                for (int cc = 0; cc < K; cc++) {
+                    double e = 0.0;
+                    for (int t = 0; t < K; t++) e = fma(sm.pinv[r * K + t], sm.Dm[t * K + cc] * sm.phi[t * K + cc], e);
+                    ok = ok && isfinite(e);
+                    A.E[s * KK + r * K + cc] = cplx{e, 0.0};
+                }
+            for (int k = 0; k < K; k++)
+                for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
+            if (!ok) atomicOr(A.err, kErrNonFinite);
+        }
+        for (int t = tid; t < K * NW; t += T) A.spins[s * K * NW + t] = sm.spin[t];
+        __syncthreads();
+        // O row, layout [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239), FP32
+        float *orow = A.O + s * P;
+        for (int k = 0; k < K; k++) {
+            float *ok = orow + size_t(k) * L;
+            for (int p = tid; p < L; p += T) {
+                float v = 0.f;
+                if (p < N) {
+                    for (int kk = 0; kk < K; kk++) v += sm.bsig[(k * K + kk) * N + p];
+                } else if (p < N + M) {
+                    const int j = p - N;
+                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.Bm[k * K + kk], sm.t[(kk * K + k) * MP + j], v);
+                } else {
+                    const int q = p - N - M, i = q / M, j = q - i * M;
+                    for (int kk = 0; kk < K; kk++)
+                        v = fmaf(sm.bsig[(k * K + kk) * N + i], sm.t[(kk * K + k) * MP + j], v);
+                }
+                ok[p] = v;
+            }
+        }
+        __syncthreads();
+    }
+    if (writer) {
+        A.accepted[c] = nacc;
+        A.exact[c] = nexact;
+    }
+}
+
+// Padded tables [kk][i][MP] (padding: c = 1, s = 0, w = 0, so a padded
+// factor is exactly 1), theta's b as double-float [kk][MP], and per (kk, i)
+// the bound record of run_row: {u (sum_j cond_j + 2M + 16),
+// sum_j |s_j| / (c_j - |s_j|), max_j 1 / (c_j - |s_j|)^2, u (2 max_j cond_j + 5)}
+// with c - |s| = e^{-2|w|} and cond = (c + |s|) / (c - |s|) = e^{4|w|}, each
+// rounded up.
+__global__ void k_tables_dw(Shape sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
+                            float *wlp, float *bh, float *bl, float4 *bnd) {
+    const size_t nr = size_t(sh.K) * sh.N;
+    for (size_t r = blockIdx.x * size_t(blockDim.x) + threadIdx.x; r < nr; r += size_t(gridDim.x) * blockDim.x) {
+        double sc = 0.0, s1 = 0.0, f2 = 0.0, qm = 0.0;
+        for (int j = 0; j < sh.M; j++) {
+            const double aw = fabs(w[r * sh.M + j].re);
+            const double d = exp(-2.0 * aw), cond = exp(4.0 * aw);
+            sc += cond;
+            s1 += fabs(sinh(2.0 * aw)) / d;
+            f2 = fmax(f2, 1.0 / (d * d));
+            qm = fmax(qm, cond);
+        }
+        const double up = 1.0 + 1e-6, u = 0x1p-24;
+        bnd[r] = make_float4(float(u * (sc + 2.0 * sh.M + 16.0) * up), float(s1 * up), float(f2 * up),
+                             float(u * (2.0 * qm + 5.0) * up));
+    }
+    const size_t n = size_t(sh.K) * sh.N * MP;
+    for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
+        const int j = int(t % MP);
+        const size_t ki = t / MP;  // kk*N + i
+        float c = 1.f, s = 0.f, h = 0.f, l = 0.f;
+        if (j < sh.M) {
+            const double wv = w[ki * sh.M + j].re;
+            c = float(cosh(2.0 * wv));
+            s = float(sinh(2.0 * wv));
+            h = float(wv);
+            l = float(wv - double(h));
+        }
+        cp[t] = c;
+        spp[t] = s;
+        whp[t] = h;
+        wlp[t] = l;
+        if (t < size_t(sh.K) * MP) {
+            const int kk = int(t / MP);
+            float bh0 = 0.f, bl0 = 0.f;
+            if (j < sh.M) {
+                const double bv = b[size_t(kk) * sh.M + j].re;
+                bh0 = float(bv);
+                bl0 = float(bv - double(bh0));
+            }
+            bh[t] = bh0;
+            bl[t] = bl0;
+        }
+    }
+}
+
+using DwKernel = void (*)(const MixedArgs);
+template <int K> DwKernel dw_kernel_u(int U) {
+    switch (U) {
+    case 1: return k_sample_dw<K, 1>;
+    case 2: return k_sample_dw<K, 2>;
+    case 4: return k_sample_dw<K, 4>;
+    case 8: return k_sample_dw<K, 8>;
+    case 16: return k_sample_dw<K, 16>;
+    default: return nullptr;
+    }
+}
+DwKernel dw_kernel(int K, int U) {
+    switch (K) {
+    case 1: return dw_kernel_u<1>(U);
+    case 2: return dw_kernel_u<2>(U);
+    case 3: return dw_kernel_u<3>(U);
+    case 4: return dw_kernel_u<4>(U);
+    default: return nullptr;
+    }
+}
+
+}  // namespace
+
+// Units per lane of the decision-warp form for (M, K): G = largest power of two
+// <= 32/K lanes per RBM, U = M/G rounded up to a power of two; 0 if U > 16.
+int dw_units(const Shape &sh, int *G_out) {
+    int G = 32;
+    while (G * sh.K > 32) G >>= 1;
+    int U = 1;
+    while (U * G < sh.M) U <<= 1;
+    if (G_out) *G_out = G;
+    return U <= 16 ? U : 0;
+}
+
+size_t dw_smem_bytes(const Shape &sh, int MP) { return dsmem_bytes(sh.N, MP, sh.K); }
+
+cudaError_t prepare_sample_dw(const Shape &sh, int MP) {
+    int G = 0;
+    const DwKernel fn = dw_kernel(sh.K, dw_units(sh, &G));
+    if (!fn || G * dw_units(sh, nullptr) != MP) return cudaErrorInvalidConfiguration;
+    return cudaFuncSetAttribute(reinterpret_cast<const void *>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(dsmem_bytes(sh.N, MP, sh.K)));
+}
+
+cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm) {
+    const DwKernel fn = dw_kernel(sh.K, dw_units(sh, nullptr));
+    if (!fn) return cudaErrorInvalidConfiguration;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, reinterpret_cast<const void *>(fn), threads,
+                                                         smem);
+}
+
+cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st) {
+    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K);
+    const DwKernel fn = dw_kernel(a.sh.K, a.U);
+    if (!fn || warps < 1 || warps > 8 || a.sh.NW > 2 || a.G * a.U != a.MP) return cudaErrorInvalidConfiguration;
+    fn<<<a.chains, 32 * warps, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
+                             float *wlp, float *bh, float *bl, float *bnd, cudaStream_t st) {
+    const size_t n = size_t(sh.K) * sh.N * MP;
+    const int blocks = int(std::min<size_t>((n + 255) / 256, 4096));
+    k_tables_dw<<<blocks, 256, 0, st>>>(sh, MP, b, w, cp, spp, whp, wlp, bh, bl, reinterpret_cast<float4 *>(bnd));
+    return cudaGetLastError();
+}
+
+}  // namespace nqes

@@ -35,6 +35,10 @@ struct nqes_ctx {
     float *mch = nullptr, *msh = nullptr, *meup = nullptr, *medn = nullptr;
     double *mw = nullptr, *ma = nullptr, *mb = nullptr;
     unsigned long long *exact = nullptr;           // per chain
+    // decision-warp form of the mixed sampler (dw_U = 0: block form)
+    int dw_G = 0, dw_U = 0, dw_MP = 0;
+    float *dcp = nullptr, *dsp = nullptr, *dwh = nullptr, *dwl = nullptr, *dbh = nullptr, *dbl = nullptr;
+    float *dbnd = nullptr;  // K·N float4 bound records
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
     int step_precision = NQES_PRECISION_FP64;      // precision of the allocated step buffers
     int tk_opt = 0;
@@ -231,12 +235,56 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.exact = ctx->exact;
     A.err = ctx->err_d;
     A.exact_all = ctx->mixed_exact_all ? 1 : 0;
+    A.cp = ctx->dcp;
+    A.spp = ctx->dsp;
+    A.whp = ctx->dwh;
+    A.wlp = ctx->dwl;
+    A.bh = ctx->dbh;
+    A.bl = ctx->dbl;
+    A.bnd = ctx->dbnd;
+    A.G = ctx->dw_G;
+    A.U = ctx->dw_U;
+    A.MP = ctx->dw_MP;
     return A;
 }
 
 cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
     return launch_tables_mixed(ctx->sh, ctx->a, ctx->b, ctx->w, ctx->mch, ctx->msh, ctx->meup, ctx->medn, ctx->mw,
                                ctx->ma, ctx->mb, ctx->st);
+}
+
+// Warps per chain of the decision-warp sampler: 4 while every chain still
+// gets its own resident CTA (the extra warps rebuild rows and form samples),
+// fewer when chains must share SMs.
+int dw_warps(nqes_ctx *ctx, int chains) {
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP);
+    for (int w = 4; w > 1; w >>= 1) {
+        int per_sm = 0;
+        if (dw_occupancy(ctx->sh, 32 * w, smem, &per_sm) == cudaSuccess && per_sm * sms >= chains) return w;
+    }
+    return 1;
+}
+
+// The mixed sampler's tables, its shared-memory attribute and its launch,
+// in the decision-warp form when it applies, else the block form.
+cudaError_t launch_mixed_tables(nqes_ctx *ctx) {
+    cudaError_t e = launch_tables_mixed_ctx(ctx);
+    if (e == cudaSuccess && ctx->dw_U)
+        e = launch_tables_dw(ctx->sh, ctx->dw_MP, ctx->b, ctx->w, ctx->dcp, ctx->dsp, ctx->dwh, ctx->dwl, ctx->dbh,
+                             ctx->dbl, ctx->dbnd, ctx->st);
+    return e;
+}
+size_t mixed_sampler_smem(nqes_ctx *ctx) {
+    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP) : mixed_smem_bytes(ctx->sh);
+}
+cudaError_t prepare_mixed_sampler(nqes_ctx *ctx) {
+    return ctx->dw_U ? prepare_sample_dw(ctx->sh, ctx->dw_MP) : prepare_sample_mixed(ctx->sh);
+}
+cudaError_t launch_mixed_sampler(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
+    const MixedArgs A = mixed_args(ctx, chains, m, burn, tk);
+    return ctx->dw_U ? launch_sample_dw(A, dw_warps(ctx, chains), ctx->st) : launch_sample_mixed(A, ctx->st);
 }
 
 template <class S> Tables<S> tables(nqes_ctx *ctx) {
@@ -312,13 +360,13 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     {
         // the sampler's dynamic shared memory attribute must be set before capture
         const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
-        const size_t smem = mixed ? mixed_smem_bytes(ctx->sh) : sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
+        const size_t smem = mixed ? mixed_sampler_smem(ctx) : sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
         if (smem > 227 * 1024) {
             ctx->err = "shape needs " + std::to_string(smem) + " bytes of shared memory per chain";
             return NQES_ERR_INVALID;
         }
         if (mixed)
-            NQES_CUDA(prepare_sample_mixed(ctx->sh));
+            NQES_CUDA(prepare_mixed_sampler(ctx));
         else
             NQES_CUDA(prepare_sample<S>(ctx->sh));
     }
@@ -334,8 +382,8 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->st);
     cudaError_t le;
     if (ctx->step_precision == NQES_PRECISION_MIXED) {
-        le = launch_tables_mixed_ctx(ctx);
-        if (le == cudaSuccess) le = launch_sample_mixed(mixed_args(ctx, chains, m, burn, tk), ctx->st);
+        le = launch_mixed_tables(ctx);
+        if (le == cudaSuccess) le = launch_mixed_sampler(ctx, chains, m, burn, tk);
     } else {
         le = launch_tables_ctx<S>(ctx);
         if (le == cudaSuccess) le = launch_sample<S>(A, threads, ctx->st);
@@ -488,6 +536,15 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
         (rc = dalloc(ctx, &ctx->medn, na)) || (rc = dalloc(ctx, &ctx->mw, nw)) || (rc = dalloc(ctx, &ctx->ma, na)) ||
         (rc = dalloc(ctx, &ctx->mb, size_t(K) * M)))
         return fail(rc);
+    ctx->dw_U = dw_units(ctx->sh, &ctx->dw_G);
+    if (ctx->dw_U) {
+        ctx->dw_MP = ctx->dw_G * ctx->dw_U;
+        const size_t np = size_t(K) * N * ctx->dw_MP, nb = size_t(K) * ctx->dw_MP;
+        if ((rc = dalloc(ctx, &ctx->dcp, np)) || (rc = dalloc(ctx, &ctx->dsp, np)) || (rc = dalloc(ctx, &ctx->dwh, np)) ||
+            (rc = dalloc(ctx, &ctx->dwl, np)) || (rc = dalloc(ctx, &ctx->dbh, nb)) || (rc = dalloc(ctx, &ctx->dbl, nb)) ||
+            (rc = dalloc(ctx, &ctx->dbnd, 4 * size_t(K) * N)))
+            return fail(rc);
+    }
     if (cudaMallocHost(&ctx->sp_host, sizeof(StepParams)) != cudaSuccess ||
         cudaMallocHost(&ctx->qs_host, sizeof(QlpState)) != cudaSuccess ||
         cudaMallocHost(&ctx->err_host, sizeof(int)) != cudaSuccess ||
@@ -523,6 +580,13 @@ int nqes_destroy(nqes_ctx *ctx) {
     dfree(ctx->mw);
     dfree(ctx->ma);
     dfree(ctx->mb);
+    dfree(ctx->dcp);
+    dfree(ctx->dsp);
+    dfree(ctx->dwh);
+    dfree(ctx->dwl);
+    dfree(ctx->dbh);
+    dfree(ctx->dbl);
+    dfree(ctx->dbnd);
     dfree(ctx->sp);
     dfree(ctx->qs);
     dfree(ctx->err_d);
@@ -925,7 +989,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
         switch (kernel) {
         case NQES_KERNEL_SAMPLE: {
             if (ctx->step_precision == NQES_PRECISION_MIXED)
-                return launch_sample_mixed(mixed_args(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk), ctx->st);
+                return launch_mixed_sampler(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
             SampleArgs<S> A = sample_args<S>(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
             return launch_sample<S>(A, sample_threads(ctx->sh.K, ctx->last_tk), ctx->st);
         }
@@ -948,7 +1012,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
     }
     if (kernel == NQES_KERNEL_SAMPLE) {
         if (mixed)
-            NQES_CUDA(prepare_sample_mixed(ctx->sh));
+            NQES_CUDA(prepare_mixed_sampler(ctx));
         else
             NQES_CUDA(prepare_sample<S>(ctx->sh));
     }

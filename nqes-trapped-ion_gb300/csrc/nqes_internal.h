@@ -77,8 +77,21 @@ struct MixedArgs {
     unsigned long long *exact;           // per chain: decisions taken by the exact FP64 path
     int *err;
     int exact_all;                       // 1: every decision through the exact FP64 path (test hook)
+    // Decision-warp form (kernels_sample_warp.cu): G lanes per RBM, U units per
+    // lane, tables padded to MP = G*U units per (kk, i) row: FP32 cosh(2w),
+    // sinh(2w) and w as hi + lo [kk][i][MP]; b as hi + lo [kk][MP].
+    const float *cp, *spp, *whp, *wlp, *bh, *bl;
+    const float *bnd;                    // per (kk, i): float4 bound record (kernels_sample_warp.cu)
+    int G, U, MP;
 };
 size_t mixed_smem_bytes(const Shape &sh);
+int dw_units(const Shape &sh, int *G_out);  // U of the decision-warp form, 0 if it does not apply
+size_t dw_smem_bytes(const Shape &sh, int MP);
+cudaError_t prepare_sample_dw(const Shape &sh, int MP);
+cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st);
+cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm);
+cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
+                             float *wlp, float *bh, float *bl, float *bnd, cudaStream_t st);
 cudaError_t prepare_sample_mixed(const Shape &sh);
 cudaError_t launch_sample_mixed(const MixedArgs &a, cudaStream_t st);
 cudaError_t launch_tables_mixed(const Shape &sh, const cplx *a, const cplx *b, const cplx *w, float *ch, float *sh32,
