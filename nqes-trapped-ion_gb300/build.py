@@ -21,7 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_sample_warp.cu", "kernels_solve.cu",
            "nqes_api.cu", "sv_static.cu"]
-HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h"]
+HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h", "tma_stage.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

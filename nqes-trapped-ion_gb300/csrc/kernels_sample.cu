@@ -90,7 +90,7 @@ template <class S> __device__ S cofactor(const S *m, int K, int r, int c) {
 
 template <class S> struct Smem {
     S *tnh, *phi, *pinv, *red, *rat, *bsig, *Bm, *Dm, *pm;
-    double *jk;
+    double *jk, *jpart;
     int *pe, *rowe, *flag;
     uint64_t *spin;
     float *t32, *red32, *rbd32;  // rejection filter: FP32 tanh(theta), per-warp products and bounds
@@ -99,7 +99,7 @@ template <class S> struct Smem {
 __host__ __device__ inline size_t smem_bytes(int N, int M, int K, size_t ssz) {
     size_t KK = size_t(K) * K;
     size_t nS = KK * M + 2 * KK + 32 + 2 * KK * N + 2 * KK + KK + 32;
-    return nS * ssz + 8 * 4 + 8 * kMaxSpinWords + 4 * (32 + 4 + 4) + 4 * (KK * M + 64);
+    return nS * ssz + 8 * 4 + 8 * 32 + 8 * kMaxSpinWords + 4 * (32 + 4 + 4) + 4 * (KK * M + 64);
 }
 
 template <class S> __device__ inline Smem<S> carve(unsigned char *base, int N, int M, int K) {
@@ -117,6 +117,7 @@ template <class S> __device__ inline Smem<S> carve(unsigned char *base, int N, i
     s.pm = p; p += KK + 32;  // (mantissa of Phi entries during init) + per-warp scratch
     double *d = reinterpret_cast<double *>(p);
     s.jk = d; d += 4;
+    s.jpart = d; d += 32;
     s.spin = reinterpret_cast<uint64_t *>(d);
     int *ip = reinterpret_cast<int *>(s.spin + kMaxSpinWords);
     s.pe = ip; ip += 32;
@@ -539,20 +540,34 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
             }
         }
         __syncthreads();
-        if (warp < K) {
-            // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031)
-            const uint64_t *sk = sm.spin + warp * NW;
-            double acc = 0.0;
-            for (int i = 1 + lane; i < N; i += 32) {
-                const bool si = spin_down(sk, i);
-                const double *Jr = A.J + size_t(i) * N;
-                for (int j = 0; j < i; j++) {
-                    const double p = Jr[j];
-                    acc += (si ^ spin_down(sk, j)) ? -p : p;
+        {
+            // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031): the
+            // N x N grid strided over the block, partial sums per warp, then the
+            // warps' partials in warp order (deterministic); jk is complete after
+            // the barrier below
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+            int i = tid / N, j = tid - (tid / N) * N;
+            const int di = T / N, dj = T - (T / N) * N;
+            while (i < N) {
+                if (j < i) {
+                    const double p = A.J[size_t(i) * N + j];
+#pragma unroll
+                    for (int k = 0; k < 4; k++)
+                        if (k < K) acc[k] += (spin_down(sm.spin + k * NW, i) ^ spin_down(sm.spin + k * NW, j)) ? -p : p;
+                }
+                j += dj;
+                i += di;
+                if (j >= N) {
+                    j -= N;
+                    i++;
                 }
             }
-            acc = warp_sum(acc);
-            if (lane == 0) sm.jk[warp] = 2.0 * acc;
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (k < K) {
+                    acc[k] = warp_sum(acc[k]);
+                    if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
+                }
         }
         // Ratios Phi(flip i in row k)[k][kk] / Phi[k][kk] for every (k, kk, i),
         // the N single-flip terms of the transverse field (code/rbm.cc:1050-1058).
@@ -577,6 +592,12 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
             __syncthreads();
             continue;
         }
+        if (tid < K) {
+            double jt = 0.0;
+            for (int w2 = 0; w2 < nwarp; w2++) jt += sm.jpart[w2 * 4 + tid];
+            sm.jk[tid] = 2.0 * jt;
+        }
+        __syncthreads();
         for (int q = warp; q < KK; q += nwarp) {
             S acc = zero<S>();
             for (int i = lane; i < N; i += 32) acc = acc + sm.rat[q * N + i];
@@ -614,19 +635,29 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         S *orow = A.O + s * P;
         for (int k = 0; k < K; k++) {
             S *ok = orow + size_t(k) * L;
-            for (int p = tid; p < L; p += T) {
+            for (int p = tid; p < N + M; p += T) {
                 S v = zero<S>();
                 if (p < N) {
                     for (int kk = 0; kk < K; kk++) v = v + sm.bsig[(k * K + kk) * N + p];
-                } else if (p < N + M) {
-                    const int j = p - N;
-                    for (int kk = 0; kk < K; kk++) v = mad(sm.Bm[k * K + kk], sm.tnh[(kk * K + k) * M + j], v);
                 } else {
-                    const int q = p - N - M, i = q / M, j = q - i * M;
-                    for (int kk = 0; kk < K; kk++)
-                        v = mad(sm.bsig[(k * K + kk) * N + i], sm.tnh[(kk * K + k) * M + j], v);
+                    for (int kk = 0; kk < K; kk++) v = mad(sm.Bm[k * K + kk], sm.tnh[(kk * K + k) * M + p - N], v);
                 }
                 ok[p] = v;
+            }
+            // the w block with (i, j) stepped incrementally (no division per entry)
+            S *ow = ok + N + M;
+            int i = tid / M, j = tid - (tid / M) * M;
+            const int di = T / M, dj = T - (T / M) * M;
+            for (int p = tid; p < N * M; p += T) {
+                S v = zero<S>();
+                for (int kk = 0; kk < K; kk++) v = mad(sm.bsig[(k * K + kk) * N + i], sm.tnh[(kk * K + k) * M + j], v);
+                ow[p] = v;
+                j += dj;
+                i += di;
+                if (j >= M) {
+                    j -= M;
+                    i++;
+                }
             }
         }
         __syncthreads();

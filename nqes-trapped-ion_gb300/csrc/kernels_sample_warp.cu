@@ -38,6 +38,7 @@
 
 #include "nqes_internal.h"
 #include "pcg64.cuh"
+#include "tma_stage.cuh"
 
 namespace nqes {
 
@@ -65,17 +66,24 @@ __device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl)
 }
 
 struct DSmem {
-    double *phi, *pinv, *Dm, *jk, *lsum;
+    double *phi, *pinv, *Dm, *jk, *lsum, *jpart;
     float *th_hi, *th_lo, *t, *rat, *bsig, *Bm;
-    uint64_t *spin;
+    uint64_t *spin, *mbar;
     int *flag;
+    float *tabs;  // staged tables (cosh 2w, sinh 2w, w hi, w lo), 4 * K*N*MP floats
+    // the tables the kernel reads: staged copies or global memory
+    const float *tc, *ts, *twh, *twl;
 };
 
-__host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K) {
+// One table of K*N*MP floats in bytes (a multiple of 16: MP*4 >= 32).
+__host__ __device__ inline size_t dw_table_bytes(int N, int MP, int K) { return size_t(K) * N * MP * 4; }
+
+__host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K, bool staged) {
     const size_t KK = size_t(K) * K;
-    const size_t nd = 3 * KK + 4 + 32;
+    const size_t nd = 3 * KK + 4 + 32 + 32 * 4;
     const size_t nf = 3 * KK * MP + 2 * KK * N + KK;
-    return nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 4 * 4;  // 16: alignment pad
+    const size_t base = nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 8 + 4 * 4;  // 16: alignment pad
+    return staged ? base + 16 + 4 * dw_table_bytes(N, MP, K) : base;
 }
 
 __device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
@@ -87,6 +95,7 @@ __device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
     s.Dm = d; d += KK;
     s.jk = d; d += 4;
     s.lsum = d; d += 32;
+    s.jpart = d; d += 32 * 4;
     // float arrays start on a 16-byte boundary (vector loads of theta and tanh)
     unsigned char *fb = reinterpret_cast<unsigned char *>(d);
     fb += (16 - (reinterpret_cast<uintptr_t>(fb) & 15)) & 15;
@@ -100,7 +109,11 @@ __device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
     unsigned char *p = reinterpret_cast<unsigned char *>(f);
     p += (8 - (reinterpret_cast<uintptr_t>(p) & 7)) & 7;
     s.spin = reinterpret_cast<uint64_t *>(p);
-    s.flag = reinterpret_cast<int *>(s.spin + kMaxSpinWords);
+    s.mbar = s.spin + kMaxSpinWords;
+    s.flag = reinterpret_cast<int *>(s.mbar + 1);
+    unsigned char *tb = reinterpret_cast<unsigned char *>(s.flag + 4);
+    tb += (16 - (reinterpret_cast<uintptr_t>(tb) & 15)) & 15;
+    s.tabs = reinterpret_cast<float *>(tb);
     return s;
 }
 
@@ -137,8 +150,11 @@ __device__ void cofactor_abs(const double *m, int K, int r, int c, double &cof, 
 }
 
 // Row k from the spins: theta (double-float sums of b and +-w), tanh(theta)
-// in FP32, and Phi[k][.] in FP64 scaled by the row's largest entry.
-// Block-wide; ends with a barrier.
+// in FP32, and Phi[k][.] in FP64, scaled by a power of two that brings the
+// row's largest entry near 1:
+//   Phi[k][kk] ~ P_kk exp(A_kk - max A),  A_kk = sum_i sigma_i a_i + sum_j |theta_j|,
+//   P_kk = prod_j (1 + e^{-2|theta_j|})  (each factor in (1, 2]),
+// one exp per hidden unit and per entry. Block-wide; ends with a barrier.
 __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
     const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, MP = A.MP;
     const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
@@ -151,7 +167,7 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
             l = A.bl[kk * MP + j];
             for (int i = 0; i < N; i++) {
                 const size_t o = (size_t(kk) * N + i) * MP + j;
-                const float wh = A.whp[o], wl = A.wlp[o];
+                const float wh = sm.twh[o], wl = sm.twl[o];
                 if (down_bit(sk, i))
                     df_add(h, l, -wh, -wl);
                 else
@@ -164,25 +180,46 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
         sm.t[q * MP + j] = t;
     }
     __syncthreads();
-    for (int kk = warp; kk < K; kk += nwarp) {
-        const int q = k * K + kk;
-        double lin = 0.0, pr = 1.0, as = 0.0;
-        for (int j = lane; j < M; j += 32) {
+    // partial sums of A and products P over slots (kk, part): every warp takes
+    // slots, each slot a strided share of the row's hidden units
+    const int wpk = max(1, nwarp / K);
+    for (int v = warp; v < K * wpk; v += nwarp) {
+        const int kk = v / wpk, part = v - kk * wpk, q = k * K + kk;
+        double lin = 0.0, pr = 1.0;
+        for (int j = lane + 32 * part; j < M; j += 32 * wpk) {
             const double th = double(sm.th_hi[q * MP + j]) + double(sm.th_lo[q * MP + j]);
             lin += fabs(th);
             pr *= 1.0 + exp(-2.0 * fabs(th));
         }
-        for (int i = lane; i < N; i += 32) as += down_bit(sk, i) ? -A.a64[kk * N + i] : A.a64[kk * N + i];
+        if (part == 0)
+            for (int i = lane; i < N; i += 32) lin += down_bit(sk, i) ? -A.a64[kk * N + i] : A.a64[kk * N + i];
         lin = warp_sum(lin);
-        as = warp_sum(as);
         pr = warp_prod(pr);
-        if (lane == 0) sm.lsum[q] = as + lin + log(pr);
+        if (lane == 0) {
+            sm.jpart[2 * v] = lin;
+            sm.jpart[2 * v + 1] = pr;
+        }
     }
     __syncthreads();
-    if (tid == 0) {
-        double mx = -1e308;
-        for (int kk = 0; kk < K; kk++) mx = fmax(mx, sm.lsum[k * K + kk]);
-        for (int kk = 0; kk < K; kk++) sm.phi[k * K + kk] = exp(sm.lsum[k * K + kk] - mx);
+    if (warp == 0) {
+        // lanes kk < K: the entry from its slots; then the row's scaling
+        double a = -1e308, pp = 0.0;
+        if (lane < K) {
+            a = 0.0;
+            pp = 1.0;
+            for (int part = 0; part < wpk; part++) {
+                a += sm.jpart[2 * (lane * wpk + part)];
+                pp *= sm.jpart[2 * (lane * wpk + part) + 1];
+            }
+        }
+        double mx = a;
+        for (int o = 1; o < 4; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mx = __shfl_sync(0xffffffffu, mx, 0);
+        const double e = lane < K ? pp * exp(a - mx) : 0.0;
+        int ex = lane < K ? expo(e) : -100000;
+        for (int o = 1; o < 4; o <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, o));
+        ex = __shfl_sync(0xffffffffu, ex, 0);
+        if (lane < K) sm.phi[k * K + lane] = scale2(e, -ex);
     }
     __syncthreads();
 }
@@ -217,7 +254,8 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
     bool live[U];  // unit inside the RBM (not padding) and lane in a group
 #pragma unroll
     for (int u = 0; u < U; u++) live[u] = active && base + u < M;
-    uint64_t sk[2] = {sm.spin[k * NW], NW > 1 ? sm.spin[k * NW + 1] : 0ULL};
+    uint64_t sk0 = sm.spin[k * NW], sk1 = NW > 1 ? sm.spin[k * NW + 1] : 0ULL;
+    auto bit = [&](int b) -> bool { return ((b < 64 ? sk0 : sk1) >> (b & 63)) & 1ULL; };
 
     // Decision state, identical in every lane: exact cofactors of row k (the
     // other rows are exact), the row's entries, g and det with error bounds.
@@ -243,13 +281,13 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
     bool changed = false;
 
     for (int i = 0; i < N; i++) {
-        const bool down = (sk[i >> 6] >> (i & 63)) & 1ULL;
+        const bool down = bit(i);
         const size_t row = (size_t(kkl) * N + i) * MP + base;
         float cq[U], sq[U];
 #pragma unroll
         for (int u = 0; u < U; u++) {
-            cq[u] = __ldg(A.cp + row + u);
-            sq[u] = __ldg(A.spp + row + u);
+            cq[u] = sm.tc[row + u];
+            sq[u] = sm.ts[row + u];
         }
         float ea[K];
         float4 bd[K];
@@ -306,8 +344,8 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                     float h = A.bh[kkl * MP + j], l = A.bl[kkl * MP + j];
                     for (int i2 = 0; i2 < N; i2++) {
                         const size_t o = (size_t(kkl) * N + i2) * MP + j;
-                        const float wh = A.whp[o], wl = A.wlp[o];
-                        if ((sk[i2 >> 6] >> (i2 & 63)) & 1ULL)
+                        const float wh = sm.twh[o], wl = sm.twl[o];
+                        if (bit(i2))
                             df_add(h, l, -wh, -wl);
                         else
                             df_add(h, l, wh, wl);
@@ -328,29 +366,49 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                 pr *= __shfl_xor_sync(0xffffffffu, pr, o);
                 pr2 *= __shfl_xor_sync(0xffffffffu, pr2, o);
             }
-            double Lc[K], Ln[K], mx = -1e308;
+            // A = sum sigma a + sum |theta| and P = prod (1 + e^{-2|theta|}) per RBM,
+            // current (c) and proposed (n); entries P exp(A - max A_c), one exp
+            // per lane (lanes kk and K + kk)
+            double as[K];
 #pragma unroll
             for (int kk = 0; kk < K; kk++) {
-                double as = 0.0;
+                as[kk] = 0.0;
                 for (int i2 = lane; i2 < N; i2 += 32) {
                     const double ai = A.a64[kk * N + i2];
-                    as += ((sk[i2 >> 6] >> (i2 & 63)) & 1ULL) ? -ai : ai;
+                    as[kk] += bit(i2) ? -ai : ai;
                 }
-                as = warp_sum(as);
-                const double l1 = __shfl_sync(0xffffffffu, lin, kk * G);
-                const double l2 = __shfl_sync(0xffffffffu, lin2, kk * G);
-                const double p1 = __shfl_sync(0xffffffffu, pr, kk * G);
-                const double p2 = __shfl_sync(0xffffffffu, pr2, kk * G);
-                const double ai = A.a64[kk * N + i];
-                Lc[kk] = as + l1 + log(p1);
-                Ln[kk] = as + (down ? 2.0 * ai : -2.0 * ai) + l2 + log(p2);
-                mx = fmax(mx, Lc[kk]);
             }
-            double pc[K], pn[K], det_e = 0.0, sx = 0.0;
+            double Ac[K], An[K], Pc[K], Pn[K], mx = -1e308;
 #pragma unroll
             for (int kk = 0; kk < K; kk++) {
-                pc[kk] = exp(Lc[kk] - mx);
-                pn[kk] = exp(Ln[kk] - mx);
+                as[kk] = warp_sum(as[kk]);
+                const double ai = A.a64[kk * N + i];
+                Ac[kk] = as[kk] + __shfl_sync(0xffffffffu, lin, kk * G);
+                An[kk] = as[kk] + (down ? 2.0 * ai : -2.0 * ai) + __shfl_sync(0xffffffffu, lin2, kk * G);
+                Pc[kk] = __shfl_sync(0xffffffffu, pr, kk * G);
+                Pn[kk] = __shfl_sync(0xffffffffu, pr2, kk * G);
+                mx = fmax(mx, Ac[kk]);
+            }
+            double ev = 0.0;
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) {
+                if (lane == kk) ev = Pc[kk] * exp(Ac[kk] - mx);
+                if (lane == K + kk) ev = Pn[kk] * exp(An[kk] - mx);
+            }
+            // both rows scaled by one power of two that brings the current row's
+            // largest entry near 1 (the test is invariant; FP32 copies stay in range)
+            double pc[K], pn[K], det_e = 0.0, sx = 0.0;
+            int pex = -100000;
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) {
+                pc[kk] = __shfl_sync(0xffffffffu, ev, kk);
+                pn[kk] = __shfl_sync(0xffffffffu, ev, K + kk);
+                pex = max(pex, expo(pc[kk]));
+            }
+#pragma unroll
+            for (int kk = 0; kk < K; kk++) {
+                pc[kk] = scale2(pc[kk], -pex);
+                pn[kk] = scale2(pn[kk], -pex);
                 det_e += pc[kk] * cofd[kk];
                 sx += pn[kk] * cofd[kk];
             }
@@ -404,14 +462,17 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                 det32 *= sc;
                 edet *= sc;
             }
-            sk[i >> 6] ^= 1ULL << (i & 63);
+            if (i < 64)
+                sk0 ^= 1ULL << i;
+            else
+                sk1 ^= 1ULL << (i - 64);
             changed = true;
             nacc++;
         }
     }
     if (lane == 0) {
-        sm.spin[k * NW] = sk[0];
-        if (NW > 1) sm.spin[k * NW + 1] = sk[1];
+        sm.spin[k * NW] = sk0;
+        if (NW > 1) sm.spin[k * NW + 1] = sk1;
     }
     return changed;
 }
@@ -426,6 +487,33 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
     const int c = blockIdx.x;
     DSmem sm = dcarve(smem_raw, N, MP, K);
     const bool writer = tid == 0;
+    const size_t tb = dw_table_bytes(N, MP, K);
+    if (A.stage) {
+        // the step's tables into shared memory by bulk copies (one mbarrier phase)
+        float *stc = sm.tabs, *sts = stc + tb / 4, *stwh = sts + tb / 4, *stwl = stwh + tb / 4;
+        if (writer) {
+            mbar_init(sm.mbar, 1);
+            mbar_expect_tx(sm.mbar, unsigned(4 * tb));
+            bulk_g2s(stc, A.cp, unsigned(tb), sm.mbar);
+            bulk_g2s(sts, A.spp, unsigned(tb), sm.mbar);
+            bulk_g2s(stwh, A.whp, unsigned(tb), sm.mbar);
+            bulk_g2s(stwl, A.wlp, unsigned(tb), sm.mbar);
+            const bool ok = mbar_wait(sm.mbar, 0);
+            sm.flag[2] = ok ? 1 : 0;
+            if (!ok) atomicOr(A.err, kErrTimeout);
+        }
+        __syncthreads();
+        if (!sm.flag[2]) return;  // every thread: the copy did not complete in time
+        sm.tc = stc;
+        sm.ts = sts;
+        sm.twh = stwh;
+        sm.twl = stwl;
+    } else {
+        sm.tc = A.cp;
+        sm.ts = A.spp;
+        sm.twh = A.whp;
+        sm.twl = A.wlp;
+    }
 
     // init_multi_spin (code/rbm.cc:98-119): every thread advances the stream;
     // warp 0 keeps it for the proposals.
@@ -466,28 +554,63 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
             for (int t = 0; t < KK; t++) sm.pinv[t] = pinv[t];
         }
         __syncthreads();
-        for (int k = warp; k < K; k += nwarp) {
-            const uint64_t *sk = sm.spin + k * NW;
-            double acc = 0.0;
-            for (int i = 1 + lane; i < N; i += 32) {
-                const bool si = down_bit(sk, i);
-                const double *Jr = A.J + size_t(i) * N;
-                for (int j = 0; j < i; j++) acc += (si ^ down_bit(sk, j)) ? -Jr[j] : Jr[j];
+        {
+            // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031): the
+            // N x N grid strided over the block, partial sums per warp, then the
+            // warps' partials in order (deterministic)
+            double acc[K];
+#pragma unroll
+            for (int k = 0; k < K; k++) acc[k] = 0.0;
+            int i = tid / N, j = tid - (tid / N) * N;
+            const int di = T / N, dj = T - (T / N) * N;
+            while (i < N) {
+                if (j < i) {
+                    const double p = A.J[size_t(i) * N + j];
+#pragma unroll
+                    for (int k = 0; k < K; k++) acc[k] += (down_bit(sm.spin + k * NW, i) ^ down_bit(sm.spin + k * NW, j)) ? -p : p;
+                }
+                j += dj;
+                i += di;
+                if (j >= N) {
+                    j -= N;
+                    i++;
+                }
             }
-            acc = warp_sum(acc);
-            if (lane == 0) sm.jk[k] = 2.0 * acc;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                acc[k] = warp_sum(acc[k]);
+                if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
+            }
         }
         for (int it = tid; it < KK * N; it += T) {
             const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
             const bool down = down_bit(sm.spin + k * NW, i);
-            const float *crow = A.cp + (size_t(kk) * N + i) * MP;
-            const float *srow = A.spp + (size_t(kk) * N + i) * MP;
+            const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
+            const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
             const float *trow = sm.t + q * MP;
-            float p = 1.f;
-            for (int j = 0; j < M; j++) p *= fmaf(down ? trow[j] : -trow[j], __ldg(srow + j), __ldg(crow + j));
+            // four independent partial products over 16-byte loads; padded units
+            // (t = 0, c = 1, s = 0) contribute exactly 1, so MP needs no tail
+            const float sg = down ? 1.f : -1.f;
+            float p0 = 1.f, p1 = 1.f, p2 = 1.f, p3 = 1.f;
+            for (int j = 0; j < MP; j += 4) {
+                const float4 tt = *reinterpret_cast<const float4 *>(trow + j);
+                const float4 ss = *reinterpret_cast<const float4 *>(srow + j);
+                const float4 cc = *reinterpret_cast<const float4 *>(crow + j);
+                p0 *= fmaf(sg * tt.x, ss.x, cc.x);
+                p1 *= fmaf(sg * tt.y, ss.y, cc.y);
+                p2 *= fmaf(sg * tt.z, ss.z, cc.z);
+                p3 *= fmaf(sg * tt.w, ss.w, cc.w);
+            }
+            const float p = (p0 * p1) * (p2 * p3);
             sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
             const float B = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
             sm.bsig[it] = down_bit(sm.spin + kk * NW, i) ? -B : B;
+        }
+        __syncthreads();
+        if (tid < K) {
+            double jt = 0.0;
+            for (int w2 = 0; w2 < nwarp; w2++) jt += sm.jpart[w2 * 4 + tid];
+            sm.jk[tid] = 2.0 * jt;
         }
         __syncthreads();
         for (int q = warp; q < KK; q += nwarp) {
@@ -517,19 +640,31 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         float *orow = A.O + s * P;
         for (int k = 0; k < K; k++) {
             float *ok = orow + size_t(k) * L;
-            for (int p = tid; p < L; p += T) {
+            for (int p = tid; p < N + M; p += T) {
                 float v = 0.f;
                 if (p < N) {
+#pragma unroll
                     for (int kk = 0; kk < K; kk++) v += sm.bsig[(k * K + kk) * N + p];
-                } else if (p < N + M) {
-                    const int j = p - N;
-                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.Bm[k * K + kk], sm.t[(kk * K + k) * MP + j], v);
                 } else {
-                    const int q = p - N - M, i = q / M, j = q - i * M;
-                    for (int kk = 0; kk < K; kk++)
-                        v = fmaf(sm.bsig[(k * K + kk) * N + i], sm.t[(kk * K + k) * MP + j], v);
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.Bm[k * K + kk], sm.t[(kk * K + k) * MP + p - N], v);
                 }
                 ok[p] = v;
+            }
+            float *ow = ok + N + M;
+            int i = tid / M, j = tid - (tid / M) * M;
+            const int di = T / M, dj = T - (T / M) * M;
+            for (int p = tid; p < N * M; p += T) {
+                float v = 0.f;
+#pragma unroll
+                for (int kk = 0; kk < K; kk++) v = fmaf(sm.bsig[(k * K + kk) * N + i], sm.t[(kk * K + k) * MP + j], v);
+                ow[p] = v;
+                j += dj;
+                i += di;
+                if (j >= M) {
+                    j -= M;
+                    i++;
+                }
             }
         }
         __syncthreads();
@@ -627,14 +762,16 @@ int dw_units(const Shape &sh, int *G_out) {
     return U <= 16 ? U : 0;
 }
 
-size_t dw_smem_bytes(const Shape &sh, int MP) { return dsmem_bytes(sh.N, MP, sh.K); }
+size_t dw_smem_bytes(const Shape &sh, int MP, bool staged) { return dsmem_bytes(sh.N, MP, sh.K, staged); }
 
 cudaError_t prepare_sample_dw(const Shape &sh, int MP) {
     int G = 0;
     const DwKernel fn = dw_kernel(sh.K, dw_units(sh, &G));
     if (!fn || G * dw_units(sh, nullptr) != MP) return cudaErrorInvalidConfiguration;
+    const size_t staged = dsmem_bytes(sh.N, MP, sh.K, true);
+    const size_t smem = staged <= 227 * 1024 ? staged : dsmem_bytes(sh.N, MP, sh.K, false);
     return cudaFuncSetAttribute(reinterpret_cast<const void *>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(dsmem_bytes(sh.N, MP, sh.K)));
+                                int(smem));
 }
 
 cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm) {
@@ -645,7 +782,7 @@ cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_
 }
 
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st) {
-    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K);
+    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K, a.stage != 0);
     const DwKernel fn = dw_kernel(a.sh.K, a.U);
     if (!fn || warps < 1 || warps > 8 || a.sh.NW > 2 || a.G * a.U != a.MP) return cudaErrorInvalidConfiguration;
     fn<<<a.chains, 32 * warps, smem, st>>>(a);

@@ -253,18 +253,27 @@ cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
                                ctx->ma, ctx->mb, ctx->st);
 }
 
-// Warps per chain of the decision-warp sampler: 4 while every chain still
-// gets its own resident CTA (the extra warps rebuild rows and form samples),
-// fewer when chains must share SMs.
-int dw_warps(nqes_ctx *ctx, int chains) {
+// Launch plan of the decision-warp sampler: warps per chain (the warps past
+// the first rebuild rows and form samples) and whether the step's tables are
+// bulk-copied into shared memory. The first plan, in the order (4 warps,
+// staged), (4, global), (2, staged), ..., under which every chain gets a
+// resident CTA; else 1 warp reading global memory.
+void dw_plan(nqes_ctx *ctx, int chains, int *warps, int *stage) {
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP);
-    for (int w = 4; w > 1; w >>= 1) {
-        int per_sm = 0;
-        if (dw_occupancy(ctx->sh, 32 * w, smem, &per_sm) == cudaSuccess && per_sm * sms >= chains) return w;
-    }
-    return 1;
+    for (int w = 4; w >= 1; w >>= 1)
+        for (int st = 1; st >= 0; st--) {
+            const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1);
+            if (smem > 227 * 1024) continue;
+            int per_sm = 0;
+            if (dw_occupancy(ctx->sh, 32 * w, smem, &per_sm) == cudaSuccess && per_sm * sms >= chains) {
+                *warps = w;
+                *stage = st;
+                return;
+            }
+        }
+    *warps = 1;
+    *stage = 0;
 }
 
 // The mixed sampler's tables, its shared-memory attribute and its launch,
@@ -277,14 +286,17 @@ cudaError_t launch_mixed_tables(nqes_ctx *ctx) {
     return e;
 }
 size_t mixed_sampler_smem(nqes_ctx *ctx) {
-    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP) : mixed_smem_bytes(ctx->sh);
+    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP, false) : mixed_smem_bytes(ctx->sh);
 }
 cudaError_t prepare_mixed_sampler(nqes_ctx *ctx) {
     return ctx->dw_U ? prepare_sample_dw(ctx->sh, ctx->dw_MP) : prepare_sample_mixed(ctx->sh);
 }
 cudaError_t launch_mixed_sampler(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
-    const MixedArgs A = mixed_args(ctx, chains, m, burn, tk);
-    return ctx->dw_U ? launch_sample_dw(A, dw_warps(ctx, chains), ctx->st) : launch_sample_mixed(A, ctx->st);
+    MixedArgs A = mixed_args(ctx, chains, m, burn, tk);
+    if (!ctx->dw_U) return launch_sample_mixed(A, ctx->st);
+    int warps = 1;
+    dw_plan(ctx, chains, &warps, &A.stage);
+    return launch_sample_dw(A, warps, ctx->st);
 }
 
 template <class S> Tables<S> tables(nqes_ctx *ctx) {
@@ -786,6 +798,10 @@ int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, doub
     if (e & kErrSingular) {
         ctx->err = "a sample was taken at a singular Phi";
         return NQES_ERR_NONFINITE;
+    }
+    if (e & kErrTimeout) {
+        ctx->err = "a bounded device-side wait ran out (staging of the sampler's tables)";
+        return NQES_ERR_TIMEOUT;
     }
     return NQES_OK;
 }

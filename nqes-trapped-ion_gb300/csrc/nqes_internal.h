@@ -83,10 +83,11 @@ struct MixedArgs {
     const float *cp, *spp, *whp, *wlp, *bh, *bl;
     const float *bnd;                    // per (kk, i): float4 bound record (kernels_sample_warp.cu)
     int G, U, MP;
+    int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
 };
 size_t mixed_smem_bytes(const Shape &sh);
 int dw_units(const Shape &sh, int *G_out);  // U of the decision-warp form, 0 if it does not apply
-size_t dw_smem_bytes(const Shape &sh, int MP);
+size_t dw_smem_bytes(const Shape &sh, int MP, bool staged);
 cudaError_t prepare_sample_dw(const Shape &sh, int MP);
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st);
 cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm);
@@ -102,6 +103,7 @@ enum : int {
     kErrSingular = 2,       // a sample was taken at a singular Phi
     kErrMinresNonFinite = 4,
     kErrMinresCap = 8,      // MINRES-QLP stopped at the device-side iteration cap
+    kErrTimeout = 16,       // a bounded device-side wait ran out
 };
 
 size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith);
