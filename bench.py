@@ -195,6 +195,22 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_form(pkg, J, weights, precision, chains, steps, warmup, seed0, local):
+    """SR steps of one precision form from the same weights and schedule; device
+    time per step (CUDA events inside the library) and the K energies per site."""
+    ctx = pkg.Context(N, M, K, J, H, device=local)
+    ctx.set_weights(*weights)
+    ctx.set_option(pkg.OPT_PRECISION, precision)
+    infos, evals = [], []
+    for t in range(warmup + steps):
+        lr, reglam = schedule(t)
+        e, info = ctx.sr_step(seed0 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        if t >= warmup:
+            infos.append(info)
+        evals.append(np.sort(np.linalg.eigvals(e / N).real))
+    return ctx, infos, evals
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -262,6 +278,9 @@ def run_ours(args):
     fp64_tf = fp64_peak_tflops(torch)
     # algorithmic FLOPs of the S·v passes: one FMA per stored real log-derivative
     sv_flops = 2.0 * ns * ctx.P * (4 if infos[-1]["arith"] == pkg.ARITH_COMPLEX else 1)
+    sv_ms = kern["sv_rows"]["avg_ms"] + kern["sv_cols"]["avg_ms"]
+    sv_gbs = (kern["sv_rows"]["bytes"] + kern["sv_cols"]["bytes"]) / (sv_ms * 1e-3) / 1e9
+    sv_tf = 2.0 * sv_flops / (sv_ms * 1e-3) / 1e12
 
     # ---- end to end through the C ABI with host buffers ----
     a_h, b_h, w_h = ctx.get_weights()
@@ -309,13 +328,55 @@ def run_ours(args):
         "kernels": kern,
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                      "frac": ach / hbm, "traffic": traffic, "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
-                     "fp64": {"achieved_tflops": (sv_flops / (kern[dom]["avg_ms"] * 1e-3) / 1e12)
-                              if dom.startswith("sv") else None,
-                              "peak_tflops_dgemm": fp64_tf}},
+                     "note": ("the sampler is bound by the serial latency of each chain's proposals (one chain per "
+                              "SM at 128 chains), not by HBM or a tensor pipe: its HBM fraction is the bytes it "
+                              "writes (O, E, spins) over its time" if dom == "sample" else ""),
+                     "sv": {"achieved_gbs": sv_gbs, "frac_hbm": sv_gbs / hbm,
+                            "achieved_fp64_tflops": sv_tf, "peak_fp64_tflops_dgemm": fp64_tf,
+                            "frac_fp64": sv_tf / fp64_tf}},
         "e2e": {"value": e2e, "unit": "MC samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
     }
     if clk:
         out["clocks"] = clk
+
+    # ---- the mixed-precision form on the same weights, seeds and schedule ----
+    if not args.no_mixed:
+        seed0 = SEED + rank * 1000003
+        cf, if_, ef = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_FP64, chains, args.steps, args.warmup, seed0, local)
+        cf.close()
+        cm, im, em = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_MIXED, chains, args.steps, args.warmup, seed0, local)
+        ms_f = sum(i["ms_total"] for i in if_) / args.steps
+        ms_m = sum(i["ms_total"] for i in im) / args.steps
+        ksm, _ = cm.time_kernel(pkg.KERNEL_SAMPLE, reps=3)
+        # first step: same weights, hence the same Markov chains; the difference
+        # is the FP32 arithmetic alone. Later steps start from weights that
+        # differ by the FP32 solve (~1e-6) and so draw different chains.
+        dE = float(np.max(np.abs(em[0] - ef[0]) / np.abs(ef[0])))
+        dE_last = float(np.max(np.abs(em[-1] - ef[-1]) / np.abs(ef[-1])))
+        out["mixed"] = {
+            "value": ns / (ms_m * 1e-3), "unit": "MC samples/s", "ms_per_step": ms_m,
+            "sr_steps_per_s": 1e3 / ms_m, "speedup_vs_fp64": ms_f / ms_m, "fp64_ms_per_step": ms_f,
+            "sampler_ms": ksm, "fp64_sampler_ms": kern["sample"]["avg_ms"],
+            "dE_rel": dE, "dE_note": "max_k |E_k mixed - E_k FP64| / |E_k| per site at the first step: same "
+                                     "weights and seeds, so the same Markov chains",
+            "dE_rel_last_step": dE_last, "dE_last_note": "after %d steps the weights differ by the FP32 solve, so the "
+                                                         "chains differ: Monte Carlo noise, not arithmetic" % (args.warmup + args.steps),
+            "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for i in im])),
+            "dtype": "f32 factors/decisions (certified) + f64 theta, Phi, MINRES-QLP, update",
+        }
+        cm.close()
+
+    # ---- the 4096-chain sweep (both forms, fewer steps) ----
+    if args.sweep_chains:
+        sweep = {}
+        for prec, name in ((pkg.PRECISION_FP64, "fp64"), (pkg.PRECISION_MIXED, "mixed")):
+            c4, i4, _ = run_form(pkg, J, (a0, b0, w0), prec, args.sweep_chains, 2, 1, SEED + 7, local)
+            ms = sum(i["ms_total"] for i in i4) / len(i4)
+            sweep[name] = {"ms_per_step": ms, "value": args.sweep_chains * SAMPLES / (ms * 1e-3),
+                           "unit": "MC samples/s", "minres_iters_mean": float(np.mean([i["minres_iters"] for i in i4]))}
+            c4.close()
+        sweep["chains"] = args.sweep_chains
+        out["sweep"] = sweep
     if rank == 0 and world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, args.warmup)
     if rank == 0:
@@ -333,6 +394,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--chains", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form")
+    ap.add_argument("--sweep-chains", type=int, default=4096, help="chains of the sweep line (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -6,33 +6,27 @@
 // One warp (warp 0 of the chain's CTA) runs every proposal of a row. Its
 // lanes form K groups of G lanes (G the largest power of two <= 32/K); lane
 // (kk, jl) owns hidden units j = jl*U .. jl*U+U-1 of RBM kk and keeps their
-// tanh(theta) and theta (as an FP32 pair, hi + lo) in registers for the whole
-// row. A proposal is U fused multiply-adds, a log2(G)-level shuffle tree
-// inside each group and K broadcasts; every lane then holds all K products
-// and takes the accept decision itself, so a proposal needs no CTA barrier
-// and no shared-memory round trip. An accepted flip adds -2 sigma w to the
-// lane's theta pairs (double-float addition) and recomputes tanh in FP32: no
-// FP64 instruction on the proposal path.
+// tanh(theta) in registers for the whole row. A proposal is U fused
+// multiply-adds, a log2(G)-level shuffle tree inside each group and K
+// broadcasts; every lane then holds all K products and takes the accept
+// decision itself, so a proposal needs no CTA barrier and no shared-memory
+// round trip. An accepted flip updates tanh by the exact identity
+// t' = (t c - sigma s) / f with f already at hand: no FP64 instruction on the
+// proposal path.
 //
 // At the end of a row that changed, the whole CTA (the other warps wait at a
 // barrier meanwhile) rebuilds that row's theta from the spins as double-float
-// sums of b and the +-w, recomputes tanh, and recomputes the row of Phi in
-// FP64 from log Phi = sum_i sigma_i a_i + sum_j |theta_j| +
-// log prod_j (1 + e^{-2|theta_j|}) (up to a constant), so every row of Phi is
-// exact (to ~1e-12 relative) whenever another row is swept. The FP32 bound
-// on a decision therefore only carries the drift of the current row.
+// sums of b and the +-w, recomputes tanh with tanhf, and recomputes the row of
+// Phi in FP64, so every row of Phi is exact (to ~1e-12 relative) whenever
+// another row is swept: a decision's bound only carries the drift of the
+// swept row. The error model of a proposal is stated at run_row. A decision
+// the bound cannot make, or any value out of FP32's normal range, goes to the
+// exact path: the swept row's current and proposed entries in FP64 from theta
+// and the reference's test u |det Phi|^2 <= |det Phi'|^2 in FP64.
 //
-// Decision bound (all in units of u = 2^-24), per factor f = c - sigma t s
-// with c, s rounded once from FP64 and t = tanhf(theta_hi) within 5 u |t|:
-// ((|c| + 6 |t s|) / |f| + 1) u; per product one rounding; so the row's ratio
-// r_kk has relative error beta_kk = u (sum_j (|c| + 6|t s|)/|f| + 2M + 16).
-// det Phi' = sum_kk r_kk e^{-2 sigma a} g_kk with g_kk = Phi[k][kk] cof(k, kk)
-// (cofactors exact, from the other rows): the bound adds four roundings per
-// term, the drift rho of row k (sum of the accepted ratios' bounds) and the
-// rounding of the sum. A decision the bound cannot make, or any value out of
-// FP32's normal range, goes to the exact path: row k's current and proposed
-// entries in FP64 from theta (log cosh sums as above) and the reference's
-// test u |det Phi|^2 <= |det Phi'|^2 in FP64.
+// The step's tables (cosh 2w, sinh 2w, w as hi + lo; padded to MP units per
+// row so that padding factors are exactly 1) are bulk-copied into shared
+// memory (cp.async.bulk on an mbarrier) when the launch plan allows.
 #include <algorithm>
 #include <cfloat>
 
