@@ -55,6 +55,10 @@ extern "C" {
                                       * The filter skips the FP64 work of proposals that a rigorous
                                       * FP32 bound proves rejected, in sweeps that follow a sweep with
                                       * under 50% acceptance; results are bit-identical either way. */
+#define NQES_OPT_AUTOTUNE 7          /* 1: time the sampler's admissible launch shapes on the first step of
+                                      * each (chains, samples, burn-in, precision, arithmetic) and keep the
+                                      * fastest; 0 (default): occupancy-based choice. Results do not depend
+                                      * on the launch shape beyond FP64 rounding of the product trees. */
 #define NQES_OPT_MIXED_EXACT 6       /* 1: MIXED takes every accept decision by its exact FP64 path
                                       * (verification of that path); 0 (default): only when the FP32
                                       * bound cannot decide. */
@@ -182,6 +186,29 @@ int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double
  * Errors are described by nqes_last_error(NULL). */
 int nqes_apply_S_static(const double *O, const double *o, const double *skk, const double *v, double *out,
                         int64_t n_samples, int64_t n_params, int complex_arith, void *stream);
+
+/* ---- batched multi-solve ----
+ * No counterpart in the reference (it runs one solve per process). A batch
+ * runs one SR step of every member context in ONE CUDA graph launch: each
+ * member's step (sampling segment, MINRES-QLP while loop, update) is an
+ * independent branch of the graph, so solves of different shapes overlap on
+ * the GPU. Each member's results are exactly those of nqes_sr_step on it.
+ * Members stay owned by the caller, live on one device, may differ in N, M,
+ * K, J, h and precision, and may also be stepped on their own; the batch
+ * re-captures its graph when a member's step shape changes. Errors are
+ * described by nqes_batch_last_error (NULL: the last failed create). */
+typedef struct nqes_batch nqes_batch;
+int nqes_batch_create(nqes_ctx *const *members, int count, nqes_batch **out);
+int nqes_batch_destroy(nqes_batch *batch);
+const char *nqes_batch_last_error(const nqes_batch *batch);
+/* One SR step of every member; every array has `count` entries in member
+ * order, with nqes_sr_step's meaning. e_mats (or an entry) and infos may be
+ * NULL; statuses (may be NULL) receives each member's status; ms_total (may be
+ * NULL) the device time of the batched launch. Returns the first member error. */
+int nqes_batch_sr_step(nqes_batch *batch, const uint64_t *seeds, const int *chains, const int *samples_per_chain,
+                       const int *burn_in, const double *lr, const double *reglam, const double *rtol,
+                       const uint64_t *maxit, double *const *e_mats, nqes_step_info *infos, int *statuses,
+                       double *ms_total);
 
 #ifdef __cplusplus
 }

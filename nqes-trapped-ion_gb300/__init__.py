@@ -23,14 +23,14 @@ OK = 0
 ERR_CUDA, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_INVALID, ERR_STATE = -1, -2, -3, -4, -5, -6
 ARITH_AUTO, ARITH_COMPLEX, ARITH_REAL = 0, 1, 2
 OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP, OPT_PRECISION = 1, 2, 3, 4
-OPT_REJECT_FILTER, OPT_MIXED_EXACT = 5, 6
+OPT_REJECT_FILTER, OPT_MIXED_EXACT, OPT_AUTOTUNE = 5, 6, 7
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 
 EXPORTS = [
     "nqes_create", "nqes_destroy", "nqes_last_error", "nqes_set_option", "nqes_set_weights", "nqes_get_weights",
     "nqes_init_weights", "nqes_sr_step", "nqes_correlations", "nqes_evaluate", "nqes_get_samples",
     "nqes_get_accepts", "nqes_get_O", "nqes_get_moments", "nqes_get_solution", "nqes_apply_S", "nqes_time_kernel",
-    "nqes_apply_S_static",
+    "nqes_apply_S_static", "nqes_batch_create", "nqes_batch_destroy", "nqes_batch_last_error", "nqes_batch_sr_step",
 ]
 KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
 
@@ -90,6 +90,11 @@ def load_library(path=None):
         "nqes_apply_S": (i, [vp, _dp, _dp]),
         "nqes_time_kernel": (i, [vp, i, i, _dp, _dp]),
         "nqes_apply_S_static": (i, [vp, vp, vp, vp, vp, i64, i64, i, vp]),
+        "nqes_batch_create": (i, [ctypes.POINTER(vp), i, ctypes.POINTER(vp)]),
+        "nqes_batch_destroy": (i, [vp]),
+        "nqes_batch_last_error": (ctypes.c_char_p, [vp]),
+        "nqes_batch_sr_step": (i, [vp, _u64p, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), _dp, _dp, _dp,
+                                   _u64p, ctypes.POINTER(_dp), ctypes.POINTER(StepInfo), ctypes.POINTER(i), _dp]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(lib, name)
@@ -264,3 +269,44 @@ class Context:
         out = np.zeros(self.P, np.complex128)
         self._check(self.lib.nqes_apply_S(self._h, _cp(v), _cp(out)))
         return out
+
+
+class Batch:
+    """One SR step of several contexts (any shapes, same device) per CUDA graph launch."""
+
+    def __init__(self, contexts, lib=None):
+        self.lib = lib or load_library()
+        self.members = list(contexts)
+        arr = (ctypes.c_void_p * len(self.members))(*[c._h for c in self.members])
+        h_ = ctypes.c_void_p()
+        st = self.lib.nqes_batch_create(arr, len(self.members), ctypes.byref(h_))
+        if st != OK:
+            raise NqesError(st, self.lib.nqes_batch_last_error(None).decode())
+        self._h = h_
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.nqes_batch_destroy(self._h)
+            self._h = None
+
+    def sr_step(self, seeds, chains, samples_per_chain, burn_in, lr, reglam, rtol, maxit):
+        """Per-member arguments (sequences, member order); returns (e_mats, infos, statuses, ms_total)."""
+        n = len(self.members)
+        ci = ctypes.c_int * n
+        cd = ctypes.c_double * n
+        cu = ctypes.c_uint64 * n
+        emats = [np.zeros((c.K, c.K), np.complex128) for c in self.members]
+        eptr = (_dp * n)(*[_cp(e) for e in emats])
+        infos = (StepInfo * n)()
+        stat = ci()
+        ms = ctypes.c_double()
+        st = self.lib.nqes_batch_sr_step(self._h, cu(*map(int, seeds)), ci(*map(int, chains)),
+                                         ci(*map(int, samples_per_chain)), ci(*map(int, burn_in)), cd(*map(float, lr)),
+                                         cd(*map(float, reglam)), cd(*map(float, rtol)), cu(*map(int, maxit)), eptr,
+                                         infos, stat, ctypes.byref(ms))
+        if st != OK:
+            raise NqesError(st, self.lib.nqes_batch_last_error(self._h).decode())
+        for c, ch, m in zip(self.members, chains, samples_per_chain):
+            c.chains = int(ch)
+            c.ns = int(ch) * int(m)
+        return emats, [x.as_dict() for x in infos], list(stat), ms.value

@@ -44,6 +44,11 @@ struct nqes_ctx {
     int tk_opt = 0;
     uint64_t minres_cap = 100000;
     bool reject_filter = false;  // FP32 rejection filter in the FP64 real sampler (opt-in)
+    // autotuner (NQES_OPT_AUTOTUNE): launch shape of the sampler chosen by timing,
+    // valid for tune_key = (chains, samples, burn-in, precision, arith)
+    bool autotune = false;
+    long long tune_key[5] = {-1, -1, -1, -1, -1};
+    int tk_tuned = 0, dw_force_warps = 0, dw_force_stage = 0;
     bool mixed_exact_all = false;  // MIXED: every decision through the exact FP64 path
     bool weights_real = true;
     std::string err;
@@ -259,6 +264,11 @@ cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
 // staged), (4, global), (2, staged), ..., under which every chain gets a
 // resident CTA; else 1 warp reading global memory.
 void dw_plan(nqes_ctx *ctx, int chains, int *warps, int *stage) {
+    if (ctx->dw_force_warps) {
+        *warps = ctx->dw_force_warps;
+        *stage = ctx->dw_force_stage;
+        return;
+    }
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     for (int w = 4; w >= 1; w >>= 1)
@@ -353,6 +363,8 @@ int choose_tk(nqes_ctx *ctx, int chains) {
     int tk;
     if (ctx->tk_opt) {
         tk = ctx->tk_opt;
+    } else if (ctx->tk_tuned) {
+        tk = ctx->tk_tuned;
     } else {
         int dev_sms = 152;
         cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -361,11 +373,10 @@ int choose_tk(nqes_ctx *ctx, int chains) {
     return std::min(std::max(tk, tmin), tmax);
 }
 
-template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
-    if (ctx->exec) {
-        cudaGraphExecDestroy(ctx->exec);
-        ctx->exec = nullptr;
-    }
+// Appends one SR step of ctx to graph g as three nodes with no dependency on
+// anything else in g: the sampling segment (tables, sampler, moments, MINRES
+// init), a conditional while node running the MINRES-QLP body, the update.
+template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, int m, int burn, int tk) {
     SampleArgs<S> A = sample_args<S>(ctx, chains, m, burn, tk);
     SolveBufs<S> B = solve_bufs<S>(ctx);
     const int threads = sample_threads(ctx->sh.K, tk);
@@ -382,8 +393,7 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
         else
             NQES_CUDA(prepare_sample<S>(ctx->sh));
     }
-    cudaGraph_t g = nullptr, gA = nullptr, gC = nullptr;
-    NQES_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraph_t gA = nullptr, gC = nullptr;
     cudaGraphConditionalHandle cond;
     // Default value 1 on every launch: the body runs at least once, and its
     // scalar kernel writes 0 as soon as the solve has finished (or was
@@ -406,7 +416,6 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     if (le != cudaSuccess || ce != cudaSuccess) {
         ctx->err = std::string("capture of the sampling segment: ") +
                    cudaGetErrorString(le != cudaSuccess ? le : ce);
-        cudaGraphDestroy(g);
         return NQES_ERR_CUDA;
     }
     cudaGraphNode_t nA, nW, nC;
@@ -425,7 +434,6 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
     ce = cudaStreamEndCapture(ctx->st, &body);
     if (le != cudaSuccess || ce != cudaSuccess) {
         ctx->err = std::string("capture of the MINRES-QLP body: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
-        cudaGraphDestroy(g);
         cudaGraphDestroy(gA);
         return NQES_ERR_CUDA;
     }
@@ -437,10 +445,25 @@ template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, i
         return NQES_ERR_CUDA;
     }
     NQES_CUDA(cudaGraphAddChildGraphNode(&nC, g, &nW, 1, gC));
-    NQES_CUDA(cudaGraphInstantiate(&ctx->exec, g, 0));
     cudaGraphDestroy(gA);
     cudaGraphDestroy(gC);
+    return NQES_OK;
+}
+
+template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
+    if (ctx->exec) {
+        cudaGraphExecDestroy(ctx->exec);
+        ctx->exec = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    NQES_CUDA(cudaGraphCreate(&g, 0));
+    int rc = add_step_nodes<S>(ctx, g, chains, m, burn, tk);
+    if (rc == NQES_OK && cudaGraphInstantiate(&ctx->exec, g, 0) != cudaSuccess) {
+        ctx->err = "cudaGraphInstantiate failed";
+        rc = NQES_ERR_CUDA;
+    }
     cudaGraphDestroy(g);
+    if (rc) return rc;
     ctx->g_chains = chains;
     ctx->g_m = m;
     ctx->g_burn = burn;
@@ -479,6 +502,174 @@ int copy_out_c(nqes_ctx *ctx, const void *src, size_t n, double *dst) {
             dst[2 * t + 1] = 0.0;
         }
     }
+    return NQES_OK;
+}
+
+// ---- one SR step in pieces (shared by nqes_sr_step and the batch) ----
+
+template <class S> int tune_sampler(nqes_ctx *ctx, int chains, int m, int burn);
+
+// Validates the arguments, sizes the step buffers, fills the step scalars and,
+// with NQES_OPT_AUTOTUNE, picks the sampler's launch shape by timing.
+int step_prepare(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, double lr, double reglam, double rtol,
+                 uint64_t maxit, int *arith_out) {
+    if (chains < 1 || m < 1 || burn < 0 || !std::isfinite(lr) || !std::isfinite(reglam) || !(rtol >= 0)) {
+        ctx->err = "invalid SR step arguments (chains >= 1, m >= 1, burn_in >= 0, finite lr/reglam, rtol >= 0)";
+        return NQES_ERR_INVALID;
+    }
+    NQES_CUDA(cudaSetDevice(ctx->device));
+    const int arith = resolve_arith(ctx);
+    if (ctx->precision == NQES_PRECISION_MIXED && arith != NQES_ARITH_REAL) {
+        ctx->err = "mixed precision needs real weights (NQES_ARITH_REAL)";
+        return NQES_ERR_INVALID;
+    }
+    int rc = ensure_step_buffers(ctx, chains, m, arith);
+    if (rc) return rc;
+    StepParams &p = *ctx->sp_host;
+    p.seed = seed;
+    p.lr = lr;
+    p.reglam = reglam;
+    p.rtol = rtol;
+    p.maxit = std::min<uint64_t>(maxit, ctx->minres_cap);
+    *arith_out = arith;
+    if (ctx->autotune) {
+        const long long key[5] = {chains, m, burn, ctx->step_precision, arith};
+        if (!std::equal(key, key + 5, ctx->tune_key)) {
+            rc = arith == NQES_ARITH_COMPLEX ? tune_sampler<cplx>(ctx, chains, m, burn)
+                                             : tune_sampler<double>(ctx, chains, m, burn);
+            if (rc) return rc;
+            std::copy(key, key + 5, ctx->tune_key);
+        }
+    }
+    return NQES_OK;
+}
+
+// Queues the copies of the step's results to pinned host memory on stream st.
+int step_readback(nqes_ctx *ctx, cudaStream_t st) {
+    NQES_CUDA(cudaMemcpyAsync(ctx->emat_host, ctx->emat_d, sizeof(cplx) * ctx->sh.K * ctx->sh.K,
+                              cudaMemcpyDeviceToHost, st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->emat_host + 16, ctx->eloc_d, sizeof(cplx), cudaMemcpyDeviceToHost, st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->qs_host, ctx->qs, sizeof(QlpState), cudaMemcpyDeviceToHost, st));
+    NQES_CUDA(cudaMemcpyAsync(ctx->err_host, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    return NQES_OK;
+}
+
+// After the step's stream has drained: e_mat, the step report, error bits.
+int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t maxit, float ms, double *e_mat,
+                nqes_step_info *info) {
+    ctx->have_step = true;
+    ctx->last_burn = burn;
+    if (e_mat) std::memcpy(e_mat, ctx->emat_host, sizeof(cplx) * ctx->sh.K * ctx->sh.K);
+    const QlpState &q = *ctx->qs_host;
+    if (info) {
+        std::memset(info, 0, sizeof(*info));
+        info->minres_flag = q.flag;
+        info->arith = arith;
+        info->minres_iters = q.iters;
+        info->qlp_iters = q.qlp_iters;
+        info->relres = q.relres;
+        info->anorm = q.anorm;
+        info->acond = q.acond;
+        info->xnorm = q.xnorm;
+        info->proposals = uint64_t(chains) * (burn + m) * ctx->sh.K * ctx->sh.N;
+        info->eloc_re = ctx->emat_host[16].re;
+        info->eloc_im = ctx->emat_host[16].im;
+        info->ms_total = ms;
+        std::vector<unsigned long long> acc(chains);
+        NQES_CUDA(cudaMemcpy(acc.data(), ctx->accepted, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
+        for (auto x : acc) info->accepted += x;
+        if (q.flag == 8 && q.iters >= ctx->minres_cap && maxit > ctx->minres_cap) info->warnings |= 1;
+        // tables, sampler, 3 moment kernels, 3 MINRES-QLP init kernels, update,
+        // and 6 kernels per execution of the loop body
+        info->kernel_launches = 9 + 6 * q.bodies;
+        info->precision = ctx->step_precision;
+        if (ctx->step_precision == NQES_PRECISION_MIXED) {
+            std::vector<unsigned long long> ex(chains);
+            NQES_CUDA(cudaMemcpy(ex.data(), ctx->exact, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
+            for (auto x : ex) info->exact_decisions += x;
+        }
+    }
+    const int e = *ctx->err_host;
+    if (e & (kErrNonFinite | kErrMinresNonFinite)) {
+        ctx->err = "non-finite value during the SR step (error bits " + std::to_string(e) + ")";
+        return NQES_ERR_NONFINITE;
+    }
+    if (e & kErrSingular) {
+        ctx->err = "a sample was taken at a singular Phi";
+        return NQES_ERR_NONFINITE;
+    }
+    if (e & kErrTimeout) {
+        ctx->err = "a bounded device-side wait ran out (staging of the sampler's tables)";
+        return NQES_ERR_TIMEOUT;
+    }
+    return NQES_OK;
+}
+
+// Autotuner: times the sampler alone (tables built, a shortened chain of
+// min(m, 8) samples after min(burn, 2) sweeps) for every admissible launch
+// shape and keeps the fastest: threads per column block for the FP64 and
+// block-form mixed samplers, (warps per chain, table staging) for the
+// decision-warp sampler.
+template <class S> int tune_sampler(nqes_ctx *ctx, int chains, int m, int burn) {
+    const int mt = std::min(m, 8), bt = std::min(burn, 2);
+    const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
+    NQES_CUDA(cudaMemcpyAsync(ctx->sp, ctx->sp_host, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->st));
+    if (mixed)
+        NQES_CUDA(launch_mixed_tables(ctx));
+    else
+        NQES_CUDA(launch_tables_ctx<S>(ctx));
+    auto time_one = [&](auto &&launch, float *ms) -> cudaError_t {
+        cudaError_t e = launch();  // warm-up
+        if (e != cudaSuccess) return e;
+        cudaEventRecord(ctx->ev0, ctx->st);
+        e = launch();
+        cudaEventRecord(ctx->ev1, ctx->st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1);
+        return e;
+    };
+    float best = 1e30f;
+    if (mixed && ctx->dw_U) {
+        NQES_CUDA(prepare_mixed_sampler(ctx));
+        int bw = 0, bs = 0;
+        for (int w = 1; w <= 4; w <<= 1)
+            for (int st = 0; st <= 1; st++) {
+                if (dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1) > 227 * 1024) continue;
+                ctx->dw_force_warps = w;
+                ctx->dw_force_stage = st;
+                float ms = 0;
+                NQES_CUDA(time_one([&] { return launch_mixed_sampler(ctx, chains, mt, bt, 0); }, &ms));
+                if (ms < best) {
+                    best = ms;
+                    bw = w;
+                    bs = st;
+                }
+            }
+        ctx->dw_force_warps = bw;
+        ctx->dw_force_stage = bs;
+        return NQES_OK;
+    }
+    const int M = ctx->sh.M, K = ctx->sh.K;
+    const int tmin = std::max(32, ((M + 7) / 8 + 31) / 32 * 32), tmax = std::max(32, 256 / K / 32 * 32);
+    if (mixed)
+        NQES_CUDA(prepare_mixed_sampler(ctx));
+    else
+        NQES_CUDA(prepare_sample<S>(ctx->sh));
+    int bt_k = tmin;
+    for (int tk = tmin; tk <= tmax; tk += 32) {
+        float ms = 0;
+        if (mixed) {
+            NQES_CUDA(time_one([&] { return launch_sample_mixed(mixed_args(ctx, chains, mt, bt, tk), ctx->st); }, &ms));
+        } else {
+            const SampleArgs<S> A = sample_args<S>(ctx, chains, mt, bt, tk);
+            NQES_CUDA(time_one([&] { return launch_sample<S>(A, sample_threads(K, tk), ctx->st); }, &ms));
+        }
+        if (ms < best) {
+            best = ms;
+            bt_k = tk;
+        }
+    }
+    ctx->tk_tuned = bt_k;
     return NQES_OK;
 }
 
@@ -650,6 +841,19 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         }
         ctx->precision = int(value);
         return NQES_OK;
+    case NQES_OPT_AUTOTUNE:
+        if (value != 0 && value != 1) {
+            ctx->err = "option value must be 0 or 1";
+            return NQES_ERR_INVALID;
+        }
+        ctx->autotune = value == 1;
+        std::fill(ctx->tune_key, ctx->tune_key + 5, -1LL);
+        ctx->tk_tuned = ctx->dw_force_warps = ctx->dw_force_stage = 0;
+        if (ctx->exec) {
+            cudaGraphExecDestroy(ctx->exec);
+            ctx->exec = nullptr;
+        }
+        return NQES_OK;
     case NQES_OPT_REJECT_FILTER:
     case NQES_OPT_MIXED_EXACT:
         if (value != 0 && value != 1) {
@@ -730,80 +934,17 @@ int nqes_init_weights(nqes_ctx *ctx, uint64_t seed) {
 int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, double lr, double reglam, double rtol,
                  uint64_t maxit, double *e_mat, nqes_step_info *info) {
     if (!ctx) return NQES_ERR_INVALID;
-    if (chains < 1 || m < 1 || burn < 0 || !std::isfinite(lr) || !std::isfinite(reglam) || !(rtol >= 0)) {
-        ctx->err = "invalid SR step arguments (chains >= 1, m >= 1, burn_in >= 0, finite lr/reglam, rtol >= 0)";
-        return NQES_ERR_INVALID;
-    }
-    NQES_CUDA(cudaSetDevice(ctx->device));
-    const int arith = resolve_arith(ctx);
-    if (ctx->precision == NQES_PRECISION_MIXED && arith != NQES_ARITH_REAL) {
-        ctx->err = "mixed precision needs real weights (NQES_ARITH_REAL)";
-        return NQES_ERR_INVALID;
-    }
-    int rc = ensure_step_buffers(ctx, chains, m, arith);
+    int arith = 0;
+    int rc = step_prepare(ctx, seed, chains, m, burn, lr, reglam, rtol, maxit, &arith);
     if (rc) return rc;
-    StepParams &p = *ctx->sp_host;
-    p.seed = seed;
-    p.lr = lr;
-    p.reglam = reglam;
-    p.rtol = rtol;
-    p.maxit = std::min<uint64_t>(maxit, ctx->minres_cap);
     rc = arith == NQES_ARITH_COMPLEX ? sr_step_t<cplx>(ctx, chains, m, burn) : sr_step_t<double>(ctx, chains, m, burn);
     if (rc) return rc;
-    NQES_CUDA(cudaMemcpyAsync(ctx->emat_host, ctx->emat_d, sizeof(cplx) * ctx->sh.K * ctx->sh.K,
-                              cudaMemcpyDeviceToHost, ctx->st));
-    NQES_CUDA(cudaMemcpyAsync(ctx->emat_host + 16, ctx->eloc_d, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->st));
-    NQES_CUDA(cudaMemcpyAsync(ctx->qs_host, ctx->qs, sizeof(QlpState), cudaMemcpyDeviceToHost, ctx->st));
-    NQES_CUDA(cudaMemcpyAsync(ctx->err_host, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    rc = step_readback(ctx, ctx->st);
+    if (rc) return rc;
     NQES_CUDA(cudaStreamSynchronize(ctx->st));
-    ctx->have_step = true;
-    ctx->last_burn = burn;
-    if (e_mat) std::memcpy(e_mat, ctx->emat_host, sizeof(cplx) * ctx->sh.K * ctx->sh.K);
-    const QlpState &q = *ctx->qs_host;
-    if (info) {
-        std::memset(info, 0, sizeof(*info));
-        info->minres_flag = q.flag;
-        info->arith = arith;
-        info->minres_iters = q.iters;
-        info->qlp_iters = q.qlp_iters;
-        info->relres = q.relres;
-        info->anorm = q.anorm;
-        info->acond = q.acond;
-        info->xnorm = q.xnorm;
-        info->proposals = uint64_t(chains) * (burn + m) * ctx->sh.K * ctx->sh.N;
-        info->eloc_re = ctx->emat_host[16].re;
-        info->eloc_im = ctx->emat_host[16].im;
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-        info->ms_total = ms;
-        std::vector<unsigned long long> acc(chains);
-        NQES_CUDA(cudaMemcpy(acc.data(), ctx->accepted, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
-        for (auto x : acc) info->accepted += x;
-        if (q.flag == 8 && q.iters >= ctx->minres_cap && maxit > ctx->minres_cap) info->warnings |= 1;
-        // tables, sampler, 3 moment kernels, 3 MINRES-QLP init kernels, update,
-        // and 6 kernels per execution of the loop body
-        info->kernel_launches = 9 + 6 * q.bodies;
-        info->precision = ctx->step_precision;
-        if (ctx->step_precision == NQES_PRECISION_MIXED) {
-            std::vector<unsigned long long> ex(chains);
-            NQES_CUDA(cudaMemcpy(ex.data(), ctx->exact, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
-            for (auto x : ex) info->exact_decisions += x;
-        }
-    }
-    const int e = *ctx->err_host;
-    if (e & (kErrNonFinite | kErrMinresNonFinite)) {
-        ctx->err = "non-finite value during the SR step (error bits " + std::to_string(e) + ")";
-        return NQES_ERR_NONFINITE;
-    }
-    if (e & kErrSingular) {
-        ctx->err = "a sample was taken at a singular Phi";
-        return NQES_ERR_NONFINITE;
-    }
-    if (e & kErrTimeout) {
-        ctx->err = "a bounded device-side wait ran out (staging of the sampler's tables)";
-        return NQES_ERR_TIMEOUT;
-    }
-    return NQES_OK;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    return step_finish(ctx, chains, m, burn, arith, maxit, ms, e_mat, info);
 }
 
 int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi, double *tanh_theta, double *E,
@@ -1155,6 +1296,159 @@ int nqes_correlations(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn,
     const cplx *V = reinterpret_cast<const cplx *>(evecs);
     return arith == NQES_ARITH_COMPLEX ? correlations_t<cplx>(ctx, seed, chains, m, burn, V, x, z, xx, zz)
                                        : correlations_t<double>(ctx, seed, chains, m, burn, V, x, z, xx, zz);
+}
+
+}  // extern "C"
+
+// ---- batched multi-solve ----
+
+struct nqes_batch {
+    std::vector<nqes_ctx *> m;
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<std::vector<long long>> keys;  // per member: chains, samples, burn, arith, tk, precision
+    std::string err;
+};
+
+namespace {
+std::string g_batch_create_error;
+}
+
+extern "C" {
+
+const char *nqes_batch_last_error(const nqes_batch *b) { return b ? b->err.c_str() : g_batch_create_error.c_str(); }
+
+int nqes_batch_create(nqes_ctx *const *members, int count, nqes_batch **out) {
+    if (!out || !members || count < 1) {
+        g_batch_create_error = "members and out must be non-NULL and count >= 1";
+        return NQES_ERR_INVALID;
+    }
+    *out = nullptr;
+    for (int i = 0; i < count; i++) {
+        if (!members[i]) {
+            g_batch_create_error = "member " + std::to_string(i) + " is NULL";
+            return NQES_ERR_INVALID;
+        }
+        if (members[i]->device != members[0]->device) {
+            g_batch_create_error = "members live on different devices";
+            return NQES_ERR_INVALID;
+        }
+        for (int j = 0; j < i; j++)
+            if (members[j] == members[i]) {
+                g_batch_create_error = "a context appears twice in the batch";
+                return NQES_ERR_INVALID;
+            }
+    }
+    nqes_batch *b = new nqes_batch();
+    b->m.assign(members, members + count);
+    b->device = members[0]->device;
+    if (cudaSetDevice(b->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        g_batch_create_error = "stream or event creation failed";
+        nqes_batch_destroy(b);
+        return NQES_ERR_CUDA;
+    }
+    *out = b;
+    return NQES_OK;
+}
+
+int nqes_batch_destroy(nqes_batch *b) {
+    if (!b) return NQES_OK;
+    cudaSetDevice(b->device);
+    if (b->st) cudaStreamSynchronize(b->st);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return NQES_OK;
+}
+
+int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, const int *samples, const int *burn,
+                       const double *lr, const double *reglam, const double *rtol, const uint64_t *maxit,
+                       double *const *e_mats, nqes_step_info *infos, int *statuses, double *ms_total) {
+    if (!b || !seeds || !chains || !samples || !burn || !lr || !reglam || !rtol || !maxit) return NQES_ERR_INVALID;
+    const int n = int(b->m.size());
+    if (cudaSetDevice(b->device) != cudaSuccess) {
+        b->err = "cudaSetDevice failed";
+        return NQES_ERR_CUDA;
+    }
+    std::vector<int> arith(n), tks(n);
+    std::vector<std::vector<long long>> keys(n);
+    for (int i = 0; i < n; i++) {
+        nqes_ctx *c = b->m[i];
+        const int rc = step_prepare(c, seeds[i], chains[i], samples[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i],
+                                    &arith[i]);
+        if (statuses) statuses[i] = rc;
+        if (rc) {
+            b->err = "member " + std::to_string(i) + ": " + c->err;
+            return rc;
+        }
+        tks[i] = choose_tk(c, chains[i]);
+        keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision};
+    }
+    if (!b->exec || keys != b->keys) {
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        if (cudaGraphCreate(&g, 0) != cudaSuccess) {
+            b->err = "cudaGraphCreate failed";
+            return NQES_ERR_CUDA;
+        }
+        for (int i = 0; i < n; i++) {
+            nqes_ctx *c = b->m[i];
+            const int rc = arith[i] == NQES_ARITH_COMPLEX ? add_step_nodes<cplx>(c, g, chains[i], samples[i], burn[i], tks[i])
+                                                          : add_step_nodes<double>(c, g, chains[i], samples[i], burn[i], tks[i]);
+            if (rc) {
+                b->err = "member " + std::to_string(i) + ": " + c->err;
+                cudaGraphDestroy(g);
+                return rc;
+            }
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            b->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie);
+            return NQES_ERR_CUDA;
+        }
+        b->keys = keys;
+    }
+    for (int i = 0; i < n; i++) {
+        nqes_ctx *c = b->m[i];
+        if (cudaMemcpyAsync(c->sp, c->sp_host, sizeof(StepParams), cudaMemcpyHostToDevice, b->st) != cudaSuccess) {
+            b->err = "step parameter copy failed";
+            return NQES_ERR_CUDA;
+        }
+        c->last_tk = tks[i];
+    }
+    cudaEventRecord(b->ev0, b->st);
+    cudaError_t le = cudaGraphLaunch(b->exec, b->st);
+    cudaEventRecord(b->ev1, b->st);
+    for (int i = 0; i < n && le == cudaSuccess; i++)
+        if (step_readback(b->m[i], b->st)) le = cudaErrorUnknown;
+    if (le == cudaSuccess) le = cudaStreamSynchronize(b->st);
+    if (le != cudaSuccess) {
+        b->err = std::string("batched step: ") + cudaGetErrorString(le);
+        return NQES_ERR_CUDA;
+    }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    if (ms_total) *ms_total = ms;
+    int first = NQES_OK;
+    for (int i = 0; i < n; i++) {
+        const int rc = step_finish(b->m[i], chains[i], samples[i], burn[i], arith[i], maxit[i], ms,
+                                   e_mats ? e_mats[i] : nullptr, infos ? &infos[i] : nullptr);
+        if (statuses) statuses[i] = rc;
+        if (rc && !first) {
+            first = rc;
+            b->err = "member " + std::to_string(i) + ": " + b->m[i]->err;
+        }
+    }
+    return first;
 }
 
 }  // extern "C"

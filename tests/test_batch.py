@@ -1,0 +1,85 @@
+"""Batched multi-solve (one CUDA graph launch per SR step for several solves)
+and the launch-shape autotuner."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import helpers
+from helpers import synthetic_j
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    ge._load_build_module().build_library()
+    return ge.load_package()
+
+
+# (N, M, K, h, J exponent, precision, real weights)
+MEMBERS = [(8, 16, 2, 0.5, 1.2, 0, True), (12, 24, 3, 1.0, 0.9, 1, True), (10, 20, 1, 0.8, 1.5, 0, False),
+           (16, 32, 2, 0.3, 1.1, 1, True)]
+
+
+def make(pkg, idx, spec):
+    N, M, K, h, alpha, prec, real = spec
+    ctx = pkg.Context(N, M, K, synthetic_j(N, alpha), h)
+    ctx.set_weights(*helpers.random_weights(N, M, K, 0.05, 100 + idx, real=real))
+    ctx.set_option(pkg.OPT_PRECISION, prec)
+    return ctx
+
+
+def step_args(t, n):
+    seeds = [1000 + 97 * i + t * 64 for i in range(n)]
+    chains = [8 + 4 * i for i in range(n)]
+    m = [10 + i for i in range(n)]
+    burn = [4] * n
+    lr = [0.1] * n
+    reglam = [5.0 * 0.9 ** t] * n
+    return seeds, chains, m, burn, lr, reglam, [1e-9] * n, [2000] * n
+
+
+def test_batch_equals_individual_steps(pkg):
+    """Each member's e_mat, samples and updated weights are those of nqes_sr_step
+    on the same context, bit for bit, over consecutive batched steps."""
+    alone = [make(pkg, i, s) for i, s in enumerate(MEMBERS)]
+    mixed = [make(pkg, i, s) for i, s in enumerate(MEMBERS)]
+    batch = pkg.Batch(mixed)
+    n = len(MEMBERS)
+    for t in range(2):
+        seeds, chains, m, burn, lr, reglam, rtol, maxit = step_args(t, n)
+        emats, infos, stats, ms = batch.sr_step(seeds, chains, m, burn, lr, reglam, rtol, maxit)
+        assert stats == [0] * n and ms > 0
+        for i, c in enumerate(alone):
+            e, info = c.sr_step(seeds[i], chains[i], m[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i])
+            assert np.array_equal(e, emats[i]), (t, i)
+            assert info["minres_iters"] == infos[i]["minres_iters"]
+            assert info["accepted"] == infos[i]["accepted"]
+            assert np.array_equal(c.get_samples()[0], mixed[i].get_samples()[0])
+            for x, y in zip(c.get_weights(), mixed[i].get_weights()):
+                assert np.array_equal(x, y)
+    batch.close()
+    for c in alone + mixed:
+        c.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_autotune_keeps_the_chains(pkg, prec):
+    """The autotuner only changes launch shapes: the chains are the same and
+    energies agree to FP64 rounding of the reduction order."""
+    N, M, K = 16, 32, 2
+    out = []
+    for tune in (0, 1):
+        c = pkg.Context(N, M, K, synthetic_j(N), 0.6)
+        c.set_weights(*helpers.random_weights(N, M, K, 0.05, 3, real=True))
+        c.set_option(pkg.OPT_PRECISION, prec)
+        c.set_option(pkg.OPT_AUTOTUNE, tune)
+        es = []
+        for t in range(2):
+            e, _ = c.sr_step(50 + t * 32, 32, 20, 5, 0.1, 5.0, 1e-9, 2000)
+            es.append(e)
+        out.append((es, c.get_samples()[0]))
+        c.close()
+    assert np.array_equal(out[0][1], out[1][1])
+    for a, b in zip(out[0][0], out[1][0]):
+        assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b))
