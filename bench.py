@@ -211,6 +211,91 @@ def run_form(pkg, J, weights, precision, chains, steps, warmup, seed0, local):
     return ctx, infos, evals
 
 
+def batched_form(pkg, n_solves, chains, samples, steps, local):
+    """Config-4 style batch: n_solves independent solves (N in {16,24,32,48},
+    M = 2N, K in {2,3}, h ~ U[0.1,1.5], J exponent ~ U[0.8,1.5]), mixed precision,
+    autotuned launch shapes; SR steps as one graph launch for all solves vs the
+    same solves stepped one after another."""
+    rng = np.random.default_rng(SEED)
+    specs = []
+    for i in range(n_solves):
+        n = int(rng.choice([16, 24, 32, 48]))
+        specs.append((n, 2 * n, int(rng.choice([2, 3])), float(rng.uniform(0.1, 1.5)), float(rng.uniform(0.8, 1.5))))
+    ctxs = []
+    for i, (n, m, k, h, alpha) in enumerate(specs):
+        c = pkg.Context(n, m, k, pkg.synthetic_j(n, alpha), h, device=local)
+        c.set_weights(*pkg.synthetic_weights(n, m, k, 0.01, SEED + 17 * i))
+        c.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+        c.set_option(pkg.OPT_AUTOTUNE, 1)
+        ctxs.append(c)
+    batch = pkg.Batch(ctxs)
+    ns = n_solves
+    args_t = lambda t: ([SEED + 1000 * i + t * chains for i in range(ns)], [chains] * ns, [samples] * ns, [16] * ns,
+                        [schedule(t)[0]] * ns, [schedule(t)[1]] * ns, [RTOL] * ns, [MAXIT] * ns)
+    batch.sr_step(*args_t(0))  # warm-up: tuning, graph capture
+    ms_b = []
+    for t in range(1, 1 + steps):
+        _, infos, _, ms = batch.sr_step(*args_t(t))
+        ms_b.append(ms)
+    # the same solves one after another (each its own graph launch)
+    ms_s = []
+    for t in range(1 + steps, 2 + steps):
+        a = args_t(t)
+        tot = 0.0
+        for i, c in enumerate(ctxs):
+            _, info = c.sr_step(*[x[i] for x in a])
+            tot += info["ms_total"]
+        ms_s.append(tot)
+    batch.close()
+    hbm = sum(c.K * (c.N + c.M + c.N * c.M) for c in ctxs) * chains * samples * 4
+    for c in ctxs:
+        c.close()
+    mb = float(np.mean(ms_b))
+    return {"solves": ns, "chains_per_solve": chains, "samples_per_chain": samples, "burn_in": 16,
+            "precision": "mixed", "ms_per_batched_step": mb, "ms_sequential": float(np.mean(ms_s)),
+            "speedup_vs_sequential": float(np.mean(ms_s)) / mb, "solve_steps_per_s": ns / (mb * 1e-3),
+            "value": ns * chains * samples / (mb * 1e-3), "unit": "MC samples/s",
+            "O_bytes_fp32": hbm, "shapes": "N in {16,24,32,48}, M=2N, K in {2,3} (seeded)"}
+
+
+def serving_form(pkg, rate, window_s, local, max_steps=10):
+    """Config-5 style serving: Poisson arrivals at `rate` per second for
+    `window_s` seconds of solve requests (N log-uniform on [8, 96], M in
+    {N, 2N}, K uniform on 1..4, h ~ U[0, 2], tol 1e-6, 64 chains x 100 samples,
+    mixed precision, at most max_steps SR steps), admitted by device footprint
+    into the continuous batch. Returns solves/s and the time-to-converged-energy
+    percentiles (submit to completion)."""
+    import torch
+    rng = np.random.default_rng(SEED + int(rate))
+    free, _ = torch.cuda.mem_get_info(local)
+    srv = pkg.Server(hbm_budget_bytes=int(0.8 * free), max_active=256, device=local)
+    t0 = time.perf_counter()
+    t_next, n = 0.0, 0
+    while t_next < window_s:
+        now = time.perf_counter() - t0
+        if now < t_next:
+            time.sleep(t_next - now)
+        N = int(round(np.exp(rng.uniform(np.log(8), np.log(96)))))
+        M = int(N * rng.choice([1, 2]))
+        K = int(rng.integers(1, 5))
+        srv.submit(N, M, K, pkg.synthetic_j(N), weights=pkg.synthetic_weights(N, M, K, 0.01, SEED + n),
+                   h=float(rng.uniform(0.0, 2.0)), seed=SEED + 7919 * n, chains=64, samples_per_chain=100, burn_in=16,
+                   tol=1e-6, max_steps=max_steps, precision=pkg.PRECISION_MIXED)
+        n += 1
+        t_next += rng.exponential(1.0 / rate)
+    res = srv.wait_all(n, timeout=900)
+    t_end = time.perf_counter() - t0
+    srv.close()
+    lat = np.array([r["t_total"] for r in res if r["status"] == 0])
+    return {"rate_per_s": rate, "window_s": window_s, "submitted": n, "completed": int(len(lat)),
+            "failed": int(sum(r["status"] != 0 for r in res)), "converged": int(sum(r["converged"] for r in res)),
+            "step_capped": int(sum(r["status"] == 0 and not r["converged"] for r in res)),
+            "solves_per_s": len(lat) / t_end, "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "mean_queue_s": float(np.mean([r["t_queued"] for r in res])) if res else None,
+            "max_steps": max_steps}
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -377,6 +462,14 @@ def run_ours(args):
             c4.close()
         sweep["chains"] = args.sweep_chains
         out["sweep"] = sweep
+
+    # ---- batched multi-solve (config-4 style) ----
+    if args.batch_solves:
+        out["batched"] = batched_form(pkg, args.batch_solves, 1024, 64, 2, local)
+
+    # ---- serving loop (config-5 style Poisson arrivals) ----
+    if args.serve_rates:
+        out["serving"] = [serving_form(pkg, float(r), args.serve_window, local) for r in args.serve_rates.split(",")]
     if rank == 0 and world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, args.warmup)
     if rank == 0:
@@ -396,6 +489,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision form")
     ap.add_argument("--sweep-chains", type=int, default=4096, help="chains of the sweep line (0: skip)")
+    ap.add_argument("--batch-solves", type=int, default=64, help="solves of the batched line (0: skip)")
+    ap.add_argument("--serve-rates", default="4,16", help="arrival rates (1/s) of the serving lines ('' : skip)")
+    ap.add_argument("--serve-window", type=float, default=5.0, help="seconds of arrivals per serving line")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -187,6 +187,12 @@ int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double
 int nqes_apply_S_static(const double *O, const double *o, const double *skk, const double *v, double *out,
                         int64_t n_samples, int64_t n_params, int complex_arith, void *stream);
 
+/* Upper bound of the device memory (bytes) a context of this shape holds
+ * while it runs SR steps of `chains` x `samples_per_chain` samples
+ * (precision NQES_PRECISION_*, complex_arith 0/1). No GPU needed. */
+int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int chains, int samples_per_chain, int precision,
+                         int complex_arith, uint64_t *bytes);
+
 /* ---- batched multi-solve ----
  * No counterpart in the reference (it runs one solve per process). A batch
  * runs one SR step of every member context in ONE CUDA graph launch: each
@@ -203,12 +209,60 @@ int nqes_batch_destroy(nqes_batch *batch);
 const char *nqes_batch_last_error(const nqes_batch *batch);
 /* One SR step of every member; every array has `count` entries in member
  * order, with nqes_sr_step's meaning. e_mats (or an entry) and infos may be
- * NULL; statuses (may be NULL) receives each member's status; ms_total (may be
- * NULL) the device time of the batched launch. Returns the first member error. */
+ * NULL; statuses (may be NULL) receives each member's status, NQES_ERR_STATE for
+ * members not run because an earlier member's arguments failed; ms_total (may
+ * be NULL) the device time of the batched launch. Returns the first member error. */
 int nqes_batch_sr_step(nqes_batch *batch, const uint64_t *seeds, const int *chains, const int *samples_per_chain,
                        const int *burn_in, const double *lr, const double *reglam, const double *rtol,
                        const uint64_t *maxit, double *const *e_mats, nqes_step_info *infos, int *statuses,
                        double *ms_total);
+
+/* ---- serving loop ----
+ * No counterpart in the reference. A server owns a worker thread on one GPU.
+ * It admits submitted solves, oldest first, while the solve's device footprint
+ * (nqes_footprint_bytes) fits the budget and an active slot is free; runs one
+ * batched SR step over every admitted solve per iteration (nqes_batch) with
+ * the reference's schedules (code/rbm.cc:1173-1183); applies the reference's
+ * convergence test to each (sorted real eigenvalues of e_mat/N; converged at
+ * step t > 0 when |evals - best| < tol, best = lowest-sum evals so far,
+ * code/rbm.cc:1185-1194); and retires a solve when it converges, reaches
+ * max_steps or fails. Solves submitted while others run join the next step.
+ * A solve's numbers equal those of running it alone. */
+typedef struct nqes_server nqes_server;
+typedef struct nqes_request {
+    int n_spins, n_hidden, n_states;
+    const double *J;                 /* N×N, copied at submit */
+    double h;
+    const double *a, *b, *w;         /* initial weights (copied), or all NULL: nqes_init_weights(seed) */
+    uint64_t seed;                   /* step t uses seed + t*chains */
+    int chains, samples_per_chain, burn_in;
+    double lr0, lr_decay, lr_cutoff, reglam0, reglam_decay, reglam_cutoff;
+    double minres_rtol;
+    uint64_t minres_maxit;
+    double tol;
+    int max_steps;
+    int precision;                   /* NQES_PRECISION_* */
+} nqes_request;
+typedef struct nqes_result {
+    uint64_t id;
+    int status;                      /* NQES_OK, NQES_ERR_OOM (never fits the budget) or a step's error */
+    int converged;                   /* 1: tol met; 0: max_steps reached (or failed) */
+    int steps;
+    int n_states;
+    double energies[4];              /* last step's sorted per-site energies */
+    double best[4];                  /* lowest-sum energies seen */
+    double t_queued, t_total;        /* seconds from submit to admission and to completion */
+    uint64_t footprint;              /* device bytes reserved for the solve */
+} nqes_result;
+int nqes_server_create(int device, uint64_t hbm_budget_bytes, int max_active, nqes_server **out);
+/* Copies the request; returns at once with its id. Thread-safe. */
+int nqes_server_submit(nqes_server *server, const nqes_request *request, uint64_t *id);
+/* Moves up to max_results finished solves to out (oldest first). */
+int nqes_server_poll(nqes_server *server, nqes_result *out, int max_results, int *count);
+int nqes_server_status(nqes_server *server, int *queued, int *active, int *done, uint64_t *bytes_in_use);
+/* Stops the worker after its current step; unfinished solves are dropped. */
+int nqes_server_destroy(nqes_server *server);
+const char *nqes_server_last_error(const nqes_server *server);
 
 #ifdef __cplusplus
 }

@@ -31,6 +31,8 @@ EXPORTS = [
     "nqes_init_weights", "nqes_sr_step", "nqes_correlations", "nqes_evaluate", "nqes_get_samples",
     "nqes_get_accepts", "nqes_get_O", "nqes_get_moments", "nqes_get_solution", "nqes_apply_S", "nqes_time_kernel",
     "nqes_apply_S_static", "nqes_batch_create", "nqes_batch_destroy", "nqes_batch_last_error", "nqes_batch_sr_step",
+    "nqes_footprint_bytes", "nqes_server_create", "nqes_server_submit", "nqes_server_poll", "nqes_server_status",
+    "nqes_server_destroy", "nqes_server_last_error",
 ]
 KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
 
@@ -57,6 +59,33 @@ class StepInfo(ctypes.Structure):
 
 
 _LIB = None
+
+
+class Request(ctypes.Structure):
+    """nqes_request (include/nqes.h)."""
+    _fields_ = [("n_spins", ctypes.c_int), ("n_hidden", ctypes.c_int), ("n_states", ctypes.c_int),
+                ("J", ctypes.POINTER(ctypes.c_double)), ("h", ctypes.c_double),
+                ("a", ctypes.POINTER(ctypes.c_double)), ("b", ctypes.POINTER(ctypes.c_double)),
+                ("w", ctypes.POINTER(ctypes.c_double)), ("seed", ctypes.c_uint64), ("chains", ctypes.c_int),
+                ("samples_per_chain", ctypes.c_int), ("burn_in", ctypes.c_int), ("lr0", ctypes.c_double),
+                ("lr_decay", ctypes.c_double), ("lr_cutoff", ctypes.c_double), ("reglam0", ctypes.c_double),
+                ("reglam_decay", ctypes.c_double), ("reglam_cutoff", ctypes.c_double),
+                ("minres_rtol", ctypes.c_double), ("minres_maxit", ctypes.c_uint64), ("tol", ctypes.c_double),
+                ("max_steps", ctypes.c_int), ("precision", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    """nqes_result (include/nqes.h)."""
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int), ("converged", ctypes.c_int),
+                ("steps", ctypes.c_int), ("n_states", ctypes.c_int), ("energies", ctypes.c_double * 4),
+                ("best", ctypes.c_double * 4), ("t_queued", ctypes.c_double), ("t_total", ctypes.c_double),
+                ("footprint", ctypes.c_uint64)]
+
+    def as_dict(self):
+        k = self.n_states
+        return {"id": self.id, "status": self.status, "converged": bool(self.converged), "steps": self.steps,
+                "energies": list(self.energies[:k]), "best": list(self.best[:k]), "t_queued": self.t_queued,
+                "t_total": self.t_total, "footprint": self.footprint}
 _dp = ctypes.POINTER(ctypes.c_double)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 
@@ -90,6 +119,13 @@ def load_library(path=None):
         "nqes_apply_S": (i, [vp, _dp, _dp]),
         "nqes_time_kernel": (i, [vp, i, i, _dp, _dp]),
         "nqes_apply_S_static": (i, [vp, vp, vp, vp, vp, i64, i64, i, vp]),
+        "nqes_footprint_bytes": (i, [i, i, i, i, i, i, i, ctypes.POINTER(u64)]),
+        "nqes_server_create": (i, [i, u64, i, ctypes.POINTER(vp)]),
+        "nqes_server_submit": (i, [vp, ctypes.POINTER(Request), ctypes.POINTER(u64)]),
+        "nqes_server_poll": (i, [vp, ctypes.POINTER(Result), i, ctypes.POINTER(i)]),
+        "nqes_server_status": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(u64)]),
+        "nqes_server_destroy": (i, [vp]),
+        "nqes_server_last_error": (ctypes.c_char_p, [vp]),
         "nqes_batch_create": (i, [ctypes.POINTER(vp), i, ctypes.POINTER(vp)]),
         "nqes_batch_destroy": (i, [vp]),
         "nqes_batch_last_error": (ctypes.c_char_p, [vp]),
@@ -310,3 +346,83 @@ class Batch:
             c.chains = int(ch)
             c.ns = int(ch) * int(m)
         return emats, [x.as_dict() for x in infos], list(stat), ms.value
+
+
+def footprint_bytes(n_spins, n_hidden, n_states, chains, samples_per_chain, precision=0, complex_arith=False,
+                    lib=None):
+    """Device bytes a context of this shape holds during SR steps (no GPU needed)."""
+    lib = lib or load_library()
+    out = ctypes.c_uint64()
+    st = lib.nqes_footprint_bytes(int(n_spins), int(n_hidden), int(n_states), int(chains), int(samples_per_chain),
+                                  int(precision), int(bool(complex_arith)), ctypes.byref(out))
+    if st != OK:
+        raise NqesError(st, "invalid shape")
+    return out.value
+
+
+class Server:
+    """Serving loop: continuous batching of SR solves on one GPU (nqes_server_*)."""
+
+    DEFAULTS = dict(h=0.595, seed=1, chains=64, samples_per_chain=100, burn_in=16, lr0=0.1, lr_decay=0.99,
+                    lr_cutoff=0.01, reglam0=40.0, reglam_decay=0.9, reglam_cutoff=1.0, minres_rtol=1e-9,
+                    minres_maxit=100000, tol=1e-6, max_steps=50, precision=PRECISION_FP64)
+
+    def __init__(self, hbm_budget_bytes, max_active=64, device=0, lib=None):
+        self.lib = lib or load_library()
+        h_ = ctypes.c_void_p()
+        st = self.lib.nqes_server_create(int(device), int(hbm_budget_bytes), int(max_active), ctypes.byref(h_))
+        if st != OK:
+            raise NqesError(st, self.lib.nqes_server_last_error(None).decode())
+        self._h = h_
+        self._keep = {}
+
+    def submit(self, n_spins, n_hidden, n_states, J, weights=None, **kw):
+        """Queues one solve; weights = (a, b, w) complex arrays or None (the reference's init). Returns its id."""
+        p = dict(self.DEFAULTS)
+        p.update(kw)
+        Jc = np.ascontiguousarray(J, np.float64)
+        r = Request()
+        r.n_spins, r.n_hidden, r.n_states = int(n_spins), int(n_hidden), int(n_states)
+        r.J = Jc.ctypes.data_as(_dp)
+        keep = [Jc]
+        if weights is not None:
+            a, b, w = (np.ascontiguousarray(x, np.complex128) for x in weights)
+            r.a, r.b, r.w = _cp(a), _cp(b), _cp(w)
+            keep += [a, b, w]
+        for k in ("h", "seed", "chains", "samples_per_chain", "burn_in", "lr0", "lr_decay", "lr_cutoff", "reglam0",
+                  "reglam_decay", "reglam_cutoff", "minres_rtol", "minres_maxit", "tol", "max_steps", "precision"):
+            setattr(r, k, p[k])
+        rid = ctypes.c_uint64()
+        st = self.lib.nqes_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid))
+        if st != OK:
+            raise NqesError(st, self.lib.nqes_server_last_error(self._h).decode())
+        return rid.value
+
+    def poll(self, max_results=256):
+        out = (Result * max_results)()
+        n = ctypes.c_int()
+        st = self.lib.nqes_server_poll(self._h, out, max_results, ctypes.byref(n))
+        if st != OK:
+            raise NqesError(st, "poll failed")
+        return [out[i].as_dict() for i in range(n.value)]
+
+    def status(self):
+        q, a, d = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        b = ctypes.c_uint64()
+        self.lib.nqes_server_status(self._h, ctypes.byref(q), ctypes.byref(a), ctypes.byref(d), ctypes.byref(b))
+        return {"queued": q.value, "active": a.value, "done": d.value, "bytes_in_use": b.value}
+
+    def wait_all(self, n_expected, timeout=600.0):
+        """Polls until n_expected results arrived (or timeout seconds passed)."""
+        import time
+        res, t0 = [], time.time()
+        while len(res) < n_expected and time.time() - t0 < timeout:
+            res += self.poll()
+            if len(res) < n_expected:
+                time.sleep(0.005)
+        return res
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.nqes_server_destroy(self._h)
+            self._h = None

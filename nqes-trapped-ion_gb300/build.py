@@ -19,9 +19,9 @@ LIBDIR = os.path.join(PKG, "lib")
 OBJDIR = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_sample_warp.cu", "kernels_solve.cu",
-           "nqes_api.cu", "sv_static.cu"]
-HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h", "tma_stage.cuh"]
+SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_sample_warp.cu", "kernels_sample_warp_k34.cu",
+           "kernels_solve.cu", "nqes_api.cu", "sv_static.cu", "nqes_server.cc"]
+HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h", "tma_stage.cuh", "sample_warp.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -63,7 +63,7 @@ def build_library(verbose=False):
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     lib = os.path.join(LIBDIR, "libnqes.so")
     if _stale(lib, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", lib, *objs, "-lcudart"]
+        cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", lib, *objs, "-lcudart", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libnqes.so failed:\n{r.stderr}")

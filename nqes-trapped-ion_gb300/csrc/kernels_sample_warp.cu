@@ -1,726 +1,14 @@
-// Mixed-precision sampler, decision-warp form (real weights, up to 16 hidden
-// units per lane). Same chains and same certified FP32 decisions as the
-// block form in kernels_sample_mixed.cu (code/rbm.cc:530-552 trajectories),
-// laid out for latency:
-//
-// One warp (warp 0 of the chain's CTA) runs every proposal of a row. Its
-// lanes form K groups of G lanes (G the largest power of two <= 32/K); lane
-// (kk, jl) owns hidden units j = jl*U .. jl*U+U-1 of RBM kk and keeps their
-// tanh(theta) in registers for the whole row. A proposal is U fused
-// multiply-adds, a log2(G)-level shuffle tree inside each group and K
-// broadcasts; every lane then holds all K products and takes the accept
-// decision itself, so a proposal needs no CTA barrier and no shared-memory
-// round trip. An accepted flip updates tanh by the exact identity
-// t' = (t c - sigma s) / f with f already at hand: no FP64 instruction on the
-// proposal path.
-//
-// At the end of a row that changed, the whole CTA (the other warps wait at a
-// barrier meanwhile) rebuilds that row's theta from the spins as double-float
-// sums of b and the +-w, recomputes tanh with tanhf, and recomputes the row of
-// Phi in FP64, so every row of Phi is exact (to ~1e-12 relative) whenever
-// another row is swept: a decision's bound only carries the drift of the
-// swept row. The error model of a proposal is stated at run_row. A decision
-// the bound cannot make, or any value out of FP32's normal range, goes to the
-// exact path: the swept row's current and proposed entries in FP64 from theta
-// and the reference's test u |det Phi|^2 <= |det Phi'|^2 in FP64.
-//
-// The step's tables (cosh 2w, sinh 2w, w as hi + lo; padded to MP units per
-// row so that padding factors are exactly 1) are bulk-copied into shared
-// memory (cp.async.bulk on an mbarrier) when the launch plan allows.
-#include <algorithm>
-#include <cfloat>
-
-#include "nqes_internal.h"
-#include "pcg64.cuh"
-#include "tma_stage.cuh"
+// Decision-warp sampler: instantiations for K = 1, 2 and the host-side
+// launch, occupancy and table functions (K = 3, 4 are instantiated in
+// kernels_sample_warp_k34.cu). The kernels are in sample_warp.cuh.
+#include "sample_warp.cuh"
 
 namespace nqes {
 
+// K = 3, 4 instances, from kernels_sample_warp_k34.cu
+void *dw_kernel_k34(int K, int U);
+
 namespace {
-
-constexpr float kU = 5.9604645e-8f;  // FP32 unit roundoff 2^-24
-constexpr int kMaxSpinWords = 8;
-
-__device__ __forceinline__ bool down_bit(const uint64_t *s, int i) { return (s[i >> 6] >> (i & 63)) & 1ULL; }
-__device__ __forceinline__ int expo32(float x) {
-    const int b = (__float_as_int(x) >> 23) & 0xff;
-    return b == 0 ? 0 : b - 127;
-}
-
-// (ah, al) += (bh, bl): double-float addition from two-sum (Knuth) and a
-// final fast two-sum; relative error a few 2^-48 of max(|a|, |b|).
-__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl) {
-    const float s = ah + bh;
-    const float bb = s - ah;
-    float e = (ah - (s - bb)) + (bh - bb);
-    e += al + bl;
-    const float h = s + e;
-    al = e - (h - s);
-    ah = h;
-}
-
-struct DSmem {
-    double *phi, *pinv, *Dm, *jk, *lsum, *jpart;
-    float *th_hi, *th_lo, *t, *rat, *bsig, *Bm;
-    uint64_t *spin, *mbar;
-    int *flag;
-    float *tabs;  // staged tables (cosh 2w, sinh 2w, w hi, w lo), 4 * K*N*MP floats
-    // the tables the kernel reads: staged copies or global memory
-    const float *tc, *ts, *twh, *twl;
-};
-
-// One table of K*N*MP floats in bytes (a multiple of 16: MP*4 >= 32).
-__host__ __device__ inline size_t dw_table_bytes(int N, int MP, int K) { return size_t(K) * N * MP * 4; }
-
-__host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K, bool staged) {
-    const size_t KK = size_t(K) * K;
-    const size_t nd = 3 * KK + 4 + 32 + 32 * 4;
-    const size_t nf = 3 * KK * MP + 2 * KK * N + KK;
-    const size_t base = nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 8 + 4 * 4;  // 16: alignment pad
-    return staged ? base + 16 + 4 * dw_table_bytes(N, MP, K) : base;
-}
-
-__device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
-    const int KK = K * K;
-    DSmem s;
-    double *d = reinterpret_cast<double *>(base);
-    s.phi = d; d += KK;
-    s.pinv = d; d += KK;
-    s.Dm = d; d += KK;
-    s.jk = d; d += 4;
-    s.lsum = d; d += 32;
-    s.jpart = d; d += 32 * 4;
-    // float arrays start on a 16-byte boundary (vector loads of theta and tanh)
-    unsigned char *fb = reinterpret_cast<unsigned char *>(d);
-    fb += (16 - (reinterpret_cast<uintptr_t>(fb) & 15)) & 15;
-    float *f = reinterpret_cast<float *>(fb);
-    s.th_hi = f; f += KK * MP;
-    s.th_lo = f; f += KK * MP;
-    s.t = f; f += KK * MP;
-    s.rat = f; f += KK * N;
-    s.bsig = f; f += KK * N;
-    s.Bm = f; f += KK;
-    unsigned char *p = reinterpret_cast<unsigned char *>(f);
-    p += (8 - (reinterpret_cast<uintptr_t>(p) & 7)) & 7;
-    s.spin = reinterpret_cast<uint64_t *>(p);
-    s.mbar = s.spin + kMaxSpinWords;
-    s.flag = reinterpret_cast<int *>(s.mbar + 1);
-    unsigned char *tb = reinterpret_cast<unsigned char *>(s.flag + 4);
-    tb += (16 - (reinterpret_cast<uintptr_t>(tb) & 15)) & 15;
-    s.tabs = reinterpret_cast<float *>(tb);
-    return s;
-}
-
-// Cofactor of (r, c) and the sum of |Leibniz terms| of that minor, K <= 4.
-__device__ void cofactor_abs(const double *m, int K, int r, int c, double &cof, double &cabs) {
-    if (K == 1) {
-        cof = 1.0;
-        cabs = 1.0;
-        return;
-    }
-    double sub[9], sab[9];
-    int t = 0;
-    for (int a = 0; a < K; a++) {
-        if (a == r) continue;
-        for (int b = 0; b < K; b++)
-            if (b != c) {
-                sub[t] = m[a * K + b];
-                sab[t] = fabs(m[a * K + b]);
-                t++;
-            }
-    }
-    const double d = small_det(sub, K - 1);
-    double p;
-    if (K == 2) {
-        p = sab[0];
-    } else if (K == 3) {
-        p = sab[0] * sab[3] + sab[1] * sab[2];
-    } else {
-        p = sab[0] * (sab[4] * sab[8] + sab[5] * sab[7]) + sab[1] * (sab[3] * sab[8] + sab[5] * sab[6]) +
-            sab[2] * (sab[3] * sab[7] + sab[4] * sab[6]);
-    }
-    cof = ((r + c) & 1) ? -d : d;
-    cabs = p;
-}
-
-// Row k from the spins: theta (double-float sums of b and +-w), tanh(theta)
-// in FP32, and Phi[k][.] in FP64, scaled by a power of two that brings the
-// row's largest entry near 1:
-//   Phi[k][kk] ~ P_kk exp(A_kk - max A),  A_kk = sum_i sigma_i a_i + sum_j |theta_j|,
-//   P_kk = prod_j (1 + e^{-2|theta_j|})  (each factor in (1, 2]),
-// one exp per hidden unit and per entry. Block-wide; ends with a barrier.
-__device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
-    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, MP = A.MP;
-    const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
-    const uint64_t *sk = sm.spin + k * NW;
-    for (int idx = tid; idx < K * MP; idx += T) {
-        const int kk = idx / MP, j = idx - kk * MP, q = k * K + kk;
-        float h = 0.f, l = 0.f, t = 0.f;
-        if (j < M) {
-            h = A.bh[kk * MP + j];
-            l = A.bl[kk * MP + j];
-            for (int i = 0; i < N; i++) {
-                const size_t o = (size_t(kk) * N + i) * MP + j;
-                const float wh = sm.twh[o], wl = sm.twl[o];
-                if (down_bit(sk, i))
-                    df_add(h, l, -wh, -wl);
-                else
-                    df_add(h, l, wh, wl);
-            }
-            t = tanhf(h);
-        }
-        sm.th_hi[q * MP + j] = h;
-        sm.th_lo[q * MP + j] = l;
-        sm.t[q * MP + j] = t;
-    }
-    __syncthreads();
-    // partial sums of A and products P over slots (kk, part): every warp takes
-    // slots, each slot a strided share of the row's hidden units
-    const int wpk = max(1, nwarp / K);
-    for (int v = warp; v < K * wpk; v += nwarp) {
-        const int kk = v / wpk, part = v - kk * wpk, q = k * K + kk;
-        double lin = 0.0, pr = 1.0;
-        for (int j = lane + 32 * part; j < M; j += 32 * wpk) {
-            const double th = double(sm.th_hi[q * MP + j]) + double(sm.th_lo[q * MP + j]);
-            lin += fabs(th);
-            pr *= 1.0 + exp(-2.0 * fabs(th));
-        }
-        if (part == 0)
-            for (int i = lane; i < N; i += 32) lin += down_bit(sk, i) ? -A.a64[kk * N + i] : A.a64[kk * N + i];
-        lin = warp_sum(lin);
-        pr = warp_prod(pr);
-        if (lane == 0) {
-            sm.jpart[2 * v] = lin;
-            sm.jpart[2 * v + 1] = pr;
-        }
-    }
-    __syncthreads();
-    if (warp == 0) {
-        // lanes kk < K: the entry from its slots; then the row's scaling
-        double a = -1e308, pp = 0.0;
-        if (lane < K) {
-            a = 0.0;
-            pp = 1.0;
-            for (int part = 0; part < wpk; part++) {
-                a += sm.jpart[2 * (lane * wpk + part)];
-                pp *= sm.jpart[2 * (lane * wpk + part) + 1];
-            }
-        }
-        double mx = a;
-        for (int o = 1; o < 4; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        mx = __shfl_sync(0xffffffffu, mx, 0);
-        const double e = lane < K ? pp * exp(a - mx) : 0.0;
-        int ex = lane < K ? expo(e) : -100000;
-        for (int o = 1; o < 4; o <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, o));
-        ex = __shfl_sync(0xffffffffu, ex, 0);
-        if (lane < K) sm.phi[k * K + lane] = scale2(e, -ex);
-    }
-    __syncthreads();
-}
-
-// All proposals of row k, run by one warp. Returns whether the row changed.
-//
-// Error model of the FP32 proposal (u = 2^-24). tanh(theta) of the lane's
-// units is held in FP32 with an absolute error of at most Et (one bound per
-// RBM, the same in every lane): 5u after the row's rebuild (tanhf), and
-// after an accepted flip, whose update t' = (t c - sigma s) / f has
-// derivative dt'/dt = 1/f^2, Et' = Et max_j 1/f_j^2 + u (2 max_j cond_j + 5)
-// with cond_j = (c + |s|)/(c - |s|) >= (|c| + |t s|)/|f| (|t| <= 1). A factor
-// f_j = c - sigma t s then has relative error at most u (cond_j + 1) +
-// Et |s| / (c - |s|), and the product over the row's M factors (M - 1 + 16
-// roundings, the 16 also covering the FP64 tables' own rounding)
-//   beta = u (sum_j cond_j + 2M + 16) + Et sum_j |s_j| / (c_j - |s_j|).
-// The per-(kk, i) sums and maxima come from a table built with the weights.
-template <int K, int U>
-__device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsigned long long &nacc,
-                        unsigned long long &nexact) {
-    constexpr int G = K == 1 ? 32 : (K == 2 ? 16 : 8);
-    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
-    const int lane = threadIdx.x & 31;
-    const int gkk = lane / G, gjl = lane % G;
-    const bool active = gkk < K;
-    const int kkl = active ? gkk : 0;  // idle lanes (K = 3) read RBM 0's tables and contribute factor 1
-    const int q = k * K + kkl, base = gjl * U;
-
-    float t[U];
-#pragma unroll
-    for (int u = 0; u < U; u++) t[u] = sm.t[q * MP + base + u];
-    bool live[U];  // unit inside the RBM (not padding) and lane in a group
-#pragma unroll
-    for (int u = 0; u < U; u++) live[u] = active && base + u < M;
-    uint64_t sk0 = sm.spin[k * NW], sk1 = NW > 1 ? sm.spin[k * NW + 1] : 0ULL;
-    auto bit = [&](int b) -> bool { return ((b < 64 ? sk0 : sk1) >> (b & 63)) & 1ULL; };
-
-    // Decision state, identical in every lane: exact cofactors of row k (the
-    // other rows are exact), the row's entries, g and det with error bounds.
-    double cofd[K], cabsd[K];
-    float phik[K], g[K], gabs[K], Et[K];
-    float det32, edet, rho = 0.f;
-    {
-        double det = 0.0, perm = 0.0;
-#pragma unroll
-        for (int kk = 0; kk < K; kk++) {
-            cofactor_abs(sm.phi, K, k, kk, cofd[kk], cabsd[kk]);
-            const double p = sm.phi[k * K + kk];
-            phik[kk] = float(p);
-            g[kk] = float(p * cofd[kk]);
-            gabs[kk] = float(fabs(p) * cabsd[kk]);
-            det += p * cofd[kk];
-            perm += fabs(p) * cabsd[kk];
-            Et[kk] = 5.f * kU;
-        }
-        det32 = float(det);
-        edet = 4.f * kU * fabsf(det32) + float(perm * 0x1p-50);
-    }
-    bool changed = false;
-
-    for (int i = 0; i < N; i++) {
-        const bool down = bit(i);
-        const size_t row = (size_t(kkl) * N + i) * MP + base;
-        float cq[U], sq[U];
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            cq[u] = sm.tc[row + u];
-            sq[u] = sm.ts[row + u];
-        }
-        float ea[K];
-        float4 bd[K];
-#pragma unroll
-        for (int kk = 0; kk < K; kk++) {
-            ea[kk] = __ldg((down ? A.edn : A.eup) + kk * N + i);
-            bd[kk] = __ldg(reinterpret_cast<const float4 *>(A.bnd) + kk * N + i);
-        }
-        const uint64_t draw = pcg_next(rng);
-        const float u32 = __ull2float_rn(draw) * 0x1p-64f;
-
-        // factors f = c - sigma t s and their product within the lane's group
-        float f[U], prod = 1.f;
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-            f[u] = fmaf(down ? t[u] : -t[u], sq[u], cq[u]);
-            if (live[u]) prod *= f[u];
-        }
-#pragma unroll
-        for (int o = G >> 1; o > 0; o >>= 1) prod *= __shfl_xor_sync(0xffffffffu, prod, o);
-        float x[K], rr[K], s = 0.f, ed = 0.f, bmax = 0.f;
-#pragma unroll
-        for (int kk = 0; kk < K; kk++) {
-            rr[kk] = __shfl_sync(0xffffffffu, prod, kk * G);
-            const float beta = fmaf(Et[kk], bd[kk].y, bd[kk].x);
-            const float re = rr[kk] * ea[kk];
-            x[kk] = re * g[kk];
-            s += x[kk];
-            ed += fabsf(re) * ((beta + 3.f * kU) * fabsf(g[kk]) + 1.02f * rho * gabs[kk]) + 3.f * kU * fabsf(x[kk]);
-            bmax = fmaxf(bmax, beta);
-        }
-        ed = ed * 1.01f + 4.f * kU * fabsf(s);
-
-        bool acc = false, exact_path = false;
-        {
-            const float ad = fabsf(s), lo = ad - ed, hi = ad + ed;
-            const float dd = fabsf(det32), dlo = fmaxf(dd - edet, 0.f), dhi = dd + edet;
-            const float su = u32 * (1.f + 16.f * kU), sl = u32 * (1.f - 16.f * kU);
-            if (A.exact_all || !(dd > 1e-15f) || !(dd < 1e15f) || !(bmax < 0.01f))
-                exact_path = true;  // det == 0 (accepted, code/rbm.cc:542), range, loose bound
-            else if (lo > 0.f && lo * lo * (1.f - 16.f * kU) >= su * dhi * dhi)
-                acc = true;
-            else if (!(hi * hi * (1.f + 16.f * kU) < sl * dlo * dlo))
-                exact_path = true;  // NaN lands here as well
-        }
-        if (exact_path) {
-            // Row k current and proposed, in FP64: theta of the lane's units from
-            // the spins (double-float sums of b and +-w), then the log cosh sums.
-            double lin = 0.0, pr = 1.0, lin2 = 0.0, pr2 = 1.0;
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                if (live[u]) {
-                    const int j = base + u;
-                    float h = A.bh[kkl * MP + j], l = A.bl[kkl * MP + j];
-                    for (int i2 = 0; i2 < N; i2++) {
-                        const size_t o = (size_t(kkl) * N + i2) * MP + j;
-                        const float wh = sm.twh[o], wl = sm.twl[o];
-                        if (bit(i2))
-                            df_add(h, l, -wh, -wl);
-                        else
-                            df_add(h, l, wh, wl);
-                    }
-                    const double tt = double(h) + double(l);
-                    const double w = A.w64[(size_t(kkl) * N + i) * M + j];
-                    const double t2 = down ? tt + 2.0 * w : tt - 2.0 * w;
-                    lin += fabs(tt);
-                    pr *= 1.0 + exp(-2.0 * fabs(tt));
-                    lin2 += fabs(t2);
-                    pr2 *= 1.0 + exp(-2.0 * fabs(t2));
-                }
-            }
-#pragma unroll
-            for (int o = G >> 1; o > 0; o >>= 1) {
-                lin += __shfl_xor_sync(0xffffffffu, lin, o);
-                lin2 += __shfl_xor_sync(0xffffffffu, lin2, o);
-                pr *= __shfl_xor_sync(0xffffffffu, pr, o);
-                pr2 *= __shfl_xor_sync(0xffffffffu, pr2, o);
-            }
-            // A = sum sigma a + sum |theta| and P = prod (1 + e^{-2|theta|}) per RBM,
-            // current (c) and proposed (n); entries P exp(A - max A_c), one exp
-            // per lane (lanes kk and K + kk)
-            double as[K];
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                as[kk] = 0.0;
-                for (int i2 = lane; i2 < N; i2 += 32) {
-                    const double ai = A.a64[kk * N + i2];
-                    as[kk] += bit(i2) ? -ai : ai;
-                }
-            }
-            double Ac[K], An[K], Pc[K], Pn[K], mx = -1e308;
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                as[kk] = warp_sum(as[kk]);
-                const double ai = A.a64[kk * N + i];
-                Ac[kk] = as[kk] + __shfl_sync(0xffffffffu, lin, kk * G);
-                An[kk] = as[kk] + (down ? 2.0 * ai : -2.0 * ai) + __shfl_sync(0xffffffffu, lin2, kk * G);
-                Pc[kk] = __shfl_sync(0xffffffffu, pr, kk * G);
-                Pn[kk] = __shfl_sync(0xffffffffu, pr2, kk * G);
-                mx = fmax(mx, Ac[kk]);
-            }
-            double ev = 0.0;
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                if (lane == kk) ev = Pc[kk] * exp(Ac[kk] - mx);
-                if (lane == K + kk) ev = Pn[kk] * exp(An[kk] - mx);
-            }
-            // both rows scaled by one power of two that brings the current row's
-            // largest entry near 1 (the test is invariant; FP32 copies stay in range)
-            double pc[K], pn[K], det_e = 0.0, sx = 0.0;
-            int pex = -100000;
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                pc[kk] = __shfl_sync(0xffffffffu, ev, kk);
-                pn[kk] = __shfl_sync(0xffffffffu, ev, K + kk);
-                pex = max(pex, expo(pc[kk]));
-            }
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                pc[kk] = scale2(pc[kk], -pex);
-                pn[kk] = scale2(pn[kk], -pex);
-                det_e += pc[kk] * cofd[kk];
-                sx += pn[kk] * cofd[kk];
-            }
-            acc = det_e == 0.0 || pcg_u01(draw) * (det_e * det_e) <= sx * sx;
-            nexact++;
-            // continue from the exact row
-            double perm = 0.0;
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                const double p = acc ? pn[kk] : pc[kk];
-                phik[kk] = float(p);
-                g[kk] = float(p * cofd[kk]);
-                gabs[kk] = float(fabs(p) * cabsd[kk]);
-                perm += fabs(p) * cabsd[kk];
-            }
-            det32 = float(acc ? sx : det_e);
-            edet = 4.f * kU * fabsf(det32) + float(perm * 0x1p-50);
-            rho = 0.f;
-        }
-        if (acc) {
-            // tanh' = (t c - sigma s) / f (code/rbm.cc:185) in FP32, and its bound
-#pragma unroll
-            for (int u = 0; u < U; u++) t[u] = __fdividef(fmaf(t[u], cq[u], down ? sq[u] : -sq[u]), f[u]);
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) Et[kk] = fmaf(Et[kk] * (1.f + 4.f * kU), bd[kk].z, bd[kk].w);
-            if (!exact_path) {
-                // row k times r e^{-2 sigma a}: g_kk becomes x_kk (cofactors exclude row k)
-#pragma unroll
-                for (int kk = 0; kk < K; kk++) {
-                    const float re = rr[kk] * ea[kk];
-                    phik[kk] *= re;
-                    g[kk] = x[kk];
-                    gabs[kk] *= fabsf(re);
-                }
-                det32 = s;
-                edet = ed;
-                rho += bmax + 4.f * kU;
-            }
-            // keep the row's largest entry near 1 (exact power-of-two scaling)
-            int ex = -100000;
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) ex = max(ex, expo32(phik[kk]));
-            if (ex > 20 || ex < -20) {
-                const float sc = ldexpf(1.f, -ex);
-#pragma unroll
-                for (int kk = 0; kk < K; kk++) {
-                    phik[kk] *= sc;
-                    g[kk] *= sc;
-                    gabs[kk] *= sc;
-                }
-                det32 *= sc;
-                edet *= sc;
-            }
-            if (i < 64)
-                sk0 ^= 1ULL << i;
-            else
-                sk1 ^= 1ULL << (i - 64);
-            changed = true;
-            nacc++;
-        }
-    }
-    if (lane == 0) {
-        sm.spin[k * NW] = sk0;
-        if (NW > 1) sm.spin[k * NW + 1] = sk1;
-    }
-    return changed;
-}
-
-template <int K_, int U>
-__global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int K = K_, KK = K * K;
-    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, L = A.sh.L, MP = A.MP;
-    const size_t P = size_t(A.sh.P);
-    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
-    const int c = blockIdx.x;
-    DSmem sm = dcarve(smem_raw, N, MP, K);
-    const bool writer = tid == 0;
-    const size_t tb = dw_table_bytes(N, MP, K);
-    if (A.stage) {
-        // the step's tables into shared memory by bulk copies (one mbarrier phase)
-        float *stc = sm.tabs, *sts = stc + tb / 4, *stwh = sts + tb / 4, *stwl = stwh + tb / 4;
-        if (writer) {
-            mbar_init(sm.mbar, 1);
-            mbar_expect_tx(sm.mbar, unsigned(4 * tb));
-            bulk_g2s(stc, A.cp, unsigned(tb), sm.mbar);
-            bulk_g2s(sts, A.spp, unsigned(tb), sm.mbar);
-            bulk_g2s(stwh, A.whp, unsigned(tb), sm.mbar);
-            bulk_g2s(stwl, A.wlp, unsigned(tb), sm.mbar);
-            const bool ok = mbar_wait(sm.mbar, 0);
-            sm.flag[2] = ok ? 1 : 0;
-            if (!ok) atomicOr(A.err, kErrTimeout);
-        }
-        __syncthreads();
-        if (!sm.flag[2]) return;  // every thread: the copy did not complete in time
-        sm.tc = stc;
-        sm.ts = sts;
-        sm.twh = stwh;
-        sm.twl = stwl;
-    } else {
-        sm.tc = A.cp;
-        sm.ts = A.spp;
-        sm.twh = A.whp;
-        sm.twl = A.wlp;
-    }
-
-    // init_multi_spin (code/rbm.cc:98-119): every thread advances the stream;
-    // warp 0 keeps it for the proposals.
-    Pcg64 rng = pcg_seed(A.sp->seed + uint64_t(c));
-    if (writer)
-        for (int t = 0; t < K * NW; t++) sm.spin[t] = 0;
-    __syncthreads();
-    for (int k = 0; k < K; k++)
-        for (int i = 0; i < N; i++) {
-            const bool d = pcg_bernoulli_half(rng);
-            if (d && writer) sm.spin[k * NW + (i >> 6)] |= 1ULL << (i & 63);
-        }
-    __syncthreads();
-    for (int k = 0; k < K; k++) rebuild_row(A, sm, k);
-
-    unsigned long long nacc = 0, nexact = 0;
-    int rowctr = 0;
-    const int total = A.burn + A.m;
-    for (int sw = 0; sw < total; sw++) {
-        for (int k = 0; k < K; k++, rowctr++) {
-            if (warp == 0) {
-                const bool ch = run_row<K_, U>(A, sm, k, rng, nacc, nexact);
-                if (lane == 0) sm.flag[rowctr & 1] = ch ? 1 : 0;
-            }
-            __syncthreads();
-            if (sm.flag[rowctr & 1]) rebuild_row(A, sm, k);  // uniform after the barrier
-        }
-        if (sw < A.burn) continue;
-
-        // ---- sample: local energy (FP32 ratios, FP64 combination) and FP32 O ----
-        const size_t s = size_t(c) * A.m + (sw - A.burn);
-        if (writer) {
-            double pinv[16];
-            if (!small_inv(sm.phi, pinv, K)) {
-                atomicOr(A.err, kErrSingular);
-                for (int t = 0; t < KK; t++) pinv[t] = 0.0;
-            }
-            for (int t = 0; t < KK; t++) sm.pinv[t] = pinv[t];
-        }
-        __syncthreads();
-        {
-            // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031): the
-            // N x N grid strided over the block, partial sums per warp, then the
-            // warps' partials in order (deterministic)
-            double acc[K];
-#pragma unroll
-            for (int k = 0; k < K; k++) acc[k] = 0.0;
-            int i = tid / N, j = tid - (tid / N) * N;
-            const int di = T / N, dj = T - (T / N) * N;
-            while (i < N) {
-                if (j < i) {
-                    const double p = A.J[size_t(i) * N + j];
-#pragma unroll
-                    for (int k = 0; k < K; k++) acc[k] += (down_bit(sm.spin + k * NW, i) ^ down_bit(sm.spin + k * NW, j)) ? -p : p;
-                }
-                j += dj;
-                i += di;
-                if (j >= N) {
-                    j -= N;
-                    i++;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                acc[k] = warp_sum(acc[k]);
-                if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
-            }
-        }
-        for (int it = tid; it < KK * N; it += T) {
-            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-            const bool down = down_bit(sm.spin + k * NW, i);
-            const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
-            const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
-            const float *trow = sm.t + q * MP;
-            // four independent partial products over 16-byte loads; padded units
-            // (t = 0, c = 1, s = 0) contribute exactly 1, so MP needs no tail
-            const float sg = down ? 1.f : -1.f;
-            float p0 = 1.f, p1 = 1.f, p2 = 1.f, p3 = 1.f;
-            for (int j = 0; j < MP; j += 4) {
-                const float4 tt = *reinterpret_cast<const float4 *>(trow + j);
-                const float4 ss = *reinterpret_cast<const float4 *>(srow + j);
-                const float4 cc = *reinterpret_cast<const float4 *>(crow + j);
-                p0 *= fmaf(sg * tt.x, ss.x, cc.x);
-                p1 *= fmaf(sg * tt.y, ss.y, cc.y);
-                p2 *= fmaf(sg * tt.z, ss.z, cc.z);
-                p3 *= fmaf(sg * tt.w, ss.w, cc.w);
-            }
-            const float p = (p0 * p1) * (p2 * p3);
-            sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
-            const float B = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
-            sm.bsig[it] = down_bit(sm.spin + kk * NW, i) ? -B : B;
-        }
-        __syncthreads();
-        if (tid < K) {
-            double jt = 0.0;
-            for (int w2 = 0; w2 < nwarp; w2++) jt += sm.jpart[w2 * 4 + tid];
-            sm.jk[tid] = 2.0 * jt;
-        }
-        __syncthreads();
-        for (int q = warp; q < KK; q += nwarp) {
-            float acc = 0.f;
-            for (int i = lane; i < N; i += 32) acc += sm.rat[q * N + i];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) sm.Dm[q] = sm.jk[q / K] - A.h * double(acc);
-        }
-        __syncthreads();
-        if (writer) {
-            bool ok = true;
-            for (int r = 0; r < K; r++)
-                for (int cc = 0; cc < K; cc++) {
-                    double e = 0.0;
-                    for (int t = 0; t < K; t++) e = fma(sm.pinv[r * K + t], sm.Dm[t * K + cc] * sm.phi[t * K + cc], e);
-                    ok = ok && isfinite(e);
-                    A.E[s * KK + r * K + cc] = cplx{e, 0.0};
-                }
-            for (int k = 0; k < K; k++)
-                for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
-            if (!ok) atomicOr(A.err, kErrNonFinite);
-        }
-        for (int t = tid; t < K * NW; t += T) A.spins[s * K * NW + t] = sm.spin[t];
-        __syncthreads();
-        // O row, layout [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239), FP32
-        float *orow = A.O + s * P;
-        for (int k = 0; k < K; k++) {
-            float *ok = orow + size_t(k) * L;
-            for (int p = tid; p < N + M; p += T) {
-                float v = 0.f;
-                if (p < N) {
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v += sm.bsig[(k * K + kk) * N + p];
-                } else {
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.Bm[k * K + kk], sm.t[(kk * K + k) * MP + p - N], v);
-                }
-                ok[p] = v;
-            }
-            float *ow = ok + N + M;
-            int i = tid / M, j = tid - (tid / M) * M;
-            const int di = T / M, dj = T - (T / M) * M;
-            for (int p = tid; p < N * M; p += T) {
-                float v = 0.f;
-#pragma unroll
-                for (int kk = 0; kk < K; kk++) v = fmaf(sm.bsig[(k * K + kk) * N + i], sm.t[(kk * K + k) * MP + j], v);
-                ow[p] = v;
-                j += dj;
-                i += di;
-                if (j >= M) {
-                    j -= M;
-                    i++;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    if (writer) {
-        A.accepted[c] = nacc;
-        A.exact[c] = nexact;
-    }
-}
-
-// Padded tables [kk][i][MP] (padding: c = 1, s = 0, w = 0, so a padded
-// factor is exactly 1), theta's b as double-float [kk][MP], and per (kk, i)
-// the bound record of run_row: {u (sum_j cond_j + 2M + 16),
-// sum_j |s_j| / (c_j - |s_j|), max_j 1 / (c_j - |s_j|)^2, u (2 max_j cond_j + 5)}
-// with c - |s| = e^{-2|w|} and cond = (c + |s|) / (c - |s|) = e^{4|w|}, each
-// rounded up.
-__global__ void k_tables_dw(Shape sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
-                            float *wlp, float *bh, float *bl, float4 *bnd) {
-    const size_t nr = size_t(sh.K) * sh.N;
-    for (size_t r = blockIdx.x * size_t(blockDim.x) + threadIdx.x; r < nr; r += size_t(gridDim.x) * blockDim.x) {
-        double sc = 0.0, s1 = 0.0, f2 = 0.0, qm = 0.0;
-        for (int j = 0; j < sh.M; j++) {
-            const double aw = fabs(w[r * sh.M + j].re);
-            const double d = exp(-2.0 * aw), cond = exp(4.0 * aw);
-            sc += cond;
-            s1 += fabs(sinh(2.0 * aw)) / d;
-            f2 = fmax(f2, 1.0 / (d * d));
-            qm = fmax(qm, cond);
-        }
-        const double up = 1.0 + 1e-6, u = 0x1p-24;
-        bnd[r] = make_float4(float(u * (sc + 2.0 * sh.M + 16.0) * up), float(s1 * up), float(f2 * up),
-                             float(u * (2.0 * qm + 5.0) * up));
-    }
-    const size_t n = size_t(sh.K) * sh.N * MP;
-    for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
-        const int j = int(t % MP);
-        const size_t ki = t / MP;  // kk*N + i
-        float c = 1.f, s = 0.f, h = 0.f, l = 0.f;
-        if (j < sh.M) {
-            const double wv = w[ki * sh.M + j].re;
-            c = float(cosh(2.0 * wv));
-            s = float(sinh(2.0 * wv));
-            h = float(wv);
-            l = float(wv - double(h));
-        }
-        cp[t] = c;
-        spp[t] = s;
-        whp[t] = h;
-        wlp[t] = l;
-        if (t < size_t(sh.K) * MP) {
-            const int kk = int(t / MP);
-            float bh0 = 0.f, bl0 = 0.f;
-            if (j < sh.M) {
-                const double bv = b[size_t(kk) * sh.M + j].re;
-                bh0 = float(bv);
-                bl0 = float(bv - double(bh0));
-            }
-            bh[t] = bh0;
-            bl[t] = bl0;
-        }
-    }
-}
 
 using DwKernel = void (*)(const MixedArgs);
 template <int K> DwKernel dw_kernel_u(int U) {
@@ -730,6 +18,7 @@ template <int K> DwKernel dw_kernel_u(int U) {
     case 4: return k_sample_dw<K, 4>;
     case 8: return k_sample_dw<K, 8>;
     case 16: return k_sample_dw<K, 16>;
+    case 32: return k_sample_dw<K, 32>;
     default: return nullptr;
     }
 }
@@ -737,23 +26,21 @@ DwKernel dw_kernel(int K, int U) {
     switch (K) {
     case 1: return dw_kernel_u<1>(U);
     case 2: return dw_kernel_u<2>(U);
-    case 3: return dw_kernel_u<3>(U);
-    case 4: return dw_kernel_u<4>(U);
-    default: return nullptr;
+    default: return reinterpret_cast<DwKernel>(dw_kernel_k34(K, U));
     }
 }
 
 }  // namespace
 
 // Units per lane of the decision-warp form for (M, K): G = largest power of two
-// <= 32/K lanes per RBM, U = M/G rounded up to a power of two; 0 if U > 16.
+// <= 32/K lanes per RBM, U = M/G rounded up to a power of two; 0 if U > 32.
 int dw_units(const Shape &sh, int *G_out) {
     int G = 32;
     while (G * sh.K > 32) G >>= 1;
     int U = 1;
     while (U * G < sh.M) U <<= 1;
     if (G_out) *G_out = G;
-    return U <= 16 ? U : 0;
+    return U <= 32 ? U : 0;
 }
 
 size_t dw_smem_bytes(const Shape &sh, int MP, bool staged) { return dsmem_bytes(sh.N, MP, sh.K, staged); }

@@ -1300,6 +1300,25 @@ int nqes_correlations(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn,
 
 }  // extern "C"
 
+extern "C" int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int chains, int samples_per_chain,
+                                    int precision, int complex_arith, uint64_t *bytes) {
+    if (!bytes || n_spins < 1 || n_hidden < 1 || n_states < 1 || chains < 1 || samples_per_chain < 1)
+        return NQES_ERR_INVALID;
+    const uint64_t N = n_spins, M = n_hidden, K = n_states, NW = (N + 63) / 64, P = K * (N + M + N * M);
+    const uint64_t Ns = uint64_t(chains) * samples_per_chain, ss = complex_arith ? 16 : 8;
+    const bool mixed = precision == NQES_PRECISION_MIXED;
+    const uint64_t rchunks = 32, nw = K * N * M, na = K * N;
+    uint64_t b = Ns * P * (mixed ? 4 : ss);                       // O
+    b += Ns * K * K * 16 + Ns * K * NW * 8 + uint64_t(chains) * 16;  // E, spins, accept / exact counts
+    b += Ns * ss + 3 * rchunks * P * ss + 14 * P * ss + 4 * kPartStride * 8;
+    if (mixed) b += P * 4 + Ns * 4 + rchunks * P * 4;
+    b += (3 * nw + 2 * na + K * M) * 16 + N * N * 8;  // weights, FP64 tables (complex-sized), J
+    b += nw * 4 * 2 + na * 4 * 2 + (nw + na + K * M) * 8;  // FP32 tables and FP64 copies of the real weights
+    b += 4 * K * N * 512 * 4 + 6 * K * 512 * 4;              // padded decision-warp tables (upper bound)
+    *bytes = b + (uint64_t(4) << 20);                        // small buffers and allocation rounding
+    return NQES_OK;
+}
+
 // ---- batched multi-solve ----
 
 struct nqes_batch {
@@ -1377,6 +1396,8 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
     }
     std::vector<int> arith(n), tks(n);
     std::vector<std::vector<long long>> keys(n);
+    if (statuses)
+        for (int i = 0; i < n; i++) statuses[i] = NQES_ERR_STATE;  // not run (yet)
     for (int i = 0; i < n; i++) {
         nqes_ctx *c = b->m[i];
         const int rc = step_prepare(c, seeds[i], chains[i], samples[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i],

@@ -1,0 +1,94 @@
+"""Serving loop: admission by device footprint, continuous batching, results
+independent of what else runs."""
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+import helpers
+from helpers import synthetic_j
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    ge._load_build_module().build_library()
+    return ge.load_package()
+
+
+def test_footprint_counts_the_o_matrix(pkg):
+    """The footprint bound grows with the samples and covers O (FP64 real,
+    FP64 complex, FP32 in the mixed form)."""
+    N, M, K, c, m = 32, 64, 2, 128, 200
+    P = K * (N + M + N * M)
+    f64 = pkg.footprint_bytes(N, M, K, c, m, pkg.PRECISION_FP64)
+    c128 = pkg.footprint_bytes(N, M, K, c, m, pkg.PRECISION_FP64, complex_arith=True)
+    mix = pkg.footprint_bytes(N, M, K, c, m, pkg.PRECISION_MIXED)
+    assert f64 >= c * m * P * 8 and c128 >= c * m * P * 16 and mix >= c * m * P * 4
+    assert mix < f64 < c128
+    assert pkg.footprint_bytes(N, M, K, c, 2 * m) > f64
+
+
+def test_server_reports_failures_without_hanging(pkg):
+    """Host logic: a request that can never fit fails with NQES_ERR_OOM; on a
+    machine without a GPU an admitted request fails with NQES_ERR_CUDA."""
+    torch = pytest.importorskip("torch")
+    srv = pkg.Server(hbm_budget_bytes=1 << 20, max_active=2)
+    big = srv.submit(32, 64, 2, synthetic_j(32), chains=128, samples_per_chain=200)
+    res = srv.wait_all(1, timeout=30)
+    srv.close()
+    assert [r["id"] for r in res] == [big] and res[0]["status"] == pkg.ERR_OOM
+    if not torch.cuda.is_available():
+        srv = pkg.Server(hbm_budget_bytes=1 << 40, max_active=2)
+        srv.submit(8, 16, 2, synthetic_j(8), max_steps=2)
+        res = srv.wait_all(1, timeout=30)
+        srv.close()
+        assert len(res) == 1 and res[0]["status"] == pkg.ERR_CUDA
+
+
+SPECS = [dict(n=8, m=16, k=2, h=0.7, prec=0, seed=11), dict(n=12, m=12, k=3, h=1.1, prec=1, seed=23),
+         dict(n=10, m=20, k=1, h=0.4, prec=0, seed=37), dict(n=16, m=32, k=2, h=0.9, prec=1, seed=41)]
+
+
+def submit_all(pkg, srv, specs):
+    ids = []
+    for s in specs:
+        w = helpers.random_weights(s["n"], s["m"], s["k"], 0.05, s["seed"], real=True)
+        ids.append(srv.submit(s["n"], s["m"], s["k"], synthetic_j(s["n"]), weights=w, h=s["h"], seed=s["seed"],
+                              chains=16, samples_per_chain=20, burn_in=5, reglam0=5.0, tol=1e-12, max_steps=4,
+                              precision=s["prec"]))
+    return ids
+
+
+@pytest.mark.gpu
+def test_results_same_alone_and_in_the_mix(pkg):
+    """Each solve's energies are bit-identical whether it runs alone or batched
+    with solves of other shapes and precisions."""
+    alone = {}
+    for s in SPECS:
+        srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=1)
+        (rid,) = submit_all(pkg, srv, [s])
+        (r,) = srv.wait_all(1)
+        srv.close()
+        assert r["status"] == 0 and r["steps"] == 4
+        alone[s["seed"]] = r
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=8)
+    ids = submit_all(pkg, srv, SPECS)
+    res = {r["id"]: r for r in srv.wait_all(len(SPECS))}
+    srv.close()
+    for rid, s in zip(ids, SPECS):
+        r, a = res[rid], alone[s["seed"]]
+        assert r["status"] == 0 and r["steps"] == a["steps"]
+        assert r["energies"] == a["energies"] and r["best"] == a["best"]
+
+
+@pytest.mark.gpu
+def test_admission_waits_for_memory(pkg):
+    """With room for one solve at a time, every solve still completes; later
+    ones queue until memory frees up."""
+    one = max(pkg.footprint_bytes(s["n"], s["m"], s["k"], 16, 20, s["prec"]) for s in SPECS)
+    srv = pkg.Server(hbm_budget_bytes=int(1.5 * one), max_active=8)
+    ids = submit_all(pkg, srv, SPECS)
+    res = srv.wait_all(len(SPECS))
+    srv.close()
+    assert sorted(r["id"] for r in res) == sorted(ids)
+    assert all(r["status"] == 0 for r in res)
+    assert max(r["t_queued"] for r in res) > 0.0
