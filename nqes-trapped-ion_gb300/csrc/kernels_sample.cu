@@ -65,6 +65,17 @@ __device__ __forceinline__ cplx shfl0(cplx v) {
     return {__shfl_sync(0xffffffffu, v.re, 0), __shfl_sync(0xffffffffu, v.im, 0)};
 }
 
+// det == 0 and a <= b (a, b >= 0) on the bit patterns: the same answers as the
+// FP64 compares (a NaN compares false), without FP64 instructions.
+__device__ __forceinline__ bool zero_bits(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ bool zero_bits(const cplx &v) { return zero_bits(v.re) && zero_bits(v.im); }
+__device__ __forceinline__ bool le_nonneg(double a, double b) {
+    const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+    const long long nan = 0x7FF0000000000000LL;
+    if ((ia & 0x7FFFFFFFFFFFFFFFLL) > nan || (ib & 0x7FFFFFFFFFFFFFFFLL) > nan) return false;
+    return ia <= ib;
+}
+
 // Multiply v by 2^-e where e is v's binary exponent when it leaves [-256, 256].
 template <class S> __device__ __forceinline__ void renorm(S &v, int &e) {
     int x = expo(v);
@@ -472,7 +483,9 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
                         ea = ldg((down ? A.tab.edn : A.tab.eup) + lane * N + i);
                         eg = ea * g;
                     }
-                    const double ud = (loaded ? pcg_u01(draw) : pcg_uniform(rng)) * detn;
+                    // u from the draw with integer instructions, one FP64 multiply
+                    const uint64_t dr = loaded ? draw : pcg_next(rng);
+                    const double ud = __longlong_as_double(static_cast<long long>(pcg_u01_bits(dr))) * detn;
                     __syncthreads();
                     // det Phi' = sum_kk r_kk e^{-2 sigma a} g_kk over lanes 0..K-1 (K <= 4)
                     S x = zero<S>(), r = one<S>();
@@ -488,7 +501,7 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
                     // Accept iff u <= min(1, |det Phi'|^2 / |det Phi|^2), with
                     // probability one when det Phi == 0 (code/rbm.cc:541-543),
                     // evaluated as u |det Phi|^2 <= |det Phi'|^2.
-                    const bool acc = is_zero(det) || ud <= np;
+                    const bool acc = zero_bits(det) || le_nonneg(ud, np);
                     if (acc) {
                         // tanh' = (tanh cosh(ws) - sinh(ws)) / f  (code/rbm.cc:185)
 #pragma unroll

@@ -65,6 +65,30 @@ __device__ __forceinline__ double pcg_u01(uint64_t x) {
     double u = __ull2double_rn(x) * 0x1p-64;
     return u >= 1.0 ? 0x1.fffffffffffffp-1 : u;
 }
+
+// The same value built with integer instructions only: round x to 53
+// significant bits (to nearest, ties to even), scale by 2^-64 through the
+// exponent field, clamp 1.0 to the largest double below it. Returns the IEEE
+// bit pattern. On GB300 this keeps the conversion off the FP64 pipe.
+__host__ __device__ __forceinline__ uint64_t pcg_u01_bits(uint64_t x) {
+    if (x == 0) return 0;
+#ifdef __CUDA_ARCH__
+    const int lz = __clzll(static_cast<long long>(x));
+#else
+    const int lz = __builtin_clzll(x);
+#endif
+    const uint64_t y = x << lz;          // leading one at bit 63
+    uint64_t m = y >> 11;                // 53 significant bits
+    const uint64_t rem = y & 0x7FFULL;   // the 11 bits rounded away
+    if (rem > 0x400ULL || (rem == 0x400ULL && (m & 1ULL))) m++;
+    int e = 63 - lz - 64;                // x * 2^-64 = 1.f * 2^e before rounding
+    if (m >> 53) {                       // rounding carried into a new bit
+        m >>= 1;
+        e++;
+    }
+    if (e >= 0) return 0x3FEFFFFFFFFFFFFFULL;  // rounded to 1.0: clamp below 1
+    return (uint64_t(e + 1023) << 52) | (m & 0xFFFFFFFFFFFFFULL);
+}
 __device__ __forceinline__ double pcg_uniform(Pcg64 &g) { return pcg_u01(pcg_next(g)); }
 
 // bernoulli_distribution(0.5): true (spin down) iff u < 0.5.
