@@ -262,7 +262,9 @@ def serving_form(pkg, rate, window_s, local, max_steps=10):
     """Config-5 style serving: Poisson arrivals at `rate` per second for
     `window_s` seconds of solve requests (N log-uniform on [8, 96], M in
     {N, 2N}, K uniform on 1..4, h ~ U[0, 2], tol 1e-6, 64 chains x 100 samples,
-    mixed precision, at most max_steps SR steps), admitted by device footprint
+    MINRES-QLP capped at 200 iterations (the reference's --minres-maxit: with up
+    to 75k parameters and 6400 samples S is rank-deficient), mixed precision, at
+    most max_steps SR steps), admitted by device footprint
     into the continuous batch. Returns solves/s and the time-to-converged-energy
     percentiles (submit to completion)."""
     import torch
@@ -280,11 +282,12 @@ def serving_form(pkg, rate, window_s, local, max_steps=10):
         K = int(rng.integers(1, 5))
         srv.submit(N, M, K, pkg.synthetic_j(N), weights=pkg.synthetic_weights(N, M, K, 0.01, SEED + n),
                    h=float(rng.uniform(0.0, 2.0)), seed=SEED + 7919 * n, chains=64, samples_per_chain=100, burn_in=16,
-                   tol=1e-6, max_steps=max_steps, precision=pkg.PRECISION_MIXED)
+                   tol=1e-6, max_steps=max_steps, minres_maxit=200, precision=pkg.PRECISION_MIXED)
         n += 1
         t_next += rng.exponential(1.0 / rate)
     res = srv.wait_all(n, timeout=900)
     t_end = time.perf_counter() - t0
+    phases = srv.times()
     srv.close()
     lat = np.array([r["t_total"] for r in res if r["status"] == 0])
     return {"rate_per_s": rate, "window_s": window_s, "submitted": n, "completed": int(len(lat)),
@@ -293,7 +296,7 @@ def serving_form(pkg, rate, window_s, local, max_steps=10):
             "solves_per_s": len(lat) / t_end, "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "mean_queue_s": float(np.mean([r["t_queued"] for r in res])) if res else None,
-            "max_steps": max_steps}
+            "max_steps": max_steps, "worker_phases": phases}
 
 
 def run_ours(args):

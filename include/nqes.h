@@ -260,6 +260,13 @@ int nqes_server_submit(nqes_server *server, const nqes_request *request, uint64_
 /* Moves up to max_results finished solves to out (oldest first). */
 int nqes_server_poll(nqes_server *server, nqes_result *out, int max_results, int *count);
 int nqes_server_status(nqes_server *server, int *queued, int *active, int *done, uint64_t *bytes_in_use);
+/* Cumulative worker time by phase (seconds): admitting solves (context
+ * creation, weights), creating batches after the active set changed, batched
+ * SR steps (including the graph capture of a new batch), and the host-side
+ * convergence tests and retirement; and the counts of steps and batch
+ * rebuilds. Any output may be NULL. */
+int nqes_server_times(nqes_server *server, double *admit_s, double *rebuild_s, double *step_s, double *post_s,
+                      uint64_t *steps, uint64_t *rebuilds);
 /* Stops the worker after its current step; unfinished solves are dropped. */
 int nqes_server_destroy(nqes_server *server);
 const char *nqes_server_last_error(const nqes_server *server);

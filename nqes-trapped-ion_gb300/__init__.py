@@ -32,7 +32,7 @@ EXPORTS = [
     "nqes_get_accepts", "nqes_get_O", "nqes_get_moments", "nqes_get_solution", "nqes_apply_S", "nqes_time_kernel",
     "nqes_apply_S_static", "nqes_batch_create", "nqes_batch_destroy", "nqes_batch_last_error", "nqes_batch_sr_step",
     "nqes_footprint_bytes", "nqes_server_create", "nqes_server_submit", "nqes_server_poll", "nqes_server_status",
-    "nqes_server_destroy", "nqes_server_last_error",
+    "nqes_server_destroy", "nqes_server_last_error", "nqes_server_times",
 ]
 KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
 
@@ -125,6 +125,7 @@ def load_library(path=None):
         "nqes_server_poll": (i, [vp, ctypes.POINTER(Result), i, ctypes.POINTER(i)]),
         "nqes_server_status": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(u64)]),
         "nqes_server_destroy": (i, [vp]),
+        "nqes_server_times": (i, [vp, _dp, _dp, _dp, _dp, ctypes.POINTER(u64), ctypes.POINTER(u64)]),
         "nqes_server_last_error": (ctypes.c_char_p, [vp]),
         "nqes_batch_create": (i, [ctypes.POINTER(vp), i, ctypes.POINTER(vp)]),
         "nqes_batch_destroy": (i, [vp]),
@@ -411,6 +412,14 @@ class Server:
         b = ctypes.c_uint64()
         self.lib.nqes_server_status(self._h, ctypes.byref(q), ctypes.byref(a), ctypes.byref(d), ctypes.byref(b))
         return {"queued": q.value, "active": a.value, "done": d.value, "bytes_in_use": b.value}
+
+    def times(self):
+        """Cumulative worker seconds by phase and the step / batch-rebuild counts."""
+        v = [ctypes.c_double() for _ in range(4)]
+        n = [ctypes.c_uint64() for _ in range(2)]
+        self.lib.nqes_server_times(self._h, *[ctypes.byref(x) for x in v], *[ctypes.byref(x) for x in n])
+        return {"admit_s": v[0].value, "rebuild_s": v[1].value, "step_s": v[2].value, "post_s": v[3].value,
+                "steps": n[0].value, "rebuilds": n[1].value}
 
     def wait_all(self, n_expected, timeout=600.0):
         """Polls until n_expected results arrived (or timeout seconds passed)."""

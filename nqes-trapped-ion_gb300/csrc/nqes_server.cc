@@ -58,6 +58,9 @@ struct nqes_server {
     std::deque<nqes_result> done;
     uint64_t next_id = 1;
     int n_active = 0;  // active solves, published by the worker under mu
+    // cumulative worker time (seconds) by phase, and counts, published under mu
+    double t_admit = 0, t_rebuild = 0, t_step = 0, t_post = 0;
+    uint64_t n_steps = 0, n_rebuilds = 0;
     bool stop = false;
     std::thread worker;
     nqes_batch *batch = nullptr;
@@ -138,6 +141,7 @@ void worker_loop(nqes_server *srv) {
                 continue;
             }
         }
+        const auto c0 = Clock::now();
         for (Solve *s : admitted) {
             s->t_admit = Clock::now();
             const int st = start_solve(srv, s);
@@ -149,9 +153,12 @@ void worker_loop(nqes_server *srv) {
         if (srv->active.empty()) continue;
 
         // one batched step over the active solves
+        const auto c1 = Clock::now();
         std::vector<nqes_ctx *> members;
         for (Solve *s : srv->active) members.push_back(s->ctx);
+        bool rebuilt = false;
         if (!srv->batch || members != srv->batch_members) {
+            rebuilt = true;
             if (srv->batch) nqes_batch_destroy(srv->batch);
             srv->batch = nullptr;
             if (nqes_batch_create(members.data(), int(members.size()), &srv->batch)) {
@@ -179,8 +186,10 @@ void worker_loop(nqes_server *srv) {
             maxit[i] = r.minres_maxit;
             emats[i] = reinterpret_cast<double *>(srv->active[i]->emat.data());
         }
+        const auto c2 = Clock::now();
         nqes_batch_sr_step(srv->batch, seeds.data(), chains.data(), m.data(), burn.data(), lr.data(), reglam.data(),
                            rtol.data(), maxit.data(), emats.data(), nullptr, status.data(), nullptr);
+        const auto c3 = Clock::now();
         std::vector<Solve *> keep;
         for (size_t i = 0; i < n; i++) {
             Solve *s = srv->active[i];
@@ -217,8 +226,18 @@ void worker_loop(nqes_server *srv) {
                 keep.push_back(s);
         }
         srv->active.swap(keep);
+        const auto c4 = Clock::now();
+        auto sec = [](Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); };
         std::lock_guard<std::mutex> g(srv->mu);
         srv->n_active = int(srv->active.size());
+        srv->t_admit += sec(c0, c1);
+        srv->t_step += sec(c2, c3);
+        srv->t_post += sec(c3, c4);
+        srv->n_steps++;
+        if (rebuilt) {
+            srv->t_rebuild += sec(c1, c2);  // batch creation; its graph is captured inside the first step
+            srv->n_rebuilds++;
+        }
     }
     if (srv->batch) nqes_batch_destroy(srv->batch);
     srv->batch = nullptr;
@@ -310,6 +329,19 @@ int nqes_server_status(nqes_server *s, int *queued, int *active, int *done, uint
     if (active) *active = s->n_active;
     if (done) *done = int(s->done.size());
     if (bytes_in_use) *bytes_in_use = s->in_use;
+    return NQES_OK;
+}
+
+int nqes_server_times(nqes_server *s, double *admit_s, double *rebuild_s, double *step_s, double *post_s,
+                      uint64_t *steps, uint64_t *rebuilds) {
+    if (!s) return NQES_ERR_INVALID;
+    std::lock_guard<std::mutex> g(s->mu);
+    if (admit_s) *admit_s = s->t_admit;
+    if (rebuild_s) *rebuild_s = s->t_rebuild;
+    if (step_s) *step_s = s->t_step;
+    if (post_s) *post_s = s->t_post;
+    if (steps) *steps = s->n_steps;
+    if (rebuilds) *rebuilds = s->n_rebuilds;
     return NQES_OK;
 }
 
