@@ -15,9 +15,11 @@
 // arithmetic is FP32.
 //
 // Exact state: theta in FP64 (one add per hidden unit per accepted flip);
-// tanh(theta) in FP32 is recomputed from it, so it never drifts; Phi is
-// recomputed exactly from theta after every sweep. Local energies are formed
-// in FP32 ratios and combined in FP64; log-derivatives are written in FP32.
+// tanh(theta) in FP32 is recomputed from it, so it never drifts; a row of Phi
+// is recomputed exactly from theta at the end of each row that changed. Local
+// energies are formed in FP32 ratios and combined in FP64; log-derivatives are
+// written in FP32. This block form serves shapes beyond the decision-warp
+// sampler's 32 hidden units per lane (kernels_sample_warp.cu).
 #include <cfloat>
 
 #include "nqes_internal.h"
