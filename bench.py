@@ -299,6 +299,49 @@ def serving_form(pkg, rate, window_s, local, max_steps=10):
             "max_steps": max_steps, "worker_phases": phases}
 
 
+def precision_form(pkg, chains, samples, steps, local):
+    """Config-3 style precision form: N=64, M=128, K=4, h ~ U[0.2, 1.2] (seeded),
+    `chains` x `samples` per SR step in the mixed form (FP32 O resident: 16384 x 64
+    samples x 33536 parameters = 141 GB), energies compared per state with the
+    all-FP64 GPU form on the same weights and seeds at a size whose FP64 O fits
+    (the FP64 O of the full size would be 281 GB)."""
+    n, m, k = 64, 128, 4
+    h = float(np.random.default_rng(SEED).uniform(0.2, 1.2))
+    J = pkg.synthetic_j(n)
+    w = pkg.synthetic_weights(n, m, k, 0.01, SEED)
+
+    def steps_of(prec, ch, sm, nsteps):
+        c = pkg.Context(n, m, k, J, h, device=local)
+        c.set_weights(*w)
+        c.set_option(pkg.OPT_PRECISION, prec)
+        res = []
+        for t in range(nsteps):
+            lr, reglam = schedule(t)
+            e, info = c.sr_step(SEED + t * ch, ch, sm, BURN, lr, reglam, RTOL, MAXIT)
+            res.append((np.sort(np.linalg.eigvals(e / n).real), info))
+        c.close()
+        return res
+
+    import torch
+    free = torch.cuda.mem_get_info(local)[0]
+    need = pkg.footprint_bytes(n, m, k, chains, samples, pkg.PRECISION_MIXED)
+    if need > 0.9 * free:
+        return {"shape": "N64 M128 K4", "skipped": "footprint %.1f GB > 90%% of free %.1f GB" % (need / 1e9, free / 1e9)}
+    full = steps_of(pkg.PRECISION_MIXED, chains, samples, 1 + steps)
+    ms = float(np.mean([i["ms_total"] for _, i in full[1:]]))
+    small = 2048
+    em = steps_of(pkg.PRECISION_MIXED, small, samples, 1)[0][0]
+    ef = steps_of(pkg.PRECISION_FP64, small, samples, 1)[0][0]
+    return {"shape": "N64 M128 K4", "h": h, "chains": chains, "samples_per_chain": samples, "burn_in": BURN,
+            "precision": "mixed", "ms_per_step": ms, "value": chains * samples / (ms * 1e-3), "unit": "MC samples/s",
+            "minres_iters_mean": float(np.mean([i["minres_iters"] for _, i in full[1:]])),
+            "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for _, i in full[1:]])),
+            "energies_per_site": [float(x) for x in full[-1][0]],
+            "dE_rel_vs_fp64": float(np.max(np.abs(em - ef) / np.abs(ef))),
+            "dE_note": "first step at %d chains x %d samples, same weights and seeds (same chains) in both forms"
+                       % (small, samples)}
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -470,6 +513,10 @@ def run_ours(args):
     if args.batch_solves:
         out["batched"] = batched_form(pkg, args.batch_solves, 1024, 64, 2, local)
 
+    # ---- precision form (config-3 style) ----
+    if args.precision_chains:
+        out["precision_form"] = precision_form(pkg, args.precision_chains, 64, 1, local)
+
     # ---- serving loop (config-5 style Poisson arrivals) ----
     if args.serve_rates:
         out["serving"] = [serving_form(pkg, float(r), args.serve_window, local) for r in args.serve_rates.split(",")]
@@ -494,6 +541,7 @@ def main():
     ap.add_argument("--sweep-chains", type=int, default=4096, help="chains of the sweep line (0: skip)")
     ap.add_argument("--batch-solves", type=int, default=64, help="solves of the batched line (0: skip)")
     ap.add_argument("--serve-rates", default="4,16", help="arrival rates (1/s) of the serving lines ('' : skip)")
+    ap.add_argument("--precision-chains", type=int, default=16384, help="chains of the precision-form line (0: skip)")
     ap.add_argument("--serve-window", type=float, default=5.0, help="seconds of arrivals per serving line")
     args = ap.parse_args()
     if args.impl == "reference":
