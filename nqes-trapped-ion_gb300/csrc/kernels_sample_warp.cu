@@ -74,6 +74,8 @@ cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx 
                              float *wlp, float *bh, float *bl, float *bnd, cudaStream_t st) {
     const size_t n = size_t(sh.K) * sh.N * MP;
     const int blocks = int(std::min<size_t>((n + 255) / 256, 4096));
+    const cudaError_t e = cudaMemsetAsync(bnd + 4 * size_t(sh.K) * sh.N, 0, sizeof(float) * sh.K, st);
+    if (e != cudaSuccess) return e;
     k_tables_dw<<<blocks, 256, 0, st>>>(sh, MP, b, w, cp, spp, whp, wlp, bh, bl, reinterpret_cast<float4 *>(bnd));
     return cudaGetLastError();
 }

@@ -38,7 +38,7 @@ struct nqes_ctx {
     // decision-warp form of the mixed sampler (dw_U = 0: block form)
     int dw_G = 0, dw_U = 0, dw_MP = 0;
     float *dcp = nullptr, *dsp = nullptr, *dwh = nullptr, *dwl = nullptr, *dbh = nullptr, *dbl = nullptr;
-    float *dbnd = nullptr;  // K·N float4 bound records
+    float *dbnd = nullptr;  // K·N float4 bound records, then K row-sum maxima
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
     int step_precision = NQES_PRECISION_FP64;      // precision of the allocated step buffers
     int tk_opt = 0;
@@ -745,7 +745,7 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
         const size_t np = size_t(K) * N * ctx->dw_MP, nb = size_t(K) * ctx->dw_MP;
         if ((rc = dalloc(ctx, &ctx->dcp, np)) || (rc = dalloc(ctx, &ctx->dsp, np)) || (rc = dalloc(ctx, &ctx->dwh, np)) ||
             (rc = dalloc(ctx, &ctx->dwl, np)) || (rc = dalloc(ctx, &ctx->dbh, nb)) || (rc = dalloc(ctx, &ctx->dbl, nb)) ||
-            (rc = dalloc(ctx, &ctx->dbnd, 4 * size_t(K) * N)))
+            (rc = dalloc(ctx, &ctx->dbnd, 4 * size_t(K) * N + 4 * size_t(K))))
             return fail(rc);
     }
     if (cudaMallocHost(&ctx->sp_host, sizeof(StepParams)) != cudaSuccess ||
@@ -1314,7 +1314,7 @@ extern "C" int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int
     if (mixed) b += P * 4 + Ns * 4 + rchunks * P * 4;
     b += (3 * nw + 2 * na + K * M) * 16 + N * N * 8;  // weights, FP64 tables (complex-sized), J
     b += nw * 4 * 2 + na * 4 * 2 + (nw + na + K * M) * 8;  // FP32 tables and FP64 copies of the real weights
-    b += 4 * K * N * 512 * 4 + 6 * K * 512 * 4;              // padded decision-warp tables (upper bound)
+    b += 4 * K * N * 512 * 4 + 6 * K * 512 * 4 + (4 * K * N + 4 * K) * 4;  // decision-warp tables (upper bound)
     *bytes = b + (uint64_t(4) << 20);                        // small buffers and allocation rounding
     return NQES_OK;
 }

@@ -81,7 +81,7 @@ struct MixedArgs {
     // lane, tables padded to MP = G*U units per (kk, i) row: FP32 cosh(2w),
     // sinh(2w) and w as hi + lo [kk][i][MP]; b as hi + lo [kk][MP].
     const float *cp, *spp, *whp, *wlp, *bh, *bl;
-    const float *bnd;                    // per (kk, i): float4 bound record (kernels_sample_warp.cu)
+    const float *bnd;                    // per (kk, i): float4 bound record, then per kk 2 max_j sum_i |w_ij|
     int G, U, MP;
     int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
 };

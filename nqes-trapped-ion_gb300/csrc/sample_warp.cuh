@@ -221,17 +221,41 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
 
 // All proposals of row k, run by one warp. Returns whether the row changed.
 //
-// Error model of the FP32 proposal (u = 2^-24). tanh(theta) of the lane's
-// units is held in FP32 with an absolute error of at most Et (one bound per
-// RBM, the same in every lane): 5u after the row's rebuild (tanhf), and
-// after an accepted flip, whose update t' = (t c - sigma s) / f has
-// derivative dt'/dt = 1/f^2, Et' = Et max_j 1/f_j^2 + u (2 max_j cond_j + 5)
-// with cond_j = (c + |s|)/(c - |s|) >= (|c| + |t s|)/|f| (|t| <= 1). A factor
-// f_j = c - sigma t s then has relative error at most u (cond_j + 1) +
+// Error model of the FP32 proposal (u = 2^-24).
+//
+// tanh. tanh(theta) of the lane's units is held in FP32 with an absolute
+// error of at most Et (one bound per RBM, the same in every lane): 5u after
+// the row's rebuild (tanhf). An accepted flip updates t' = (t c - sigma s) / f,
+// a map with derivative 1/f^2, and rounds with eps <= u (2 max_j cond_j + 5),
+// cond_j = (c + |s|)/(c - |s|) >= (|c| + |t s|)/|f| (|t| <= 1). Two bounds hold
+// and the smaller is kept:
+//  - stepwise: Et' = Et max_j 1/f_j^2 + eps, with 1/f^2 <= 1/(c - |s|)^2;
+//  - telescoped: 1/f_j = cosh(theta_j) / cosh(theta_j'), so the product of the
+//    derivatives from any step to now is cosh^2(theta_then) / cosh^2(theta_now)
+//    <= cosh^2(|theta_0| + 2 sum_i |w_ij|) =: Am (each spin of the row flips at
+//    most once per row). Evaluating the derivative between the held and the
+//    exact t adds a factor (1 - Et q)^-2 <= 1 + 2.05 Et q per step (Et q <=
+//    0.01), q = max_j |s|/(c - |s|) = (max_j cond_j - 1) / 2. Hence
+//    Et <= Am F (5u + sum of eps), F the product of those factors.
+// A factor f_j = c - sigma t s then has relative error at most u (cond_j + 1) +
 // Et |s| / (c - |s|), and the product over the row's M factors (M - 1 + 16
 // roundings, the 16 also covering the FP64 tables' own rounding)
 //   beta = u (sum_j cond_j + 2M + 16) + Et sum_j |s_j| / (c_j - |s_j|).
 // The per-(kk, i) sums and maxima come from a table built with the weights.
+//
+// Decision. The FP64 test u |det|^2 <= |det'|^2 is u <= |rho|^2 with rho =
+// det'/det = sum_kk re_kk g_kk / sum_kk g_kk (g_kk = Phi[k][kk] cof_kk; re_kk
+// the entry's ratio, including e^{-2 sigma a}). The held g_kk differ from the
+// exact ones by at most dr |g_kk| + ga_kk (dr: the row's relative drift from
+// accepted FP32 flips; ga: the FP64 rows' own error) and the held det from
+// sum_kk g_kk by at most edet. The drift enters only through
+// sum_kk (re_kk - rho) (g_kk - g*_kk) / det, which is small when the states
+// are alike, so with rh = s / det the error of rh is at most
+//   E = [sum_kk |g| |re| (beta + 3u) + 1.03 sum_kk (dr |g| + ga) (|re - rh| + 1.02 bmax |re|)
+//        + (K + 1) u sum_kk |x| + |rh| edet] / |det| / (1 - q) + 3u |rh|,
+//   q = (1.03 dr sum|g| + sum ga + edet) / |det|  (required < 1/2).
+// A decision the margins (16u on each side) cannot make goes to the exact
+// path.
 template <int K, int U>
 __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsigned long long &nacc,
                         unsigned long long &nexact) {
@@ -253,25 +277,55 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
     auto bit = [&](int b) -> bool { return ((b < 64 ? sk0 : sk1) >> (b & 63)) & 1ULL; };
 
     // Decision state, identical in every lane: exact cofactors of row k (the
-    // other rows are exact), the row's entries, g and det with error bounds.
+    // other rows are exact), the row's entries, g, det and 1/det with the
+    // error bounds of the model above.
     double cofd[K], cabsd[K];
-    float phik[K], g[K], gabs[K], Et[K];
-    float det32, edet, rho = 0.f;
+    float phik[K], g[K], ga[K], Et[K], Eacc[K], Fq[K], Am[K];
+    float det32, rdet, edet, gsum, gasum, dr;
+    auto exact_state = [&](const double *pp, double det) {
+        double perm = 0.0;
+        gsum = 0.f;
+        gasum = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < K; kk++) {
+            const double p = pp[kk];
+            phik[kk] = float(p);
+            g[kk] = float(p * cofd[kk]);
+            ga[kk] = float(fabs(p) * cabsd[kk] * 0x1p-30);  // rows exact to far better than 2^-30
+            perm += fabs(p) * cabsd[kk];
+            gsum += fabsf(g[kk]);
+            gasum += ga[kk];
+        }
+        det32 = float(det);
+        rdet = 1.f / det32;
+        edet = kU * (fabsf(det32) + gsum) * 1.01f + float(perm * 0x1p-50);
+        dr = 2.f * kU;
+    };
     {
-        double det = 0.0, perm = 0.0;
+        double det = 0.0, pp[K];
 #pragma unroll
         for (int kk = 0; kk < K; kk++) {
             cofactor_abs(sm.phi, K, k, kk, cofd[kk], cabsd[kk]);
-            const double p = sm.phi[k * K + kk];
-            phik[kk] = float(p);
-            g[kk] = float(p * cofd[kk]);
-            gabs[kk] = float(fabs(p) * cabsd[kk]);
-            det += p * cofd[kk];
-            perm += fabs(p) * cabsd[kk];
+            pp[kk] = sm.phi[k * K + kk];
+            det += pp[kk] * cofd[kk];
             Et[kk] = 5.f * kU;
+            Eacc[kk] = 5.f * kU;
+            Fq[kk] = 1.f;
         }
-        det32 = float(det);
-        edet = 4.f * kU * fabsf(det32) + float(perm * 0x1p-50);
+        exact_state(pp, det);
+        // Am = cosh^2(|theta_0| + 2 max_j sum_i |w_ij|), |theta_0| = atanh(max |t|)
+        float tm = 0.f;
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (live[u]) tm = fmaxf(tm, fabsf(t[u]));
+#pragma unroll
+        for (int o = G >> 1; o > 0; o >>= 1) tm = fmaxf(tm, __shfl_xor_sync(0xffffffffu, tm, o));
+#pragma unroll
+        for (int kk = 0; kk < K; kk++) {
+            const float tk = __shfl_sync(0xffffffffu, tm, kk * G) + 6.f * kU;
+            const float ch = coshf(fmaf(atanhf(tk), 1.f + 8.f * kU, __ldg(A.bnd + 4 * K * N + kk)));
+            Am[kk] = tk < 0.9999f ? ch * ch * (1.f + 1e-5f) : INFINITY;
+        }
     }
     bool changed = false;
 
@@ -303,29 +357,38 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
         }
 #pragma unroll
         for (int o = G >> 1; o > 0; o >>= 1) prod *= __shfl_xor_sync(0xffffffffu, prod, o);
-        float x[K], rr[K], s = 0.f, ed = 0.f, bmax = 0.f;
+        float x[K], re[K], beta[K], s = 0.f, sax = 0.f, bmax = 0.f;
 #pragma unroll
         for (int kk = 0; kk < K; kk++) {
-            rr[kk] = __shfl_sync(0xffffffffu, prod, kk * G);
-            const float beta = fmaf(Et[kk], bd[kk].y, bd[kk].x);
-            const float re = rr[kk] * ea[kk];
-            x[kk] = re * g[kk];
+            const float rr = __shfl_sync(0xffffffffu, prod, kk * G);
+            beta[kk] = fmaf(Et[kk], bd[kk].y, bd[kk].x);
+            re[kk] = rr * ea[kk];
+            x[kk] = re[kk] * g[kk];
             s += x[kk];
-            ed += fabsf(re) * ((beta + 3.f * kU) * fabsf(g[kk]) + 1.02f * rho * gabs[kk]) + 3.f * kU * fabsf(x[kk]);
-            bmax = fmaxf(bmax, beta);
+            sax += fabsf(x[kk]);
+            bmax = fmaxf(bmax, beta[kk]);
         }
-        ed = ed * 1.01f + 4.f * kU * fabsf(s);
+        const float rh = s * rdet;
+        float e1 = 0.f, e2 = 0.f;
+#pragma unroll
+        for (int kk = 0; kk < K; kk++) {
+            const float ar = fabsf(re[kk]), ag = fabsf(g[kk]);
+            e1 = fmaf(ag * ar, beta[kk] + 3.f * kU, e1);
+            e2 = fmaf(fmaf(dr, ag, ga[kk]), fmaf(1.02f * bmax, ar, fabsf(re[kk] - rh)), e2);
+        }
 
         bool acc = false, exact_path = false;
         {
-            const float ad = fabsf(s), lo = ad - ed, hi = ad + ed;
-            const float dd = fabsf(det32), dlo = fmaxf(dd - edet, 0.f), dhi = dd + edet;
-            const float su = u32 * (1.f + 16.f * kU), sl = u32 * (1.f - 16.f * kU);
-            if (A.exact_all || !(dd > 1e-15f) || !(dd < 1e15f) || !(bmax < 0.01f))
+            const float ad = fabsf(det32), ard = fabsf(rdet), arh = fabsf(rh);
+            const float q = fmaf(1.03f * dr, gsum, gasum + edet) * ard;
+            const float num = fmaf(1.03f, e2, e1) + fmaf(float(K + 1) * kU, sax, arh * edet);
+            const float E = fmaf(1.02f * num, ard / (1.f - q), 3.f * kU * arh);
+            const float lo = arh - E, hi = arh + E;
+            if (A.exact_all || !(ad > 1e-15f) || !(ad < 1e15f) || !(bmax < 0.01f) || !(q < 0.5f))
                 exact_path = true;  // det == 0 (accepted, code/rbm.cc:542), range, loose bound
-            else if (lo > 0.f && lo * lo * (1.f - 16.f * kU) >= su * dhi * dhi)
+            else if (lo > 0.f && lo * lo * (1.f - 16.f * kU) >= u32 * (1.f + 16.f * kU))
                 acc = true;
-            else if (!(hi * hi * (1.f + 16.f * kU) < sl * dlo * dlo))
+            else if (!(hi * hi * (1.f + 16.f * kU) < u32 * (1.f - 16.f * kU)))
                 exact_path = true;  // NaN lands here as well
         }
         if (exact_path) {
@@ -410,37 +473,34 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
             acc = det_e == 0.0 || pcg_u01(draw) * (det_e * det_e) <= sx * sx;
             nexact++;
             // continue from the exact row
-            double perm = 0.0;
-#pragma unroll
-            for (int kk = 0; kk < K; kk++) {
-                const double p = acc ? pn[kk] : pc[kk];
-                phik[kk] = float(p);
-                g[kk] = float(p * cofd[kk]);
-                gabs[kk] = float(fabs(p) * cabsd[kk]);
-                perm += fabs(p) * cabsd[kk];
-            }
-            det32 = float(acc ? sx : det_e);
-            edet = 4.f * kU * fabsf(det32) + float(perm * 0x1p-50);
-            rho = 0.f;
+            exact_state(acc ? pn : pc, acc ? sx : det_e);
         }
         if (acc) {
             // tanh' = (t c - sigma s) / f (code/rbm.cc:185) in FP32, and its bound
 #pragma unroll
             for (int u = 0; u < U; u++) t[u] = __fdividef(fmaf(t[u], cq[u], down ? sq[u] : -sq[u]), f[u]);
 #pragma unroll
-            for (int kk = 0; kk < K; kk++) Et[kk] = fmaf(Et[kk] * (1.f + 4.f * kU), bd[kk].z, bd[kk].w);
+            for (int kk = 0; kk < K; kk++) {
+                Eacc[kk] += bd[kk].w;
+                Fq[kk] *= fmaf(1.025f * Et[kk], bd[kk].z - 1.f, 1.f + 2.f * kU);
+                const float tel = Am[kk] * Fq[kk] * Eacc[kk] * (1.f + 16.f * kU);
+                Et[kk] = fminf(tel, fmaf(Et[kk] * (1.f + 4.f * kU), bd[kk].z, bd[kk].w));
+            }
             if (!exact_path) {
                 // row k times r e^{-2 sigma a}: g_kk becomes x_kk (cofactors exclude row k)
+                gasum = 0.f;
 #pragma unroll
                 for (int kk = 0; kk < K; kk++) {
-                    const float re = rr[kk] * ea[kk];
-                    phik[kk] *= re;
+                    phik[kk] *= re[kk];
                     g[kk] = x[kk];
-                    gabs[kk] *= fabsf(re);
+                    ga[kk] *= 1.02f * fabsf(re[kk]);
+                    gasum += ga[kk];
                 }
                 det32 = s;
-                edet = ed;
-                rho += bmax + 4.f * kU;
+                rdet = 1.f / s;
+                gsum = sax;
+                edet = float(K) * kU * sax * 1.01f;
+                dr = fmaf(dr, 1.f + bmax + 8.f * kU, fmaf(bmax, 1.01f, 5.f * kU));
             }
             // keep the row's largest entry near 1 (exact power-of-two scaling)
             int ex = -100000;
@@ -452,10 +512,13 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                 for (int kk = 0; kk < K; kk++) {
                     phik[kk] *= sc;
                     g[kk] *= sc;
-                    gabs[kk] *= sc;
+                    ga[kk] *= sc;
                 }
                 det32 *= sc;
+                rdet *= ldexpf(1.f, ex);
                 edet *= sc;
+                gsum *= sc;
+                gasum *= sc;
             }
             if (i < 64)
                 sk0 ^= 1ULL << i;
@@ -675,7 +738,8 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
 // the bound record of run_row: {u (sum_j cond_j + 2M + 16),
 // sum_j |s_j| / (c_j - |s_j|), max_j 1 / (c_j - |s_j|)^2, u (2 max_j cond_j + 5)}
 // with c - |s| = e^{-2|w|} and cond = (c + |s|) / (c - |s|) = e^{4|w|}, each
-// rounded up.
+// rounded up; after the K*N records, per RBM 2 max_j sum_i |w_ij| (float bits,
+// rounded up, maximised with atomicMax over a zeroed slot).
 __global__ void k_tables_dw(Shape sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
                             float *wlp, float *bh, float *bl, float4 *bnd) {
     const size_t nr = size_t(sh.K) * sh.N;
@@ -692,6 +756,14 @@ __global__ void k_tables_dw(Shape sh, int MP, const cplx *b, const cplx *w, floa
         const double up = 1.0 + 1e-6, u = 0x1p-24;
         bnd[r] = make_float4(float(u * (sc + 2.0 * sh.M + 16.0) * up), float(s1 * up), float(f2 * up),
                              float(u * (2.0 * qm + 5.0) * up));
+    }
+    unsigned *wsum = reinterpret_cast<unsigned *>(bnd + nr);
+    for (size_t r = blockIdx.x * size_t(blockDim.x) + threadIdx.x; r < size_t(sh.K) * sh.M;
+         r += size_t(gridDim.x) * blockDim.x) {
+        const size_t kk = r / sh.M, j = r % sh.M;
+        double sw = 0.0;
+        for (int i = 0; i < sh.N; i++) sw += fabs(w[(kk * sh.N + i) * sh.M + j].re);
+        atomicMax(wsum + kk, __float_as_uint(float(2.0 * sw * (1.0 + 1e-6))));
     }
     const size_t n = size_t(sh.K) * sh.N * MP;
     for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
