@@ -1,0 +1,516 @@
+// Factored S·v and moments of the mixed form (real arithmetic, FP32 data).
+//
+// The log-derivatives of a sample (code/rbm.cc:199-239, closed form) are, for
+// state k and parameter p of the augmented (N+1) x (M+1) grid of that state,
+//     O_{s,k,(i,j)} = sum_kk B_s(kk->k) sigma~_{s,kk,i} T~_{s,k,kk,j}
+// with B_s(kk->k) = (Phi^-1)_{k,kk} Phi_{kk,k}, sigma~_{s,kk,i} = sigma_i of
+// configuration kk (i < N) or 1 (i = N), T~_{s,k,kk,j} = tanh theta_j of
+// configuration kk under RBM k (j < M) or 1 (j = M). Grid entry (i, j) is the
+// weight w_ij, (i, M) the visible bias a_i, (N, j) the hidden bias b_j; (N, M)
+// is unused. A sample therefore needs K^2 M tanh values and K^2 coefficients
+// (the spins are stored anyway) instead of the P = K(N + M + NM) entries of O.
+//
+// With a "row" r = (s, kk) (a sample and one of its configurations) and, for
+// state k, W_k / va_k / vb_k the w / a / b blocks of a parameter vector:
+//   rows:    u_s = sum_k sum_kk B [ sum_j (vb_j + sum_i sigma_i W_ij) T_j + sum_i sigma_i va_i ]
+//   columns: Y_k(i, j) = sum_r w_r sigma_{r,i} T_{r,j}, plus the a and b blocks
+//            (w_r = u_s B, B, or E_loc,s B)
+//   squares: sum_s O^2 = the column sum over the virtual rows (s, kk <= kk2)
+//            with weight c B B', signs sigma sigma' (XOR of the spin words) and
+//            T T' (c = 2 off the diagonal)
+// Both passes are register-blocked products over the sample dimension: a
+// thread keeps an RB x JB (rows) or IB x JB (columns) block of accumulators,
+// the step's W_k (rows) or the rows' w T (columns) are staged in shared
+// memory, and the +-1 signs come straight from the spin words. The rows pass
+// costs K^2 N M fused multiply-adds per sample and reads K^2 M floats; the
+// dense form read P = K(N + M + N M) floats per sample and pass.
+//
+// Column-type results are written as per-chunk partials in the P layout that
+// the MINRES-QLP epilogue and the moment finalisation read; all sums run in a
+// fixed order.
+#include <algorithm>
+
+#include "nqes_internal.h"
+
+namespace nqes {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kJT = 8;       // j-threads per i group (columns)
+constexpr int kGroups = kThreads / kJT;
+// rows per double-buffered batch of the column kernel (64 KB of tanh rows)
+__host__ __device__ constexpr int cols_stage(int JB) { return JB >= 64 ? 8 : JB >= 32 ? 16 : 32; }
+constexpr int kMaxN = 128;
+
+__device__ __forceinline__ bool down_bit(const uint64_t *s, int i) { return (s[i >> 6] >> (i & 63)) & 1ULL; }
+
+// +1 for spin up (bit clear), -1 for spin down (bit set); i < 128.
+__device__ __forceinline__ float sgn(uint64_t b0, uint64_t b1, int i) {
+    const uint64_t w = i < 64 ? b0 : b1;
+    return __int_as_float(0x3f800000 | (int((w >> (i & 63)) & 1ULL) << 31));
+}
+
+// u_s = O_s . v. Block: kThreads / JT row groups x JT j-threads; a row group
+// owns RB consecutive rows (s, kk), a j-thread the JB / 4 float4 column
+// chunks q JT + tj (interleaved, so that the JT threads of a group read
+// consecutive 16-byte pieces of a staged row: no bank conflicts). W_k is
+// staged in chunks of F.ic rows of JT JB floats (zero beyond M).
+template <int JT, int JB, int RB>
+__global__ void __launch_bounds__(kThreads, 2) k_frows(FactArgs F, const float *__restrict__ v, float *__restrict__ u) {
+    extern __shared__ float4 smem4[];
+    constexpr int WS = JT * JB, NG = kThreads / JT;
+    const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K, IC = F.ic;
+    float *sw = reinterpret_cast<float *>(smem4);  // IC x WS
+    float *sva = sw + IC * WS;                     // N (rounded to 4)
+    float *svb = sva + ((N + 3) & ~3);             // WS
+    float *surow = svb + WS;                       // NG * RB
+    const int tj = threadIdx.x & (JT - 1), rg = threadIdx.x / JT;
+    const int spb = (NG * RB) / K;                 // samples per block
+    const int rows_here = min(spb, F.Ns - int(blockIdx.x) * spb) * K;
+    const int rl0 = rg * RB;                       // first local row of the group
+    const size_t rbase = size_t(blockIdx.x) * spb * K;
+    uint64_t b0[RB], b1[RB];
+#pragma unroll
+    for (int rb = 0; rb < RB; rb++) {
+        const size_t r = rbase + min(rl0 + rb, max(rows_here - 1, 0));
+        b0[rb] = F.spins[r * NW];
+        b1[rb] = NW > 1 ? F.spins[r * NW + 1] : 0ULL;
+    }
+    float tot[RB];
+#pragma unroll
+    for (int rb = 0; rb < RB; rb++) tot[rb] = 0.f;
+    for (int k = 0; k < K; k++) {
+        const float *vk = v + size_t(k) * L;
+        __syncthreads();
+        for (int t = threadIdx.x; t < WS; t += kThreads) svb[t] = t < M ? vk[N + t] : 0.f;
+        for (int t = threadIdx.x; t < N; t += kThreads) sva[t] = vk[t];
+        __syncthreads();
+        float z[RB][JB];
+#pragma unroll
+        for (int jb = 0; jb < JB; jb++) {
+            const float b = svb[((jb >> 2) * JT + tj) * 4 + (jb & 3)];
+#pragma unroll
+            for (int rb = 0; rb < RB; rb++) z[rb][jb] = b;
+        }
+        for (int i0 = 0; i0 < N; i0 += IC) {
+            const int ni = min(IC, N - i0);
+            __syncthreads();
+            for (int t = threadIdx.x; t < ni * WS; t += kThreads) {
+                const int ii = t / WS, j = t - ii * WS;
+                sw[t] = j < M ? vk[N + M + size_t(i0 + ii) * M + j] : 0.f;
+            }
+            __syncthreads();
+            for (int ii = 0; ii < ni; ii++) {
+                const float4 *wr = reinterpret_cast<const float4 *>(sw + ii * WS) + tj;
+                float wv[JB];
+#pragma unroll
+                for (int q = 0; q < JB / 4; q++) {
+                    const float4 x = wr[q * JT];
+                    wv[4 * q] = x.x;
+                    wv[4 * q + 1] = x.y;
+                    wv[4 * q + 2] = x.z;
+                    wv[4 * q + 3] = x.w;
+                }
+#pragma unroll
+                for (int rb = 0; rb < RB; rb++) {
+                    const float sg = sgn(b0[rb], b1[rb], i0 + ii);
+#pragma unroll
+                    for (int jb = 0; jb < JB; jb++) z[rb][jb] = fmaf(sg, wv[jb], z[rb][jb]);
+                }
+            }
+        }
+        // the a block: sum_i sigma_i va_i over i = tj (mod JT)
+        float a[RB];
+#pragma unroll
+        for (int rb = 0; rb < RB; rb++) a[rb] = 0.f;
+        for (int i = tj; i < N; i += JT) {
+            const float va = sva[i];
+#pragma unroll
+            for (int rb = 0; rb < RB; rb++) a[rb] = fmaf(sgn(b0[rb], b1[rb], i), va, a[rb]);
+        }
+        // dot with the row's tanh values, times B
+#pragma unroll
+        for (int rb = 0; rb < RB; rb++) {
+            const int rl = rl0 + rb;
+            if (rl < rows_here) {
+                const size_t r = rbase + rl, s = r / K;
+                const int kk = int(r - s * K), q = k * K + kk;
+                const float *tr = F.T + (s * KK + q) * size_t(MT);
+                float d = a[rb];
+#pragma unroll
+                for (int c = 0; c < JB / 4; c++) {
+                    const int j = (c * JT + tj) * 4;
+                    if (j < MT) {
+                        const float4 x = __ldg(reinterpret_cast<const float4 *>(tr + j));
+                        d = fmaf(z[rb][4 * c], x.x, d);
+                        d = fmaf(z[rb][4 * c + 1], x.y, d);
+                        d = fmaf(z[rb][4 * c + 2], x.z, d);
+                        d = fmaf(z[rb][4 * c + 3], x.w, d);
+                    }
+                }
+                tot[rb] = fmaf(__ldg(F.B + s * KK + q), d, tot[rb]);
+            }
+        }
+    }
+    // sum over the j-threads of the group, then over the configurations
+#pragma unroll
+    for (int rb = 0; rb < RB; rb++) {
+#pragma unroll
+        for (int o = 1; o < JT; o <<= 1) tot[rb] += __shfl_xor_sync(0xffffffffu, tot[rb], o);
+        if (tj == 0) surow[rl0 + rb] = tot[rb];
+    }
+    __syncthreads();
+    for (int sl = threadIdx.x; sl * K < rows_here; sl += kThreads) {
+        float acc = 0.f;
+        for (int kk = 0; kk < K; kk++) acc += surow[sl * K + kk];
+        u[size_t(blockIdx.x) * spb + sl] = acc;
+    }
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Column-type partial sums over chunk blockIdx.x of the rows of state
+// k = blockIdx.y, grid rows i in block blockIdx.z (kGroups * IB of them).
+//   mode 0: w_r = u_s B          (the O^T u pass of S·v)
+//   mode 1: w_r = B              (sum of O)
+//   mode 2: w_r = E_loc,s B      (sum of E_loc O)
+//   mode 3: squares: virtual rows (s, kk <= kk2), w = c B B', T T', XOR'ed signs
+// out gets the chunk's partial in the P layout at out + chunk * P.
+// Batches of cols_stage(JB) rows are double-buffered: the tanh rows of the next batch
+// stream into shared memory (cp.async) and its weights and sign words are
+// formed while the current batch is summed.
+template <int IB, int JB>
+__global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, const float *__restrict__ w,
+                                                     const cplx *__restrict__ E, float *__restrict__ out) {
+    constexpr int WS = kJT * JB, kStage = cols_stage(JB);
+    extern __shared__ float4 smem4[];
+    float *st = reinterpret_cast<float *>(smem4);          // [2][kStage][WS] tanh rows (second factor: [2][kStage][WS])
+    float *sw1 = st + 2 * 2 * kStage * WS;                 // [2][kStage]
+    uint64_t *sb = reinterpret_cast<uint64_t *>(sw1 + 2 * kStage);  // [2][kStage][2]
+    const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K;
+    const int P = K * L;
+    const int c = blockIdx.x, k = blockIdx.y;
+    const int tj = threadIdx.x & (kJT - 1), ig = threadIdx.x / kJT;
+    const int ibase = blockIdx.z * (kGroups * IB) + ig * IB;
+    const int vpr = mode == 3 ? K * (K + 1) / 2 : K;  // (virtual) rows per sample
+    const size_t nrows = size_t(F.Ns) * vpr;
+    const size_t r0 = nrows * c / F.rchunks, r1 = nrows * (c + 1) / F.rchunks;
+    const int nbat = int((r1 - r0 + kStage - 1) / kStage);
+    const int nf = mode == 3 ? 2 : 1;
+    // zero the column padding of all buffers once (copies write [0, MT) only)
+    for (int t = threadIdx.x; t < 2 * 2 * kStage * WS; t += kThreads) st[t] = 0.f;
+    __syncthreads();
+
+    // issue batch b into buffer b & 1: tanh rows by cp.async, weights and signs directly
+    auto issue = [&](int bi) {
+        const int buf = bi & 1;
+        const size_t rb0 = r0 + size_t(bi) * kStage;
+        const int nb = int(min(size_t(kStage), r1 - rb0));
+        const int per = MT / 4;  // 16-byte pieces per row
+        for (int t = threadIdx.x; t < nf * nb * per; t += kThreads) {
+            const int f = t / (nb * per), rem = t - f * nb * per, rr = rem / per, pc = rem - rr * per;
+            const size_t r = rb0 + rr, s = r / vpr;
+            int kk = int(r - s * vpr), kk2 = kk;
+            if (mode == 3) {
+                int a = 0;
+                while (kk >= K - a) {
+                    kk -= K - a;
+                    a++;
+                }
+                kk2 = a + kk;
+                kk = a;
+            }
+            const size_t row = s * KK + size_t(k) * K + (f == 0 ? kk : kk2);
+            cp_async16(st + ((f * 2 + buf) * kStage + rr) * WS + 4 * pc, F.T + row * MT + 4 * pc);
+        }
+        cp_async_commit();
+        if (threadIdx.x < nb) {
+            const int rr = threadIdx.x;
+            const size_t r = rb0 + rr, s = r / vpr;
+            int kk = int(r - s * vpr), kk2 = -1;
+            if (mode == 3) {
+                int a = 0;
+                while (kk >= K - a) {
+                    kk -= K - a;
+                    a++;
+                }
+                kk2 = a + kk;
+                kk = a;
+            }
+            const size_t qo = s * KK + size_t(k) * K;
+            float wr = __ldg(F.B + qo + kk);
+            if (mode == 0) wr *= __ldg(w + s);
+            if (mode == 2) {
+                double el = 0.0;
+                for (int q = 0; q < K; q++) el += E[s * KK + q * K + q].re;
+                wr *= float(el);
+            }
+            uint64_t x0 = F.spins[(s * K + kk) * NW], x1 = NW > 1 ? F.spins[(s * K + kk) * NW + 1] : 0ULL;
+            if (mode == 3) {
+                wr *= (kk == kk2 ? 1.f : 2.f) * __ldg(F.B + qo + kk2);
+                x0 ^= F.spins[(s * K + kk2) * NW];
+                if (NW > 1) x1 ^= F.spins[(s * K + kk2) * NW + 1];
+            }
+            sw1[buf * kStage + rr] = wr;
+            sb[(buf * kStage + rr) * 2] = x0;
+            sb[(buf * kStage + rr) * 2 + 1] = x1;
+        }
+    };
+
+    float acc[IB][JB], acca[IB], accb[JB];
+#pragma unroll
+    for (int ii = 0; ii < IB; ii++) {
+        acca[ii] = 0.f;
+#pragma unroll
+        for (int jb = 0; jb < JB; jb++) acc[ii][jb] = 0.f;
+    }
+#pragma unroll
+    for (int jb = 0; jb < JB; jb++) accb[jb] = 0.f;
+    const bool bgroup = blockIdx.z == 0 && ig == 0;
+    if (nbat > 0) issue(0);
+    for (int bi = 0; bi < nbat; bi++) {
+        const int buf = bi & 1;
+        const int nb = int(min(size_t(kStage), r1 - (r0 + size_t(bi) * kStage)));
+        if (bi + 1 < nbat) {
+            issue(bi + 1);
+        } else {
+            cp_async_commit();  // an empty group keeps the wait count uniform
+        }
+        cp_async_wait1();
+        __syncthreads();
+        const float *tb = st + (size_t(buf) * kStage) * WS, *tb2 = st + (size_t(2 + buf) * kStage) * WS;
+        for (int rr = 0; rr < nb; rr++) {
+            float tv[JB];
+            const float4 *tp = reinterpret_cast<const float4 *>(tb + rr * WS) + tj;
+#pragma unroll
+            for (int q = 0; q < JB / 4; q++) {
+                const float4 x = tp[q * kJT];
+                tv[4 * q] = x.x;
+                tv[4 * q + 1] = x.y;
+                tv[4 * q + 2] = x.z;
+                tv[4 * q + 3] = x.w;
+            }
+            if (mode == 3) {
+                const float4 *tp2 = reinterpret_cast<const float4 *>(tb2 + rr * WS) + tj;
+#pragma unroll
+                for (int q = 0; q < JB / 4; q++) {
+                    const float4 x = tp2[q * kJT];
+                    tv[4 * q] *= x.x;
+                    tv[4 * q + 1] *= x.y;
+                    tv[4 * q + 2] *= x.z;
+                    tv[4 * q + 3] *= x.w;
+                }
+            }
+            const float wr = sw1[buf * kStage + rr];
+            const uint64_t x0 = sb[(buf * kStage + rr) * 2], x1 = sb[(buf * kStage + rr) * 2 + 1];
+#pragma unroll
+            for (int ii = 0; ii < IB; ii++) {
+                const float sw = sgn(x0, x1, min(ibase + ii, kMaxN - 1)) * wr;
+#pragma unroll
+                for (int jb = 0; jb < JB; jb++) acc[ii][jb] = fmaf(sw, tv[jb], acc[ii][jb]);
+            }
+            if (bgroup) {
+#pragma unroll
+                for (int jb = 0; jb < JB; jb++) accb[jb] = fmaf(wr, tv[jb], accb[jb]);
+            }
+        }
+        // the a block: row rr = tj (mod kJT) per j-thread
+        for (int rr = tj; rr < nb; rr += kJT) {
+            const float wr = sw1[buf * kStage + rr];
+            const uint64_t x0 = sb[(buf * kStage + rr) * 2], x1 = sb[(buf * kStage + rr) * 2 + 1];
+#pragma unroll
+            for (int ii = 0; ii < IB; ii++) acca[ii] = fmaf(sgn(x0, x1, min(ibase + ii, kMaxN - 1)), wr, acca[ii]);
+        }
+        __syncthreads();  // buffer buf is refilled by the next issue
+    }
+#pragma unroll
+    for (int ii = 0; ii < IB; ii++)
+#pragma unroll
+        for (int o = 1; o < kJT; o <<= 1) acca[ii] += __shfl_xor_sync(0xffffffffu, acca[ii], o);
+    float *o = out + size_t(c) * P + size_t(k) * L;
+#pragma unroll
+    for (int ii = 0; ii < IB; ii++) {
+        const int i = ibase + ii;
+        if (i < N) {
+#pragma unroll
+            for (int jb = 0; jb < JB; jb++) {
+                const int j = ((jb >> 2) * kJT + tj) * 4 + (jb & 3);
+                if (j < M) o[N + M + size_t(i) * M + j] = acc[ii][jb];
+            }
+            if (tj == 0) o[i] = acca[ii];
+        }
+    }
+    if (bgroup) {
+#pragma unroll
+        for (int jb = 0; jb < JB; jb++) {
+            const int j = ((jb >> 2) * kJT + tj) * 4 + (jb & 3);
+            if (j < M) o[N + j] = accb[jb];
+        }
+    }
+}
+
+// o, skk = reglam (<O^2> - o^2), f = <E_loc O> - eloc o from the chunk partials.
+__global__ void k_fmoment_final(int Ns, int P, int rchunks, const StepParams *sp, const float *po, const float *pf,
+                                const float *ps2, const cplx *eloc, double *o, double *skk, double *f, int *err) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    double so = 0.0, sf = 0.0, s2 = 0.0;
+    for (int r = 0; r < rchunks; r++) {
+        so += po[size_t(r) * P + p];
+        sf += pf[size_t(r) * P + p];
+        s2 += ps2[size_t(r) * P + p];
+    }
+    const double inv = 1.0 / double(Ns), om = so * inv;
+    const double dg = (s2 * inv - om * om) * sp->reglam;
+    const double fv = sf * inv - eloc[0].re * om;
+    o[p] = om;
+    skk[p] = dg;
+    f[p] = fv;
+    if (!isfinite(om) || !isfinite(dg) || !isfinite(fv)) atomicOr(err, kErrNonFinite);
+}
+
+// Rows [first, first + count) of O from the factors (for inspection).
+__global__ void k_fO(FactArgs F, int first, int count, float *O) {
+    const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, P = K * L, KK = K * K;
+    const size_t total = size_t(count) * P;
+    for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
+        const size_t s = size_t(first) + e / P;
+        const int p = int(e % P), k = p / L, q = p - k * L;
+        int i, j;
+        if (q < N) {
+            i = q;
+            j = M;
+        } else if (q < N + M) {
+            i = N;
+            j = q - N;
+        } else {
+            i = (q - N - M) / M;
+            j = (q - N - M) - i * M;
+        }
+        float v = 0.f;
+        for (int kk = 0; kk < K; kk++) {
+            const float b = F.B[s * KK + k * K + kk];
+            const float tt = j < M ? F.T[(s * KK + k * K + kk) * F.MT + j] : 1.f;
+            const bool dn = i < N && down_bit(F.spins + (s * K + kk) * NW, i);
+            v += dn ? -b * tt : b * tt;
+        }
+        O[e] = v;
+    }
+}
+
+// Launch shapes. Rows: JT j-threads of JB columns (JT JB >= M), RB rows per
+// row group (RB JB <= 64, <= 32 below 16 columns). Columns: kJT j-threads of
+// JB columns, IB grid rows per i group (IB JB <= 64, <= 32 from 32 columns).
+int pick_jb(int M) {
+    const int jb = (M + kJT - 1) / kJT;
+    return jb <= 4 ? 4 : jb <= 8 ? 8 : jb <= 16 ? 16 : jb <= 32 ? 32 : 64;
+}
+int pick_ib(int N, int JB) {
+    const int want = (N + kGroups - 1) / kGroups;  // cover N with one block of i groups
+    int ib = want <= 1 ? 1 : want <= 2 ? 2 : 4;
+    while (ib > 1 && ib * JB > (JB >= 32 ? 32 : 64)) ib >>= 1;
+    return ib;
+}
+template <int JT, int JB>
+cudaError_t rows_launch(FactArgs F, const float *v, float *u, cudaStream_t st, bool prepare) {
+    constexpr int RB = JB >= 16 ? 64 / JB : 32 / JB, WS = JT * JB, NG = kThreads / JT;
+    F.ic = std::max(1, std::min(F.N, (48 * 1024 / 4) / WS));
+    const size_t smem = (size_t(F.ic) * WS + ((F.N + 3) & ~3) + WS + NG * RB) * sizeof(float);
+    if (prepare)
+        return cudaFuncSetAttribute(k_frows<JT, JB, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    const int spb = (NG * RB) / F.K;
+    const int blocks = (F.Ns + spb - 1) / spb;
+    k_frows<JT, JB, RB><<<blocks, kThreads, smem, st>>>(F, v, u);
+    return cudaGetLastError();
+}
+cudaError_t rows_dispatch(const FactArgs &F, const float *v, float *u, cudaStream_t st, bool prepare) {
+    const int M = F.M;
+    if (M <= 16) return rows_launch<4, 4>(F, v, u, st, prepare);
+    if (M <= 32) return rows_launch<4, 8>(F, v, u, st, prepare);
+    if (M <= 64) return rows_launch<4, 16>(F, v, u, st, prepare);
+    if (M <= 128) return rows_launch<8, 16>(F, v, u, st, prepare);
+    if (M <= 256) return rows_launch<8, 32>(F, v, u, st, prepare);
+    return rows_launch<8, 64>(F, v, u, st, prepare);
+}
+
+template <int IB, int JB> constexpr size_t cols_smem() {
+    constexpr size_t st = cols_stage(JB);
+    return (size_t(2) * 2 * st * kJT * JB + 2 * st) * sizeof(float) + size_t(2) * st * 2 * 8;
+}
+template <int IB, int JB>
+cudaError_t cols_launch(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, cudaStream_t st,
+                        bool prepare) {
+    constexpr size_t smem = cols_smem<IB, JB>();
+    if (prepare) return cudaFuncSetAttribute(k_fcols<IB, JB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    dim3 g(F.rchunks, F.K, (F.N + kGroups * IB - 1) / (kGroups * IB));
+    k_fcols<IB, JB><<<g, kThreads, smem, st>>>(F, mode, w, E, out);
+    return cudaGetLastError();
+}
+template <int JB>
+cudaError_t cols_ib(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, cudaStream_t st,
+                    bool prepare) {
+    switch (pick_ib(F.N, JB)) {
+    case 1: return cols_launch<1, JB>(F, mode, w, E, out, st, prepare);
+    case 2:
+        if constexpr (JB < 32) return cols_launch<2, JB>(F, mode, w, E, out, st, prepare);
+        return cudaErrorInvalidConfiguration;
+    default:
+        if constexpr (4 * JB <= 64) return cols_launch<4, JB>(F, mode, w, E, out, st, prepare);
+        return cudaErrorInvalidConfiguration;
+    }
+}
+cudaError_t cols_dispatch(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, cudaStream_t st,
+                          bool prepare = false) {
+    switch (pick_jb(F.M)) {
+    case 4: return cols_ib<4>(F, mode, w, E, out, st, prepare);
+    case 8: return cols_ib<8>(F, mode, w, E, out, st, prepare);
+    case 16: return cols_ib<16>(F, mode, w, E, out, st, prepare);
+    case 32: return cols_ib<32>(F, mode, w, E, out, st, prepare);
+    default: return cols_ib<64>(F, mode, w, E, out, st, prepare);
+    }
+}
+
+}  // namespace
+
+// Sets the rows and column kernels' shared-memory limits; call outside stream capture.
+cudaError_t prepare_frows(const FactArgs &F) {
+    cudaError_t e = rows_dispatch(F, nullptr, nullptr, nullptr, true);
+    if (e == cudaSuccess) e = cols_dispatch(F, 0, nullptr, nullptr, nullptr, nullptr, true);
+    return e;
+}
+
+cudaError_t launch_frows(const FactArgs &F, const float *v, float *u, cudaStream_t st) {
+    return rows_dispatch(F, v, u, st, false);
+}
+
+cudaError_t launch_fcols(const FactArgs &F, const float *w, float *ypart, cudaStream_t st) {
+    return cols_dispatch(F, 0, w, nullptr, ypart, st);
+}
+
+cudaError_t launch_fmoments(const FactArgs &F, const cplx *E, float *po, float *pf, float *ps2, cudaStream_t st) {
+    cudaError_t e = cols_dispatch(F, 1, nullptr, nullptr, po, st);
+    if (e == cudaSuccess) e = cols_dispatch(F, 2, nullptr, E, pf, st);
+    if (e == cudaSuccess) e = cols_dispatch(F, 3, nullptr, nullptr, ps2, st);
+    return e;
+}
+
+cudaError_t launch_fmoment_final(const FactArgs &F, const StepParams *sp, const float *po, const float *pf,
+                                 const float *ps2, const cplx *eloc, double *o, double *skk, double *f, int *err,
+                                 cudaStream_t st) {
+    const int P = F.K * (F.N + F.M + F.N * F.M);
+    k_fmoment_final<<<(P + 255) / 256, 256, 0, st>>>(F.Ns, P, F.rchunks, sp, po, pf, ps2, eloc, o, skk, f, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fO(const FactArgs &F, int first, int count, float *O, cudaStream_t st) {
+    k_fO<<<1024, 256, 0, st>>>(F, first, count, O);
+    return cudaGetLastError();
+}
+
+}  // namespace nqes

@@ -17,9 +17,10 @@
 // Exact state: theta in FP64 (one add per hidden unit per accepted flip);
 // tanh(theta) in FP32 is recomputed from it, so it never drifts; a row of Phi
 // is recomputed exactly from theta at the end of each row that changed. Local
-// energies are formed in FP32 ratios and combined in FP64; log-derivatives are
-// written in FP32. This block form serves shapes beyond the decision-warp
-// sampler's 32 hidden units per lane (kernels_sample_warp.cu).
+// energies are formed in FP32 ratios and combined in FP64; the log-derivatives
+// are written as their factors (kernels_factored.cu). This block form serves
+// shapes beyond the decision-warp sampler's 32 hidden units per lane
+// (kernels_sample_warp.cu).
 #include <cfloat>
 
 #include "nqes_internal.h"
@@ -175,8 +176,7 @@ __device__ void cofactors(const double *m, int K, int r, int c, double &cof, dou
 template <int UMAX>
 __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K, L = A.sh.L;
-    const size_t P = size_t(A.sh.P);
+    const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int TK = A.tk, WK = TK >> 5;
     const int my_kk = tid / TK, my_jl = tid - (tid / TK) * TK;
@@ -471,23 +471,14 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
         }
         for (int t = tid; t < K * NW; t += T) A.spins[s * K * NW + t] = sm.spin[t];
         __syncthreads();
-        float *orow = A.O + s * P;
-        for (int k = 0; k < K; k++) {
-            float *ok = orow + size_t(k) * L;
-            for (int p = tid; p < L; p += T) {
-                float v = 0.f;
-                if (p < N) {
-                    for (int kk = 0; kk < K; kk++) v += sm.bsig[(k * K + kk) * N + p];
-                } else if (p < N + M) {
-                    const int j = p - N;
-                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.Bm[k * K + kk], sm.t[(kk * K + k) * M + j], v);
-                } else {
-                    const int q = p - N - M, i = q / M, j = q - i * M;
-                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.bsig[(k * K + kk) * N + i], sm.t[(kk * K + k) * M + j], v);
-                }
-                ok[p] = v;
-            }
+        // the factors of the O row (see kernels_factored.cu)
+        const int MT = fact_mt(M);
+        float *ft = A.FT + s * size_t(KK) * MT;
+        for (int e = tid; e < KK * MT; e += T) {
+            const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
+            ft[e] = j < M ? sm.t[(kk * K + k) * M + j] : 0.f;
         }
+        if (tid < KK) A.FB[s * KK + tid] = sm.Bm[tid];
         __syncthreads();
     }
     if (writer) {

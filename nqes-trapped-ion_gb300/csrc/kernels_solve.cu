@@ -160,29 +160,6 @@ template <class S> __global__ void k_sv_cols(int Ns, int P, int rchunks, const S
     ypart[size_t(r) * P + p] = acc;
 }
 
-// FP32 passes of the mixed form: u = O v and partial O^T u with FP32 storage
-// and FP32 accumulation (real arithmetic).
-__global__ void k_sv_rows_f32(int Ns, int P, const float *O, const float *v, float *u) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= Ns) return;
-    const float *row = O + size_t(warp) * P;
-    float acc = 0.f;
-    for (int p = lane; p < P; p += 32) acc = fmaf(row[p], __ldg(v + p), acc);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) u[warp] = acc;
-}
-
-__global__ void k_sv_cols_f32(int Ns, int P, int rchunks, const float *O, const float *u, float *ypart) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    const int r = blockIdx.y;
-    if (p >= P) return;
-    const int s0 = int(int64_t(Ns) * r / rchunks), s1 = int(int64_t(Ns) * (r + 1) / rchunks);
-    float acc = 0.f;
-    for (int s = s0; s < s1; s++) acc = fmaf(O[size_t(s) * P + p], __ldg(u + s), acc);
-    ypart[size_t(r) * P + p] = acc;
-}
-
 __global__ void k_to_f32(int n, const double *x, float *y) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) y[t] = float(x[t]);
@@ -197,7 +174,7 @@ __device__ __forceinline__ void mirror_f32(float *, int, cplx) {}
 template <class S>
 __device__ __forceinline__ S sv_epilogue(const SolveBufs<S> &B, int p, const S *v, S ov) {
     S y = zero<S>();
-    if (B.O32) {
+    if (B.fact) {
         for (int r = 0; r < B.rchunks; r++) y = y + one<S>() * double(B.ypart32[size_t(r) * B.sh.P + p]);
     } else {
         for (int r = 0; r < B.rchunks; r++) y = y + B.ypart[size_t(r) * B.sh.P + p];
@@ -644,10 +621,15 @@ template <class S> cudaError_t launch_moments(const SolveBufs<S> &B, cudaStream_
     double *ps2 = reinterpret_cast<double *>(B.ypart + size_t(2) * B.rchunks * P);
     dim3 g(nb, B.rchunks);
     if constexpr (std::is_same<S, double>::value) {
-        if (B.O32) k_moment_part<S, float><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O32, B.E, po, ps2, pf);
+        if (B.fact) {
+            float *fo = B.ypart32, *ff = fo + size_t(B.rchunks) * P, *fs = ff + size_t(B.rchunks) * P;
+            cudaError_t e = launch_fmoments(B.F, B.E, fo, ff, fs, st);
+            if (e == cudaSuccess)
+                e = launch_fmoment_final(B.F, B.sp, fo, ff, fs, B.eloc, B.o, B.skk, B.f, B.err, st);
+            return e;
+        }
     }
-    if (!B.O32)
-        k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
+    k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
     k_moment_final<S><<<nb, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.sp, po, ps2, pf, B.eloc, B.o, B.skk, B.f,
                                                    B.err);
     return cudaGetLastError();
@@ -668,9 +650,9 @@ template <class S> static void launch_sv_passes(const SolveBufs<S> &B, const S *
     const int rows_per_block = kVecThreads / 32;
     const int rb = (B.Ns + rows_per_block - 1) / rows_per_block;
     dim3 g(nb, B.rchunks);
-    if (B.O32) {
-        k_sv_rows_f32<<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O32, B.v32, B.u32);
-        k_sv_cols_f32<<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O32, B.u32, B.ypart32);
+    if (B.fact) {
+        launch_frows(B.F, B.v32, B.u32, st);
+        launch_fcols(B.F, B.u32, B.ypart32, st);
     } else {
         k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u);
         k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart);
@@ -690,8 +672,8 @@ template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &B, cudaStr
 template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &B, cudaStream_t st) {
     const int rows_per_block = kVecThreads / 32;
     const int rb = (B.Ns + rows_per_block - 1) / rows_per_block;
-    if (B.O32)
-        k_sv_rows_f32<<<rb, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O32, B.v32, B.u32);
+    if (B.fact)
+        return launch_frows(B.F, B.v32, B.u32, st);
     else
         k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O, B.v, B.u);
     return cudaGetLastError();
@@ -700,8 +682,8 @@ template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &B, cudaSt
 template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &B, cudaStream_t st) {
     const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
     dim3 g(nb, B.rchunks);
-    if (B.O32)
-        k_sv_cols_f32<<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O32, B.u32, B.ypart32);
+    if (B.fact)
+        return launch_fcols(B.F, B.u32, B.ypart32, st);
     else
         k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O, B.u, B.ypart);
     return cudaGetLastError();
@@ -713,18 +695,18 @@ template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &B, cu
     S *pf = B.ypart + size_t(B.rchunks) * P;
     double *ps2 = reinterpret_cast<double *>(B.ypart + size_t(2) * B.rchunks * P);
     dim3 g(nb, B.rchunks);
-    if constexpr (std::is_same<S, double>::value) {
-        if (B.O32) k_moment_part<S, float><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O32, B.E, po, ps2, pf);
+    if (B.fact) {
+        float *fo = B.ypart32, *ff = fo + size_t(B.rchunks) * P, *fs = ff + size_t(B.rchunks) * P;
+        return launch_fmoments(B.F, B.E, fo, ff, fs, st);
     }
-    if (!B.O32)
-        k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
+    k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
     return cudaGetLastError();
 }
 
 template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &B, const S *v, S *out, cudaStream_t st) {
     const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
     k_ov_part<S><<<nb, kVecThreads, 0, st>>>(B.sh.P, B.o, v, B.ovpart);
-    if (B.O32) k_to_f32<<<nb, kVecThreads, 0, st>>>(B.sh.P, reinterpret_cast<const double *>(v), B.v32);
+    if (B.fact) k_to_f32<<<nb, kVecThreads, 0, st>>>(B.sh.P, reinterpret_cast<const double *>(v), B.v32);
     launch_sv_passes(B, v, st);
     k_apply_out<S><<<nb, kVecThreads, 0, st>>>(B, v, out);
     return cudaGetLastError();

@@ -149,12 +149,17 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     ctx->rchunks = std::max(1, std::min(ctx->rchunks, std::max(1, 600 / std::max(1, ctiles))));
     int rc;
     const bool mixed = ctx->precision == NQES_PRECISION_MIXED;
-    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * (mixed ? sizeof(float) : ss))))
-        return rc;
     if (mixed) {
-        if ((rc = dalloc(ctx, &ctx->exact, size_t(chains))) || (rc = dalloc(ctx, &ctx->v32, P)) ||
-            (rc = dalloc(ctx, &ctx->u32, Ns)) || (rc = dalloc(ctx, &ctx->ypart32, size_t(ctx->rchunks) * P)))
+        // O as its factors (K^2 (M + 1) floats per sample); column sums over
+        // chunks of ~128 samples, 3 partial sets for the moments
+        ctx->rchunks = int(std::max<size_t>(1, std::min<size_t>(256, (Ns + 127) / 128)));
+        const size_t KK = size_t(sh.K) * sh.K;
+        if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * KK * (fact_mt(sh.M) + 1) * sizeof(float))) ||
+            (rc = dalloc(ctx, &ctx->exact, size_t(chains))) || (rc = dalloc(ctx, &ctx->v32, P)) ||
+            (rc = dalloc(ctx, &ctx->u32, Ns)) || (rc = dalloc(ctx, &ctx->ypart32, 3 * size_t(ctx->rchunks) * P)))
             return rc;
+    } else if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * ss))) {
+        return rc;
     }
     ctx->step_precision = ctx->precision;
     if ((rc = dalloc(ctx, &ctx->E, Ns * sh.K * sh.K))) return rc;
@@ -162,7 +167,8 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     if ((rc = dalloc(ctx, &ctx->accepted, size_t(chains)))) return rc;
     if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->u), Ns * ss))) return rc;
     // ypart doubles as scratch for the moment partials: 3 × rchunks × P scalars
-    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ypart), 3 * size_t(ctx->rchunks) * P * ss)))
+    // (the mixed form keeps its partials in ypart32)
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ypart), mixed ? 1 : 3 * size_t(ctx->rchunks) * P * ss)))
         return rc;
     if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->vecs), 14 * P * ss))) return rc;
     if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ovpart), size_t(kPartStride) * ss))) return rc;
@@ -172,6 +178,22 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     ctx->arith = arith;
     ctx->Ns = Ns;
     return NQES_OK;
+}
+
+// The factors of O in the mixed form: tanh rows then coefficients, in ctx->O.
+FactArgs fact_args(nqes_ctx *ctx) {
+    FactArgs F{};
+    F.N = ctx->sh.N;
+    F.M = ctx->sh.M;
+    F.K = ctx->sh.K;
+    F.NW = ctx->sh.NW;
+    F.Ns = int(ctx->Ns);
+    F.rchunks = ctx->rchunks;
+    F.MT = fact_mt(F.M);
+    F.T = static_cast<const float *>(ctx->O);
+    F.B = F.T + ctx->Ns * size_t(F.K) * F.K * F.MT;
+    F.spins = ctx->spins;
+    return F;
 }
 
 template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
@@ -208,7 +230,8 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     B.use_cond = 0;
     if (ctx->step_precision == NQES_PRECISION_MIXED) {
         B.O = nullptr;
-        B.O32 = static_cast<const float *>(ctx->O);
+        B.fact = 1;
+        B.F = fact_args(ctx);
         B.v32 = ctx->v32;
         B.u32 = ctx->u32;
         B.ypart32 = ctx->ypart32;
@@ -233,7 +256,8 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.b64 = ctx->mb;
     A.J = ctx->J;
     A.h = ctx->h;
-    A.O = static_cast<float *>(ctx->O);
+    A.FT = static_cast<float *>(ctx->O);
+    A.FB = A.FT + size_t(chains) * m * size_t(ctx->sh.K) * ctx->sh.K * fact_mt(ctx->sh.M);
     A.E = ctx->E;
     A.spins = ctx->spins;
     A.accepted = ctx->accepted;
@@ -298,7 +322,14 @@ cudaError_t launch_mixed_tables(nqes_ctx *ctx) {
 size_t mixed_sampler_smem(nqes_ctx *ctx) {
     return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP, false) : mixed_smem_bytes(ctx->sh);
 }
+// The mixed sampler's and the factored S·v's shared-memory limits.
 cudaError_t prepare_mixed_sampler(nqes_ctx *ctx) {
+    FactArgs F{};
+    F.N = ctx->sh.N;
+    F.M = ctx->sh.M;
+    F.K = ctx->sh.K;
+    cudaError_t e = prepare_frows(F);
+    if (e != cudaSuccess) return e;
     return ctx->dw_U ? prepare_sample_dw(ctx->sh, ctx->dw_MP) : prepare_sample_mixed(ctx->sh);
 }
 cudaError_t launch_mixed_sampler(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
@@ -1060,9 +1091,18 @@ int nqes_get_O(nqes_ctx *ctx, int first, int count, double *O) {
     NQES_CUDA(cudaSetDevice(ctx->device));
     const size_t P = ctx->sh.P;
     if (ctx->step_precision == NQES_PRECISION_MIXED) {
+        // the rows rebuilt from the factors the mixed form keeps
         std::vector<float> tmp(size_t(count) * P);
-        NQES_CUDA(cudaMemcpy(tmp.data(), static_cast<const float *>(ctx->O) + size_t(first) * P,
-                             tmp.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        float *d = nullptr;
+        NQES_CUDA(cudaMalloc(&d, tmp.size() * sizeof(float)));
+        cudaError_t e = launch_fO(fact_args(ctx), first, count, d, ctx->st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tmp.data(), d, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+        cudaFree(d);
+        if (e != cudaSuccess) {
+            ctx->err = cudaGetErrorString(e);
+            return NQES_ERR_CUDA;
+        }
         for (size_t t = 0; t < tmp.size(); t++) {
             O[2 * t] = tmp[t];
             O[2 * t + 1] = 0.0;
@@ -1124,6 +1164,7 @@ int nqes_apply_S(nqes_ctx *ctx, const double *v, double *out) {
             for (size_t t = 0; t < P; t++) tmp[t] = v[2 * t];
             NQES_CUDA(cudaMemcpy(dv, tmp.data(), P * sizeof(double), cudaMemcpyHostToDevice));
             SolveBufs<double> B = solve_bufs<double>(ctx);
+            if (B.fact) NQES_CUDA(prepare_mixed_sampler(ctx));
             NQES_CUDA(launch_apply_S<double>(B, reinterpret_cast<double *>(dv), reinterpret_cast<double *>(dout),
                                              ctx->st));
         }
@@ -1162,10 +1203,16 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
     default: *bytes = double(Ns) * P * ss + double(Ns) * KK * sizeof(cplx) + 3.0 * ctx->rchunks * P * ss; break;
     }
     const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
-    if (mixed && kernel != NQES_KERNEL_MOMENTS) {
-        // FP32 O: the sampler writes 4 bytes per entry, the S·v passes read 4
-        const double s32 = double(Ns) * P * (ss - sizeof(float));
-        *bytes -= s32;
+    if (mixed) {
+        // the factors of O: K^2 (M + 1) floats per sample, plus the spins for the signs
+        const double fac = double(Ns) * (double(KK) * (ctx->sh.M + 1) * 4 + ctx->sh.K * ctx->sh.NW * 8);
+        switch (kernel) {
+        case NQES_KERNEL_SAMPLE: *bytes = fac + double(Ns) * KK * sizeof(cplx); break;
+        case NQES_KERNEL_SV_ROWS: *bytes = fac + double(P) * 4 + double(Ns) * 4; break;
+        case NQES_KERNEL_SV_COLS: *bytes = fac + double(Ns) * 4 + double(ctx->rchunks) * P * 4; break;
+        default: *bytes = fac + double(Ns) * KK * sizeof(cplx) + 3.0 * ctx->rchunks * P * 4; break;
+        }
+        NQES_CUDA(prepare_mixed_sampler(ctx));
     }
     if (kernel == NQES_KERNEL_SAMPLE) {
         if (mixed)
@@ -1308,10 +1355,10 @@ extern "C" int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int
     const uint64_t Ns = uint64_t(chains) * samples_per_chain, ss = complex_arith ? 16 : 8;
     const bool mixed = precision == NQES_PRECISION_MIXED;
     const uint64_t rchunks = 32, nw = K * N * M, na = K * N;
-    uint64_t b = Ns * P * (mixed ? 4 : ss);                       // O
+    uint64_t b = mixed ? Ns * K * K * (((M + 3) & ~3ULL) + 1) * 4 : Ns * P * ss;  // O, or its factors (mixed)
     b += Ns * K * K * 16 + Ns * K * NW * 8 + uint64_t(chains) * 16;  // E, spins, accept / exact counts
     b += Ns * ss + 3 * rchunks * P * ss + 14 * P * ss + 4 * kPartStride * 8;
-    if (mixed) b += P * 4 + Ns * 4 + rchunks * P * 4;
+    if (mixed) b += P * 4 + Ns * 4 + 3 * 256 * P * 4;
     b += (3 * nw + 2 * na + K * M) * 16 + N * N * 8;  // weights, FP64 tables (complex-sized), J
     b += nw * 4 * 2 + na * 4 * 2 + (nw + na + K * M) * 8;  // FP32 tables and FP64 copies of the real weights
     b += 4 * K * N * 512 * 4 + 6 * K * 512 * 4 + (4 * K * N + 4 * K) * 4;  // decision-warp tables (upper bound)

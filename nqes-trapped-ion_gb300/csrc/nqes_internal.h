@@ -70,7 +70,7 @@ struct MixedArgs {
     const double *w64, *a64, *b64;       // real weights [kk][i][j], [kk][i], [kk][j]
     const double *J;
     double h;
-    float *O;                            // Ns × P log-derivatives in FP32
+    float *FT, *FB;                      // factors of O (kernels_factored.cu): FT Ns×K×K×fact_mt(M), FB Ns×K×K
     cplx *E;                             // Ns × K² local-energy matrices (FP64)
     uint64_t *spins;
     unsigned long long *accepted;        // per chain
@@ -143,6 +143,26 @@ constexpr int kPartStride = 2048;
 
 template <class S> cudaError_t prepare_sample(const Shape &sh);
 
+// Factors of O in the mixed form (kernels_factored.cu): for sample s,
+// T[s][k][kk][j] = tanh theta_j of configuration kk under RBM k (rows padded
+// with zeros to MT = fact_mt(M) floats) and B[s][k][kk] =
+// (Phi^-1)_{k,kk} Phi_{kk,k}; the spins give the signs.
+struct FactArgs {
+    int N, M, K, NW, Ns, rchunks, MT;
+    int ic;  // rows of W staged per chunk by the rows pass (set at launch)
+    const float *T, *B;
+    const uint64_t *spins;
+};
+__host__ __device__ inline int fact_mt(int M) { return (M + 3) & ~3; }
+cudaError_t prepare_frows(const FactArgs &F);
+cudaError_t launch_frows(const FactArgs &F, const float *v, float *u, cudaStream_t st);
+cudaError_t launch_fcols(const FactArgs &F, const float *w, float *ypart, cudaStream_t st);
+cudaError_t launch_fmoments(const FactArgs &F, const cplx *E, float *po, float *pf, float *ps2, cudaStream_t st);
+cudaError_t launch_fmoment_final(const FactArgs &F, const StepParams *sp, const float *po, const float *pf,
+                                 const float *ps2, const cplx *eloc, double *o, double *skk, double *f, int *err,
+                                 cudaStream_t st);
+cudaError_t launch_fO(const FactArgs &F, int first, int count, float *O, cudaStream_t st);
+
 template <class S> struct SolveBufs {
     Shape sh;
     int Ns;
@@ -162,10 +182,12 @@ template <class S> struct SolveBufs {
     int *err;
     cudaGraphConditionalHandle cond;
     int use_cond;
-    // Mixed precision (real arithmetic only): O stored in FP32 and the two
-    // O passes of S·v in FP32 with FP32 accumulation; v is mirrored into v32
-    // by the kernels that produce it. Null in the FP64 form.
-    const float *O32;
+    // Mixed precision (real arithmetic only, fact = 1): O held as its factors
+    // and the two passes of S·v and the moments computed from them in FP32
+    // (kernels_factored.cu); v is mirrored into v32 by the kernels that
+    // produce it; ypart32 holds rchunks × P partials (3 × for the moments).
+    int fact;
+    FactArgs F;
     float *v32, *u32, *ypart32;
 };
 

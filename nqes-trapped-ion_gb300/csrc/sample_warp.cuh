@@ -539,8 +539,7 @@ template <int K_, int U>
 __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int K = K_, KK = K * K;
-    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, L = A.sh.L, MP = A.MP;
-    const size_t P = size_t(A.sh.P);
+    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int c = blockIdx.x;
     DSmem sm = dcarve(smem_raw, N, MP, K);
@@ -694,37 +693,16 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         }
         for (int t = tid; t < K * NW; t += T) A.spins[s * K * NW + t] = sm.spin[t];
         __syncthreads();
-        // O row, layout [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239), FP32
-        float *orow = A.O + s * P;
-        for (int k = 0; k < K; k++) {
-            float *ok = orow + size_t(k) * L;
-            for (int p = tid; p < N + M; p += T) {
-                float v = 0.f;
-                if (p < N) {
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v += sm.bsig[(k * K + kk) * N + p];
-                } else {
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v = fmaf(sm.Bm[k * K + kk], sm.t[(kk * K + k) * MP + p - N], v);
-                }
-                ok[p] = v;
-            }
-            float *ow = ok + N + M;
-            int i = tid / M, j = tid - (tid / M) * M;
-            const int di = T / M, dj = T - (T / M) * M;
-            for (int p = tid; p < N * M; p += T) {
-                float v = 0.f;
-#pragma unroll
-                for (int kk = 0; kk < K; kk++) v = fmaf(sm.bsig[(k * K + kk) * N + i], sm.t[(kk * K + k) * MP + j], v);
-                ow[p] = v;
-                j += dj;
-                i += di;
-                if (j >= M) {
-                    j -= M;
-                    i++;
-                }
-            }
+        // the factors of the O row (code/rbm.cc:199-239 in closed form): tanh rows
+        // T[s][k][kk][j] = tanh theta_j of configuration kk under RBM k, and
+        // B[s][k][kk] = (Phi^-1)_{k,kk} Phi_{kk,k}; the signs come from the spins
+        const int MT = fact_mt(M);
+        float *ft = A.FT + s * size_t(KK) * MT;
+        for (int e = tid; e < KK * MT; e += T) {
+            const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
+            ft[e] = j < M ? sm.t[(kk * K + k) * MP + j] : 0.f;
         }
+        if (tid < KK) A.FB[s * KK + tid] = sm.Bm[tid];
         __syncthreads();
     }
     if (writer) {

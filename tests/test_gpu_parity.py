@@ -188,11 +188,13 @@ def test_mixed_precision_keeps_fp64_chains(pkg, N, M, K, chains, m):
     """MIXED: FP32 decisions with a certified bound and an exact FP64 fallback
     give the FP64 chains bit for bit (decision-warp form for up to 16 hidden
     units per lane, block form beyond: M=300, K=4); energies within 1e-6 relative, FP32
-    log-derivatives within 1e-5, the updated weights within 5e-5 (the solve
-    runs its O passes in FP32; 24 samples at P = 33536 make S ill-conditioned)."""
+    log-derivatives, moments and S·v (factored FP32 passes) within 1e-5 / 1e-4,
+    the updated weights within 5e-5 (2e-4 where 24 samples meet P > 10^4)."""
     J = synthetic_j(N)
     w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 5 + N, real=True)
     out = {}
+    P = K * (N + M + N * M)
+    vrand = np.random.default_rng(N + M).normal(size=P).astype(np.complex128)
     for prec in (pkg.PRECISION_FP64, pkg.PRECISION_MIXED):
         ctx = pkg.Context(N, M, K, J, 0.595)
         ctx.set_weights(*w)
@@ -200,7 +202,8 @@ def test_mixed_precision_keeps_fp64_chains(pkg, N, M, K, chains, m):
         e, info = ctx.sr_step(4242, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
         spins, eloc, E = ctx.get_samples()
         out[prec] = dict(e=e, info=info, spins=spins, E=E, O=ctx.get_O(0, 4), acc=ctx.get_accepts(),
-                         mom=ctx.get_moments(), w=np.concatenate([x.ravel() for x in ctx.get_weights()]))
+                         mom=ctx.get_moments(), w=np.concatenate([x.ravel() for x in ctx.get_weights()]),
+                         sv=ctx.apply_S(vrand), Oall=ctx.get_O(0, chains * m))
         ctx.close()
     f, x = out[0], out[1]
     assert np.array_equal(f["spins"], x["spins"]), "mixed chains left the FP64 chains"
@@ -209,8 +212,16 @@ def test_mixed_precision_keeps_fp64_chains(pkg, N, M, K, chains, m):
     assert rel_err(x["E"], f["E"]) < 1e-5
     assert rel_err(x["e"], f["e"]) < 1e-6
     assert rel_err(x["O"], f["O"]) < 1e-5
-    assert rel_err(x["mom"][0], f["mom"][0]) < 1e-5
-    assert rel_err(x["w"], f["w"]) < 5e-5
+    assert rel_err(x["Oall"], f["Oall"]) < 1e-5
+    # o, the regularised diagonal of S and the force, from the factored passes
+    for a, b in zip(x["mom"], f["mom"]):
+        assert rel_err(a, b) < 1e-4
+    # the factored S·v (FP32 passes) against the dense FP64 one on the same chains
+    assert rel_err(x["sv"], f["sv"]) < 1e-4
+    # the update solves S x = f with FP32 operator passes; with 24 samples for
+    # P > 10^4 parameters S is the regulariser plus a rank-24 term, and the
+    # solve amplifies the operator's ~1e-6 rounding differences
+    assert rel_err(x["w"], f["w"]) < (5e-5 if P < 10000 else 2e-4)
 
 
 @pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 24, 20), (12, 24, 3, 8, 20),

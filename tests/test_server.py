@@ -16,13 +16,14 @@ def pkg():
 
 def test_footprint_counts_the_o_matrix(pkg):
     """The footprint bound grows with the samples and covers O (FP64 real,
-    FP64 complex, FP32 in the mixed form)."""
+    FP64 complex) or, in the mixed form, its factors (K^2 (M + 1) floats per
+    sample)."""
     N, M, K, c, m = 32, 64, 2, 128, 200
     P = K * (N + M + N * M)
     f64 = pkg.footprint_bytes(N, M, K, c, m, pkg.PRECISION_FP64)
     c128 = pkg.footprint_bytes(N, M, K, c, m, pkg.PRECISION_FP64, complex_arith=True)
     mix = pkg.footprint_bytes(N, M, K, c, m, pkg.PRECISION_MIXED)
-    assert f64 >= c * m * P * 8 and c128 >= c * m * P * 16 and mix >= c * m * P * 4
+    assert f64 >= c * m * P * 8 and c128 >= c * m * P * 16 and mix >= c * m * K * K * (M + 1) * 4
     assert mix < f64 < c128
     assert pkg.footprint_bytes(N, M, K, c, 2 * m) > f64
 
