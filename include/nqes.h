@@ -59,6 +59,10 @@ extern "C" {
                                       * each (chains, samples, burn-in, precision, arithmetic) and keep the
                                       * fastest; 0 (default): occupancy-based choice. Results do not depend
                                       * on the launch shape beyond FP64 rounding of the product trees. */
+#define NQES_OPT_TENSOR_CORES 8      /* 1 (default): in the MIXED form, the rows pass of the factored S·v
+                                      * runs on the tensor cores (tcgen05, B split into three BF16 terms,
+                                      * FP32 accumulation) where the shape allows (N <= 143, M <= 255);
+                                      * 0: FP32 CUDA cores. Both agree to FP32 rounding. */
 #define NQES_OPT_MIXED_EXACT 6       /* 1: MIXED takes every accept decision by its exact FP64 path
                                       * (verification of that path); 0 (default): only when the FP32
                                       * bound cannot decide. */
@@ -199,7 +203,8 @@ int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int chains, in
  * member's step (sampling segment, MINRES-QLP while loop, update) is an
  * independent branch of the graph, so solves of different shapes overlap on
  * the GPU. Each member's results are exactly those of nqes_sr_step on it.
- * Members stay owned by the caller, live on one device, may differ in N, M,
+ * Members stay owned by the caller and must outlive the batch (a graph
+ * captured for a member keeps its device buffers), live on one device, may differ in N, M,
  * K, J, h and precision, and may also be stepped on their own; the batch
  * re-captures its graph when a member's step shape changes. Errors are
  * described by nqes_batch_last_error (NULL: the last failed create). */

@@ -20,8 +20,8 @@ OBJDIR = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_sample_warp.cu", "kernels_sample_warp_k34.cu",
-           "kernels_solve.cu", "kernels_factored.cu", "nqes_api.cu", "sv_static.cu", "nqes_server.cc"]
-HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h", "tma_stage.cuh", "sample_warp.cuh"]
+           "kernels_solve.cu", "kernels_factored.cu", "kernels_factored_tc.cu", "nqes_api.cu", "sv_static.cu", "nqes_server.cc"]
+HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h", "tma_stage.cuh", "sample_warp.cuh", "tc_util.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

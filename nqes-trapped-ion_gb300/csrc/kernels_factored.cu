@@ -423,7 +423,7 @@ cudaError_t rows_launch(FactArgs F, const float *v, float *u, cudaStream_t st, b
     F.ic = std::max(1, std::min(F.N, (48 * 1024 / 4) / WS));
     const size_t smem = (size_t(F.ic) * WS + ((F.N + 3) & ~3) + WS + NG * RB) * sizeof(float);
     if (prepare)
-        return cudaFuncSetAttribute(k_frows<JT, JB, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_frows<JT, JB, RB>));
     const int spb = (NG * RB) / F.K;
     const int blocks = (F.Ns + spb - 1) / spb;
     k_frows<JT, JB, RB><<<blocks, kThreads, smem, st>>>(F, v, u);
@@ -447,7 +447,7 @@ template <int IB, int JB>
 cudaError_t cols_launch(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, cudaStream_t st,
                         bool prepare) {
     constexpr size_t smem = cols_smem<IB, JB>();
-    if (prepare) return cudaFuncSetAttribute(k_fcols<IB, JB>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (prepare) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_fcols<IB, JB>));
     dim3 g(F.rchunks, F.K, (F.N + kGroups * IB - 1) / (kGroups * IB));
     k_fcols<IB, JB><<<g, kThreads, smem, st>>>(F, mode, w, E, out);
     return cudaGetLastError();
@@ -482,10 +482,12 @@ cudaError_t cols_dispatch(const FactArgs &F, int mode, const float *w, const cpl
 cudaError_t prepare_frows(const FactArgs &F) {
     cudaError_t e = rows_dispatch(F, nullptr, nullptr, nullptr, true);
     if (e == cudaSuccess) e = cols_dispatch(F, 0, nullptr, nullptr, nullptr, nullptr, true);
+    if (e == cudaSuccess) e = prepare_frows_tc(F);
     return e;
 }
 
 cudaError_t launch_frows(const FactArgs &F, const float *v, float *u, cudaStream_t st) {
+    if (F.tc) return launch_frows_tc(F, v, u, F.err, st);
     return rows_dispatch(F, v, u, st, false);
 }
 

@@ -703,23 +703,22 @@ size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith) {
 
 int sample_threads(int K, int tk) { return K * tk; }
 
-// Sets the sampler's dynamic shared-memory limit; call outside stream capture.
-template <class S, bool FILT> cudaError_t prepare_variants(int smem) {
-    cudaError_t e = cudaFuncSetAttribute(k_sample<S, 1, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+// Raises the sampler's dynamic shared-memory limit; call outside stream capture.
+template <class S, bool FILT> cudaError_t prepare_variants() {
+    cudaError_t e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 1, FILT>));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_sample<S, 2, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 2, FILT>));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_sample<S, 4, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 4, FILT>));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_sample<S, 8, FILT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 8, FILT>));
     return e;
 }
 
-template <class S> cudaError_t prepare_sample(const Shape &sh) {
-    const int smem = int(smem_bytes(sh.N, sh.M, sh.K, sizeof(S)));
-    cudaError_t e = prepare_variants<S, false>(smem);
+template <class S> cudaError_t prepare_sample(const Shape &) {
+    cudaError_t e = prepare_variants<S, false>();
     if constexpr (std::is_same<S, double>::value)
-        if (e == cudaSuccess) e = prepare_variants<S, true>(smem);
+        if (e == cudaSuccess) e = prepare_variants<S, true>();
     return e;
 }
 

@@ -508,12 +508,11 @@ __global__ void k_tables_mixed(Shape sh, const cplx *a, const cplx *b, const cpl
 
 size_t mixed_smem_bytes(const Shape &sh) { return msmem_bytes(sh.N, sh.M, sh.K); }
 
-cudaError_t prepare_sample_mixed(const Shape &sh) {
-    const int smem = int(msmem_bytes(sh.N, sh.M, sh.K));
-    cudaError_t e = cudaFuncSetAttribute(k_sample_mixed<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample_mixed<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample_mixed<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_sample_mixed<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+cudaError_t prepare_sample_mixed(const Shape &) {
+    cudaError_t e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample_mixed<1>));
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample_mixed<2>));
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample_mixed<4>));
+    if (e == cudaSuccess) e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample_mixed<8>));
     return e;
 }
 

@@ -49,10 +49,7 @@ cudaError_t prepare_sample_dw(const Shape &sh, int MP) {
     int G = 0;
     const DwKernel fn = dw_kernel(sh.K, dw_units(sh, &G));
     if (!fn || G * dw_units(sh, nullptr) != MP) return cudaErrorInvalidConfiguration;
-    const size_t staged = dsmem_bytes(sh.N, MP, sh.K, true);
-    const size_t smem = staged <= 227 * 1024 ? staged : dsmem_bytes(sh.N, MP, sh.K, false);
-    return cudaFuncSetAttribute(reinterpret_cast<const void *>(fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(smem));
+    return allow_max_dynamic_smem(reinterpret_cast<const void *>(fn));
 }
 
 cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm) {

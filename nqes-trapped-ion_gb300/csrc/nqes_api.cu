@@ -40,6 +40,8 @@ struct nqes_ctx {
     float *dcp = nullptr, *dsp = nullptr, *dwh = nullptr, *dwl = nullptr, *dbh = nullptr, *dbl = nullptr;
     float *dbnd = nullptr;  // K·N float4 bound records, then K row-sum maxima
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
+    uint16_t *tcimg = nullptr;  // BF16 split image of v for the tensor-core rows pass
+    bool tensor_cores = false;  // NQES_OPT_TENSOR_CORES
     int step_precision = NQES_PRECISION_FP64;      // precision of the allocated step buffers
     int tk_opt = 0;
     uint64_t minres_cap = 100000;
@@ -128,6 +130,7 @@ void free_step_buffers(nqes_ctx *ctx) {
     dfree(ctx->v32);
     dfree(ctx->u32);
     dfree(ctx->ypart32);
+    dfree(ctx->tcimg);
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
     ctx->exec = nullptr;
     ctx->g_chains = -1;
@@ -158,6 +161,11 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
             (rc = dalloc(ctx, &ctx->exact, size_t(chains))) || (rc = dalloc(ctx, &ctx->v32, P)) ||
             (rc = dalloc(ctx, &ctx->u32, Ns)) || (rc = dalloc(ctx, &ctx->ypart32, 3 * size_t(ctx->rchunks) * P)))
             return rc;
+        FactArgs F{};
+        F.N = sh.N;
+        F.M = sh.M;
+        F.K = sh.K;
+        if ((rc = dalloc(ctx, &ctx->tcimg, rows_tc_image_elems(F)))) return rc;
     } else if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * ss))) {
         return rc;
     }
@@ -193,6 +201,9 @@ FactArgs fact_args(nqes_ctx *ctx) {
     F.T = static_cast<const float *>(ctx->O);
     F.B = F.T + ctx->Ns * size_t(F.K) * F.K * F.MT;
     F.spins = ctx->spins;
+    F.tcimg = ctx->tcimg;
+    F.err = ctx->err_d;
+    F.tc = ctx->tensor_cores && ctx->tcimg && rows_tc_fits(F);
     return F;
 }
 
@@ -881,6 +892,17 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         std::fill(ctx->tune_key, ctx->tune_key + 5, -1LL);
         ctx->tk_tuned = ctx->dw_force_warps = ctx->dw_force_stage = 0;
         if (ctx->exec) {
+            cudaGraphExecDestroy(ctx->exec);
+            ctx->exec = nullptr;
+        }
+        return NQES_OK;
+    case NQES_OPT_TENSOR_CORES:
+        if (value != 0 && value != 1) {
+            ctx->err = "option value must be 0 or 1";
+            return NQES_ERR_INVALID;
+        }
+        ctx->tensor_cores = value == 1;
+        if (ctx->exec) {  // the captured step bakes the S·v kernels in
             cudaGraphExecDestroy(ctx->exec);
             ctx->exec = nullptr;
         }

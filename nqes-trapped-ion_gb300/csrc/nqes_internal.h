@@ -152,8 +152,30 @@ struct FactArgs {
     int ic;  // rows of W staged per chunk by the rows pass (set at launch)
     const float *T, *B;
     const uint64_t *spins;
+    int tc;            // rows pass on the tensor cores (kernels_factored_tc.cu)
+    uint16_t *tcimg;   // its BF16 split image of the parameter vector
+    int *err;
 };
 __host__ __device__ inline int fact_mt(int M) { return (M + 3) & ~3; }
+
+// Lets kernel `fn` take as much dynamic shared memory as the device allows.
+// The limit is a per-kernel global: set to one context's need, it would cap
+// the same kernel launched (or replayed from a captured graph) by a context of
+// a larger shape, so it is only ever raised, to the device maximum.
+inline cudaError_t allow_max_dynamic_smem(const void *fn) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fn);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - int(fa.sharedSizeBytes));
+    return e;
+}
+bool rows_tc_fits(const FactArgs &F);
+size_t rows_tc_image_elems(const FactArgs &F);
+cudaError_t prepare_frows_tc(const FactArgs &F);
+cudaError_t launch_frows_tc(const FactArgs &F, const float *v, float *u, int *err, cudaStream_t st);
 cudaError_t prepare_frows(const FactArgs &F);
 cudaError_t launch_frows(const FactArgs &F, const float *v, float *u, cudaStream_t st);
 cudaError_t launch_fcols(const FactArgs &F, const float *w, float *ypart, cudaStream_t st);

@@ -64,7 +64,9 @@ struct nqes_server {
     bool stop = false;
     std::thread worker;
     nqes_batch *batch = nullptr;
-    std::vector<nqes_ctx *> batch_members;
+    // the batch's members by solve id: a retired solve's context is freed and a
+    // new context may reuse its address, so pointers cannot tell batches apart
+    std::vector<uint64_t> batch_members;
     std::string err;
 };
 
@@ -155,9 +157,13 @@ void worker_loop(nqes_server *srv) {
         // one batched step over the active solves
         const auto c1 = Clock::now();
         std::vector<nqes_ctx *> members;
-        for (Solve *s : srv->active) members.push_back(s->ctx);
+        std::vector<uint64_t> ids;
+        for (Solve *s : srv->active) {
+            members.push_back(s->ctx);
+            ids.push_back(s->id);
+        }
         bool rebuilt = false;
-        if (!srv->batch || members != srv->batch_members) {
+        if (!srv->batch || ids != srv->batch_members) {
             rebuilt = true;
             if (srv->batch) nqes_batch_destroy(srv->batch);
             srv->batch = nullptr;
@@ -166,7 +172,7 @@ void worker_loop(nqes_server *srv) {
                 srv->active.clear();
                 continue;
             }
-            srv->batch_members = members;
+            srv->batch_members = ids;
         }
         const size_t n = srv->active.size();
         std::vector<uint64_t> seeds(n), maxit(n);

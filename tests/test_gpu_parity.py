@@ -266,3 +266,31 @@ def test_mixed_exact_path_keeps_fp64_chains(pkg, N, M, K, chains, m):
             assert info["exact_decisions"] > 0
         ctx.close()
     assert np.array_equal(spins[0], spins[1])
+
+
+@pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 32, 20), (12, 24, 3, 8, 20),
+                                            (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (10, 300, 4, 4, 6)])
+def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
+    """MIXED: the tcgen05 rows pass (BF16 x3 splits, FP32 accumulation) and the
+    FP32 CUDA-core rows pass give the same S·v to FP32 rounding, the same chains
+    and energies, and updated weights within the solve's FP32 sensitivity
+    (M = 300 exceeds the tensor-core shape and runs on the CUDA cores either way)."""
+    J = synthetic_j(N)
+    w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 11 + N, real=True)
+    P = K * (N + M + N * M)
+    vrand = np.random.default_rng(3 * N + M).normal(size=P).astype(np.complex128)
+    out = []
+    for tc in (0, 1):
+        ctx = pkg.Context(N, M, K, J, 0.595)
+        ctx.set_weights(*w)
+        ctx.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+        ctx.set_option(pkg.OPT_TENSOR_CORES, tc)
+        e, info = ctx.sr_step(99, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
+        out.append(dict(e=e, spins=ctx.get_samples()[0], sv=ctx.apply_S(vrand),
+                        w=np.concatenate([x.ravel() for x in ctx.get_weights()])))
+        ctx.close()
+    a, b = out
+    assert np.array_equal(a["spins"], b["spins"])
+    assert rel_err(b["sv"], a["sv"]) < 1e-5
+    assert rel_err(b["e"], a["e"]) < 1e-6
+    assert rel_err(b["w"], a["w"]) < (5e-5 if P < 10000 else 2e-4)

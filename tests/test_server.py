@@ -93,3 +93,31 @@ def test_admission_waits_for_memory(pkg):
     assert sorted(r["id"] for r in res) == sorted(ids)
     assert all(r["status"] == 0 for r in res)
     assert max(r["t_queued"] for r in res) > 0.0
+
+
+@pytest.mark.gpu
+def test_turnover_rebuilds_the_batch(pkg):
+    """One active solve at a time, one step each, alternating shapes: every
+    retirement is followed by an admission whose context may reuse the retired
+    one's address; each solve still gets its own batch and the results of
+    running it alone."""
+    specs = [dict(SPECS[i % 2], seed=101 + i) for i in range(6)]
+
+    def run(srv, ss):
+        ids = []
+        for s in ss:
+            w = helpers.random_weights(s["n"], s["m"], s["k"], 0.05, s["seed"], real=True)
+            ids.append(srv.submit(s["n"], s["m"], s["k"], synthetic_j(s["n"]), weights=w, h=s["h"], seed=s["seed"],
+                                  chains=16, samples_per_chain=20, burn_in=5, reglam0=5.0, tol=1e-12, max_steps=1,
+                                  precision=s["prec"]))
+        return ids, {r["id"]: r for r in srv.wait_all(len(ss))}
+
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=1)
+    ids, res = run(srv, specs)
+    srv.close()
+    for rid, s in zip(ids, specs):
+        alone = pkg.Server(hbm_budget_bytes=1 << 36, max_active=1)
+        (aid,), ares = run(alone, [s])
+        alone.close()
+        assert res[rid]["status"] == 0 and ares[aid]["status"] == 0
+        assert res[rid]["energies"] == ares[aid]["energies"]
