@@ -274,7 +274,8 @@ def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
     """MIXED: the tcgen05 rows pass (BF16 x3 splits, FP32 accumulation) and the
     FP32 CUDA-core rows pass give the same S·v to FP32 rounding, the same chains
     and energies, and updated weights within the solve's FP32 sensitivity
-    (M = 300 exceeds the tensor-core shape and runs on the CUDA cores either way)."""
+    (M = 300 exceeds the tensor-core shape and N M < 4096 stays on the CUDA
+    cores, so those cases check that the option changes nothing there)."""
     J = synthetic_j(N)
     w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 11 + N, real=True)
     P = K * (N + M + N * M)
