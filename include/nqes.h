@@ -62,8 +62,8 @@ extern "C" {
 #define NQES_OPT_TENSOR_CORES 8      /* 1 (default): in the MIXED form, the rows pass of the factored S·v
                                       * runs on the tensor cores (tcgen05, B split into three BF16 terms,
                                       * FP32 accumulation) where the shape allows (N <= 143, M <= 255) and
-                                      * pays off (N M >= 4096); 0: FP32 CUDA cores. Both agree to FP32
-                                      * rounding. */
+                                      * pays off (N M >= 4096); 2: wherever the shape allows; 0: FP32
+                                      * CUDA cores. All agree to FP32 rounding. */
 #define NQES_OPT_MIXED_EXACT 6       /* 1: MIXED takes every accept decision by its exact FP64 path
                                       * (verification of that path); 0 (default): only when the FP32
                                       * bound cannot decide. */

@@ -41,7 +41,7 @@ struct nqes_ctx {
     float *dbnd = nullptr;  // K·N float4 bound records, then K row-sum maxima
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
     uint16_t *tcimg = nullptr;  // BF16 split image of v for the tensor-core rows pass
-    bool tensor_cores = true;   // NQES_OPT_TENSOR_CORES
+    int tensor_cores = 1;       // NQES_OPT_TENSOR_CORES: 0 off, 1 where it pays off, 2 wherever it fits
     int step_precision = NQES_PRECISION_FP64;      // precision of the allocated step buffers
     int tk_opt = 0;
     uint64_t minres_cap = 100000;
@@ -205,7 +205,7 @@ FactArgs fact_args(nqes_ctx *ctx) {
     F.err = ctx->err_d;
     // the tensor-core rows pass pays off from N M = 4096 (N64 M128 K4: 1.15 -> 0.88 ms
     // per pass at 2048 x 64 samples; N32 M64 K2 stays faster on the CUDA cores)
-    F.tc = ctx->tensor_cores && ctx->tcimg && rows_tc_fits(F) && F.N * F.M >= 4096;
+    F.tc = ctx->tensor_cores && ctx->tcimg && rows_tc_fits(F) && (ctx->tensor_cores == 2 || F.N * F.M >= 4096);
     return F;
 }
 
@@ -899,11 +899,11 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         }
         return NQES_OK;
     case NQES_OPT_TENSOR_CORES:
-        if (value != 0 && value != 1) {
-            ctx->err = "option value must be 0 or 1";
+        if (value < 0 || value > 2) {
+            ctx->err = "option value must be 0, 1 or 2";
             return NQES_ERR_INVALID;
         }
-        ctx->tensor_cores = value == 1;
+        ctx->tensor_cores = int(value);
         if (ctx->exec) {  // the captured step bakes the S·v kernels in
             cudaGraphExecDestroy(ctx->exec);
             ctx->exec = nullptr;

@@ -269,13 +269,15 @@ def test_mixed_exact_path_keeps_fp64_chains(pkg, N, M, K, chains, m):
 
 
 @pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 32, 20), (12, 24, 3, 8, 20),
-                                            (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (10, 300, 4, 4, 6)])
+                                            (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (70, 45, 3, 8, 10),
+                                            (100, 200, 2, 4, 8), (10, 300, 4, 4, 6)])
 def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
     """MIXED: the tcgen05 rows pass (BF16 x3 splits, FP32 accumulation) and the
     FP32 CUDA-core rows pass give the same S·v to FP32 rounding, the same chains
     and energies, and updated weights within the solve's FP32 sensitivity
-    (M = 300 exceeds the tensor-core shape and N M < 4096 stays on the CUDA
-    cores, so those cases check that the option changes nothing there)."""
+    (forced on wherever the shape fits: K = 1..4, N > 64, M not a multiple of
+    16; M = 300 exceeds the tensor-core shape and checks that the option
+    changes nothing there)."""
     J = synthetic_j(N)
     w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 11 + N, real=True)
     P = K * (N + M + N * M)
@@ -285,7 +287,7 @@ def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
         ctx = pkg.Context(N, M, K, J, 0.595)
         ctx.set_weights(*w)
         ctx.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
-        ctx.set_option(pkg.OPT_TENSOR_CORES, tc)
+        ctx.set_option(pkg.OPT_TENSOR_CORES, 2 * tc)
         e, info = ctx.sr_step(99, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
         out.append(dict(e=e, spins=ctx.get_samples()[0], sv=ctx.apply_S(vrand),
                         w=np.concatenate([x.ravel() for x in ctx.get_weights()])))
