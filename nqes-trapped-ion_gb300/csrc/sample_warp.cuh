@@ -154,25 +154,33 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
     const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, MP = A.MP;
     const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const uint64_t *sk = sm.spin + k * NW;
-    for (int idx = tid; idx < K * MP; idx += T) {
-        const int kk = idx / MP, j = idx - kk * MP, q = k * K + kk;
-        float h = 0.f, l = 0.f, t = 0.f;
-        if (j < M) {
-            h = A.bh[kk * MP + j];
-            l = A.bl[kk * MP + j];
-            for (int i = 0; i < N; i++) {
-                const size_t o = (size_t(kk) * N + i) * MP + j;
-                const float wh = sm.twh[o], wl = sm.twl[o];
-                if (down_bit(sk, i))
-                    df_add(h, l, -wh, -wl);
-                else
-                    df_add(h, l, wh, wl);
-            }
-            t = tanhf(h);
+    // four adjacent hidden units per thread (MP is a multiple of 8): one float4
+    // of each table per spin and four independent double-float chains, so a
+    // thread has four loads and sums in flight instead of one
+    for (int qd = tid; qd < K * MP / 4; qd += T) {
+        const int j0 = qd * 4 - (qd * 4 / MP) * MP, kk = qd * 4 / MP, q = k * K + kk;
+        const float4 bh4 = *reinterpret_cast<const float4 *>(A.bh + kk * MP + j0);
+        const float4 bl4 = *reinterpret_cast<const float4 *>(A.bl + kk * MP + j0);
+        float h[4] = {bh4.x, bh4.y, bh4.z, bh4.w}, l[4] = {bl4.x, bl4.y, bl4.z, bl4.w};
+#pragma unroll 2
+        for (int i = 0; i < N; i++) {
+            const size_t o = (size_t(kk) * N + i) * MP + j0;
+            const float4 wh = *reinterpret_cast<const float4 *>(sm.twh + o);
+            const float4 wl = *reinterpret_cast<const float4 *>(sm.twl + o);
+            const bool dn = down_bit(sk, i);
+            df_add(h[0], l[0], dn ? -wh.x : wh.x, dn ? -wl.x : wl.x);
+            df_add(h[1], l[1], dn ? -wh.y : wh.y, dn ? -wl.y : wl.y);
+            df_add(h[2], l[2], dn ? -wh.z : wh.z, dn ? -wl.z : wl.z);
+            df_add(h[3], l[3], dn ? -wh.w : wh.w, dn ? -wl.w : wl.w);
         }
-        sm.th_hi[q * MP + j] = h;
-        sm.th_lo[q * MP + j] = l;
-        sm.t[q * MP + j] = t;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int j = j0 + e;
+            const bool in = j < M;
+            sm.th_hi[q * MP + j] = in ? h[e] : 0.f;
+            sm.th_lo[q * MP + j] = in ? l[e] : 0.f;
+            sm.t[q * MP + j] = in ? tanhf(h[e]) : 0.f;
+        }
     }
     __syncthreads();
     // partial sums of A and products P over slots (kk, part): every warp takes
