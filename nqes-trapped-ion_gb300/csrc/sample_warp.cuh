@@ -288,7 +288,12 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
     // other rows are exact), the row's entries, g, det and 1/det with the
     // error bounds of the model above.
     double cofd[K], cabsd[K];
-    float phik[K], g[K], ga[K], Et[K], Eacc[K], Fq[K], Am[K];
+    float phik[K], g[K], ga[K], Et[K], Eacc[K], Fq[K], Am[K], Qs[K];
+    // third tanh bound for the wider shapes: the amplification from step s to
+    // now is at most cosh^2 theta_s = 1 / (1 - T_s^2) <= 1 / (1 - M_s^2), M_s the
+    // RBM's largest |tanh| after step s (plus its error), so E_t <= F Qs with
+    // Qs = sum_s eps_s / (1 - M_s^2); one group max per accepted flip
+    constexpr bool kTmax = U * K >= 16;
     float det32, rdet, edet, gsum, gasum, dr;
     auto exact_state = [&](const double *pp, double det) {
         double perm = 0.0;
@@ -333,6 +338,7 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
             const float tk = __shfl_sync(0xffffffffu, tm, kk * G) + 6.f * kU;
             const float ch = coshf(fmaf(atanhf(tk), 1.f + 8.f * kU, __ldg(A.bnd + 4 * K * N + kk)));
             Am[kk] = tk < 0.9999f ? ch * ch * (1.f + 1e-5f) : INFINITY;
+            Qs[kk] = tk < 0.9999f ? 5.f * kU * (1.f + 16.f * kU) * __frcp_ru((1.f - tk) * (1.f + tk)) : INFINITY;
         }
     }
     bool changed = false;
@@ -356,13 +362,21 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
         const uint64_t draw = pcg_next(rng);
         const float u32 = __ull2float_rn(draw) * 0x1p-64f;
 
-        // factors f = c - sigma t s and their product within the lane's group
-        float f[U], prod = 1.f;
+        // factors f = c - sigma t s and their product within the lane's group,
+        // as up to four interleaved partial products (a shorter dependent chain;
+        // the same number of roundings, so beta still bounds it)
+        constexpr int NPP = U < 4 ? U : 4;
+        float f[U], pp[NPP];
+#pragma unroll
+        for (int e = 0; e < NPP; e++) pp[e] = 1.f;
 #pragma unroll
         for (int u = 0; u < U; u++) {
             f[u] = fmaf(down ? t[u] : -t[u], sq[u], cq[u]);
-            if (live[u]) prod *= f[u];
+            if (live[u]) pp[u % NPP] *= f[u];
         }
+        float prod = pp[0];
+#pragma unroll
+        for (int e = 1; e < NPP; e++) prod *= pp[e];
 #pragma unroll
         for (int o = G >> 1; o > 0; o >>= 1) prod *= __shfl_xor_sync(0xffffffffu, prod, o);
         float x[K], re[K], beta[K], s = 0.f, sax = 0.f, bmax = 0.f;
@@ -400,29 +414,59 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                 exact_path = true;  // NaN lands here as well
         }
         if (exact_path) {
-            // Row k current and proposed, in FP64: theta of the lane's units from
-            // the spins (double-float sums of b and +-w), then the log cosh sums.
+            // Row k current and proposed, in FP64. theta of the lane's units is
+            // the row's start value (double-float, left in shared memory by the
+            // last rebuild of this row) plus 2 sigma w for each spin flipped
+            // since (a spin flips at most once per row), four units at a time;
+            // then the log cosh sums.
             double lin = 0.0, pr = 1.0, lin2 = 0.0, pr2 = 1.0;
+            const uint64_t fl0 = sk0 ^ sm.spin[k * NW], fl1 = NW > 1 ? (sk1 ^ sm.spin[k * NW + 1]) : 0ULL;
+            constexpr int UC = U < 4 ? U : 4;
+#pragma unroll 1
+            for (int u0 = 0; u0 < U; u0 += UC) {
+                float h[UC], l[UC];
 #pragma unroll
-            for (int u = 0; u < U; u++) {
-                if (live[u]) {
-                    const int j = base + u;
-                    float h = A.bh[kkl * MP + j], l = A.bl[kkl * MP + j];
-                    for (int i2 = 0; i2 < N; i2++) {
-                        const size_t o = (size_t(kkl) * N + i2) * MP + j;
-                        const float wh = sm.twh[o], wl = sm.twl[o];
-                        if (bit(i2))
-                            df_add(h, l, -wh, -wl);
-                        else
-                            df_add(h, l, wh, wl);
+                for (int e = 0; e < UC; e++) {
+                    h[e] = sm.th_hi[q * MP + base + u0 + e];
+                    l[e] = sm.th_lo[q * MP + base + u0 + e];
+                }
+#pragma unroll 1
+                for (int half = 0; half < 2; half++) {
+                    uint64_t f = half ? fl1 : fl0;
+                    while (f) {
+                        const int i2 = __ffsll(static_cast<long long>(f)) - 1 + 64 * half;
+                        f &= f - 1;
+                        const size_t o = (size_t(kkl) * N + i2) * MP + base + u0;
+                        const float sg = bit(i2) ? -2.f : 2.f;  // sigma now - sigma at the row start
+                        float wh[UC], wl[UC];
+                        if constexpr (UC == 4) {
+                            const float4 a4 = *reinterpret_cast<const float4 *>(sm.twh + o);
+                            const float4 b4 = *reinterpret_cast<const float4 *>(sm.twl + o);
+                            wh[0] = a4.x; wh[1] = a4.y; wh[2] = a4.z; wh[3] = a4.w;
+                            wl[0] = b4.x; wl[1] = b4.y; wl[2] = b4.z; wl[3] = b4.w;
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < UC; e++) {
+                                wh[e] = sm.twh[o + e];
+                                wl[e] = sm.twl[o + e];
+                            }
+                        }
+#pragma unroll
+                        for (int e = 0; e < UC; e++) df_add(h[e], l[e], sg * wh[e], sg * wl[e]);
                     }
-                    const double tt = double(h) + double(l);
-                    const double w = A.w64[(size_t(kkl) * N + i) * M + j];
-                    const double t2 = down ? tt + 2.0 * w : tt - 2.0 * w;
-                    lin += fabs(tt);
-                    pr *= 1.0 + exp(-2.0 * fabs(tt));
-                    lin2 += fabs(t2);
-                    pr2 *= 1.0 + exp(-2.0 * fabs(t2));
+                }
+#pragma unroll
+                for (int e = 0; e < UC; e++) {
+                    const int j = base + u0 + e;
+                    if (active && j < M) {
+                        const double tt = double(h[e]) + double(l[e]);
+                        const double w = A.w64[(size_t(kkl) * N + i) * M + j];
+                        const double t2 = down ? tt + 2.0 * w : tt - 2.0 * w;
+                        lin += fabs(tt);
+                        pr *= 1.0 + exp(-2.0 * fabs(tt));
+                        lin2 += fabs(t2);
+                        pr2 *= 1.0 + exp(-2.0 * fabs(t2));
+                    }
                 }
             }
 #pragma unroll
@@ -487,12 +531,28 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
             // tanh' = (t c - sigma s) / f (code/rbm.cc:185) in FP32, and its bound
 #pragma unroll
             for (int u = 0; u < U; u++) t[u] = __fdividef(fmaf(t[u], cq[u], down ? sq[u] : -sq[u]), f[u]);
+            float tmx = 0.f;
+            if constexpr (kTmax) {
+#pragma unroll
+                for (int u = 0; u < U; u++)
+                    if (live[u]) tmx = fmaxf(tmx, fabsf(t[u]));
+#pragma unroll
+                for (int o = G >> 1; o > 0; o >>= 1) tmx = fmaxf(tmx, __shfl_xor_sync(0xffffffffu, tmx, o));
+            }
 #pragma unroll
             for (int kk = 0; kk < K; kk++) {
                 Eacc[kk] += bd[kk].w;
                 Fq[kk] *= fmaf(1.025f * Et[kk], bd[kk].z - 1.f, 1.f + 2.f * kU);
                 const float tel = Am[kk] * Fq[kk] * Eacc[kk] * (1.f + 16.f * kU);
-                Et[kk] = fminf(tel, fmaf(Et[kk] * (1.f + 4.f * kU), bd[kk].z, bd[kk].w));
+                const float stp = fmaf(Et[kk] * (1.f + 4.f * kU), bd[kk].z, bd[kk].w);
+                float e = fminf(tel, stp);
+                if constexpr (kTmax) {
+                    const float Mk = __shfl_sync(0xffffffffu, tmx, kk * G) + stp + 2.f * kU;
+                    Qs[kk] = Mk < 0.9999f ? fmaf(bd[kk].w * (1.f + 16.f * kU), __frcp_ru((1.f - Mk) * (1.f + Mk)), Qs[kk])
+                                          : INFINITY;
+                    e = fminf(e, Fq[kk] * Qs[kk] * (1.f + 16.f * kU));
+                }
+                Et[kk] = e;
             }
             if (!exact_path) {
                 // row k times r e^{-2 sigma a}: g_kk becomes x_kk (cofactors exclude row k)
