@@ -483,6 +483,7 @@ cudaError_t prepare_frows(const FactArgs &F) {
     cudaError_t e = rows_dispatch(F, nullptr, nullptr, nullptr, true);
     if (e == cudaSuccess) e = cols_dispatch(F, 0, nullptr, nullptr, nullptr, nullptr, true);
     if (e == cudaSuccess) e = prepare_frows_tc(F);
+    if (e == cudaSuccess) e = prepare_fcols_tc();
     return e;
 }
 
@@ -492,13 +493,17 @@ cudaError_t launch_frows(const FactArgs &F, const float *v, float *u, cudaStream
 }
 
 cudaError_t launch_fcols(const FactArgs &F, const float *w, float *ypart, cudaStream_t st) {
+    if (F.tcc) return launch_fcols_tc(F, 0, w, nullptr, ypart, F.err, st);
     return cols_dispatch(F, 0, w, nullptr, ypart, st);
 }
 
 cudaError_t launch_fmoments(const FactArgs &F, const cplx *E, float *po, float *pf, float *ps2, cudaStream_t st) {
-    cudaError_t e = cols_dispatch(F, 1, nullptr, nullptr, po, st);
-    if (e == cudaSuccess) e = cols_dispatch(F, 2, nullptr, E, pf, st);
-    if (e == cudaSuccess) e = cols_dispatch(F, 3, nullptr, nullptr, ps2, st);
+    auto one = [&](int mode, const cplx *e, float *out) {
+        return F.tcc ? launch_fcols_tc(F, mode, nullptr, e, out, F.err, st) : cols_dispatch(F, mode, nullptr, e, out, st);
+    };
+    cudaError_t e = one(1, nullptr, po);
+    if (e == cudaSuccess) e = one(2, E, pf);
+    if (e == cudaSuccess) e = one(3, nullptr, ps2);
     return e;
 }
 

@@ -206,6 +206,7 @@ FactArgs fact_args(nqes_ctx *ctx) {
     // the tensor-core rows pass pays off from N M = 4096 (N64 M128 K4: 1.15 -> 0.88 ms
     // per pass at 2048 x 64 samples; N32 M64 K2 stays faster on the CUDA cores)
     F.tc = ctx->tensor_cores && ctx->tcimg && rows_tc_fits(F) && (ctx->tensor_cores == 2 || F.N * F.M >= 4096);
+    F.tcc = ctx->tensor_cores == 2 && cols_tc_fits(F);
     return F;
 }
 

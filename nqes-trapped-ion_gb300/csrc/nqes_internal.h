@@ -153,6 +153,7 @@ struct FactArgs {
     const float *T, *B;
     const uint64_t *spins;
     int tc;            // rows pass on the tensor cores (kernels_factored_tc.cu)
+    int tcc;           // column passes (S·v and moments) on the tensor cores
     uint16_t *tcimg;   // its BF16 split image of the parameter vector
     int *err;
 };
@@ -176,6 +177,10 @@ bool rows_tc_fits(const FactArgs &F);
 size_t rows_tc_image_elems(const FactArgs &F);
 cudaError_t prepare_frows_tc(const FactArgs &F);
 cudaError_t launch_frows_tc(const FactArgs &F, const float *v, float *u, int *err, cudaStream_t st);
+bool cols_tc_fits(const FactArgs &F);
+cudaError_t prepare_fcols_tc();
+cudaError_t launch_fcols_tc(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, int *err,
+                            cudaStream_t st);
 cudaError_t prepare_frows(const FactArgs &F);
 cudaError_t launch_frows(const FactArgs &F, const float *v, float *u, cudaStream_t st);
 cudaError_t launch_fcols(const FactArgs &F, const float *w, float *ypart, cudaStream_t st);

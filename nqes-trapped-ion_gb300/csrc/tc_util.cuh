@@ -99,6 +99,18 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int q = 0; q < 16; q++) v[q] = __uint_as_float(r[q]);
 }
 
+// x = hi + mid + lo exactly, each a BF16 (truncation keeps 8 significant bits
+// per term: 24 in all, the whole FP32 significand). Returned as BF16 bits.
+__device__ __forceinline__ void bf16_split3_trunc(float x, uint32_t &hi, uint32_t &mid, uint32_t &lo) {
+    const uint32_t b = __float_as_uint(x) & 0xFFFF0000u;
+    const float r1 = x - __uint_as_float(b);
+    const uint32_t m = __float_as_uint(r1) & 0xFFFF0000u;
+    const float r2 = r1 - __uint_as_float(m);
+    hi = b >> 16;
+    mid = m >> 16;
+    lo = __float_as_uint(r2) >> 16;
+}
+
 // Round-to-nearest bf16 of x and the remainder x - bf16(x) (exact in FP32).
 __device__ __forceinline__ uint16_t bf16_split(float x, float &rest) {
     const uint32_t b = __float_as_uint(x);

@@ -272,8 +272,9 @@ def test_mixed_exact_path_keeps_fp64_chains(pkg, N, M, K, chains, m):
                                             (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (70, 45, 3, 8, 10),
                                             (100, 200, 2, 4, 8), (10, 300, 4, 4, 6)])
 def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
-    """MIXED: the tcgen05 rows pass (BF16 x3 splits, FP32 accumulation) and the
-    FP32 CUDA-core rows pass give the same S·v to FP32 rounding, the same chains
+    """MIXED: the tcgen05 rows and column passes (BF16 x3 splits, FP32
+    accumulation) and the FP32 CUDA-core passes give the same S·v and moments
+    to FP32 rounding, the same chains
     and energies, and updated weights within the solve's FP32 sensitivity
     (forced on wherever the shape fits: K = 1..4, N > 64, M not a multiple of
     16; M = 300 exceeds the tensor-core shape and checks that the option
@@ -289,11 +290,13 @@ def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
         ctx.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
         ctx.set_option(pkg.OPT_TENSOR_CORES, 2 * tc)
         e, info = ctx.sr_step(99, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
-        out.append(dict(e=e, spins=ctx.get_samples()[0], sv=ctx.apply_S(vrand),
+        out.append(dict(e=e, spins=ctx.get_samples()[0], sv=ctx.apply_S(vrand), mom=ctx.get_moments(),
                         w=np.concatenate([x.ravel() for x in ctx.get_weights()])))
         ctx.close()
     a, b = out
     assert np.array_equal(a["spins"], b["spins"])
     assert rel_err(b["sv"], a["sv"]) < 1e-5
+    for x, y in zip(b["mom"], a["mom"]):  # o, lambda-scaled diagonal of S, force
+        assert rel_err(x, y) < 1e-5
     assert rel_err(b["e"], a["e"]) < 1e-6
     assert rel_err(b["w"], a["w"]) < (5e-5 if P < 10000 else 2e-4)
