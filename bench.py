@@ -529,6 +529,28 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def kernel_case(spec):
+    """One mixed SR step of shape "N,M,K,chains,samples" (seeded synthetic
+    weights, h = 0.7, lambda 40), then each kernel of the step timed on its own
+    through nqes_time_kernel (the launches a profiler can attribute; the step's
+    own kernels run inside a CUDA graph with a conditional node)."""
+    import torch  # noqa: F401  (initialises the device as the other legs do)
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    n, m, k, chains, samples = (int(x) for x in spec.split(","))
+    c = pkg.Context(n, m, k, pkg.synthetic_j(n), 0.7, device=0)
+    c.set_weights(*pkg.synthetic_weights(n, m, k, 0.01, SEED))
+    c.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+    _, info = c.sr_step(SEED, chains, samples, 16, 0.1, 40.0, RTOL, 6)
+    out = {"case": spec, "ms_total": info["ms_total"], "exact_decision_rate": info["exact_decisions"] / info["proposals"]}
+    for kn, name in ((pkg.KERNEL_SAMPLE, "sample"), (pkg.KERNEL_SV_ROWS, "sv_rows"), (pkg.KERNEL_SV_COLS, "sv_cols"),
+                     (pkg.KERNEL_MOMENTS, "moments")):
+        ms, by = c.time_kernel(kn, reps=1)
+        out[name] = {"ms": ms, "bytes": by}
+    c.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -543,8 +565,11 @@ def main():
     ap.add_argument("--serve-rates", default="4,16", help="arrival rates (1/s) of the serving lines ('' : skip)")
     ap.add_argument("--precision-chains", type=int, default=16384, help="chains of the precision-form line (0: skip)")
     ap.add_argument("--serve-window", type=float, default=5.0, help="seconds of arrivals per serving line")
+    ap.add_argument("--kernel-case", default="", help="N,M,K,chains,samples: one mixed step, then its kernels timed alone")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.kernel_case:
+        kernel_case(args.kernel_case)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
