@@ -273,6 +273,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
 #pragma unroll
     for (int jb = 0; jb < JB; jb++) accb[jb] = 0.f;
     const bool bgroup = blockIdx.z == 0 && ig == 0;
+    // the thread's IB grid rows share one 32-bit half of the sign words (IB | 32):
+    // a sign is that word shifted so the row's bit is the top bit, XORed into the weight
+    const uint32_t *sb32 = reinterpret_cast<const uint32_t *>(sb);
+    const int ib_c = min(ibase, kMaxN - IB), wsel = ib_c >> 5, sh0 = ib_c & 31;
     if (nbat > 0) issue(0);
     for (int bi = 0; bi < nbat; bi++) {
         const int buf = bi & 1;
@@ -308,10 +312,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
                 }
             }
             const float wr = sw1[buf * kStage + rr];
-            const uint64_t x0 = sb[(buf * kStage + rr) * 2], x1 = sb[(buf * kStage + rr) * 2 + 1];
+            const uint32_t wd = sb32[(buf * kStage + rr) * 4 + wsel];
 #pragma unroll
             for (int ii = 0; ii < IB; ii++) {
-                const float sw = sgn(x0, x1, min(ibase + ii, kMaxN - 1)) * wr;
+                const uint32_t sbit = (wd << (31 - (sh0 + ii))) & 0x80000000u;  // bit set: spin down
+                const float sw = __uint_as_float(__float_as_uint(wr) ^ sbit);
 #pragma unroll
                 for (int jb = 0; jb < JB; jb++) acc[ii][jb] = fmaf(sw, tv[jb], acc[ii][jb]);
             }
@@ -323,9 +328,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
         // the a block: row rr = tj (mod kJT) per j-thread
         for (int rr = tj; rr < nb; rr += kJT) {
             const float wr = sw1[buf * kStage + rr];
-            const uint64_t x0 = sb[(buf * kStage + rr) * 2], x1 = sb[(buf * kStage + rr) * 2 + 1];
+            const uint32_t wd = sb32[(buf * kStage + rr) * 4 + wsel];
 #pragma unroll
-            for (int ii = 0; ii < IB; ii++) acca[ii] = fmaf(sgn(x0, x1, min(ibase + ii, kMaxN - 1)), wr, acca[ii]);
+            for (int ii = 0; ii < IB; ii++)
+                acca[ii] += __uint_as_float(__float_as_uint(wr) ^ ((wd << (31 - (sh0 + ii))) & 0x80000000u));
         }
         __syncthreads();  // buffer buf is refilled by the next issue
     }

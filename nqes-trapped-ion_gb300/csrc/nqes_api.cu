@@ -155,7 +155,16 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     if (mixed) {
         // O as its factors (K^2 (M + 1) floats per sample); column sums over
         // chunks of ~128 samples, 3 partial sets for the moments
+        // chunks of ~128 samples, at most 256, a multiple of 2 SMs / K when that
+        // many: the column pass (2 CTAs per SM, one per chunk and state) then
+        // fills whole waves
         ctx->rchunks = int(std::max<size_t>(1, std::min<size_t>(256, (Ns + 127) / 128)));
+        {
+            int sms = 148;
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+            const int q = std::max(1, 2 * sms / sh.K);
+            if (ctx->rchunks >= q) ctx->rchunks = ctx->rchunks / q * q;
+        }
         const size_t KK = size_t(sh.K) * sh.K;
         if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * KK * (fact_mt(sh.M) + 1) * sizeof(float))) ||
             (rc = dalloc(ctx, &ctx->exact, size_t(chains))) || (rc = dalloc(ctx, &ctx->v32, P)) ||
