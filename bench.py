@@ -402,10 +402,13 @@ def run_ours(args):
     hbm, hbm_src = measured_peaks()
     ach = kern[dom]["bytes"] / (kern[dom]["avg_ms"] * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "traffic.txt")  # "kernel bytes" lines from an ncu capture
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(dom)
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#") and parts[0] == dom:
+                    traffic = float(parts[1])
     fp64_tf = fp64_peak_tflops(torch)
     # algorithmic FLOPs of the S·v passes: one FMA per stored real log-derivative
     sv_flops = 2.0 * ns * ctx.P * (4 if infos[-1]["arith"] == pkg.ARITH_COMPLEX else 1)
