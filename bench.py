@@ -499,6 +499,19 @@ def run_ours(args):
             "dtype": "f32 factors/decisions (certified) + f64 theta, Phi, MINRES-QLP, update",
         }
         cm.close()
+        # FP64 results from the certified sampler: the FP64 form's chains and
+        # FP64 E, O, moments, S·v, MINRES-QLP and update
+        cc, ic, ec = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_CERTIFIED, chains, args.steps, args.warmup, seed0, local)
+        ms_c = sum(i["ms_total"] for i in ic) / args.steps
+        ksc, _ = cc.time_kernel(pkg.KERNEL_SAMPLE, reps=3)
+        out["certified"] = {
+            "value": ns / (ms_c * 1e-3), "unit": "MC samples/s", "ms_per_step": ms_c, "speedup_vs_fp64": ms_f / ms_c,
+            "sampler_ms": ksc, "dE_rel_first_step": float(np.max(np.abs(ec[0] - ef[0]) / np.abs(ef[0]))),
+            "dE_rel_last_step": float(np.max(np.abs(ec[-1] - ef[-1]) / np.abs(ef[-1]))),
+            "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for i in ic])),
+            "dtype": "f64 results; accept decisions certified in f32 (identical to f64), exact f64 fallback",
+        }
+        cc.close()
 
     # ---- the 4096-chain sweep (both forms, fewer steps) ----
     if args.sweep_chains:

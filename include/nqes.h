@@ -74,9 +74,15 @@ extern "C" {
  *   in FP32 with a certified error bound and an exact FP64 decision whenever
  *   the bound cannot decide, so the Markov chains are the FP64 chains;
  *   theta, Phi, local-energy sums, moments, MINRES-QLP and the update in FP64;
- *   log-derivatives stored in FP32 and the two O passes of S·v in FP32. */
+ *   log-derivatives stored as their FP32 factors (tanh rows, Phi coefficients)
+ *   and S·v and the moments computed from them in FP32. */
 #define NQES_PRECISION_FP64 0
 #define NQES_PRECISION_MIXED 1
+/* FP64 results (E, O, moments, S·v, MINRES-QLP, update as NQES_PRECISION_FP64)
+ * with the mixed form's sampler: accept decisions from certified FP32 bounds
+ * with the exact FP64 fallback, so the same configurations; real weights and
+ * shapes of the decision-warp sampler (otherwise the FP64 sampler runs). */
+#define NQES_PRECISION_CERTIFIED 2
 
 typedef struct nqes_ctx nqes_ctx;
 

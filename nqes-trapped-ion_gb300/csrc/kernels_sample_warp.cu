@@ -43,7 +43,9 @@ int dw_units(const Shape &sh, int *G_out) {
     return U <= 32 ? U : 0;
 }
 
-size_t dw_smem_bytes(const Shape &sh, int MP, bool staged) { return dsmem_bytes(sh.N, MP, sh.K, staged); }
+size_t dw_smem_bytes(const Shape &sh, int MP, bool staged, bool out64) {
+    return dsmem_bytes(sh.N, MP, sh.K, staged, out64);
+}
 
 cudaError_t prepare_sample_dw(const Shape &sh, int MP) {
     int G = 0;
@@ -60,7 +62,7 @@ cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_
 }
 
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st) {
-    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K, a.stage != 0);
+    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K, a.stage != 0, a.out64 != 0);
     const DwKernel fn = dw_kernel(a.sh.K, a.U);
     if (!fn || warps < 1 || warps > 8 || a.sh.NW > 2 || a.G * a.U != a.MP) return cudaErrorInvalidConfiguration;
     fn<<<a.chains, 32 * warps, smem, st>>>(a);

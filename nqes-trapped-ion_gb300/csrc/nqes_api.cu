@@ -154,10 +154,9 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     const bool mixed = ctx->precision == NQES_PRECISION_MIXED;
     if (mixed) {
         // O as its factors (K^2 (M + 1) floats per sample); column sums over
-        // chunks of ~128 samples, 3 partial sets for the moments
-        // chunks of ~128 samples, at most 256, a multiple of 2 SMs / K when that
-        // many: the column pass (2 CTAs per SM, one per chunk and state) then
-        // fills whole waves
+        // chunks of ~128 samples, 3 partial sets for the moments; at most 256
+        // chunks, a multiple of 2 SMs / K when that many: the column pass (2
+        // CTAs per SM, one per chunk and state) then fills whole waves
         ctx->rchunks = int(std::max<size_t>(1, std::min<size_t>(256, (Ns + 127) / 128)));
         {
             int sms = 148;
@@ -176,6 +175,8 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
         F.K = sh.K;
         if ((rc = dalloc(ctx, &ctx->tcimg, rows_tc_image_elems(F)))) return rc;
     } else if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->O), Ns * P * ss))) {
+        return rc;
+    } else if (ctx->precision == NQES_PRECISION_CERTIFIED && (rc = dalloc(ctx, &ctx->exact, size_t(chains)))) {
         return rc;
     }
     ctx->step_precision = ctx->precision;
@@ -297,7 +298,29 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.G = ctx->dw_G;
     A.U = ctx->dw_U;
     A.MP = ctx->dw_MP;
+    A.out64 = ctx->step_precision == NQES_PRECISION_CERTIFIED ? 1 : 0;
+    if (A.out64) {
+        // dense FP64 O and the FP64 tables of the step (ch, sh, eup, edn)
+        const size_t nw = size_t(ctx->sh.K) * ctx->sh.N * ctx->sh.M, na = size_t(ctx->sh.K) * ctx->sh.N;
+        const double *t = static_cast<const double *>(ctx->tab);
+        A.O64 = static_cast<double *>(ctx->O);
+        A.FT = A.FB = nullptr;
+        A.c64 = t;
+        A.s64 = t + nw;
+        A.eup64 = t + 2 * nw;
+        A.edn64 = t + 2 * nw + na;
+    }
     return A;
+}
+
+// The decision-warp sampler (certified FP32 decisions) runs for MIXED and, with
+// FP64 outputs, for CERTIFIED with real arithmetic on the shapes it covers; a
+// CERTIFIED step beyond those runs the FP64 sampler.
+bool certified_dw(const nqes_ctx *ctx) {
+    return ctx->step_precision == NQES_PRECISION_CERTIFIED && ctx->dw_U && ctx->arith == NQES_ARITH_REAL;
+}
+bool uses_mixed_sampler(const nqes_ctx *ctx) {
+    return ctx->step_precision == NQES_PRECISION_MIXED || certified_dw(ctx);
 }
 
 cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
@@ -320,7 +343,7 @@ void dw_plan(nqes_ctx *ctx, int chains, int *warps, int *stage) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     for (int w = 4; w >= 1; w >>= 1)
         for (int st = 1; st >= 0; st--) {
-            const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1);
+            const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1, certified_dw(ctx));
             if (smem > 227 * 1024) continue;
             int per_sm = 0;
             if (dw_occupancy(ctx->sh, 32 * w, smem, &per_sm) == cudaSuccess && per_sm * sms >= chains) {
@@ -343,7 +366,7 @@ cudaError_t launch_mixed_tables(nqes_ctx *ctx) {
     return e;
 }
 size_t mixed_sampler_smem(nqes_ctx *ctx) {
-    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP, false) : mixed_smem_bytes(ctx->sh);
+    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP, false, certified_dw(ctx)) : mixed_smem_bytes(ctx->sh);
 }
 // The mixed sampler's and the factored S·v's shared-memory limits.
 cudaError_t prepare_mixed_sampler(nqes_ctx *ctx) {
@@ -436,7 +459,7 @@ template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, 
     const int threads = sample_threads(ctx->sh.K, tk);
     {
         // the sampler's dynamic shared memory attribute must be set before capture
-        const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
+        const bool mixed = uses_mixed_sampler(ctx);
         const size_t smem = mixed ? mixed_sampler_smem(ctx) : sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
         if (smem > 227 * 1024) {
             ctx->err = "shape needs " + std::to_string(smem) + " bytes of shared memory per chain";
@@ -457,8 +480,9 @@ template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, 
     NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->st);
     cudaError_t le;
-    if (ctx->step_precision == NQES_PRECISION_MIXED) {
+    if (uses_mixed_sampler(ctx)) {
         le = launch_mixed_tables(ctx);
+        if (le == cudaSuccess && certified_dw(ctx)) le = launch_tables_ctx<S>(ctx);  // the FP64 outputs' tables
         if (le == cudaSuccess) le = launch_mixed_sampler(ctx, chains, m, burn, tk);
     } else {
         le = launch_tables_ctx<S>(ctx);
@@ -637,7 +661,7 @@ int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t 
         // and 6 kernels per execution of the loop body
         info->kernel_launches = 9 + 6 * q.bodies;
         info->precision = ctx->step_precision;
-        if (ctx->step_precision == NQES_PRECISION_MIXED) {
+        if (uses_mixed_sampler(ctx)) {
             std::vector<unsigned long long> ex(chains);
             NQES_CUDA(cudaMemcpy(ex.data(), ctx->exact, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
             for (auto x : ex) info->exact_decisions += x;
@@ -666,12 +690,10 @@ int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t 
 // decision-warp sampler.
 template <class S> int tune_sampler(nqes_ctx *ctx, int chains, int m, int burn) {
     const int mt = std::min(m, 8), bt = std::min(burn, 2);
-    const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
+    const bool mixed = uses_mixed_sampler(ctx);
     NQES_CUDA(cudaMemcpyAsync(ctx->sp, ctx->sp_host, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->st));
-    if (mixed)
-        NQES_CUDA(launch_mixed_tables(ctx));
-    else
-        NQES_CUDA(launch_tables_ctx<S>(ctx));
+    if (mixed) NQES_CUDA(launch_mixed_tables(ctx));
+    if (!mixed || certified_dw(ctx)) NQES_CUDA(launch_tables_ctx<S>(ctx));
     auto time_one = [&](auto &&launch, float *ms) -> cudaError_t {
         cudaError_t e = launch();  // warm-up
         if (e != cudaSuccess) return e;
@@ -889,8 +911,8 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         ctx->minres_cap = uint64_t(value);
         return NQES_OK;
     case NQES_OPT_PRECISION:
-        if (value != NQES_PRECISION_FP64 && value != NQES_PRECISION_MIXED) {
-            ctx->err = "precision must be NQES_PRECISION_FP64 or NQES_PRECISION_MIXED";
+        if (value != NQES_PRECISION_FP64 && value != NQES_PRECISION_MIXED && value != NQES_PRECISION_CERTIFIED) {
+            ctx->err = "precision must be NQES_PRECISION_FP64, NQES_PRECISION_MIXED or NQES_PRECISION_CERTIFIED";
             return NQES_ERR_INVALID;
         }
         ctx->precision = int(value);
@@ -1220,7 +1242,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
     auto launch = [&]() -> cudaError_t {
         switch (kernel) {
         case NQES_KERNEL_SAMPLE: {
-            if (ctx->step_precision == NQES_PRECISION_MIXED)
+            if (uses_mixed_sampler(ctx))
                 return launch_mixed_sampler(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
             SampleArgs<S> A = sample_args<S>(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
             return launch_sample<S>(A, sample_threads(ctx->sh.K, ctx->last_tk), ctx->st);
@@ -1249,7 +1271,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
         NQES_CUDA(prepare_mixed_sampler(ctx));
     }
     if (kernel == NQES_KERNEL_SAMPLE) {
-        if (mixed)
+        if (uses_mixed_sampler(ctx))
             NQES_CUDA(prepare_mixed_sampler(ctx));
         else
             NQES_CUDA(prepare_sample<S>(ctx->sh));

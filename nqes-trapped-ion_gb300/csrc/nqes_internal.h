@@ -84,10 +84,15 @@ struct MixedArgs {
     const float *bnd;                    // per (kk, i): float4 bound record, then per kk 2 max_j sum_i |w_ij|
     int G, U, MP;
     int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
+    // FP64 outputs (NQES_PRECISION_CERTIFIED): E from FP64 flip ratios and the
+    // dense FP64 O (P per sample) instead of the FP32 factors
+    int out64;
+    double *O64;
+    const double *c64, *s64, *eup64, *edn64;  // FP64 tables [kk][i][j], [kk][i]
 };
 size_t mixed_smem_bytes(const Shape &sh);
 int dw_units(const Shape &sh, int *G_out);  // U of the decision-warp form, 0 if it does not apply
-size_t dw_smem_bytes(const Shape &sh, int MP, bool staged);
+size_t dw_smem_bytes(const Shape &sh, int MP, bool staged, bool out64 = false);
 cudaError_t prepare_sample_dw(const Shape &sh, int MP);
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st);
 cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm);

@@ -280,7 +280,8 @@ int nqes_server_submit(nqes_server *s, const nqes_request *r, uint64_t *id) {
     if (!s || !r || !r->J) return NQES_ERR_INVALID;
     if (r->n_states < 1 || r->n_states > 4 || r->n_spins < 1 || r->n_spins > 128 || r->n_hidden < 1 ||
         r->n_hidden > 512 || r->chains < 1 || r->samples_per_chain < 1 || r->burn_in < 0 || r->max_steps < 1 ||
-        (r->precision != NQES_PRECISION_FP64 && r->precision != NQES_PRECISION_MIXED) || ((r->a == nullptr) != (r->b == nullptr)) ||
+        (r->precision != NQES_PRECISION_FP64 && r->precision != NQES_PRECISION_MIXED &&
+         r->precision != NQES_PRECISION_CERTIFIED) || ((r->a == nullptr) != (r->b == nullptr)) ||
         ((r->a == nullptr) != (r->w == nullptr))) {
         std::lock_guard<std::mutex> g(s->mu);
         s->err = "invalid request";

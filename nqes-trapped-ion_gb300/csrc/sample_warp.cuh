@@ -65,6 +65,7 @@ struct DSmem {
     float *th_hi, *th_lo, *t, *rat, *bsig, *Bm;
     uint64_t *spin, *mbar;
     int *flag;
+    double *t64;  // FP64 outputs: tanh of the exact theta [K*K][MP]
     float *tabs;  // staged tables (cosh 2w, sinh 2w, w hi, w lo), 4 * K*N*MP floats
     // the tables the kernel reads: staged copies or global memory
     const float *tc, *ts, *twh, *twl;
@@ -73,15 +74,16 @@ struct DSmem {
 // One table of K*N*MP floats in bytes (a multiple of 16: MP*4 >= 32).
 __host__ __device__ inline size_t dw_table_bytes(int N, int MP, int K) { return size_t(K) * N * MP * 4; }
 
-__host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K, bool staged) {
+__host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K, bool staged, bool out64 = false) {
     const size_t KK = size_t(K) * K;
     const size_t nd = 3 * KK + 4 + 32 + 32 * 4;
     const size_t nf = 3 * KK * MP + 2 * KK * N + KK;
-    const size_t base = nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 8 + 4 * 4;  // 16: alignment pad
+    size_t base = nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 8 + 4 * 4;  // 16: alignment pad
+    if (out64) base += 16 + KK * MP * 8;
     return staged ? base + 16 + 4 * dw_table_bytes(N, MP, K) : base;
 }
 
-__device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
+__device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K, bool out64) {
     const int KK = K * K;
     DSmem s;
     double *d = reinterpret_cast<double *>(base);
@@ -108,6 +110,11 @@ __device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K) {
     s.flag = reinterpret_cast<int *>(s.mbar + 1);
     unsigned char *tb = reinterpret_cast<unsigned char *>(s.flag + 4);
     tb += (16 - (reinterpret_cast<uintptr_t>(tb) & 15)) & 15;
+    s.t64 = reinterpret_cast<double *>(tb);
+    if (out64) {
+        tb += size_t(KK) * MP * 8;
+        tb += (16 - (reinterpret_cast<uintptr_t>(tb) & 15)) & 15;
+    }
     s.tabs = reinterpret_cast<float *>(tb);
     return s;
 }
@@ -610,7 +617,7 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
     const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int c = blockIdx.x;
-    DSmem sm = dcarve(smem_raw, N, MP, K);
+    DSmem sm = dcarve(smem_raw, N, MP, K, A.out64 != 0);
     const bool writer = tid == 0;
     const size_t tb = dw_table_bytes(N, MP, K);
     if (A.stage) {
@@ -668,7 +675,10 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         }
         if (sw < A.burn) continue;
 
-        // ---- sample: local energy (FP32 ratios, FP64 combination) and FP32 O ----
+        // ---- sample: local energy and log-derivatives. Mixed form: FP32 flip
+        // ratios combined in FP64, O as its FP32 factors. FP64 outputs: tanh of
+        // the exact theta, flip ratios over the FP64 tables, the dense FP64 O row
+        // (what the FP64 sampler produces from the same configurations). ----
         const size_t s = size_t(c) * A.m + (sw - A.burn);
         if (writer) {
             double pinv[16];
@@ -707,29 +717,51 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
                 if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
             }
         }
-        for (int it = tid; it < KK * N; it += T) {
-            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-            const bool down = down_bit(sm.spin + k * NW, i);
-            const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
-            const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
-            const float *trow = sm.t + q * MP;
-            // four independent partial products over 16-byte loads; padded units
-            // (t = 0, c = 1, s = 0) contribute exactly 1, so MP needs no tail
-            const float sg = down ? 1.f : -1.f;
-            float p0 = 1.f, p1 = 1.f, p2 = 1.f, p3 = 1.f;
-            for (int j = 0; j < MP; j += 4) {
-                const float4 tt = *reinterpret_cast<const float4 *>(trow + j);
-                const float4 ss = *reinterpret_cast<const float4 *>(srow + j);
-                const float4 cc = *reinterpret_cast<const float4 *>(crow + j);
-                p0 *= fmaf(sg * tt.x, ss.x, cc.x);
-                p1 *= fmaf(sg * tt.y, ss.y, cc.y);
-                p2 *= fmaf(sg * tt.z, ss.z, cc.z);
-                p3 *= fmaf(sg * tt.w, ss.w, cc.w);
+        if (A.out64) {
+            for (int e = tid; e < KK * MP; e += T) {
+                const int j = e % MP;
+                sm.t64[e] = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
             }
-            const float p = (p0 * p1) * (p2 * p3);
-            sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
-            const float B = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
-            sm.bsig[it] = down_bit(sm.spin + kk * NW, i) ? -B : B;
+            __syncthreads();
+            double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
+            for (int it = tid; it < KK * N; it += T) {
+                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+                const bool down = down_bit(sm.spin + k * NW, i);
+                const double sg = down ? 1.0 : -1.0;
+                const double *crow = A.c64 + (size_t(kk) * N + i) * M, *srow = A.s64 + (size_t(kk) * N + i) * M;
+                const double *trow = sm.t64 + q * MP;
+                double p0 = 1.0, p1 = 1.0;
+                int j = 0;
+                for (; j + 1 < M; j += 2) {
+                    p0 *= fma(sg * trow[j], srow[j], crow[j]);
+                    p1 *= fma(sg * trow[j + 1], srow[j + 1], crow[j + 1]);
+                }
+                if (j < M) p0 *= fma(sg * trow[j], srow[j], crow[j]);
+                rat64[it] = (p0 * p1) * (down ? A.edn64 : A.eup64)[kk * N + i];
+            }
+        } else {
+            for (int it = tid; it < KK * N; it += T) {
+                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+                const bool down = down_bit(sm.spin + k * NW, i);
+                const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
+                const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
+                const float *trow = sm.t + q * MP;
+                // four independent partial products over 16-byte loads; padded units
+                // (t = 0, c = 1, s = 0) contribute exactly 1, so MP needs no tail
+                const float sg = down ? 1.f : -1.f;
+                float p0 = 1.f, p1 = 1.f, p2 = 1.f, p3 = 1.f;
+                for (int j = 0; j < MP; j += 4) {
+                    const float4 tt = *reinterpret_cast<const float4 *>(trow + j);
+                    const float4 ss = *reinterpret_cast<const float4 *>(srow + j);
+                    const float4 cc = *reinterpret_cast<const float4 *>(crow + j);
+                    p0 *= fmaf(sg * tt.x, ss.x, cc.x);
+                    p1 *= fmaf(sg * tt.y, ss.y, cc.y);
+                    p2 *= fmaf(sg * tt.z, ss.z, cc.z);
+                    p3 *= fmaf(sg * tt.w, ss.w, cc.w);
+                }
+                const float p = (p0 * p1) * (p2 * p3);
+                sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
+            }
         }
         __syncthreads();
         if (tid < K) {
@@ -739,11 +771,19 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         }
         __syncthreads();
         for (int q = warp; q < KK; q += nwarp) {
-            float acc = 0.f;
-            for (int i = lane; i < N; i += 32) acc += sm.rat[q * N + i];
+            double acc = 0.0;
+            if (A.out64) {
+                const double *rat64 = reinterpret_cast<const double *>(sm.rat);
+                for (int i = lane; i < N; i += 32) acc += rat64[q * N + i];
+                acc = warp_sum(acc);
+            } else {
+                float a32 = 0.f;
+                for (int i = lane; i < N; i += 32) a32 += sm.rat[q * N + i];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) sm.Dm[q] = sm.jk[q / K] - A.h * double(acc);
+                for (int o = 16; o > 0; o >>= 1) a32 += __shfl_xor_sync(0xffffffffu, a32, o);
+                acc = double(a32);
+            }
+            if (lane == 0) sm.Dm[q] = sm.jk[q / K] - A.h * acc;
         }
         __syncthreads();
         if (writer) {
@@ -764,13 +804,48 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         // the factors of the O row (code/rbm.cc:199-239 in closed form): tanh rows
         // T[s][k][kk][j] = tanh theta_j of configuration kk under RBM k, and
         // B[s][k][kk] = (Phi^-1)_{k,kk} Phi_{kk,k}; the signs come from the spins
-        const int MT = fact_mt(M);
-        float *ft = A.FT + s * size_t(KK) * MT;
-        for (int e = tid; e < KK * MT; e += T) {
-            const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
-            ft[e] = j < M ? sm.t[(kk * K + k) * MP + j] : 0.f;
+        if (A.out64) {
+            // O_{k,p} = sum_kk (Phi^-1)_{k,kk} Phi_{kk,k} d_p(configuration kk) in FP64, layout
+            // [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239). The coefficients
+            // times the spin signs, bs[k][kk][i], go to the ratio space (free once
+            // Dm is formed) and the coefficients themselves to Dm (free once E is
+            // formed): K FMAs per entry.
+            const int L = N + M + N * M;
+            double *bs = reinterpret_cast<double *>(sm.rat);  // K*K*N doubles: the rat and bsig space
+            for (int e = tid; e < KK * N; e += T) {
+                const int q = e / N, i = e - q * N, k = q / K, kk = q - k * K;
+                const double b = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
+                bs[e] = down_bit(sm.spin + kk * NW, i) ? -b : b;
+            }
+            if (tid < KK) sm.Dm[tid] = sm.pinv[(tid / K) * K + tid % K] * sm.phi[(tid % K) * K + tid / K];
+            __syncthreads();
+            double *orow = A.O64 + s * size_t(A.sh.P);
+            for (int e = tid; e < K * L; e += T) {
+                const int k = e / L, p = e - k * L;
+                double v = 0.0;
+                if (p < N) {
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) v += bs[(k * K + kk) * N + p];
+                } else if (p < N + M) {
+                    const int j = p - N;
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) v = fma(sm.Dm[k * K + kk], sm.t64[(kk * K + k) * MP + j], v);
+                } else {
+                    const int i = (p - N - M) / M, j = (p - N - M) - i * M;
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
+                }
+                orow[e] = v;
+            }
+        } else {
+            const int MT = fact_mt(M);
+            float *ft = A.FT + s * size_t(KK) * MT;
+            for (int e = tid; e < KK * MT; e += T) {
+                const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
+                ft[e] = j < M ? sm.t[(kk * K + k) * MP + j] : 0.f;
+            }
+            if (tid < KK) A.FB[s * KK + tid] = sm.Bm[tid];
         }
-        if (tid < KK) A.FB[s * KK + tid] = sm.Bm[tid];
         __syncthreads();
     }
     if (writer) {

@@ -300,3 +300,41 @@ def test_tensor_core_rows_pass_matches_cuda_cores(pkg, N, M, K, chains, m):
         assert rel_err(x, y) < 1e-5
     assert rel_err(b["e"], a["e"]) < 1e-6
     assert rel_err(b["w"], a["w"]) < (5e-5 if P < 10000 else 2e-4)
+
+
+@pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 32, 20), (12, 24, 3, 8, 20),
+                                            (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (66, 66, 2, 4, 8),
+                                            (10, 300, 4, 4, 6)])
+def test_certified_matches_fp64(pkg, N, M, K, chains, m):
+    """CERTIFIED: the mixed form's sampler (certified FP32 decisions, exact FP64
+    fallback) with FP64 outputs gives the FP64 form's configurations and accept
+    counts bit for bit, and its local energies, log-derivatives, moments and
+    S·v to FP64 rounding (tanh of the exact theta instead of the FP64 sampler's
+    incrementally updated tanh); M = 300 runs the FP64 sampler (beyond the
+    decision-warp shapes)."""
+    J = synthetic_j(N)
+    w = helpers.random_weights(N, M, K, 0.05 if N < 20 else 0.02, 7 + N, real=True)
+    P = K * (N + M + N * M)
+    vrand = np.random.default_rng(N + 2 * M).normal(size=P).astype(np.complex128)
+    out = {}
+    for prec in (pkg.PRECISION_FP64, pkg.PRECISION_CERTIFIED):
+        ctx = pkg.Context(N, M, K, J, 0.595)
+        ctx.set_weights(*w)
+        ctx.set_option(pkg.OPT_PRECISION, prec)
+        e, info = ctx.sr_step(4243, chains, m, 10, 0.1, 5.0, 1e-9, 2000)
+        spins, eloc, E = ctx.get_samples()
+        out[prec] = dict(e=e, info=info, spins=spins, E=E, O=ctx.get_O(0, chains * m), acc=ctx.get_accepts(),
+                         mom=ctx.get_moments(), sv=ctx.apply_S(vrand),
+                         w=np.concatenate([x.ravel() for x in ctx.get_weights()]))
+        ctx.close()
+    f, c = out[pkg.PRECISION_FP64], out[pkg.PRECISION_CERTIFIED]
+    assert np.array_equal(f["spins"], c["spins"]), "certified chains left the FP64 chains"
+    assert np.array_equal(f["acc"], c["acc"])
+    assert c["info"]["precision"] == pkg.PRECISION_CERTIFIED
+    assert rel_err(c["E"], f["E"]) < 1e-11
+    assert rel_err(c["O"], f["O"]) < 1e-11
+    assert rel_err(c["e"], f["e"]) < 1e-11
+    for a, b in zip(c["mom"], f["mom"]):
+        assert rel_err(a, b) < 1e-10
+    assert rel_err(c["sv"], f["sv"]) < 1e-10
+    assert rel_err(c["w"], f["w"]) < 1e-6
