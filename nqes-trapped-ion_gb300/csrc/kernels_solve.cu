@@ -645,23 +645,24 @@ template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &B, cudaStr
 
 // u = O v then the row-chunk partials of O^H u. In the mixed form v must
 // already be mirrored in B.v32.
-template <class S> static void launch_sv_passes(const SolveBufs<S> &B, const S *v, cudaStream_t st) {
+template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, const S *v, cudaStream_t st) {
     const int P = B.sh.P, nb = (P + kVecThreads - 1) / kVecThreads;
     const int rows_per_block = kVecThreads / 32;
     const int rb = (B.Ns + rows_per_block - 1) / rows_per_block;
     dim3 g(nb, B.rchunks);
     if (B.fact) {
-        launch_frows(B.F, B.v32, B.u32, st);
-        launch_fcols(B.F, B.u32, B.ypart32, st);
-    } else {
-        k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u);
-        k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart);
+        const cudaError_t e = launch_frows(B.F, B.v32, B.u32, st);
+        return e != cudaSuccess ? e : launch_fcols(B.F, B.u32, B.ypart32, st);
     }
+    k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u);
+    k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart);
+    return cudaGetLastError();
 }
 
 template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &B, cudaStream_t st) {
     const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
-    launch_sv_passes(B, B.v, st);
+    const cudaError_t e = launch_sv_passes(B, B.v, st);
+    if (e != cudaSuccess) return e;
     k_lanczos_a<S><<<nb, kVecThreads, 0, st>>>(B);
     k_lanczos_b<S><<<nb, kVecThreads, 0, st>>>(B);
     k_qlp_scalar<S><<<1, 32, 0, st>>>(B);
@@ -707,7 +708,8 @@ template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &B, const S *v,
     const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
     k_ov_part<S><<<nb, kVecThreads, 0, st>>>(B.sh.P, B.o, v, B.ovpart);
     if (B.fact) k_to_f32<<<nb, kVecThreads, 0, st>>>(B.sh.P, reinterpret_cast<const double *>(v), B.v32);
-    launch_sv_passes(B, v, st);
+    const cudaError_t e = launch_sv_passes(B, v, st);
+    if (e != cudaSuccess) return e;
     k_apply_out<S><<<nb, kVecThreads, 0, st>>>(B, v, out);
     return cudaGetLastError();
 }
