@@ -267,8 +267,9 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
 // sum_kk (re_kk - rho) (g_kk - g*_kk) / det, which is small when the states
 // are alike, so with rh = s / det the error of rh is at most
 //   E = [sum_kk |g| |re| (beta + 3u) + 1.03 sum_kk (dr |g| + ga) (|re - rh| + 1.02 bmax |re|)
-//        + (K + 1) u sum_kk |x| + |rh| edet] / |det| / (1 - q) + 3u |rh|,
-//   q = (1.03 dr sum|g| + sum ga + edet) / |det|  (required < 1/2).
+//        + (K + 1) u sum_kk |x| + |rh| edet] / |det| (1 + 2q) + 3u |rh|,
+//   q = (1.03 dr sum|g| + sum ga + edet) / |det|  (required < 1/2, so that
+//   1 / (1 - q) <= 1 + 2q).
 // A decision the margins (16u on each side) cannot make goes to the exact
 // path.
 template <int K, int U>
@@ -317,7 +318,7 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
             gasum += ga[kk];
         }
         det32 = float(det);
-        rdet = 1.f / det32;
+        rdet = __frcp_rn(det32);  // correctly rounded, as the bound assumes
         edet = kU * (fabsf(det32) + gsum) * 1.01f + float(perm * 0x1p-50);
         dr = 2.f * kU;
     };
@@ -411,7 +412,8 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
             const float ad = fabsf(det32), ard = fabsf(rdet), arh = fabsf(rh);
             const float q = fmaf(1.03f * dr, gsum, gasum + edet) * ard;
             const float num = fmaf(1.03f, e2, e1) + fmaf(float(K + 1) * kU, sax, arh * edet);
-            const float E = fmaf(1.02f * num, ard / (1.f - q), 3.f * kU * arh);
+            // 1 / (1 - q) <= 1 + 2q for q <= 1/2 (required below): no division
+            const float E = fmaf(1.02f * num * ard, fmaf(2.f, q, 1.f), 3.f * kU * arh);
             const float lo = arh - E, hi = arh + E;
             if (A.exact_all || !(ad > 1e-15f) || !(ad < 1e15f) || !(bmax < 0.01f) || !(q < 0.5f))
                 exact_path = true;  // det == 0 (accepted, code/rbm.cc:542), range, loose bound
@@ -572,7 +574,7 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                     gasum += ga[kk];
                 }
                 det32 = s;
-                rdet = 1.f / s;
+                rdet = __frcp_rn(s);
                 gsum = sax;
                 edet = float(K) * kU * sax * 1.01f;
                 dr = fmaf(dr, 1.f + bmax + 8.f * kU, fmaf(bmax, 1.01f, 5.f * kU));
