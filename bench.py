@@ -368,6 +368,7 @@ def run_ours(args):
     for t in range(args.warmup):
         lr, reglam = schedule(t)
         ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+    a_start, b_start, w_start = ctx.get_weights()  # the end-to-end leg replays the timed steps from here
     clocks = ClockSampler(local)
     barrier()
     clocks.start()
@@ -416,14 +417,15 @@ def run_ours(args):
     sv_gbs = (kern["sv_rows"]["bytes"] + kern["sv_cols"]["bytes"]) / (sv_ms * 1e-3) / 1e9
     sv_tf = 2.0 * sv_flops / (sv_ms * 1e-3) / 1e12
 
-    # ---- end to end through the C ABI with host buffers ----
-    a_h, b_h, w_h = ctx.get_weights()
+    # ---- end to end through the C ABI with host buffers: the same steps (weights,
+    # seeds, schedule) as the device-timed loop, each with its weights copied in
+    # from the host and the updated weights and energy matrix copied back ----
+    a_h, b_h, w_h = a_start, b_start, w_start
     h2d = a_h.nbytes + b_h.nbytes + w_h.nbytes
     d2h = K * K * 16 + h2d
     barrier()
     t0 = time.perf_counter()
-    t_base = args.warmup + args.steps
-    for t in range(t_base, t_base + args.steps):
+    for t in range(args.warmup, args.warmup + args.steps):
         lr, reglam = schedule(t)
         ctx.set_weights(a_h, b_h, w_h)
         ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
