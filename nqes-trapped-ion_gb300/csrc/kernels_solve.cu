@@ -89,24 +89,40 @@ __global__ void k_emat(int Ns, int K, const cplx *E, cplx *emat, cplx *eloc) {
 }
 
 // Partial column sums over a chunk of rows: o, |O|^2 and E_loc conj(O).
+// Launched with kVecThreads threads: the block stages the local energies
+// (traces of E) of kVecThreads samples at a time in shared memory, so a column
+// costs three FP64 operations per sample.
 template <class S, class TO>
-__global__ void k_moment_part(int Ns, int P, int K, int rchunks, const TO *O, const cplx *E, S *po, double *ps2,
-                              S *pf) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kVecThreads) k_moment_part(int Ns, int P, int K, int rchunks, const TO *O,
+                                                             const cplx *E, S *po, double *ps2, S *pf) {
+    __shared__ S els[kVecThreads];
+    const int p = blockIdx.x * kVecThreads + threadIdx.x;
     const int r = blockIdx.y;
     const int s0 = int(int64_t(Ns) * r / rchunks), s1 = int(int64_t(Ns) * (r + 1) / rchunks);
-    if (p >= P) return;
     const int KK = K * K;
     S o = zero<S>(), f = zero<S>();
     double s2 = 0.0;
-    for (int s = s0; s < s1; s++) {
-        const S v = O[size_t(s) * P + p];
-        cplx el{0, 0};
-        for (int k = 0; k < K; k++) el += E[size_t(s) * KK + k * K + k];
-        o = o + v;
-        s2 += norm2(v);
-        f = cmad(v, from_c<S>(el), f);  // conj(O) * E_loc
+    for (int t0 = s0; t0 < s1; t0 += kVecThreads) {
+        const int nt = min(kVecThreads, s1 - t0);
+        if (int(threadIdx.x) < nt) {
+            const size_t s = size_t(t0) + threadIdx.x;
+            cplx el{0, 0};
+            for (int k = 0; k < K; k++) el += E[s * KK + k * K + k];
+            els[threadIdx.x] = from_c<S>(el);
+        }
+        __syncthreads();
+        if (p < P) {
+            const TO *col = O + size_t(t0) * P + p;
+            for (int q = 0; q < nt; q++) {
+                const S v = col[size_t(q) * P];
+                o = o + v;
+                s2 += norm2(v);
+                f = cmad(v, els[q], f);  // conj(O) * E_loc
+            }
+        }
+        __syncthreads();
     }
+    if (p >= P) return;
     po[size_t(r) * P + p] = o;
     ps2[size_t(r) * P + p] = s2;
     pf[size_t(r) * P + p] = f;
