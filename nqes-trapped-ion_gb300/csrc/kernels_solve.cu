@@ -24,6 +24,11 @@ namespace nqes {
 namespace {
 
 constexpr int kVecThreads = 256;
+// MINRES-QLP vector kernels: 64-thread blocks, so that at P = 4288 the 67
+// blocks put one warp on each FP64 pipe they use (every FP64 warp
+// instruction holds its pipe ~64 cycles) instead of two warps on 17 SMs.
+constexpr int kMrThreads = 64;
+__host__ __device__ constexpr int mr_blocks(int P) { return (P + kMrThreads - 1) / kMrThreads; }
 
 __device__ __forceinline__ double ldg(const double *p) { return __ldg(p); }
 __device__ __forceinline__ cplx ldg(const cplx *p) {
@@ -186,31 +191,82 @@ __device__ __forceinline__ void mirror_f32(float *v32, int p, double v) {
 }
 __device__ __forceinline__ void mirror_f32(float *, int, cplx) {}
 
-// out = ypart-sum / Ns + skk v - (o·v) conj(o), with o·v from per-block partials.
+// S·v epilogue for column p. The column sums of the row-chunk partials are
+// split over kRG groups of threads per column so that many loads are in flight
+// (one thread walking ~150 partials is load-latency bound); the groups then
+// combine in a fixed order.
+constexpr int kRG = 8;
+constexpr int kMrColThreads = kMrThreads * kRG;
+
+// hi + lo += x exactly (TwoSum): a two-float accumulator on the FP32 pipe.
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
+    const float sum = hi + x, bb = sum - hi;
+    lo += (hi - (sum - bb)) + (x - bb);
+    hi = sum;
+}
+
+template <class S> struct ColSumSmem {
+    float hi[kRG][kMrThreads], lo[kRG][kMrThreads];
+    S y[kRG][kMrThreads];
+};
+
+// sum over r of ypart[r][p] in the threads of group 0 (pl = column in the block,
+// rg = group); every thread of the block must call it. FP32 partials (mixed
+// form) are summed with two-float accumulators, converted to FP64 once.
 template <class S>
-__device__ __forceinline__ S sv_epilogue(const SolveBufs<S> &B, int p, const S *v, S ov) {
+__device__ S sv_colsum(const SolveBufs<S> &B, int p, int pl, int rg, ColSumSmem<S> &cs) {
+    const int R = B.rchunks, r0 = int(int64_t(R) * rg / kRG), r1 = int(int64_t(R) * (rg + 1) / kRG);
+    const bool in = p < B.sh.P;
     S y = zero<S>();
     if (B.fact) {
-        for (int r = 0; r < B.rchunks; r++) y = y + one<S>() * double(B.ypart32[size_t(r) * B.sh.P + p]);
+        float hi = 0.f, lo = 0.f;
+        if (in)
+            for (int r = r0; r < r1; r++) two_sum_acc(hi, lo, B.ypart32[size_t(r) * B.sh.P + p]);
+        cs.hi[rg][pl] = hi;
+        cs.lo[rg][pl] = lo;
+        __syncthreads();
+        if (rg == 0) {
+            hi = cs.hi[0][pl];
+            lo = cs.lo[0][pl];
+            for (int g = 1; g < kRG; g++) {
+                two_sum_acc(hi, lo, cs.hi[g][pl]);
+                lo += cs.lo[g][pl];
+            }
+            y = one<S>() * (double(hi) + double(lo));
+        }
     } else {
-        for (int r = 0; r < B.rchunks; r++) y = y + B.ypart[size_t(r) * B.sh.P + p];
+        if (in)
+            for (int r = r0; r < r1; r++) y = y + B.ypart[size_t(r) * B.sh.P + p];
+        cs.y[rg][pl] = y;
+        __syncthreads();
+        if (rg == 0) {
+            y = cs.y[0][pl];
+            for (int g = 1; g < kRG; g++) y = y + cs.y[g][pl];
+        }
     }
+    return y;
+}
+
+// out = column sum / Ns + skk v - (o·v) conj(o) (code/rbm.cc:660-683).
+template <class S>
+__device__ __forceinline__ S sv_finish(const SolveBufs<S> &B, int p, const S *v, S ov, S y) {
     y = y * (1.0 / double(B.Ns));
     y = mad(B.skk[p], v[p], y);
     y = y - ov * conj(B.o[p]);
     return y;
 }
 
-template <class S> __global__ void k_apply_out(SolveBufs<S> B, const S *v, S *out) {
+template <class S> __global__ void __launch_bounds__(kMrColThreads) k_apply_out(SolveBufs<S> B, const S *v, S *out) {
     __shared__ S ovs;
+    __shared__ ColSumSmem<S> cs;
     if (threadIdx.x < 32) {
-        const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
-        S ov = warp_sum_array_s(B.ovpart, nb);
+        S ov = warp_sum_array_s(B.ovpart, mr_blocks(B.sh.P));
         if (threadIdx.x == 0) ovs = ov;
     }
-    __syncthreads();
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < B.sh.P) out[p] = sv_epilogue(B, p, v, ovs);
+    const int pl = threadIdx.x % kMrThreads, rg = threadIdx.x / kMrThreads;
+    const int p = blockIdx.x * kMrThreads + pl;
+    const S y = sv_colsum(B, p, pl, rg, cs);  // its barrier also publishes ovs
+    if (rg == 0 && p < B.sh.P) out[p] = sv_finish(B, p, v, ovs, y);
 }
 
 // Per-block partials of o·v (no conjugation, code/rbm.cc:673-676).
@@ -251,7 +307,7 @@ template <class S> __global__ void k_minres_init_vec(SolveBufs<S> B) {
 
 template <class S> __global__ void k_minres_init_scalar(SolveBufs<S> B) {
     QlpState &q = *B.qs;
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
+    const int nb = mr_blocks(B.sh.P);
     const double b2 = warp_sum_array(B.part + 2 * kPartStride, nb);
     if (threadIdx.x != 0) return;
     const double beta1 = sqrt(b2);
@@ -290,23 +346,25 @@ template <class S> __global__ void k_minres_first_v(SolveBufs<S> B) {
 }
 
 // Lanczos part 1: r3 = S v - (beta/betal) r1; partials of Re(r3^H v).
-template <class S> __global__ void k_lanczos_a(SolveBufs<S> B) {
+template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(SolveBufs<S> B) {
     __shared__ double sh[32];
     __shared__ S ovs;
+    __shared__ ColSumSmem<S> cs;
     const QlpState &q = *B.qs;
     if (!q.running) return;
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
+    const int nb = mr_blocks(B.sh.P);
     if (threadIdx.x < 32) {
         S ov = warp_sum_array_s(B.ovpart, nb);
         if (threadIdx.x == 0) ovs = ov;
     }
-    __syncthreads();
-    const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = B.sh.P, pl = threadIdx.x % kMrThreads, rg = threadIdx.x / kMrThreads;
+    const int p = blockIdx.x * kMrThreads + pl;
+    const S y = sv_colsum(B, p, pl, rg, cs);  // its barrier also publishes ovs
     const bool first = q.iters == 0;
     const double c1 = first ? 0.0 : q.betan / q.beta;  // beta_new / betal_new
     double t = 0.0;
-    if (p < P) {
-        S r3 = sv_epilogue(B, p, B.v, ovs);
+    if (rg == 0 && p < P) {
+        S r3 = sv_finish(B, p, B.v, ovs, y);
         if (!first) r3 = r3 - B.r1[p] * c1;
         B.r3[p] = r3;
         t = re_dot(r3, B.v[p]);
@@ -321,7 +379,7 @@ template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
     __shared__ double alfa_s;
     const QlpState &q = *B.qs;
     if (!q.running) return;
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
+    const int nb = mr_blocks(B.sh.P);
     if (threadIdx.x < 32) {
         double a = warp_sum_array(B.part, nb);
         if (threadIdx.x == 0) alfa_s = a;
@@ -366,21 +424,10 @@ __device__ void givens(double a, double b, double &c, double &s, double &r) {
 
 // The scalar part of one MINRES-QLP iteration (code/minresqlp.h:158-374), in
 // the reference's order, recording the coefficients the vector kernel needs.
-template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) {
-    QlpState &q = *B.qs;
-    if (threadIdx.x == 0) q.bodies++;
-    if (!q.running) {
-        // The while node's condition defaults to 1 on every graph launch; a
-        // solve that needs no iteration (b = 0, maxit = 0) ends the loop here.
-        q.mode = 0;
-        if (B.use_cond && threadIdx.x == 0) cudaGraphSetConditional(B.cond, 0);
-        return;
-    }
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
-    const double alfa = warp_sum_array(B.part, nb);
-    const double bn2 = warp_sum_array(B.part + kPartStride, nb);
-    if (threadIdx.x != 0) return;
-
+// q is a register copy of the state: every FP64 instruction of this one-thread
+// chain costs ~64 cycles, so none of them waits on a global load in between.
+template <class S>
+__device__ __forceinline__ void qlp_scalar_step(const SolveBufs<S> &B, QlpState &q, double alfa, double bn2) {
     q.iters++;
     const double betal = q.beta;
     q.beta = q.betan;
@@ -544,6 +591,25 @@ template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) {
     if (B.use_cond) cudaGraphSetConditional(B.cond, q.running);
 }
 
+template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) {
+    QlpState &gq = *B.qs;
+    if (threadIdx.x == 0) gq.bodies++;
+    if (!gq.running) {
+        // The while node's condition defaults to 1 on every graph launch; a
+        // solve that needs no iteration (b = 0, maxit = 0) ends the loop here.
+        gq.mode = 0;
+        if (B.use_cond && threadIdx.x == 0) cudaGraphSetConditional(B.cond, 0);
+        return;
+    }
+    const int nb = mr_blocks(B.sh.P);
+    const double alfa = warp_sum_array(B.part, nb);
+    const double bn2 = warp_sum_array(B.part + kPartStride, nb);
+    if (threadIdx.x != 0) return;
+    QlpState q = gq;
+    qlp_scalar_step(B, q, alfa, bn2);
+    gq = q;
+}
+
 // Vector part: w / x updates (code/minresqlp.h:253-299), then the next v and
 // its o·v partials.
 template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
@@ -652,10 +718,10 @@ template <class S> cudaError_t launch_moments(const SolveBufs<S> &B, cudaStream_
 }
 
 template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &B, cudaStream_t st) {
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
-    k_minres_init_vec<S><<<nb, kVecThreads, 0, st>>>(B);
+    const int nb = mr_blocks(B.sh.P);
+    k_minres_init_vec<S><<<nb, kMrThreads, 0, st>>>(B);
     k_minres_init_scalar<S><<<1, 32, 0, st>>>(B);
-    k_minres_first_v<S><<<nb, kVecThreads, 0, st>>>(B);
+    k_minres_first_v<S><<<nb, kMrThreads, 0, st>>>(B);
     return cudaGetLastError();
 }
 
@@ -676,13 +742,13 @@ template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, co
 }
 
 template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &B, cudaStream_t st) {
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
+    const int nb = mr_blocks(B.sh.P);
     const cudaError_t e = launch_sv_passes(B, B.v, st);
     if (e != cudaSuccess) return e;
-    k_lanczos_a<S><<<nb, kVecThreads, 0, st>>>(B);
-    k_lanczos_b<S><<<nb, kVecThreads, 0, st>>>(B);
+    k_lanczos_a<S><<<nb, kMrColThreads, 0, st>>>(B);
+    k_lanczos_b<S><<<nb, kMrThreads, 0, st>>>(B);
     k_qlp_scalar<S><<<1, 32, 0, st>>>(B);
-    k_qlp_vectors<S><<<nb, kVecThreads, 0, st>>>(B);
+    k_qlp_vectors<S><<<nb, kMrThreads, 0, st>>>(B);
     return cudaGetLastError();
 }
 
@@ -721,12 +787,12 @@ template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &B, cu
 }
 
 template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &B, const S *v, S *out, cudaStream_t st) {
-    const int nb = (B.sh.P + kVecThreads - 1) / kVecThreads;
-    k_ov_part<S><<<nb, kVecThreads, 0, st>>>(B.sh.P, B.o, v, B.ovpart);
-    if (B.fact) k_to_f32<<<nb, kVecThreads, 0, st>>>(B.sh.P, reinterpret_cast<const double *>(v), B.v32);
+    const int nb = mr_blocks(B.sh.P);
+    k_ov_part<S><<<nb, kMrThreads, 0, st>>>(B.sh.P, B.o, v, B.ovpart);
+    if (B.fact) k_to_f32<<<nb, kMrThreads, 0, st>>>(B.sh.P, reinterpret_cast<const double *>(v), B.v32);
     const cudaError_t e = launch_sv_passes(B, v, st);
     if (e != cudaSuccess) return e;
-    k_apply_out<S><<<nb, kVecThreads, 0, st>>>(B, v, out);
+    k_apply_out<S><<<nb, kMrColThreads, 0, st>>>(B, v, out);
     return cudaGetLastError();
 }
 

@@ -141,10 +141,10 @@ struct QlpState {
     int running;
 };
 
-// Reduction partial buffers: one slot per 256-element vector block. P <= 4 *
-// (128 + 512 + 128*512) gives at most 1034 blocks; three regions of this
-// stride live in SolveBufs::part (alfa, |r3|^2, |b|^2) and one in ovpart.
-constexpr int kPartStride = 2048;
+// Reduction partial buffers: one slot per 64-element MINRES-QLP vector block.
+// P <= 4 * (128 + 512 + 128*512) gives at most 4136 blocks; three regions of
+// this stride live in SolveBufs::part (alfa, |r3|^2, |b|^2) and one in ovpart.
+constexpr int kPartStride = 4160;
 
 template <class S> cudaError_t prepare_sample(const Shape &sh);
 
