@@ -185,8 +185,12 @@ __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_g
 // Batches of cols_stage(JB) rows are double-buffered: the tanh rows of the next batch
 // stream into shared memory (cp.async) and its weights and sign words are
 // formed while the current batch is summed.
+// Row sets: gn i groups cover the block's gn IB grid rows; the kGroups / gn
+// sets of groups take every nset-th staged row, so a staged tanh row is read by
+// gn groups instead of kGroups, and the sets' sums meet in shared memory at the
+// end (in set order).
 template <int IB, int JB>
-__global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, const float *__restrict__ w,
+__global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int gn, const float *__restrict__ w,
                                                      const cplx *__restrict__ E, float *__restrict__ out) {
     constexpr int WS = kJT * JB, kStage = cols_stage(JB);
     extern __shared__ float4 smem4[];
@@ -197,7 +201,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
     const int P = K * L;
     const int c = blockIdx.x, k = blockIdx.y;
     const int tj = threadIdx.x & (kJT - 1), ig = threadIdx.x / kJT;
-    const int ibase = blockIdx.z * (kGroups * IB) + ig * IB;
+    const int nset = kGroups / gn, set = ig / gn, igl = ig - set * gn;
+    const int ibase = blockIdx.z * (gn * IB) + igl * IB;
     const int vpr = mode == 3 ? K * (K + 1) / 2 : K;  // (virtual) rows per sample
     const size_t nrows = size_t(F.Ns) * vpr;
     const size_t r0 = nrows * c / F.rchunks, r1 = nrows * (c + 1) / F.rchunks;
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
     }
 #pragma unroll
     for (int jb = 0; jb < JB; jb++) accb[jb] = 0.f;
-    const bool bgroup = blockIdx.z == 0 && ig == 0;
+    const bool bgroup = blockIdx.z == 0 && igl == 0;
     // the thread's IB grid rows share one 32-bit half of the sign words (IB | 32):
     // a sign is that word shifted so the row's bit is the top bit, XORed into the weight
     const uint32_t *sb32 = reinterpret_cast<const uint32_t *>(sb);
@@ -289,7 +294,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
         cp_async_wait1();
         __syncthreads();
         const float *tb = st + (size_t(buf) * kStage) * WS, *tb2 = st + (size_t(2 + buf) * kStage) * WS;
-        for (int rr = 0; rr < nb; rr++) {
+        for (int rr = set; rr < nb; rr += nset) {
             float tv[JB];
             const float4 *tp = reinterpret_cast<const float4 *>(tb + rr * WS) + tj;
 #pragma unroll
@@ -325,8 +330,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
                 for (int jb = 0; jb < JB; jb++) accb[jb] = fmaf(wr, tv[jb], accb[jb]);
             }
         }
-        // the a block: row rr = tj (mod kJT) per j-thread
-        for (int rr = tj; rr < nb; rr += kJT) {
+        // the a block: the set's rows, one in kJT per j-thread
+        for (int rr = set + nset * tj; rr < nb; rr += nset * kJT) {
             const float wr = sw1[buf * kStage + rr];
             const uint32_t wd = sb32[(buf * kStage + rr) * 4 + wsel];
 #pragma unroll
@@ -339,6 +344,36 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, con
     for (int ii = 0; ii < IB; ii++)
 #pragma unroll
         for (int o = 1; o < kJT; o <<= 1) acca[ii] += __shfl_xor_sync(0xffffffffu, acca[ii], o);
+    if constexpr (JB < 32) {  // wider tiles run as one set
+      if (nset > 1) {
+        // sets 1.. hand their sums to set 0 through the (now idle) staging buffers:
+        // value v of thread t at red[v * kThreads + t]
+        constexpr int R = IB * JB + IB + JB;
+        float *red = st;
+#pragma unroll
+        for (int ii = 0; ii < IB; ii++) {
+#pragma unroll
+            for (int jb = 0; jb < JB; jb++) red[(ii * JB + jb) * kThreads + threadIdx.x] = acc[ii][jb];
+            red[(IB * JB + ii) * kThreads + threadIdx.x] = acca[ii];
+        }
+#pragma unroll
+        for (int jb = 0; jb < JB; jb++) red[(IB * JB + IB + jb) * kThreads + threadIdx.x] = accb[jb];
+        __syncthreads();
+        if (set != 0) return;
+        for (int s2 = 1; s2 < nset; s2++) {
+            const int t2 = threadIdx.x + s2 * gn * kJT;
+#pragma unroll
+            for (int ii = 0; ii < IB; ii++) {
+#pragma unroll
+                for (int jb = 0; jb < JB; jb++) acc[ii][jb] += red[(ii * JB + jb) * kThreads + t2];
+                acca[ii] += red[(IB * JB + ii) * kThreads + t2];
+            }
+#pragma unroll
+            for (int jb = 0; jb < JB; jb++) accb[jb] += red[(IB * JB + IB + jb) * kThreads + t2];
+        }
+        static_assert(R > 0, "reduction layout");
+      }
+    }
     float *o = out + size_t(c) * P + size_t(k) * L;
 #pragma unroll
     for (int ii = 0; ii < IB; ii++) {
@@ -417,11 +452,21 @@ int pick_jb(int M) {
     const int jb = (M + kJT - 1) / kJT;
     return jb <= 4 ? 4 : jb <= 8 ? 8 : jb <= 16 ? 16 : jb <= 32 ? 32 : 64;
 }
+// Grid rows per thread of the column kernel: 4 where JB <= 16 and N needs them
+// (each staged tanh value then feeds 4 FMAs), 1 beyond.
 int pick_ib(int N, int JB) {
-    const int want = (N + kGroups - 1) / kGroups;  // cover N with one block of i groups
-    int ib = want <= 1 ? 1 : want <= 2 ? 2 : 4;
-    while (ib > 1 && ib * JB > (JB >= 32 ? 32 : 64)) ib >>= 1;
-    return ib;
+    if (JB >= 32) return 1;
+    return N <= 1 ? 1 : N <= 2 ? 2 : 4;
+}
+// i groups per row set: the smallest power of two covering N with IB rows each
+// (capped at kGroups); with JB >= 32 every group covers rows (one set), since
+// the sets' sums would not fit the shared memory of two blocks per SM.
+int pick_gn(int N, int IB, int JB) {
+    if (JB >= 32) return kGroups;
+    const int need = (N + IB - 1) / IB;
+    int gn = 1;
+    while (gn < need && gn < kGroups) gn <<= 1;
+    return gn;
 }
 template <int JT, int JB>
 cudaError_t rows_launch(FactArgs F, const float *v, float *u, cudaStream_t st, bool prepare) {
@@ -445,17 +490,21 @@ cudaError_t rows_dispatch(const FactArgs &F, const float *v, float *u, cudaStrea
     return rows_launch<8, 64>(F, v, u, st, prepare);
 }
 
-template <int IB, int JB> constexpr size_t cols_smem() {
+// Staging buffers, then weights and sign words; with row sets the staging
+// buffers must also hold every thread's IB JB + IB + JB sums.
+template <int IB, int JB> constexpr size_t cols_smem(bool sets) {
     constexpr size_t st = cols_stage(JB);
-    return (size_t(2) * 2 * st * kJT * JB + 2 * st) * sizeof(float) + size_t(2) * st * 2 * 8;
+    constexpr size_t stage = size_t(2) * 2 * st * kJT * JB, red = size_t(kThreads) * (IB * JB + IB + JB);
+    return ((sets && red > stage ? red : stage) + 2 * st) * sizeof(float) + size_t(2) * st * 2 * 8;
 }
 template <int IB, int JB>
 cudaError_t cols_launch(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, cudaStream_t st,
                         bool prepare) {
-    constexpr size_t smem = cols_smem<IB, JB>();
+    const int gn = pick_gn(F.N, IB, JB);
+    const size_t smem = cols_smem<IB, JB>(gn < kGroups);
     if (prepare) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_fcols<IB, JB>));
-    dim3 g(F.rchunks, F.K, (F.N + kGroups * IB - 1) / (kGroups * IB));
-    k_fcols<IB, JB><<<g, kThreads, smem, st>>>(F, mode, w, E, out);
+    dim3 g(F.rchunks, F.K, (F.N + gn * IB - 1) / (gn * IB));
+    k_fcols<IB, JB><<<g, kThreads, smem, st>>>(F, mode, gn, w, E, out);
     return cudaGetLastError();
 }
 template <int JB>
