@@ -323,6 +323,12 @@ template <class S> __global__ void k_minres_init_scalar(SolveBufs<S> B) {
     const unsigned long long mi = B.sp->maxit;
     q.cap = mi;
     q.running = (q.flag == kInternal && mi > 0) ? 1 : 0;
+    LzState &lz = *B.lz;
+    lz.j = 1;
+    lz.beta[0] = 0;
+    lz.beta[1] = beta1;
+    lz.beta[2] = 0;
+    lz.arrived = 0;
     if (!isfinite(beta1)) {
         atomicOr(B.err, kErrMinresNonFinite);
         q.running = 0;
@@ -338,6 +344,7 @@ template <class S> __global__ void k_minres_first_v(SolveBufs<S> B) {
     if (p < P) {
         const S v = B.r3[p] * (1.0 / beta);
         B.v[p] = v;
+        B.vq[size_t(1) * P + p] = v;
         mirror_f32(B.v32, p, v);
         t = B.o[p] * v;
     }
@@ -345,13 +352,15 @@ template <class S> __global__ void k_minres_first_v(SolveBufs<S> B) {
     if (threadIdx.x == 0) B.ovpart[blockIdx.x] = s;
 }
 
-// Lanczos part 1: r3 = S v - (beta/betal) r1; partials of Re(r3^H v).
+// Lanczos part 1 of step j: r3 = S v_j - (beta_j / beta_{j-1}) r1; partials
+// of Re(r3^H v_j). The Lanczos chain runs whether or not the QLP chain beside
+// it ends the solve (a step past the end only costs its time).
 template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(SolveBufs<S> B) {
     __shared__ double sh[32];
     __shared__ S ovs;
     __shared__ ColSumSmem<S> cs;
-    const QlpState &q = *B.qs;
-    if (!q.running) return;
+    const LzState &lz = *B.lz;
+    const unsigned long long j = lz.j;
     const int nb = mr_blocks(B.sh.P);
     if (threadIdx.x < 32) {
         S ov = warp_sum_array_s(B.ovpart, nb);
@@ -360,8 +369,8 @@ template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(
     const int P = B.sh.P, pl = threadIdx.x % kMrThreads, rg = threadIdx.x / kMrThreads;
     const int p = blockIdx.x * kMrThreads + pl;
     const S y = sv_colsum(B, p, pl, rg, cs);  // its barrier also publishes ovs
-    const bool first = q.iters == 0;
-    const double c1 = first ? 0.0 : q.betan / q.beta;  // beta_new / betal_new
+    const bool first = j == 1;
+    const double c1 = first ? 0.0 : lz.beta[j % 3] / lz.beta[(j - 1) % 3];  // beta_new / betal_new
     double t = 0.0;
     if (rg == 0 && p < P) {
         S r3 = sv_finish(B, p, B.v, ovs, y);
@@ -373,12 +382,13 @@ template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(
     if (threadIdx.x == 0) B.part[blockIdx.x] = t;
 }
 
-// Lanczos part 2: r3 -= (alfa/beta) r2; r1 = r2; r2 = r3; partials of |r3|^2.
+// Lanczos part 2 of step j: r3 -= (alfa_j / beta_j) r2; r1 = r2; r2 = r3;
+// partials of |r3|^2.
 template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
     __shared__ double sh[32];
     __shared__ double alfa_s;
-    const QlpState &q = *B.qs;
-    if (!q.running) return;
+    const LzState &lz = *B.lz;
+    const unsigned long long j = lz.j;
     const int nb = mr_blocks(B.sh.P);
     if (threadIdx.x < 32) {
         double a = warp_sum_array(B.part, nb);
@@ -386,7 +396,7 @@ template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
     }
     __syncthreads();
     const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
-    const double c2 = alfa_s / q.betan;  // alfa / beta_new
+    const double c2 = alfa_s / lz.beta[j % 3];  // alfa / beta_new
     double t = 0.0;
     if (p < P) {
         S r3 = B.r3[p] - B.r2[p] * c2;
@@ -397,6 +407,54 @@ template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
     }
     t = block_sum(t, sh);
     if (threadIdx.x == 0) B.part[kPartStride + blockIdx.x] = t;
+}
+
+// Lanczos part 3 of step j: beta_{j+1} = |r3|, v_{j+1} = r3 / beta_{j+1} (into
+// v, its FP32 mirror and the QLP chain's slot), o·v_{j+1} partials; the last
+// block to finish publishes alfa_j, |r3_j|^2 and beta_{j+1} and advances j
+// (every block read j before any block arrived).
+template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
+    __shared__ double sh[32];
+    __shared__ double s_alfa, s_bn2;
+    __shared__ int last;
+    LzState &lz = *B.lz;
+    const unsigned long long j = lz.j;
+    const int nb = mr_blocks(B.sh.P);
+    if (threadIdx.x < 32) {
+        const double a = warp_sum_array(B.part, nb);
+        const double b2 = warp_sum_array(B.part + kPartStride, nb);
+        if (threadIdx.x == 0) {
+            s_alfa = a;
+            s_bn2 = b2;
+        }
+    }
+    __syncthreads();
+    const double betan = sqrt(s_bn2);
+    const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
+    S *vq = B.vq + size_t((j + 1) % 3) * P;
+    S ovt = zero<S>();
+    if (p < P) {
+        const S vn = B.r3[p] * (1.0 / betan);
+        B.v[p] = vn;
+        vq[p] = vn;
+        mirror_f32(B.v32, p, vn);
+        ovt = B.o[p] * vn;
+    }
+    S s = block_sum_s(ovt, sh);
+    if (threadIdx.x == 0) {
+        B.ovpart[blockIdx.x] = s;
+        __threadfence();
+        last = atomicAdd(&lz.arrived, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        lz.alfa[j & 1] = s_alfa;
+        lz.bn2[j & 1] = s_bn2;
+        lz.beta[(j + 1) % 3] = betan;
+        lz.arrived = 0;
+        lz.j = j + 1;
+        __threadfence();
+    }
 }
 
 __device__ __forceinline__ double sgn(double a) { return copysign(1.0, a); }
@@ -601,25 +659,24 @@ template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) {
         if (B.use_cond && threadIdx.x == 0) cudaGraphSetConditional(B.cond, 0);
         return;
     }
-    const int nb = mr_blocks(B.sh.P);
-    const double alfa = warp_sum_array(B.part, nb);
-    const double bn2 = warp_sum_array(B.part + kPartStride, nb);
     if (threadIdx.x != 0) return;
     QlpState q = gq;
+    // alfa_j and |r3_j|^2 of this step, published by the Lanczos chain
+    const LzState &lz = *B.lz;
+    const unsigned long long j = q.iters + 1;
+    const double alfa = lz.alfa[j & 1], bn2 = lz.bn2[j & 1];
     qlp_scalar_step(B, q, alfa, bn2);
     gq = q;
 }
 
-// Vector part: w / x updates (code/minresqlp.h:253-299), then the next v and
-// its o·v partials.
+// Vector part: w / x updates (code/minresqlp.h:253-299) with v_j from the
+// QLP chain's slot.
 template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
-    __shared__ double sh[32];
     const QlpState &q = *B.qs;
     const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
     if (q.mode == 0 && !q.running) return;
-    S ovt = zero<S>();
     if (p < P) {
-        const S v = B.v[p];
+        const S v = B.vq[size_t(q.iters_snapshot % 3) * P + p];
         S w = B.w[p], wl = B.wl[p], wl2 = B.wl2[p], x = B.x[p], xl2 = B.xl2[p];
         const unsigned long long it = q.iters_snapshot;
         if (q.mode == 1 || q.mode == 4) {
@@ -662,16 +719,6 @@ template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
         B.wl2[p] = wl2;
         B.x[p] = x;
         B.xl2[p] = xl2;
-        if (q.running) {
-            const S vn = B.r3[p] * (1.0 / q.betan);
-            B.v[p] = vn;
-            mirror_f32(B.v32, p, vn);
-            ovt = B.o[p] * vn;
-        }
-    }
-    if (q.running) {
-        S s = block_sum_s(ovt, sh);
-        if (threadIdx.x == 0) B.ovpart[blockIdx.x] = s;
     }
 }
 
@@ -722,7 +769,7 @@ template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &B, cudaStr
     k_minres_init_vec<S><<<nb, kMrThreads, 0, st>>>(B);
     k_minres_init_scalar<S><<<1, 32, 0, st>>>(B);
     k_minres_first_v<S><<<nb, kMrThreads, 0, st>>>(B);
-    return cudaGetLastError();
+    return launch_lanczos_step(B, st);  // step 1; its QLP step runs in the first loop body
 }
 
 // u = O v then the row-chunk partials of O^H u. In the mixed form v must
@@ -741,14 +788,19 @@ template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, co
     return cudaGetLastError();
 }
 
-template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &B, cudaStream_t st) {
+template <class S> cudaError_t launch_lanczos_step(const SolveBufs<S> &B, cudaStream_t st) {
     const int nb = mr_blocks(B.sh.P);
     const cudaError_t e = launch_sv_passes(B, B.v, st);
     if (e != cudaSuccess) return e;
     k_lanczos_a<S><<<nb, kMrColThreads, 0, st>>>(B);
     k_lanczos_b<S><<<nb, kMrThreads, 0, st>>>(B);
+    k_lanczos_next<S><<<nb, kMrThreads, 0, st>>>(B);
+    return cudaGetLastError();
+}
+
+template <class S> cudaError_t launch_qlp_step(const SolveBufs<S> &B, cudaStream_t st) {
     k_qlp_scalar<S><<<1, 32, 0, st>>>(B);
-    k_qlp_vectors<S><<<nb, kMrThreads, 0, st>>>(B);
+    k_qlp_vectors<S><<<mr_blocks(B.sh.P), kMrThreads, 0, st>>>(B);
     return cudaGetLastError();
 }
 
@@ -806,7 +858,8 @@ cudaError_t launch_update(const Shape &sh, const StepParams *sp, const S *x, cpl
 #define NQES_INST(S)                                                                                     \
     template cudaError_t launch_moments<S>(const SolveBufs<S> &, cudaStream_t);                          \
     template cudaError_t launch_minres_init<S>(const SolveBufs<S> &, cudaStream_t);                      \
-    template cudaError_t launch_minres_iter<S>(const SolveBufs<S> &, cudaStream_t);                      \
+    template cudaError_t launch_lanczos_step<S>(const SolveBufs<S> &, cudaStream_t);                     \
+    template cudaError_t launch_qlp_step<S>(const SolveBufs<S> &, cudaStream_t);                         \
     template cudaError_t launch_apply_S<S>(const SolveBufs<S> &, const S *, S *, cudaStream_t);          \
     template cudaError_t launch_sv_rows_only<S>(const SolveBufs<S> &, cudaStream_t);                     \
     template cudaError_t launch_sv_cols_only<S>(const SolveBufs<S> &, cudaStream_t);                     \

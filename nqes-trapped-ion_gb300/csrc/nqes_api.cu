@@ -28,6 +28,8 @@ struct nqes_ctx {
     Shape sh{};
     int device = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t st_qlp = nullptr;                       // the QLP chain's capture stream
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // its fork from / join to st in the loop body
     double h = 0;
     int arith_opt = NQES_ARITH_AUTO;
     int precision = NQES_PRECISION_FP64;
@@ -60,6 +62,7 @@ struct nqes_ctx {
     void *tab = nullptr;  // ch, sh (K·N·M each), eup, edn (K·N each), sized for complex
     StepParams *sp = nullptr, *sp_host = nullptr;
     QlpState *qs = nullptr, *qs_host = nullptr;
+    LzState *lz = nullptr;
     int *err_d = nullptr, *err_host = nullptr;
     cplx *emat_d = nullptr, *eloc_d = nullptr, *emat_host = nullptr;
 
@@ -188,7 +191,7 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     // (the mixed form keeps its partials in ypart32)
     if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ypart), mixed ? 1 : 3 * size_t(ctx->rchunks) * P * ss)))
         return rc;
-    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->vecs), 14 * P * ss))) return rc;
+    if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->vecs), 16 * P * ss))) return rc;
     if ((rc = dalloc(ctx, reinterpret_cast<unsigned char **>(&ctx->ovpart), size_t(kPartStride) * ss))) return rc;
     if ((rc = dalloc(ctx, &ctx->part, size_t(3 * kPartStride)))) return rc;
     ctx->chains = chains;
@@ -235,7 +238,7 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     B.r2 = vec + 4 * P;
     B.r3 = vec + 5 * P;
     B.v = vec + 6 * P;
-    B.vn = vec + 7 * P;
+    B.vq = vec + 13 * P;  // 3 slots
     B.w = vec + 8 * P;
     B.wl = vec + 9 * P;
     B.wl2 = vec + 10 * P;
@@ -247,6 +250,7 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     B.part = ctx->part;
     B.ovpart = static_cast<S *>(ctx->ovpart);
     B.qs = ctx->qs;
+    B.lz = ctx->lz;
     B.sp = ctx->sp;
     B.emat = ctx->emat_d;
     B.eloc = ctx->eloc_d;
@@ -507,8 +511,16 @@ template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, 
     cudaGraph_t body = cp.conditional.phGraph_out[0];
     B.cond = cond;
     B.use_cond = 1;
+    // Loop body: the Lanczos step j + 1 on st beside the QLP step j (whose
+    // scalar kernel sets the loop condition) on st_qlp; the first Lanczos step
+    // ran before the loop.
     NQES_CUDA(cudaStreamBeginCaptureToGraph(ctx->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    le = launch_minres_iter<S>(B, ctx->st);
+    le = cudaEventRecord(ctx->ev_fork, ctx->st);
+    if (le == cudaSuccess) le = cudaStreamWaitEvent(ctx->st_qlp, ctx->ev_fork, 0);
+    if (le == cudaSuccess) le = launch_qlp_step<S>(B, ctx->st_qlp);
+    if (le == cudaSuccess) le = launch_lanczos_step<S>(B, ctx->st);
+    if (le == cudaSuccess) le = cudaEventRecord(ctx->ev_join, ctx->st_qlp);
+    if (le == cudaSuccess) le = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0);
     ce = cudaStreamEndCapture(ctx->st, &body);
     if (le != cudaSuccess || ce != cudaSuccess) {
         ctx->err = std::string("capture of the MINRES-QLP body: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
@@ -657,9 +669,10 @@ int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t 
         NQES_CUDA(cudaMemcpy(acc.data(), ctx->accepted, sizeof(unsigned long long) * chains, cudaMemcpyDeviceToHost));
         for (auto x : acc) info->accepted += x;
         if (q.flag == 8 && q.iters >= ctx->minres_cap && maxit > ctx->minres_cap) info->warnings |= 1;
-        // tables, sampler, 3 moment kernels, 3 MINRES-QLP init kernels, update,
-        // and 6 kernels per execution of the loop body
-        info->kernel_launches = 9 + 6 * q.bodies;
+        // tables, sampler, 3 moment kernels, 3 MINRES-QLP init kernels, the
+        // first Lanczos step (5), update, and 7 kernels per execution of the
+        // loop body (Lanczos step 5, QLP step 2)
+        info->kernel_launches = 14 + 7 * q.bodies;
         info->precision = ctx->step_precision;
         if (uses_mixed_sampler(ctx)) {
             std::vector<unsigned long long> ex(chains);
@@ -802,6 +815,12 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
         ctx->err = "cudaStreamCreate failed";
         return fail(NQES_ERR_CUDA);
     }
+    if (cudaStreamCreateWithFlags(&ctx->st_qlp, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        ctx->err = "cudaStreamCreate / cudaEventCreate failed";
+        return fail(NQES_ERR_CUDA);
+    }
     cudaEventCreate(&ctx->ev0);
     cudaEventCreate(&ctx->ev1);
     const size_t nw = size_t(K) * N * M, na = size_t(K) * N;
@@ -809,7 +828,8 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
     if ((rc = dalloc(ctx, &ctx->a, na)) || (rc = dalloc(ctx, &ctx->b, size_t(K) * M)) ||
         (rc = dalloc(ctx, &ctx->w, nw)) || (rc = dalloc(ctx, &ctx->J, size_t(N) * N)) ||
         (rc = dalloc(ctx, reinterpret_cast<cplx **>(&ctx->tab), 2 * nw + 2 * na)) ||
-        (rc = dalloc(ctx, &ctx->sp, 1)) || (rc = dalloc(ctx, &ctx->qs, 1)) || (rc = dalloc(ctx, &ctx->err_d, 1)) ||
+        (rc = dalloc(ctx, &ctx->sp, 1)) || (rc = dalloc(ctx, &ctx->qs, 1)) || (rc = dalloc(ctx, &ctx->lz, 1)) ||
+        (rc = dalloc(ctx, &ctx->err_d, 1)) ||
         (rc = dalloc(ctx, &ctx->emat_d, 16)) || (rc = dalloc(ctx, &ctx->eloc_d, 1)) ||
         (rc = dalloc(ctx, &ctx->mch, nw)) || (rc = dalloc(ctx, &ctx->msh, nw)) || (rc = dalloc(ctx, &ctx->meup, na)) ||
         (rc = dalloc(ctx, &ctx->medn, na)) || (rc = dalloc(ctx, &ctx->mw, nw)) || (rc = dalloc(ctx, &ctx->ma, na)) ||
@@ -868,6 +888,7 @@ int nqes_destroy(nqes_ctx *ctx) {
     dfree(ctx->dbnd);
     dfree(ctx->sp);
     dfree(ctx->qs);
+    dfree(ctx->lz);
     dfree(ctx->err_d);
     dfree(ctx->emat_d);
     dfree(ctx->eloc_d);
@@ -877,6 +898,9 @@ int nqes_destroy(nqes_ctx *ctx) {
     if (ctx->emat_host) cudaFreeHost(ctx->emat_host);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->st_qlp) cudaStreamDestroy(ctx->st_qlp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return NQES_OK;
@@ -1413,7 +1437,7 @@ extern "C" int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int
     const uint64_t rchunks = 32, nw = K * N * M, na = K * N;
     uint64_t b = mixed ? Ns * K * K * (((M + 3) & ~3ULL) + 1) * 4 : Ns * P * ss;  // O, or its factors (mixed)
     b += Ns * K * K * 16 + Ns * K * NW * 8 + uint64_t(chains) * 16;  // E, spins, accept / exact counts
-    b += Ns * ss + 3 * rchunks * P * ss + 14 * P * ss + 4 * kPartStride * 8;
+    b += Ns * ss + 3 * rchunks * P * ss + 16 * P * ss + 4 * kPartStride * 8;
     if (mixed) b += P * 4 + Ns * 4 + 3 * 256 * P * 4;
     b += (3 * nw + 2 * na + K * M) * 16 + N * N * 8;  // weights, FP64 tables (complex-sized), J
     b += nw * 4 * 2 + na * 4 * 2 + (nw + na + K * M) * 8;  // FP32 tables and FP64 copies of the real weights

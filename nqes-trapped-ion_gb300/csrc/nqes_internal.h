@@ -141,6 +141,18 @@ struct QlpState {
     int running;
 };
 
+// Lanczos-side scalars of MINRES-QLP. The Lanczos chain of step j (S v_j,
+// r3, the next v) runs beside the QLP chain of step j - 1, so the scalars the
+// QLP chain reads live in slots: beta_j at beta[j % 3], alfa_j and |r3_j|^2
+// (= beta_{j+1}^2) at alfa[j % 2] and bn2[j % 2]. j is the step whose v the
+// next S·v multiplies; arrived counts the blocks of the kernel that advances it.
+struct LzState {
+    double beta[3];
+    double alfa[2], bn2[2];
+    unsigned long long j;
+    unsigned int arrived;
+};
+
 // Reduction partial buffers: one slot per 64-element MINRES-QLP vector block.
 // P <= 4 * (128 + 512 + 128*512) gives at most 4136 blocks; three regions of
 // this stride live in SolveBufs::part (alfa, |r3|^2, |b|^2) and one in ovpart.
@@ -204,10 +216,13 @@ template <class S> struct SolveBufs {
     S *u;                // Ns: O v
     S *ypart;            // rchunks × P partial O^H u
     int rchunks;
-    S *r1, *r2, *r3, *v, *vn, *w, *wl, *wl2, *x, *xl2;
+    S *r1, *r2, *r3, *v, *w, *wl, *wl2, *x, *xl2;
+    S *vq;               // v_j for the QLP chain at vq + (j % 3) P (written two
+                         // loop bodies before the QLP step that reads it)
     double *part;        // reduction partials (>= 2 * 1024)
     S *ovpart;           // partial o·v
     QlpState *qs;
+    LzState *lz;
     const StepParams *sp;
     cplx *emat;          // K² mean E (unnormalised by N)
     cplx *eloc;          // mean trace
@@ -225,7 +240,11 @@ template <class S> struct SolveBufs {
 
 template <class S> cudaError_t launch_moments(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &b, cudaStream_t st);
-template <class S> cudaError_t launch_minres_iter(const SolveBufs<S> &b, cudaStream_t st);
+// One MINRES-QLP iteration as two chains: the Lanczos step (S v_j, r3,
+// v_{j+1}) and the QLP step of the previous iteration (scalar recurrence, w
+// and x updates); launch_minres_init also runs the first Lanczos step.
+template <class S> cudaError_t launch_lanczos_step(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_qlp_step(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &b, const S *v, S *out, cudaStream_t st);
 template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &b, cudaStream_t st);
