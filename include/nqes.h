@@ -122,6 +122,18 @@ int nqes_destroy(nqes_ctx *ctx);
 const char *nqes_last_error(const nqes_ctx *ctx);
 int nqes_set_option(nqes_ctx *ctx, int option, int64_t value);
 
+/* Local-energy form (nqes_set_hamiltonian). */
+#define NQES_HAM_ISING_LIKE 0      /* the nqes_create form: ising, periodicising, longrange, trappedion
+                                      (ising_like_hamiltonian, code/rbm.cc:1033-1062) */
+#define NQES_HAM_HEISENBERG_LIKE 1 /* H = sum_{i>j} J_ij (sx_i sx_j + sy_i sy_j + delta sz_i sz_j) with the
+                                      lower triangle of the nqes_create J: hs (J_ij = 1/d_ij^2, delta 1)
+                                      and xxz (J = -1 on the periodic chain's bonds, delta -1)
+                                      (hs_like_hamiltonian, code/rbm.cc:1064-1119); h is unused.
+                                      FP64 form only (NQES_PRECISION_FP64). */
+/* Select the local-energy form of the following SR steps, evaluations and
+ * runs. Replaces the choice of the `hamiltonian` callable in code/rbm.cc:1293-1325. */
+int nqes_set_hamiltonian(nqes_ctx *ctx, int form, double delta);
+
 /* Weights, reference layout, complex interleaved.  Replaces the in-memory
  * MultiRBM of code/rbm.cc:127-132 (load_rbm / dump_rbm read and write it). */
 int nqes_set_weights(nqes_ctx *ctx, const double *a, const double *b, const double *w);

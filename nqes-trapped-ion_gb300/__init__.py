@@ -25,6 +25,7 @@ ARITH_AUTO, ARITH_COMPLEX, ARITH_REAL = 0, 1, 2
 OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP, OPT_PRECISION = 1, 2, 3, 4
 OPT_REJECT_FILTER, OPT_MIXED_EXACT, OPT_AUTOTUNE, OPT_TENSOR_CORES = 5, 6, 7, 8
 PRECISION_FP64, PRECISION_MIXED, PRECISION_CERTIFIED = 0, 1, 2
+HAM_ISING_LIKE, HAM_HEISENBERG_LIKE = 0, 1
 
 EXPORTS = [
     "nqes_create", "nqes_destroy", "nqes_last_error", "nqes_set_option", "nqes_set_weights", "nqes_get_weights",
@@ -32,7 +33,7 @@ EXPORTS = [
     "nqes_get_accepts", "nqes_get_O", "nqes_get_moments", "nqes_get_solution", "nqes_apply_S", "nqes_time_kernel",
     "nqes_apply_S_static", "nqes_batch_create", "nqes_batch_destroy", "nqes_batch_last_error", "nqes_batch_sr_step",
     "nqes_footprint_bytes", "nqes_server_create", "nqes_server_submit", "nqes_server_poll", "nqes_server_status",
-    "nqes_server_destroy", "nqes_server_last_error", "nqes_server_times",
+    "nqes_server_destroy", "nqes_server_last_error", "nqes_server_times", "nqes_set_hamiltonian",
 ]
 KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
 
@@ -105,6 +106,7 @@ def load_library(path=None):
         "nqes_destroy": (i, [vp]),
         "nqes_last_error": (ctypes.c_char_p, [vp]),
         "nqes_set_option": (i, [vp, i, i64]),
+        "nqes_set_hamiltonian": (i, [vp, i, d]),
         "nqes_set_weights": (i, [vp, _dp, _dp, _dp]),
         "nqes_get_weights": (i, [vp, _dp, _dp, _dp]),
         "nqes_init_weights": (i, [vp, u64]),
@@ -214,6 +216,11 @@ class Context:
 
     def set_option(self, option, value):
         self._check(self.lib.nqes_set_option(self._h, option, int(value)))
+
+    def set_hamiltonian(self, form, delta=0.0):
+        """HAM_ISING_LIKE (the create-time J and h) or HAM_HEISENBERG_LIKE
+        (J_ij (sx sx + sy sy + delta sz sz) over the same J)."""
+        self._check(self.lib.nqes_set_hamiltonian(self._h, int(form), float(delta)))
 
     def set_weights(self, a, b, w):
         a = np.ascontiguousarray(a, np.complex128).reshape(self.K, self.N)

@@ -164,11 +164,24 @@ void dump_corrs(const std::vector<double> &x, const std::vector<double> &z, cons
     if (!nqes_cli::mat_write(fname, {{"x", X}, {"z", Z}, {"xx", XX}, {"zz", ZZ}}, err)) throw MatioCreateFileError(fname);
 }
 
-// The coupling of each ising-like model as 2 sum_{i>j} J_ij s_i s_j with J
-// in the lower triangle (code/rbm.cc:963-1031).
+// The coupling of each model in the lower triangle of J: the ising-like
+// models as 2 sum_{i>j} J_ij s_i s_j (code/rbm.cc:963-1031), the
+// Heisenberg-like ones as sum_{i>j} J_ij (sx sx + sy sy + delta sz sz)
+// (code/rbm.cc:1064-1089).
 std::vector<double> build_J(const nqes_cli::CmdArgs &args) {
     std::vector<double> J(size_t(N) * N, 0.0);
     switch (args.model) {
+    case Model::HS:  // J_ij = 1 / d_ij^2, d_ij = (N / pi) sin(pi (i - j) / N)
+        for (int i = 1; i < N; i++)
+            for (int j = 0; j < i; j++) {
+                const double d = std::sin(M_PI * (i - j) / N) * N / M_PI;
+                J[i * N + j] = 1.0 / (d * d);
+            }
+        break;
+    case Model::XXZ:  // -1 on the bonds of the periodic chain
+        for (int i = 1; i < N; i++) J[i * N + i - 1] = -1.0;
+        if (N > 2) J[(N - 1) * N + 0] = -1.0;
+        break;
     case Model::Ising:  // -sum_i s_i s_{i-1}
         for (int i = 1; i < N; i++) J[i * N + i - 1] = -0.5;
         break;
@@ -253,6 +266,8 @@ void run(const nqes_cli::CmdArgs &args) {
         std::cerr << "nqes: " << nqes_last_error(nullptr) << std::endl;
         std::exit(1);
     }
+    if (args.model == Model::HS || args.model == Model::XXZ)  // delta 1 (hs), -1 (xxz): code/rbm.cc:1314-1325
+        check(ctx, nqes_set_hamiltonian(ctx, NQES_HAM_HEISENBERG_LIKE, args.model == Model::HS ? 1.0 : -1.0));
     Weights rbm;
     if (!args.load_rbm.empty()) {
         rbm = load_rbm(args.load_rbm, K);
@@ -364,10 +379,6 @@ int main(int argc, char *argv[]) {
     const nqes_cli::CmdArgs args = nqes_cli::parse_args(argc, argv, welcome.str(), N * K < 32);
     if (!args.ncpus) {
         std::cerr << "Number of CPU cores cannot be zero." << std::endl;
-        return 1;
-    }
-    if (args.model == Model::HS || args.model == Model::XXZ) {
-        std::cerr << "models hs and xxz (two-spin-flip Hamiltonians) are not provided by this build" << std::endl;
         return 1;
     }
     run(args);

@@ -583,16 +583,20 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
                 }
         }
         // Ratios Phi(flip i in row k)[k][kk] / Phi[k][kk] for every (k, kk, i),
-        // the N single-flip terms of the transverse field (code/rbm.cc:1050-1058).
+        // the N single-flip terms of the transverse field (code/rbm.cc:1050-1058)
+        // and the x observables of the correlation pass.
+        const bool single = A.ham == 0 || A.corr;
         for (int it = tid; it < KK * N; it += T) {
             const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-            const bool down = spin_down(sm.spin + k * NW, i);
-            const S *crow = A.tab.ch + (size_t(kk) * N + i) * M;
-            const S *srow = A.tab.sh + (size_t(kk) * N + i) * M;
-            const S *trow = sm.tnh + q * M;
-            S p = one<S>();
-            for (int j = 0; j < M; j++) p = p * mad(neg_if(trow[j], !down), ldg(srow + j), ldg(crow + j));
-            sm.rat[it] = p * ldg((down ? A.tab.edn : A.tab.eup) + kk * N + i);
+            if (single) {
+                const bool down = spin_down(sm.spin + k * NW, i);
+                const S *crow = A.tab.ch + (size_t(kk) * N + i) * M;
+                const S *srow = A.tab.sh + (size_t(kk) * N + i) * M;
+                const S *trow = sm.tnh + q * M;
+                S p = one<S>();
+                for (int j = 0; j < M; j++) p = p * mad(neg_if(trow[j], !down), ldg(srow + j), ldg(crow + j));
+                sm.rat[it] = p * ldg((down ? A.tab.edn : A.tab.eup) + kk * N + i);
+            }
             // B(kk->k) sigma^{(kk)}_i for the a and w derivatives, where
             // B(kk->k) = (Phi^-1)[k][kk] Phi[kk][k] (closed form of the
             // determinants in code/rbm.cc:211-236).
@@ -608,14 +612,58 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         if (tid < K) {
             double jt = 0.0;
             for (int w2 = 0; w2 < nwarp; w2++) jt += sm.jpart[w2 * 4 + tid];
-            sm.jk[tid] = 2.0 * jt;
+            sm.jk[tid] = A.ham == 0 ? 2.0 * jt : A.delta * jt;
         }
         __syncthreads();
-        for (int q = warp; q < KK; q += nwarp) {
-            S acc = zero<S>();
-            for (int i = lane; i < N; i += 32) acc = acc + sm.rat[q * N + i];
-            acc = warp_sum(acc);
-            if (lane == 0) sm.Dm[q] = one<S>() * sm.jk[q / K] - A.h * acc;
+        if (A.ham == 0) {
+            for (int q = warp; q < KK; q += nwarp) {
+                S acc = zero<S>();
+                for (int i = lane; i < N; i += 32) acc = acc + sm.rat[q * N + i];
+                acc = warp_sum(acc);
+                if (lane == 0) sm.Dm[q] = one<S>() * sm.jk[q / K] - A.h * acc;
+            }
+        } else {
+            // Heisenberg-like (code/rbm.cc:1091-1119): for each pair i > j with
+            // J_ij != 0 and spins i, j of row k anti-aligned, the two-flip ratio
+            // Phi(flip i, j)[k][kk] / Phi[k][kk] = e^{-2 s_i a_i - 2 s_j a_j}
+            // prod_m [cosh(d_i + d_j) - tanh(theta_m) sinh(d_i + d_j)],
+            // d = 2 s w_{.m}, each factor formed as c_i (c_j - t u_j) + u_i (u_j - t c_j)
+            // from the per-step tables (c = cosh 2w, u = s sinh 2w); D_k =
+            // delta sum_{i>j} J_ij s_i s_j + 2 sum_{anti-aligned} J_ij ratio.
+            // Per (k, kk): the pairs strided over the block, per-warp partials
+            // added in warp order (deterministic).
+            for (int q = 0; q < KK; q++) {
+                const int k = q / K, kk = q - k * K;
+                const uint64_t *sk = sm.spin + k * NW;
+                const S *trow = sm.tnh + q * M;
+                S acc = zero<S>();
+                for (int pr = tid; pr < N * N; pr += T) {
+                    const int i = pr / N, j = pr - (pr / N) * N;
+                    if (j >= i) continue;
+                    const double p = A.J[size_t(i) * N + j];
+                    const bool di = spin_down(sk, i), dj = spin_down(sk, j);
+                    if (p == 0.0 || di == dj) continue;
+                    const S *ci = A.tab.ch + (size_t(kk) * N + i) * M, *si = A.tab.sh + (size_t(kk) * N + i) * M;
+                    const S *cj = A.tab.ch + (size_t(kk) * N + j) * M, *sj = A.tab.sh + (size_t(kk) * N + j) * M;
+                    S r = one<S>();
+                    for (int m = 0; m < M; m++) {
+                        const S t = trow[m], c1 = ldg(ci + m), c2 = ldg(cj + m);
+                        const S u1 = neg_if(ldg(si + m), di), u2 = neg_if(ldg(sj + m), dj);
+                        r = r * mad(c1, mad(neg_if(t, true), u2, c2), u1 * mad(neg_if(t, true), c2, u2));
+                    }
+                    r = r * ldg((di ? A.tab.edn : A.tab.eup) + kk * N + i) * ldg((dj ? A.tab.edn : A.tab.eup) + kk * N + j);
+                    acc = mad(one<S>() * (2.0 * p), r, acc);
+                }
+                acc = warp_sum(acc);
+                if (lane == 0) sm.red[warp] = acc;
+                __syncthreads();
+                if (tid == 0) {
+                    S tot = zero<S>();
+                    for (int w2 = 0; w2 < nwarp; w2++) tot = tot + sm.red[w2];
+                    sm.Dm[q] = one<S>() * sm.jk[k] + tot;
+                }
+                __syncthreads();
+            }
         }
         __syncthreads();
         if (tid == 0) {

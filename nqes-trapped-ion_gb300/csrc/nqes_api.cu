@@ -44,6 +44,8 @@ struct nqes_ctx {
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
     uint16_t *tcimg = nullptr;  // BF16 split image of v for the tensor-core rows pass
     int tensor_cores = 1;       // NQES_OPT_TENSOR_CORES: 0 off, 1 where it pays off, 2 wherever it fits
+    int ham = NQES_HAM_ISING_LIKE;  // local-energy form (nqes_set_hamiltonian)
+    double ham_delta = 0.0;
     int step_precision = NQES_PRECISION_FP64;      // precision of the allocated step buffers
     int tk_opt = 0;
     uint64_t minres_cap = 100000;
@@ -410,6 +412,8 @@ template <class S> SampleArgs<S> sample_args(nqes_ctx *ctx, int chains, int m, i
     A.w = ctx->w;
     A.J = ctx->J;
     A.h = ctx->h;
+    A.ham = ctx->ham;
+    A.delta = ctx->ham_delta;
     A.O = static_cast<S *>(ctx->O);
     A.E = ctx->E;
     A.spins = ctx->spins;
@@ -611,6 +615,10 @@ int step_prepare(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, doub
     const int arith = resolve_arith(ctx);
     if (ctx->precision == NQES_PRECISION_MIXED && arith != NQES_ARITH_REAL) {
         ctx->err = "mixed precision needs real weights (NQES_ARITH_REAL)";
+        return NQES_ERR_INVALID;
+    }
+    if (ctx->ham != NQES_HAM_ISING_LIKE && ctx->precision != NQES_PRECISION_FP64) {
+        ctx->err = "the Heisenberg-like local energy runs in the FP64 form (NQES_PRECISION_FP64)";
         return NQES_ERR_INVALID;
     }
     int rc = ensure_step_buffers(ctx, chains, m, arith);
@@ -903,6 +911,21 @@ int nqes_destroy(nqes_ctx *ctx) {
     if (ctx->st_qlp) cudaStreamDestroy(ctx->st_qlp);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
+    return NQES_OK;
+}
+
+int nqes_set_hamiltonian(nqes_ctx *ctx, int form, double delta) {
+    if (!ctx) return NQES_ERR_INVALID;
+    if ((form != NQES_HAM_ISING_LIKE && form != NQES_HAM_HEISENBERG_LIKE) || !std::isfinite(delta)) {
+        ctx->err = "hamiltonian form must be NQES_HAM_ISING_LIKE or NQES_HAM_HEISENBERG_LIKE, delta finite";
+        return NQES_ERR_INVALID;
+    }
+    ctx->ham = form;
+    ctx->ham_delta = delta;
+    if (ctx->exec) {  // the captured step bakes the sampler's arguments in
+        cudaGraphExecDestroy(ctx->exec);
+        ctx->exec = nullptr;
+    }
     return NQES_OK;
 }
 

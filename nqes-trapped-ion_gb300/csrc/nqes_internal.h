@@ -38,6 +38,11 @@ template <class S> struct SampleArgs {
     const cplx *a, *b, *w;      // weights, reference layout
     const double *J;            // N×N row-major
     double h;
+    // Local energy: ham 0, H = sum_{i>j} J_ij sz_i sz_j - h sum_i sx_i (the
+    // ising-like models); ham 1, H = sum_{i>j} J_ij (sx_i sx_j + sy_i sy_j +
+    // delta sz_i sz_j) (the Heisenberg-like models hs and xxz).
+    int ham;
+    double delta;
     S *O;                       // Ns × P log-derivatives (row s = c*m + t)
     cplx *E;                    // Ns × K² local-energy matrices
     uint64_t *spins;            // Ns × K × NW configurations

@@ -124,6 +124,8 @@ struct Oracle {
     int N, M, K, L, P, NW;
     std::vector<double> J;  // N×N row-major; the lower triangle J[i][j], i > j, is used
     double h;
+    int ham = 0;            // 0: ising-like (J, h); 1: Heisenberg-like (J, delta)
+    double delta = 0;
     std::vector<cplx> a, b, w;
 
     // Per-sample storage of the last sr_step, for the matrix-free S·v
@@ -236,10 +238,42 @@ struct Oracle {
         return r * 2.0;
     }
 
+    // Heisenberg-like: H = sum_{i>j} J_ij (sx_i sx_j + sy_i sy_j + delta sz_i sz_j)
+    // (code/rbm.cc:1091-1119): for every pair and row k, two sequential single
+    // flips when the spins differ (res += J (2 Phi' - delta Phi)), else
+    // res += J delta Phi; E = Phi^-1 res.
+    void local_energy_hs(const uint64_t *spin, const cplx *phi, const cplx *phi_inv,
+                         const cplx *tanh_theta, cplx *E) const {
+        const int KK = K * K;
+        std::vector<cplx> res(KK, cplx(0)), phip(KK), tp(size_t(M) * KK);
+        std::vector<uint64_t> sp(size_t(K) * NW);
+        for (int i = 1; i < N; i++)
+            for (int j = 0; j < i; j++) {
+                const double p = J[size_t(i) * N + j];
+                sp.assign(spin, spin + size_t(K) * NW);
+                phip.assign(phi, phi + KK);
+                tp.assign(tanh_theta, tanh_theta + size_t(M) * KK);
+                for (int k = 0; k < K; k++) {
+                    const uint64_t *sk = spin + size_t(k) * NW;
+                    if (spin_bit(sk, i) != spin_bit(sk, j)) {
+                        flip_state_fcn(k, i, sp.data(), phip.data(), tp.data());
+                        sp[size_t(k) * NW + (i >> 6)] ^= 1ULL << (i & 63);
+                        flip_state_fcn(k, j, sp.data(), phip.data(), tp.data());
+                        for (int kk = 0; kk < K; kk++)
+                            res[k * K + kk] += p * (2.0 * phip[k * K + kk] - delta * phi[k * K + kk]);
+                    } else {
+                        for (int kk = 0; kk < K; kk++) res[k * K + kk] += p * delta * phi[k * K + kk];
+                    }
+                }
+            }
+        small_mul(phi_inv, res.data(), E, K);
+    }
+
     // E = Phi^-1 (diag(J(s_k)) Phi - h sum_i Phi(flip i in every row))
     // (code/rbm.cc:1042-1062).
     void local_energy(const uint64_t *spin, const cplx *phi, const cplx *phi_inv,
                       const cplx *tanh_theta, cplx *E) const {
+        if (ham == 1) return local_energy_hs(spin, phi, phi_inv, tanh_theta, E);
         const int KK = K * K;
         std::vector<cplx> res(phi, phi + KK), sx(KK, cplx(0)), phip(KK), tp(size_t(M) * KK);
         for (int k = 0; k < K; k++) {
@@ -570,6 +604,11 @@ using nqes_oracle::C;
 extern "C" {
 
 void *orc_create(int N, int M, int K, const double *J, double h) { return new Oracle(N, M, K, J, h); }
+void orc_set_hamiltonian(void *op, int form, double delta) {
+    Oracle *o = static_cast<Oracle *>(op);
+    o->ham = form;
+    o->delta = delta;
+}
 void orc_destroy(void *o) { delete static_cast<Oracle *>(o); }
 
 void orc_set_weights(void *op, const double *a, const double *b, const double *w) {

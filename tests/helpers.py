@@ -37,6 +37,7 @@ def oracle_lib():
         vp, i, d, u64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_uint64
         sig = {
             "orc_create": (vp, [i, i, i, _dp, d]),
+            "orc_set_hamiltonian": (None, [vp, i, d]),
             "orc_destroy": (None, [vp]),
             "orc_set_weights": (None, [vp, _dp, _dp, _dp]),
             "orc_get_weights": (None, [vp, _dp, _dp, _dp]),
@@ -96,6 +97,9 @@ class Oracle:
             self.lib.orc_destroy(self.h)
         except Exception:
             pass
+
+    def set_hamiltonian(self, form, delta=0.0):
+        self.lib.orc_set_hamiltonian(self.h, int(form), float(delta))
 
     def set_weights(self, a, b, w):
         a = np.ascontiguousarray(a, np.complex128)

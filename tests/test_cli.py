@@ -141,3 +141,36 @@ def test_executable_matches_oracle_schedule(exe, tmp_path):
     assert np.allclose(c["z"], z[:, order], atol=1e-6)
     assert np.allclose(c["xx"], xx[:, order].reshape(N, N, K), atol=1e-6)
     assert np.allclose(c["zz"], zz[:, order].reshape(N, N, K), atol=1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("model", ["xxz", "hs"])
+def test_executable_heisenberg_models(exe, tmp_path, model):
+    """--model xxz / hs (code/rbm.cc:1064-1119, 1314-1325): the printed
+    energies follow the oracle through the same schedule."""
+    sio = pytest.importorskip("scipy.io")
+    from test_oracle_heisenberg import hs_j, xxz_j
+    N, M, K = 8, 16, 2
+    seed, chains, m, burn, niters = 17, 8, 25, 8, 3
+    w0 = helpers.random_weights(N, M, K, 0.05, 4, real=False)
+    wfile = str(tmp_path / "w0.mat")
+    sio.savemat(wfile, {"a": w0[0], "b": w0[1], "w": w0[2]})
+    args = [exe, "--model", model, "-h", "0", "-n", str(niters), "-m", str(m), "-c", str(chains), "--burn-in-steps", str(burn),
+            "--seed", str(seed), "--load-rbm", wfile, "--reglam-init", "5", "--minres-rtol", "1e-9", "--tol", "1e-12",
+            "--correlation-data", str(tmp_path / "corr.mat"), "--dump-rbm", str(tmp_path / "out")]
+    r = run(args)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.strip().split("\n")
+    got = np.array([[float(v) for v in ln.split()] for ln in lines[1:1 + niters]])
+    J, delta = (hs_j(N), 1.0) if model == "hs" else (xxz_j(N), -1.0)
+    orc = helpers.Oracle(N, M, K, J, 0.0)
+    orc.set_hamiltonian(1, delta)
+    orc.set_weights(*w0)
+    lr, reglam = 0.1, 5.0
+    want = []
+    for it in range(niters):
+        e, _ = orc.sr_step(seed + it * chains, chains, m, burn, max(lr, 0.01), max(reglam, 0.001), 1e-9, 2 ** 63)
+        lr *= 0.99
+        reglam *= 0.9
+        want.append(np.sort(np.linalg.eigvals(e / N).real))
+    assert np.allclose(got, np.array(want), rtol=0, atol=2e-5), (got, want)
