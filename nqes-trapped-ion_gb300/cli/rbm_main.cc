@@ -256,6 +256,50 @@ void fp_error_exit() {
     std::exit(127);
 }
 
+// --dump-states / --dump-ham / --dump-deriv (code/rbm.cc:473-524, 1150-1172):
+// Phi, E = Phi^+ H Phi or the log-derivatives O at every multi-spin
+// configuration (row k = bits k N .. k N + N - 1 of the enumeration index),
+// evaluated on the device in chunks, written as the complex variable "s" of
+// <prefix>N{N}M{M}K{K}.mat, dimensions [2^(K N), rows, cols] without the
+// singleton ones, column-major. Only built for K N < 32, as the reference.
+enum class DumpWhat { Phi, E, O };
+void dump_states(nqes_ctx *ctx, const std::string &prefix, DumpWhat what) {
+    if (N * K >= 32) return;
+    constexpr int L = N + M + N * M, P = K * L;
+    const uint64_t n = 1ULL << (K * N), mask = (1ULL << N) - 1;
+    const int rows = what == DumpWhat::O ? P : K, cols = what == DumpWhat::O ? 1 : K;
+    MatArray s;
+    s.is_complex = true;
+    s.dims = {size_t(n)};
+    if (rows > 1) s.dims.push_back(size_t(rows));
+    if (cols > 1) s.dims.push_back(size_t(cols));
+    s.re.assign(size_t(n) * rows * cols, 0.0);
+    s.im.assign(size_t(n) * rows * cols, 0.0);
+    const uint64_t chunk = 1ULL << 14;
+    std::vector<uint64_t> cfg(chunk * K);
+    std::vector<cplx> out(chunk * size_t(rows) * cols);
+    for (uint64_t base = 0; base < n; base += chunk) {
+        const int cnt = int(std::min<uint64_t>(chunk, n - base));
+        for (int c = 0; c < cnt; c++)
+            for (int k = 0; k < K; k++) cfg[size_t(c) * K + k] = ((base + c) >> (k * N)) & mask;
+        double *o = reinterpret_cast<double *>(out.data());
+        check(ctx, nqes_evaluate(ctx, cfg.data(), cnt, what == DumpWhat::Phi ? o : nullptr, nullptr,
+                                 what == DumpWhat::E ? o : nullptr, what == DumpWhat::O ? o : nullptr));
+        for (int c = 0; c < cnt; c++)
+            for (int i = 0; i < rows; i++)
+                for (int j = 0; j < cols; j++) {
+                    const cplx v = out[size_t(c) * rows * cols + size_t(i) * cols + j];
+                    const size_t at = (size_t(j) * rows + i) * n + base + c;
+                    s.re[at] = v.real();
+                    s.im[at] = v.imag();
+                }
+    }
+    std::ostringstream fname;
+    fname << prefix << "N" << N << "M" << M << "K" << K << ".mat";
+    std::string err;
+    if (!nqes_cli::mat_write(fname.str(), {{"s", s}}, err)) throw MatioCreateFileError(fname.str());
+}
+
 void run(const nqes_cli::CmdArgs &args) {
     std::random_device rd;
     const uint64_t seed = args.seed.value_or(rd());
@@ -289,10 +333,9 @@ void run(const nqes_cli::CmdArgs &args) {
     } else {
         check(ctx, nqes_init_weights(ctx, seed));
     }
-    if (!args.dump_states.empty() || !args.dump_ham.empty() || !args.dump_deriv.empty()) {
-        std::cerr << "--dump-states/--dump-ham/--dump-deriv are not provided by this build" << std::endl;
-        std::exit(1);
-    }
+    if (!args.dump_states.empty()) dump_states(ctx, args.dump_states, DumpWhat::Phi);
+    if (!args.dump_ham.empty()) dump_states(ctx, args.dump_ham, DumpWhat::E);
+    if (!args.dump_deriv.empty()) dump_states(ctx, args.dump_deriv, DumpWhat::O);
 
     double reglam = args.reglam0, lrate = args.lrate0;
     std::vector<double> best(K, 0.0);

@@ -548,7 +548,11 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         __syncthreads();
         if (tid == 0) {
             if (!small_inv(sm.phi, sm.pinv, K)) {
-                atomicOr(A.err, kErrSingular);
+                // Sampling stops with an error; an evaluation at given
+                // configurations (e.g. two equal rows) leaves E to
+                // k_eval_singular (the pseudo-inverse) and its O is zero, the
+                // determinants det(Phi^+ Phi~) of a rank-deficient product.
+                if (!A.cfg) atomicOr(A.err, kErrSingular);
                 for (int t = 0; t < KK; t++) sm.pinv[t] = zero<S>();
             }
         }
@@ -676,6 +680,8 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
                     ok = ok && finite(e);
                     A.E[s * KK + r * K + cc] = to_c(e);
                 }
+            if (A.cfg && A.dm_out)
+                for (int t = 0; t < KK; t++) A.dm_out[s * KK + t] = to_c(sm.Dm[t]);
             for (int k = 0; k < K; k++)
                 for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
             if (!ok) atomicOr(A.err, kErrNonFinite);
@@ -724,6 +730,31 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         __syncthreads();
     }
     if (writer && !A.cfg && A.accepted) A.accepted[c] = nacc;
+}
+
+// Evaluation at given configurations: where Phi (unscaled, phi) is rank
+// deficient (e.g. two equal rows, whose amplitudes the sampler's threads may
+// round differently), E = Phi^+ (D o Phi) with the Moore-Penrose
+// pseudo-inverse, as the reference's completeOrthogonalDecomposition()
+// .pseudoInverse() gives it (code/rbm.cc:1159-1171), and the configuration's
+// O row is zero (det(Phi^+ Phi~) of a rank-deficient product). One thread per
+// configuration; O rows are o_doubles doubles long.
+__global__ void k_eval_singular(int count, int K, const cplx *phi, const cplx *dm, cplx *E, double *O,
+                                size_t o_doubles) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= count) return;
+    const int KK = K * K;
+    cplx a[16], pinv[16], res[16];
+    for (int t = 0; t < KK; t++) a[t] = phi[size_t(c) * KK + t];
+    if (small_pinv(a, pinv, K) == K) return;
+    for (int t = 0; t < KK; t++) res[t] = dm[size_t(c) * KK + t] * a[t];
+    for (int r = 0; r < K; r++)
+        for (int cc = 0; cc < K; cc++) {
+            cplx e{0, 0};
+            for (int t = 0; t < K; t++) e = e + pinv[r * K + t] * res[t * K + cc];
+            E[size_t(c) * KK + r * K + cc] = e;
+        }
+    for (size_t t = 0; t < o_doubles; t++) O[size_t(c) * o_doubles + t] = 0.0;
 }
 
 // Per-step tables from the weights: cosh(2w), sinh(2w), exp(-2a), exp(2a).
@@ -795,6 +826,12 @@ template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads
     } else {
         launch_variant<S, false>(a, U, threads, smem, st);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_eval_singular(int count, int K, const cplx *phi, const cplx *dm, cplx *E, double *O,
+                                 size_t o_doubles, cudaStream_t st) {
+    k_eval_singular<<<(count + 127) / 128, 128, 0, st>>>(count, K, phi, dm, E, O, o_doubles);
     return cudaGetLastError();
 }
 

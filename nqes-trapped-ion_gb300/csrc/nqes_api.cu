@@ -1089,13 +1089,13 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
     const int arith = resolve_arith(ctx);
     const size_t KK = size_t(sh.K) * sh.K, ss = ssize(arith), words = size_t(count) * sh.K * sh.NW;
     uint64_t *cfg = nullptr, *sp = nullptr;
-    cplx *dphi = nullptr, *dth = nullptr, *dE = nullptr;
+    cplx *dphi = nullptr, *dth = nullptr, *dE = nullptr, *ddm = nullptr;
     unsigned char *dO = nullptr;
     int rc;
     if ((rc = dalloc(ctx, &cfg, words)) || (rc = dalloc(ctx, &sp, words)) || (rc = dalloc(ctx, &dphi, count * KK)) ||
         (rc = dalloc(ctx, &dth, count * KK * sh.M)) || (rc = dalloc(ctx, &dE, count * KK)) ||
-        (rc = dalloc(ctx, &dO, size_t(count) * sh.P * ss))) {
-        dfree(cfg); dfree(sp); dfree(dphi); dfree(dth); dfree(dE); dfree(dO);
+        (rc = dalloc(ctx, &ddm, count * KK)) || (rc = dalloc(ctx, &dO, size_t(count) * sh.P * ss))) {
+        dfree(cfg); dfree(sp); dfree(dphi); dfree(dth); dfree(dE); dfree(ddm); dfree(dO);
         return rc;
     }
     int status = NQES_OK;
@@ -1113,6 +1113,7 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
             A.cfg = cfg;
             A.phi_out = dphi;
             A.tanh_out = dth;
+            A.dm_out = ddm;
             NQES_CUDA(launch_sample<cplx>(A, sample_threads(sh.K, tk), ctx->st));
         } else {
             NQES_CUDA(prepare_sample<double>(sh));
@@ -1124,8 +1125,11 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
             A.cfg = cfg;
             A.phi_out = dphi;
             A.tanh_out = dth;
+            A.dm_out = ddm;
             NQES_CUDA(launch_sample<double>(A, sample_threads(sh.K, tk), ctx->st));
         }
+        NQES_CUDA(launch_eval_singular(count, sh.K, dphi, ddm, dE, reinterpret_cast<double *>(dO),
+                                       size_t(sh.P) * ss / sizeof(double), ctx->st));
         NQES_CUDA(cudaStreamSynchronize(ctx->st));
         if (phi) NQES_CUDA(cudaMemcpy(phi, dphi, count * KK * sizeof(cplx), cudaMemcpyDeviceToHost));
         if (tanh_theta) NQES_CUDA(cudaMemcpy(tanh_theta, dth, count * KK * sh.M * sizeof(cplx), cudaMemcpyDeviceToHost));
@@ -1146,7 +1150,7 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
         return NQES_OK;
     };
     status = run();
-    dfree(cfg); dfree(sp); dfree(dphi); dfree(dth); dfree(dE); dfree(dO);
+    dfree(cfg); dfree(sp); dfree(dphi); dfree(dth); dfree(dE); dfree(ddm); dfree(dO);
     return status;
 }
 

@@ -52,6 +52,7 @@ template <class S> struct SampleArgs {
     // kernel evaluates Phi / tanh(theta) / E / O at cfg[c] for c < chains.
     const uint64_t *cfg;
     cplx *phi_out, *tanh_out;   // chains × K², chains × M × K² (optional)
+    cplx *dm_out;               // chains × K²: E = Phi^-1 (D o Phi)'s D (optional)
     // Correlation mode (corr != nullptr): per-chain sums of the x, z, xx, zz
     // observables instead of E and O; layout per chain [x N×K²][z N×K²]
     // [xx N×N×K²][zz N×N×K²] (corr_stride scalars), scratch N×N×K² per chain.
@@ -63,6 +64,10 @@ template <class S> struct SampleArgs {
 };
 
 template <class S> cudaError_t launch_corr_reduce(const S *acc, int chains, size_t stride, S *out, cudaStream_t st);
+// E (pseudo-inverse) and O (zero) at the evaluated configurations whose Phi is
+// rank deficient; O rows of o_doubles doubles.
+cudaError_t launch_eval_singular(int count, int K, const cplx *phi, const cplx *dm, cplx *E, double *O,
+                                 size_t o_doubles, cudaStream_t st);
 
 // Mixed-precision sampler (real weights): FP32 factors, products and accept
 // decisions with a certified error bound, FP64 shadow of theta, exact FP64

@@ -204,4 +204,79 @@ template <class S> __host__ __device__ inline bool small_inv(const S *m, S *out,
     return true;
 }
 
+// Moore-Penrose pseudo-inverse of a K×K matrix (K <= 4), the role of Eigen's
+// completeOrthogonalDecomposition().pseudoInverse() (code/rbm.cc:547, 608),
+// by full-rank factorisation: the columns that Gram-Schmidt finds
+// independent (residual norm above 1e-14 of the largest column norm, a
+// relative rank threshold as the decomposition's) form C (K×r), A = C F with
+// F = (C^H C)^-1 C^H A, and A+ = F^H (F F^H)^-1 (C^H C)^-1 C^H. Returns the
+// rank r; a zero matrix gives zero.
+template <class S> __host__ __device__ inline int small_pinv(const S *a, S *out, int K) {
+    S q[16], c[16], f[16], g[16], gi[16], h[16], hi[16], t1[16];
+    int sel[4], r = 0;
+    double maxn = 0.0;
+    for (int j = 0; j < K; j++) {
+        double n = 0.0;
+        for (int i = 0; i < K; i++) n += norm2(a[i * K + j]);
+        maxn = n > maxn ? n : maxn;
+    }
+    for (int t = 0; t < K * K; t++) out[t] = zero<S>();
+    for (int j = 0; j < K && maxn > 0.0; j++) {
+        S v[4];
+        for (int i = 0; i < K; i++) v[i] = a[i * K + j];
+        for (int t = 0; t < r; t++) {
+            S d = zero<S>();
+            for (int i = 0; i < K; i++) d = d + conj(q[i * 4 + t]) * v[i];
+            for (int i = 0; i < K; i++) v[i] = v[i] - q[i * 4 + t] * d;
+        }
+        double n2 = 0.0;
+        for (int i = 0; i < K; i++) n2 += norm2(v[i]);
+        if (n2 > 1e-28 * maxn) {
+            const double s = 1.0 / sqrt(n2);
+            for (int i = 0; i < K; i++) q[i * 4 + r] = v[i] * s;
+            sel[r++] = j;
+        }
+    }
+    if (r == 0) return 0;
+    for (int i = 0; i < K; i++)  // C = the selected columns (K×r)
+        for (int t = 0; t < r; t++) c[i * r + t] = a[i * K + sel[t]];
+    for (int s1 = 0; s1 < r; s1++)  // G = C^H C (r×r)
+        for (int s2 = 0; s2 < r; s2++) {
+            S acc = zero<S>();
+            for (int i = 0; i < K; i++) acc = acc + conj(c[i * r + s1]) * c[i * r + s2];
+            g[s1 * r + s2] = acc;
+        }
+    if (!small_inv(g, gi, r)) return r;
+    for (int s1 = 0; s1 < r; s1++)  // t1 = G^-1 C^H (r×K)
+        for (int i = 0; i < K; i++) {
+            S acc = zero<S>();
+            for (int s2 = 0; s2 < r; s2++) acc = acc + gi[s1 * r + s2] * conj(c[i * r + s2]);
+            t1[s1 * K + i] = acc;
+        }
+    for (int s1 = 0; s1 < r; s1++)  // F = G^-1 C^H A (r×K)
+        for (int j = 0; j < K; j++) {
+            S acc = zero<S>();
+            for (int i = 0; i < K; i++) acc = acc + t1[s1 * K + i] * a[i * K + j];
+            f[s1 * K + j] = acc;
+        }
+    for (int s1 = 0; s1 < r; s1++)  // H = F F^H (r×r)
+        for (int s2 = 0; s2 < r; s2++) {
+            S acc = zero<S>();
+            for (int j = 0; j < K; j++) acc = acc + f[s1 * K + j] * conj(f[s2 * K + j]);
+            h[s1 * r + s2] = acc;
+        }
+    if (!small_inv(h, hi, r)) return r;
+    for (int j = 0; j < K; j++)  // A+ = F^H H^-1 (G^-1 C^H)
+        for (int i = 0; i < K; i++) {
+            S acc = zero<S>();
+            for (int s1 = 0; s1 < r; s1++) {
+                S u = zero<S>();
+                for (int s2 = 0; s2 < r; s2++) u = u + hi[s1 * r + s2] * t1[s2 * K + i];
+                acc = acc + conj(f[s1 * K + j]) * u;
+            }
+            out[j * K + i] = acc;
+        }
+    return r;
+}
+
 }  // namespace nqes

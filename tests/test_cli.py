@@ -174,3 +174,44 @@ def test_executable_heisenberg_models(exe, tmp_path, model):
         reglam *= 0.9
         want.append(np.sort(np.linalg.eigvals(e / N).real))
     assert np.allclose(got, np.array(want), rtol=0, atol=2e-5), (got, want)
+
+
+@pytest.mark.gpu
+def test_executable_dumps(exe, tmp_path):
+    """--dump-states / --dump-ham / --dump-deriv (code/rbm.cc:473-524,
+    1150-1172): Phi, E and O at all 2^(K N) configurations in the reference's
+    MAT layout (variable s, [2^(KN), rows, cols], column-major), against the
+    oracle at sampled configurations (the E of configurations with equal rows,
+    where the reference takes a pseudo-inverse, is checked in test_gpu_edges)."""
+    sio = pytest.importorskip("scipy.io")
+    N, M, K, h, seed = 8, 16, 2, 0.595, 5
+    w0 = helpers.random_weights(N, M, K, 0.05, 6, real=False)
+    wfile = str(tmp_path / "w0.mat")
+    sio.savemat(wfile, {"a": w0[0], "b": w0[1], "w": w0[2]})
+    pre = {k: str(tmp_path / k) for k in ("st", "ham", "der")}
+    args = [exe, "--model", "trappedion", "-h", str(h), "-n", "1", "-m", "4", "-c", "2", "--burn-in-steps", "2",
+            "--seed", str(seed), "--load-rbm", wfile, "--correlation-data", str(tmp_path / "corr.mat"),
+            "--dump-rbm", str(tmp_path / "out"), "--dump-states", pre["st"], "--dump-ham", pre["ham"],
+            "--dump-deriv", pre["der"]]
+    r = run(args)
+    assert r.returncode == 0, r.stderr
+    suffix = f"N{N}M{M}K{K}.mat"
+    st = sio.loadmat(pre["st"] + suffix)["s"]
+    ham = sio.loadmat(pre["ham"] + suffix)["s"]
+    der = sio.loadmat(pre["der"] + suffix)["s"]
+    P = K * (N + M + N * M)
+    assert st.shape == (2 ** (K * N), K, K) and ham.shape == (2 ** (K * N), K, K) and der.shape == (2 ** (K * N), P)
+    orc = helpers.Oracle(N, M, K, helpers.synthetic_j(N), h)
+    orc.set_weights(*w0)
+    rng = np.random.default_rng(1)
+    for idx in list(rng.integers(0, 2 ** (K * N), size=12)) + [0x1234, 2 ** (K * N) - 2]:
+        idx = int(idx)
+        rows = [(idx >> (k * N)) & ((1 << N) - 1) for k in range(K)]
+        if rows[0] == rows[1]:
+            continue
+        words = np.array([[r] for r in rows], dtype=np.uint64)
+        phi, _ = orc.state(words)
+        E, O = orc.local(words)
+        assert np.max(np.abs(st[idx] - phi)) <= 1e-12 * np.max(np.abs(phi))
+        assert np.max(np.abs(ham[idx] - E)) <= 1e-10 * np.max(np.abs(E))
+        assert np.max(np.abs(der[idx] - O)) <= 1e-10 * np.max(np.abs(O))

@@ -207,3 +207,43 @@ def test_invalid_step_arguments_leave_the_context_usable(pkg):
     e2, _ = ref.sr_step(*good)
     assert np.array_equal(e1, e2) and np.array_equal(s1, ref.get_samples()[0])
     ref.close()
+
+
+def psi_all(a, b, w, s):
+    return np.exp(a @ s) * np.prod(np.cosh(b + np.einsum("i,kim->km", s, w)), axis=1)
+
+
+def sig(v, n):
+    return np.array([-1.0 if (v >> i) & 1 else 1.0 for i in range(n)])
+
+
+@pytest.mark.parametrize("N,M,K,rows", [(6, 8, 2, (5, 5)), (5, 6, 3, (9, 3, 9)), (7, 5, 4, (1, 1, 1, 1))])
+def test_evaluate_singular_phi_uses_the_pseudo_inverse(pkg, N, M, K, rows):
+    """Evaluation at configurations with equal rows (Phi singular), as the
+    reference's --dump-ham enumerates them: E = Phi^+ (H Phi) with the
+    Moore-Penrose pseudo-inverse (code/rbm.cc:1159-1164), here against numpy's
+    pinv of the brute-force H Phi; O is zero (det(Phi^+ Phi~) of a
+    rank-deficient product)."""
+    J = synthetic_j(N)
+    h = 0.7
+    a, b, w = helpers.random_weights(N, M, K, 0.3, 3 + N, real=False)
+    ctx = pkg.Context(N, M, K, J, h)
+    ctx.set_weights(a, b, w)
+    cfg = np.array([[[r] for r in rows]], dtype=np.uint64)
+    phi, _, E, O = ctx.evaluate(cfg)
+    ctx.close()
+    S = [sig(r, N) for r in rows]
+    Phi = np.array([psi_all(a, b, w, S[k]) for k in range(K)])
+    assert rel_err(phi[0], Phi) < 1e-12
+    HPhi = np.zeros((K, K), complex)
+    for k in range(K):
+        s = S[k]
+        jt = sum(J[i, j] * s[i] * s[j] for i in range(N) for j in range(i))
+        HPhi[k] = 2.0 * jt * Phi[k]
+        for i in range(N):
+            sp = s.copy()
+            sp[i] = -sp[i]
+            HPhi[k] -= h * psi_all(a, b, w, sp)
+    Eref = np.linalg.pinv(Phi) @ HPhi
+    assert rel_err(E[0], Eref) < 1e-10
+    assert np.max(np.abs(O)) <= 1e-12 * max(1.0, np.max(np.abs(Phi)))
