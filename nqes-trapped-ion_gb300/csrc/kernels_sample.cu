@@ -316,7 +316,7 @@ template <class S> __device__ void corr_sample(const SampleArgs<S> &A, Smem<S> &
 // or underflow and large bounds all fall through to FP64.
 constexpr float kU32 = 5.9604645e-8f;  // FP32 unit roundoff 2^-24
 
-template <class S, int UMAX, bool FILT>
+template <class S, int UMAX, bool FILT, bool HEIS>
 __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, KK = K * K, L = A.sh.L;
@@ -549,10 +549,10 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         if (tid == 0) {
             if (!small_inv(sm.phi, sm.pinv, K)) {
                 // Sampling stops with an error; an evaluation at given
-                // configurations (e.g. two equal rows) leaves E to
-                // k_eval_singular (the pseudo-inverse) and its O is zero, the
-                // determinants det(Phi^+ Phi~) of a rank-deficient product.
-                if (!A.cfg) atomicOr(A.err, kErrSingular);
+                // configurations (e.g. two equal rows) leaves E and O to
+                // k_eval_singular (the pseudo-inverse; O is zero, the
+                // determinants det(Phi^+ Phi~) of a rank-deficient product).
+                atomicOr(A.err, kErrSingular);
                 for (int t = 0; t < KK; t++) sm.pinv[t] = zero<S>();
             }
         }
@@ -589,7 +589,7 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         // Ratios Phi(flip i in row k)[k][kk] / Phi[k][kk] for every (k, kk, i),
         // the N single-flip terms of the transverse field (code/rbm.cc:1050-1058)
         // and the x observables of the correlation pass.
-        const bool single = A.ham == 0 || A.corr;
+        const bool single = !HEIS || A.corr;
         for (int it = tid; it < KK * N; it += T) {
             const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
             if (single) {
@@ -616,15 +616,18 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
         if (tid < K) {
             double jt = 0.0;
             for (int w2 = 0; w2 < nwarp; w2++) jt += sm.jpart[w2 * 4 + tid];
-            sm.jk[tid] = A.ham == 0 ? 2.0 * jt : A.delta * jt;
+            sm.jk[tid] = HEIS ? A.delta * jt : 2.0 * jt;
         }
         __syncthreads();
-        if (A.ham == 0) {
+        if constexpr (!HEIS) {
             for (int q = warp; q < KK; q += nwarp) {
                 S acc = zero<S>();
                 for (int i = lane; i < N; i += 32) acc = acc + sm.rat[q * N + i];
                 acc = warp_sum(acc);
-                if (lane == 0) sm.Dm[q] = one<S>() * sm.jk[q / K] - A.h * acc;
+                if (lane == 0) {
+                    sm.Dm[q] = one<S>() * sm.jk[q / K] - A.h * acc;
+                    if (A.dm_out) A.dm_out[s * KK + q] = to_c(sm.Dm[q]);
+                }
             }
         } else {
             // Heisenberg-like (code/rbm.cc:1091-1119): for each pair i > j with
@@ -665,6 +668,7 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
                     S tot = zero<S>();
                     for (int w2 = 0; w2 < nwarp; w2++) tot = tot + sm.red[w2];
                     sm.Dm[q] = one<S>() * sm.jk[k] + tot;
+                    if (A.dm_out) A.dm_out[s * KK + q] = to_c(sm.Dm[q]);
                 }
                 __syncthreads();
             }
@@ -680,8 +684,7 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
                     ok = ok && finite(e);
                     A.E[s * KK + r * K + cc] = to_c(e);
                 }
-            if (A.cfg && A.dm_out)
-                for (int t = 0; t < KK; t++) A.dm_out[s * KK + t] = to_c(sm.Dm[t]);
+
             for (int k = 0; k < K; k++)
                 for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
             if (!ok) atomicOr(A.err, kErrNonFinite);
@@ -783,37 +786,42 @@ size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith) {
 int sample_threads(int K, int tk) { return K * tk; }
 
 // Raises the sampler's dynamic shared-memory limit; call outside stream capture.
-template <class S, bool FILT> cudaError_t prepare_variants() {
-    cudaError_t e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 1, FILT>));
+template <class S, bool FILT, bool HEIS> cudaError_t prepare_variants() {
+    cudaError_t e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 1, FILT, HEIS>));
     if (e == cudaSuccess)
-        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 2, FILT>));
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 2, FILT, HEIS>));
     if (e == cudaSuccess)
-        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 4, FILT>));
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 4, FILT, HEIS>));
     if (e == cudaSuccess)
-        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 8, FILT>));
+        e = allow_max_dynamic_smem(reinterpret_cast<const void *>(k_sample<S, 8, FILT, HEIS>));
     return e;
 }
 
 template <class S> cudaError_t prepare_sample(const Shape &) {
-    cudaError_t e = prepare_variants<S, false>();
+    cudaError_t e = prepare_variants<S, false, false>();
+    if (e == cudaSuccess) e = prepare_variants<S, false, true>();
     if constexpr (std::is_same<S, double>::value)
-        if (e == cudaSuccess) e = prepare_variants<S, true>();
+        if (e == cudaSuccess) e = prepare_variants<S, true, false>();
     return e;
 }
 
-template <class S, bool FILT> void launch_variant(const SampleArgs<S> &a, int U, int threads, size_t smem, cudaStream_t st) {
+template <class S, bool FILT, bool HEIS>
+void launch_variant(const SampleArgs<S> &a, int U, int threads, size_t smem, cudaStream_t st) {
     if (U <= 1)
-        k_sample<S, 1, FILT><<<a.chains, threads, smem, st>>>(a);
+        k_sample<S, 1, FILT, HEIS><<<a.chains, threads, smem, st>>>(a);
     else if (U <= 2)
-        k_sample<S, 2, FILT><<<a.chains, threads, smem, st>>>(a);
+        k_sample<S, 2, FILT, HEIS><<<a.chains, threads, smem, st>>>(a);
     else if (U <= 4)
-        k_sample<S, 4, FILT><<<a.chains, threads, smem, st>>>(a);
+        k_sample<S, 4, FILT, HEIS><<<a.chains, threads, smem, st>>>(a);
     else
-        k_sample<S, 8, FILT><<<a.chains, threads, smem, st>>>(a);
+        k_sample<S, 8, FILT, HEIS><<<a.chains, threads, smem, st>>>(a);
 }
 
 // Launch with the smallest compiled units-per-thread bound that covers M/TK;
-// the rejection filter runs when the FP32 tables are given (real arithmetic).
+// the rejection filter runs when the FP32 tables are given (real arithmetic)
+// and the local energy is ising-like (the Heisenberg-like form is its own
+// instantiation, without the filter: the filter only skips work, its
+// decisions are the unfiltered ones).
 template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads, cudaStream_t st) {
     const size_t smem = smem_bytes(a.sh.N, a.sh.M, a.sh.K, sizeof(S));
     const int U = (a.sh.M + a.tk - 1) / a.tk;
@@ -821,10 +829,12 @@ template <class S> cudaError_t launch_sample(const SampleArgs<S> &a, int threads
         return cudaErrorInvalidConfiguration;
     bool filt = false;
     if constexpr (std::is_same<S, double>::value) filt = a.c32 && a.s32 && a.eu32 && a.ed32;
-    if (filt) {
-        if constexpr (std::is_same<S, double>::value) launch_variant<S, true>(a, U, threads, smem, st);
+    if (a.ham) {
+        launch_variant<S, false, true>(a, U, threads, smem, st);
+    } else if (filt) {
+        if constexpr (std::is_same<S, double>::value) launch_variant<S, true, false>(a, U, threads, smem, st);
     } else {
-        launch_variant<S, false>(a, U, threads, smem, st);
+        launch_variant<S, false, false>(a, U, threads, smem, st);
     }
     return cudaGetLastError();
 }

@@ -1143,6 +1143,7 @@ int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi
         }
         int e = 0;
         NQES_CUDA(cudaMemcpy(&e, ctx->err_d, sizeof(int), cudaMemcpyDeviceToHost));
+        e &= ~int(kErrSingular);  // rank-deficient Phi: E and O come from k_eval_singular
         if (e) {
             ctx->err = "evaluation flagged error bits " + std::to_string(e);
             return NQES_ERR_NONFINITE;
