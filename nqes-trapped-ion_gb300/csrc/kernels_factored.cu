@@ -39,8 +39,9 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kJT = 8;       // j-threads per i group (columns)
 constexpr int kGroups = kThreads / kJT;
-// rows per double-buffered batch of the column kernel (64 KB of tanh rows)
-__host__ __device__ constexpr int cols_stage(int JB) { return JB >= 64 ? 8 : JB >= 32 ? 16 : 32; }
+// rows per double-buffered batch of the column kernel (at most 64 KB of tanh
+// rows): the narrow tiles take 64 rows, halving the barriers per row
+__host__ __device__ constexpr int cols_stage(int JB) { return JB >= 64 ? 8 : JB >= 16 ? (JB >= 32 ? 16 : 32) : 64; }
 constexpr int kMaxN = 128;
 
 __device__ __forceinline__ bool down_bit(const uint64_t *s, int i) { return (s[i >> 6] >> (i & 63)) & 1ULL; }
