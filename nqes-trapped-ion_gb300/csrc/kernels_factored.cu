@@ -58,7 +58,8 @@ __device__ __forceinline__ float sgn(uint64_t b0, uint64_t b1, int i) {
 // consecutive 16-byte pieces of a staged row: no bank conflicts). W_k is
 // staged in chunks of F.ic rows of JT JB floats (zero beyond M).
 template <int JT, int JB, int RB>
-__global__ void __launch_bounds__(kThreads, 2) k_frows(FactArgs F, const float *__restrict__ v, float *__restrict__ u) {
+__global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F, const float *__restrict__ v,
+                                                                     float *__restrict__ u) {
     extern __shared__ float4 smem4[];
     constexpr int WS = JT * JB, NG = kThreads / JT;
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K, IC = F.ic;
@@ -469,9 +470,9 @@ int pick_gn(int N, int IB, int JB) {
     while (gn < need && gn < kGroups) gn <<= 1;
     return gn;
 }
-template <int JT, int JB>
+template <int JT, int JB, int RB0 = 0>
 cudaError_t rows_launch(FactArgs F, const float *v, float *u, cudaStream_t st, bool prepare) {
-    constexpr int RB = JB >= 16 ? 64 / JB : 32 / JB, WS = JT * JB, NG = kThreads / JT;
+    constexpr int RB = RB0 ? RB0 : JB >= 16 ? 64 / JB : 32 / JB, WS = JT * JB, NG = kThreads / JT;
     F.ic = std::max(1, std::min(F.N, (48 * 1024 / 4) / WS));
     const size_t smem = (size_t(F.ic) * WS + ((F.N + 3) & ~3) + WS + NG * RB) * sizeof(float);
     if (prepare)
@@ -485,7 +486,7 @@ cudaError_t rows_dispatch(const FactArgs &F, const float *v, float *u, cudaStrea
     const int M = F.M;
     if (M <= 16) return rows_launch<4, 4>(F, v, u, st, prepare);
     if (M <= 32) return rows_launch<4, 8>(F, v, u, st, prepare);
-    if (M <= 64) return rows_launch<4, 16>(F, v, u, st, prepare);
+    if (M <= 64) return rows_launch<4, 16, 2>(F, v, u, st, prepare);  // 2 rows a group: 3 blocks per SM
     if (M <= 128) return rows_launch<8, 16>(F, v, u, st, prepare);
     if (M <= 256) return rows_launch<8, 32>(F, v, u, st, prepare);
     return rows_launch<8, 64>(F, v, u, st, prepare);
