@@ -37,7 +37,7 @@ __device__ __forceinline__ cplx ldg(const cplx *p) {
 }
 template <class S> __device__ __forceinline__ double re_dot(S a, S b) { return re(a) * re(b) + im(a) * im(b); }
 
-// Block sum of a double over kVecThreads threads (fixed order).
+// Block sum of a double over the block's threads (a multiple of 32, fixed order).
 __device__ double block_sum(double v, double *sh) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_sum(v);
