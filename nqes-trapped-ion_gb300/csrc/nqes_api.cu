@@ -1482,7 +1482,7 @@ struct nqes_batch {
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t exec = nullptr;
-    std::vector<std::vector<long long>> keys;  // per member: chains, samples, burn, arith, tk, precision
+    std::vector<std::vector<long long>> keys;  // per member: what its captured nodes depend on (see the step)
     std::string err;
 };
 
@@ -1563,7 +1563,13 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
             return rc;
         }
         tks[i] = choose_tk(c, chains[i]);
-        keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision};
+        // everything the captured nodes bake in: counts, arithmetic, launch shape,
+        // precision, local-energy form and the options that select kernels
+        long long delta_bits = 0;
+        std::memcpy(&delta_bits, &c->ham_delta, sizeof(delta_bits));
+        keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision, c->ham, delta_bits,
+                   c->tensor_cores, c->reject_filter ? 1 : 0, c->mixed_exact_all ? 1 : 0, c->dw_force_warps,
+                   c->dw_force_stage};
     }
     if (!b->exec || keys != b->keys) {
         if (b->exec) {
