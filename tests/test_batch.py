@@ -83,3 +83,29 @@ def test_autotune_keeps_the_chains(pkg, prec):
     assert np.array_equal(out[0][1], out[1][1])
     for a, b in zip(out[0][0], out[1][0]):
         assert np.max(np.abs(a - b)) <= 1e-9 * np.max(np.abs(b))
+
+
+def test_batch_rebuilds_after_a_member_changes_its_hamiltonian(pkg):
+    """A member switched to the Heisenberg-like local energy between batched
+    steps gets that energy in the next batched step (the batch graph is
+    rebuilt), equal to stepping a context set up that way alone."""
+    from test_oracle_heisenberg import xxz_j
+    N, M, K = 8, 16, 2
+    w = helpers.random_weights(N, M, K, 0.05, 7, real=True)
+    member = pkg.Context(N, M, K, xxz_j(N), 0.0)
+    member.set_weights(*w)
+    batch = pkg.Batch([member])
+    args = ([31], [8], [10], [4], [0.1], [5.0], [1e-9], [2000])
+    batch.sr_step(*args)  # ising-like form with the xxz couplings
+    member.set_weights(*w)
+    member.set_hamiltonian(pkg.HAM_HEISENBERG_LIKE, -1.0)
+    emats, _, stats, _ = batch.sr_step(*args)
+    assert stats == [0]
+    alone = pkg.Context(N, M, K, xxz_j(N), 0.0)
+    alone.set_weights(*w)
+    alone.set_hamiltonian(pkg.HAM_HEISENBERG_LIKE, -1.0)
+    e, _ = alone.sr_step(31, 8, 10, 4, 0.1, 5.0, 1e-9, 2000)
+    assert np.array_equal(e, emats[0])
+    batch.close()
+    member.close()
+    alone.close()
