@@ -165,7 +165,11 @@ int nqes_correlations(nqes_ctx *ctx, uint64_t seed, int chains, int samples_per_
  * column k*K+kk), E = Phi^-1 H Phi (K×K complex) and O (P complex) at `count`
  * given configurations (count × K × ceil(N/64) words); any output may be
  * NULL.  The same device code the sampler runs per sample (state_fcn,
- * ising_like_hamiltonian, deriv: code/rbm.cc:146-171, 1042-1062, 199-239). */
+ * ising_like_hamiltonian or hs_like_hamiltonian, deriv: code/rbm.cc:146-171,
+ * 1042-1062, 1091-1119, 199-239).  Where Phi is rank deficient (e.g. two equal
+ * rows, as the --dump-* enumerations of code/rbm.cc:473-524 meet them), E uses
+ * the Moore-Penrose pseudo-inverse, the reference's pseudoInverse(), and O is
+ * zero. */
 int nqes_evaluate(nqes_ctx *ctx, const uint64_t *configs, int count, double *phi, double *tanh_theta, double *E,
                   double *O);
 /* Per-sample records of the last SR step: configurations (Ns × K × words),
