@@ -342,6 +342,26 @@ def precision_form(pkg, chains, samples, steps, local):
                        % (small, samples)}
 
 
+def step_seed(rank, t, chains):
+    """Seed of SR step t on replica `rank`: the reference's seed + t * chains
+    (code/rbm.cc:1179), offset per replica so that replicas sample
+    independent chains."""
+    return SEED + rank * 1000003 + t * chains
+
+
+def max_over_ranks(x, world):
+    """The largest of every rank's x (the timed region ends when the slowest
+    replica does); a CPU tensor under gloo, a device tensor under NCCL."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    tt = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -367,7 +387,7 @@ def run_ours(args):
     infos = []
     for t in range(args.warmup):
         lr, reglam = schedule(t)
-        ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        ctx.sr_step(step_seed(rank, t, chains), chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
     a_start, b_start, w_start = ctx.get_weights()  # the end-to-end leg replays the timed steps from here
     clocks = ClockSampler(local)
     barrier()
@@ -375,16 +395,12 @@ def run_ours(args):
     t_wall0 = time.perf_counter()
     for t in range(args.warmup, args.warmup + args.steps):
         lr, reglam = schedule(t)
-        _, info = ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        _, info = ctx.sr_step(step_seed(rank, t, chains), chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
         infos.append(info)
     barrier()
     t_wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
-    dev_ms = sum(i["ms_total"] for i in infos)
-    if world > 1:
-        tt = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(tt.item())
+    dev_ms = max_over_ranks(sum(i["ms_total"] for i in infos), world)
     value = world * args.steps * ns / (dev_ms * 1e-3)
 
     # ---- per-kernel timing for the roofline (same data, same stream) ----
@@ -430,14 +446,10 @@ def run_ours(args):
     for t in range(args.warmup, args.warmup + args.steps):
         lr, reglam = schedule(t)
         ctx.set_weights(a_h, b_h, w_h)
-        ctx.sr_step(SEED + rank * 1000003 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        ctx.sr_step(step_seed(rank, t, chains), chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
         a_h, b_h, w_h = ctx.get_weights()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = world * args.steps * ns / e2e_s
 
     out = {
