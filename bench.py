@@ -513,7 +513,10 @@ def run_ours(args):
                      "frac": ach / hbm, "traffic": traffic, "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
                      "note": ("the sampler is bound by the serial latency of each chain's proposals (one chain per "
                               "SM at 128 chains), not by HBM or a tensor pipe: its HBM fraction is the bytes it "
-                              "writes (O, E, spins) over its time" if dom == "sample" else ""),
+                              "writes (O, E, spins) over its time; every FP64 warp instruction holds its SM "
+                              "sub-partition's FP64 pipe ~64 cycles, and the ncu capture in "
+                              "profiles/k_sample_fp64_N32M64K2_128chains.md shows the FP64 pipe 51 % active "
+                              "with 29 FP64 warp instructions per proposal" if dom == "sample" else ""),
                      "sv": {"achieved_gbs": sv_gbs, "frac_hbm": sv_gbs / hbm,
                             "achieved_fp64_tflops": sv_tf, "peak_fp64_tflops_dgemm": fp64_tf,
                             "frac_fp64": sv_tf / fp64_tf}},
