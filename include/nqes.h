@@ -203,13 +203,15 @@ int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double
  * pointer is DEVICE memory the caller owns: O is n_samples × n_params
  * row-major, o, skk, v and out have n_params entries; complex_arith = 1 means
  * interleaved complex doubles, 0 means real doubles. `stream` is the
- * cudaStream_t to run on (NULL: the default stream); the call returns once
- * the work is queued.
+ * cudaStream_t to run on (NULL: the default stream of the current device);
+ * the call runs on the stream's device, makes it current meanwhile, and
+ * returns once the work is queued.
  * Intermediates live in a 16 MiB file-scope device array that every GPU
  * loading the library holds until exit; n_samples + n_params + ceil(n_params/256)
  * scalars must fit in it, larger sizes are rejected with NQES_ERR_INVALID.
- * The first call on a device looks the array's address up (make it before
- * any stream capture). Calls share the array: overlapping calls race.
+ * The first call on a device looks the array's address up for that device
+ * (make it before any stream capture). Calls share the array: overlapping
+ * calls race.
  * Errors are described by nqes_last_error(NULL). */
 int nqes_apply_S_static(const double *O, const double *o, const double *skk, const double *v, double *out,
                         int64_t n_samples, int64_t n_params, int complex_arith, void *stream);

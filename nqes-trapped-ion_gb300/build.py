@@ -9,6 +9,7 @@ extension machinery: the library is a plain C-ABI shared object.
 import concurrent.futures as cf
 import os
 import shutil
+import struct
 import subprocess
 import sys
 
@@ -77,9 +78,37 @@ CLI = os.path.join(PKG, "cli")
 BINDIR = os.path.join(PKG, "bin")
 CLI_SOURCES = ["cmdline.cc", "matv5.cc"]
 CLI_HEADERS = ["cmdline.h", "matv5.h", "small_eig.h"]
-# The reference's build list (code/build.sh:28) plus the K=4 precision shape.
+JMATDIR = os.path.join(CLI, "jmat")
+# The reference's build list (code/build.sh:28), the K=4 precision shape and
+# N50 M150 K2, the shape of the reference's published trapped-ion runs
+# (data/energy/ion_N50_M150_K2_*).
 DEFAULT_SHAPES = [(8, 16, 2), (8, 32, 2), (16, 32, 2), (16, 64, 2), (32, 64, 2), (32, 128, 2), (64, 128, 2),
-                  (64, 256, 2), (128, 256, 2), (64, 128, 4)]
+                  (64, 256, 2), (128, 256, 2), (64, 128, 4), (50, 150, 2)]
+
+
+def jmat_header(n):
+    """Jmat{n}.h in the build folder: the reference's compiled-in couplings
+    (code/build.sh:34 writes them with code/load_jmat.py) as
+    `RealScalar Jmat[n][n]`, each value an exact hexadecimal floating literal,
+    from cli/jmat/Ising2d_N{n}_alpha1.0.f64 (raw little-endian float64,
+    row-major; written by cli/jmat/make_jmat.py). None when there is no file for n."""
+    src = os.path.join(JMATDIR, f"Ising2d_N{n}_alpha1.0.f64")
+    if not os.path.exists(src):
+        return None
+    os.makedirs(OBJDIR, exist_ok=True)
+    hdr = os.path.join(OBJDIR, f"Jmat{n}.h")
+    if _stale(hdr, [src]):
+        with open(src, "rb") as f:
+            raw = f.read()
+        if len(raw) != 8 * n * n:
+            raise RuntimeError(f"{src}: {len(raw)} bytes, expected {8 * n * n}")
+        vals = struct.unpack(f"<{n * n}d", raw)
+        rows = ["{" + ",".join(float.hex(v) for v in vals[i * n:(i + 1) * n]) + "}" for i in range(n)]
+        tmp = hdr + ".tmp"
+        with open(tmp, "w") as f:
+            f.write(f"RealScalar Jmat[{n}][{n}] = {{\n" + ",\n".join(rows) + "};\n")
+        os.replace(tmp, hdr)
+    return hdr
 
 
 def _gxx():
@@ -101,11 +130,13 @@ def _cli_binary(shape, objs, lib):
     n, m, k = shape
     name = f"rbm-matfree-N{n}-M{m}-K{k}-opt"
     out = os.path.join(BINDIR, name)
+    jh = jmat_header(n)
     deps = [os.path.join(CLI, "rbm_main.cc"), lib, os.path.join(INCLUDE, "nqes.h")] + objs + \
-        [os.path.join(CLI, h) for h in CLI_HEADERS]
+        [os.path.join(CLI, h) for h in CLI_HEADERS] + ([jh] if jh else [])
     if _stale(out, deps):
+        jdef = [f'-DJMAT_INC="{os.path.basename(jh)}"', "-I", OBJDIR] if jh else []
         cmd = [_gxx(), "-std=c++20", "-O2", f"-DNUM_SPINS={n}", f"-DNUM_HIDDEN_UNITS={m}", f"-DNUM_EIGENSTATES={k}",
-               "-I", INCLUDE, "-I", CLI, os.path.join(CLI, "rbm_main.cc"), *objs, "-L", LIBDIR, "-lnqes",
+               *jdef, "-I", INCLUDE, "-I", CLI, os.path.join(CLI, "rbm_main.cc"), *objs, "-L", LIBDIR, "-lnqes",
                "-Wl,-rpath,$ORIGIN/../lib", "-o", out]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -155,8 +155,12 @@ CmdArgs parse_args(int argc, char **argv, const std::string &welcome, bool with_
         add("dump-deriv", "If specified, will dump the derivatives for each spin config to the file with the given "
                           "prefix.", false, "", str(a.dump_deriv));
     }
-    add("jmat", "MAT file holding the N x N coupling matrix J (default: J_ij = |i-j|^-1.2).", false, "",
-        str(a.jmat));
+    add("jmat",
+        "Trapped-ion couplings: a MAT file holding the N x N matrix J, or 'synthetic' for the chain "
+        "J_ij = |i-j|^-1.2 (default: the compiled-in Jmat/Ising2d_N{N}_alpha1.0.mat).",
+        false, "", str(a.jmat));
+    add("dump-jmat", "If specified, write the coupling matrix J this run would use to the given .mat file "
+                     "(variable J) and exit.", false, "", str(a.dump_jmat));
     add("device", "CUDA device to run on.", false, "0", integer(a.device));
     bool help = false;
     add("?,help", "print help", false, "false", boolean(help), true);

@@ -31,7 +31,8 @@ struct CmdArgs {
     bool throw_fperror = false, apply_gauge = false, inverse_gauge = false;
     std::string dump_states, dump_ham, dump_deriv;
     // options of this build that the reference does not have
-    std::string jmat;  // MAT file with an N×N variable "J" (replaces the compiled-in Jmat)
+    std::string jmat;  // MAT file with an N×N variable "J", or "synthetic" (replaces the compiled-in Jmat)
+    std::string dump_jmat;  // write the J of this run to a MAT file and exit (no device needed)
     int device = 0;
 };
 

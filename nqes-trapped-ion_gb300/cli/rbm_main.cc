@@ -195,7 +195,11 @@ std::vector<double> build_J(const nqes_cli::CmdArgs &args) {
         break;
     case Model::TrappedIon:
     default:
-        if (!args.jmat.empty()) {
+        if (args.jmat == "synthetic") {
+            // the power-law chain J_ij = |i-j|^-1.2 (max |J| = 1) of the benchmark inputs
+            for (int i = 0; i < N; i++)
+                for (int j = 0; j < N; j++) J[i * N + j] = i == j ? 0.0 : std::pow(double(std::abs(i - j)), -1.2);
+        } else if (!args.jmat.empty()) {
             std::map<std::string, MatArray> vars;
             std::string err;
             if (!nqes_cli::mat_read(args.jmat, vars, err)) throw MatioCreateFileError(args.jmat);
@@ -207,14 +211,17 @@ std::vector<double> build_J(const nqes_cli::CmdArgs &args) {
                 for (int j = 0; j < N; j++) J[i * N + j] = it->second.re[size_t(j) * N + i];
         } else {
 #ifdef JMAT_INC
+            // The reference's compiled-in couplings (code/build.sh:34-41, code/rbm.cc:1015):
+            // Jmat/Ising2d_N{N}_alpha1.0.mat, generated into Jmat{N}.h by build.py.
             using RealScalar = double;
 #include JMAT_INC
+            static_assert(sizeof(Jmat) == sizeof(double) * N * N, "Jmat must be N x N");
             for (int i = 0; i < N; i++)
                 for (int j = 0; j < N; j++) J[i * N + j] = Jmat[i][j];
 #else
-            // synthetic trapped-ion chain: J_ij = |i-j|^-1.2, max |J| = 1
-            for (int i = 0; i < N; i++)
-                for (int j = 0; j < N; j++) J[i * N + j] = i == j ? 0.0 : std::pow(double(std::abs(i - j)), -1.2);
+            // The reference has no Jmat file for this N and would not compile.
+            throw CliError("no compiled-in trapped-ion couplings for N = " + std::to_string(N) +
+                           "; pass --jmat <file.mat> or --jmat synthetic");
 #endif
         }
         break;
@@ -305,6 +312,16 @@ void run(const nqes_cli::CmdArgs &args) {
     const uint64_t seed = args.seed.value_or(rd());
     std::cout << "Random seed is " << seed << std::endl;
     const std::vector<double> J = build_J(args);
+    if (!args.dump_jmat.empty()) {
+        MatArray A;
+        A.dims = {size_t(N), size_t(N)};
+        A.re.resize(size_t(N) * N);
+        for (int i = 0; i < N; i++)
+            for (int j = 0; j < N; j++) A.re[size_t(j) * N + i] = J[size_t(i) * N + j];  // column-major
+        std::string err;
+        if (!nqes_cli::mat_write(args.dump_jmat, {{"J", A}}, err)) throw MatioCreateFileError(args.dump_jmat);
+        return;
+    }
     nqes_ctx *ctx = nullptr;
     if (nqes_create(N, M, K, J.data(), args.h, args.device, &ctx) != NQES_OK) {
         std::cerr << "nqes: " << nqes_last_error(nullptr) << std::endl;

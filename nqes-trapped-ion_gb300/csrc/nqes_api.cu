@@ -79,6 +79,11 @@ struct nqes_ctx {
     double *part = nullptr;
     int rchunks = 1;
 
+    // Generation of the step buffers: bumped whenever they are freed or
+    // reallocated, so that a batch graph that baked in the old addresses is
+    // never replayed on new ones.
+    uint64_t buf_gen = 0;
+
     cudaGraphExec_t exec = nullptr;
     int g_chains = -1, g_m = -1, g_burn = -1, g_arith = -1, g_tk = -1, g_prec = -1;
     bool have_step = false;
@@ -139,6 +144,7 @@ void free_step_buffers(nqes_ctx *ctx) {
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
     ctx->exec = nullptr;
     ctx->g_chains = -1;
+    ctx->buf_gen++;
     ctx->chains = ctx->m = 0;
     ctx->Ns = 0;
     ctx->have_step = false;
@@ -1569,7 +1575,7 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
         std::memcpy(&delta_bits, &c->ham_delta, sizeof(delta_bits));
         keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision, c->ham, delta_bits,
                    c->tensor_cores, c->reject_filter ? 1 : 0, c->mixed_exact_all ? 1 : 0, c->dw_force_warps,
-                   c->dw_force_stage};
+                   c->dw_force_stage, (long long)c->buf_gen};
     }
     if (!b->exec || keys != b->keys) {
         if (b->exec) {

@@ -13,8 +13,10 @@
 // GPU that loads libnqes holds it until the process exits. Host code cannot
 // pass the array's name to a kernel (in host code it is only a stand-in, not a
 // device address), so the first call on each device looks its address up with
-// cudaGetSymbolAddress while that device is current and caches it; make that
-// first call before any stream capture begins. Every call shares the one array
+// cudaGetSymbolAddress while that device is current and caches it. The device
+// is the one `stream` belongs to (the current device for the NULL stream); the
+// call makes it current while it runs. Make the first call on each device
+// before any stream capture begins. Every call shares the one array
 // and calls that overlap on the GPU race on it, so serialise them (one stream,
 // or events). Each call writes every scratch element before reading it, so
 // nothing has to start at zero and the previous call's leftovers are harmless.
@@ -43,16 +45,14 @@ __device__ __align__(256) unsigned char g_sv_scratch[kScratchBytes];
 std::mutex g_mu;
 void *g_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_sv_scratch on the current device (looked up once).
-cudaError_t scratch_address(void **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
+// Device address of g_sv_scratch on device `dev`, which must be current
+// (looked up once per device).
+cudaError_t scratch_address(int dev, void **out) {
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_scratch_addr[dev]) {
         void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_sv_scratch);
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_sv_scratch);
         if (e != cudaSuccess) return e;
         g_scratch_addr[dev] = p;
     }
@@ -123,13 +123,16 @@ __global__ void k_finish(long long ns, long long P, int chunks, int nb, const S 
 }
 
 template <class S>
-int run(const S *O, const S *o, const S *skk, const S *v, S *out, long long ns, long long P, cudaStream_t st) {
-    const long long nb = (P + kThreads - 1) / kThreads;
+int run(const S *O, const S *o, const S *skk, const S *v, S *out, long long ns, long long P, int dev,
+        cudaStream_t st) {
     const size_t cap = kScratchBytes / sizeof(S);
-    // scratch: u[ns] | ovpart[nb] | ypart[chunks * P]
-    const size_t need_min = size_t(ns) + size_t(nb) + size_t(P);
-    if (need_min > cap) {
-        nqes::set_global_error("nqes_apply_S_static: " + std::to_string(need_min * sizeof(S)) +
+    // scratch: u[ns] | ovpart[nb] | ypart[chunks * P]; each size is checked
+    // against the capacity before any sum is formed, so nothing wraps
+    const long long nb = P <= (long long)cap ? (P + kThreads - 1) / kThreads : 0;
+    const bool fits = ns <= (long long)cap && P <= (long long)cap && size_t(ns) + size_t(nb) + size_t(P) <= cap;
+    if (!fits) {
+        const double need = (double(ns) + double(P) / kThreads + double(P)) * sizeof(S);
+        nqes::set_global_error("nqes_apply_S_static: " + std::to_string(need) +
                                " bytes of scratch needed for n_samples=" + std::to_string(ns) +
                                ", n_params=" + std::to_string(P) + "; the static scratch holds " +
                                std::to_string(kScratchBytes) + " bytes");
@@ -140,7 +143,7 @@ int run(const S *O, const S *o, const S *skk, const S *v, S *out, long long ns, 
     const long long by_rows = (ns + 255) / 256;
     if (chunks > by_rows) chunks = int(by_rows < 1 ? 1 : by_rows);
     void *base = nullptr;
-    cudaError_t e = scratch_address(&base);
+    cudaError_t e = scratch_address(dev, &base);
     if (e != cudaSuccess) {
         nqes::set_global_error(std::string("nqes_apply_S_static: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         return NQES_ERR_CUDA;
@@ -171,9 +174,21 @@ extern "C" int nqes_apply_S_static(const double *O, const double *o, const doubl
         return NQES_ERR_INVALID;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (complex_arith)
-        return run<cplx>(reinterpret_cast<const cplx *>(O), reinterpret_cast<const cplx *>(o),
-                         reinterpret_cast<const cplx *>(skk), reinterpret_cast<const cplx *>(v),
-                         reinterpret_cast<cplx *>(out), n_samples, n_params, st);
-    return run<double>(O, o, skk, v, out, n_samples, n_params, st);
+    // The work runs on the stream's device, and the scratch address looked up
+    // is that device's: make it current for the call, then restore the caller's.
+    int cur = 0, dev = 0;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e == cudaSuccess) e = st ? cudaStreamGetDevice(st, &dev) : cudaGetDevice(&dev);
+    if (e == cudaSuccess && dev != cur) e = cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        nqes::set_global_error(std::string("nqes_apply_S_static: device of the stream: ") + cudaGetErrorString(e));
+        return NQES_ERR_CUDA;
+    }
+    const int rc = complex_arith
+                       ? run<cplx>(reinterpret_cast<const cplx *>(O), reinterpret_cast<const cplx *>(o),
+                                   reinterpret_cast<const cplx *>(skk), reinterpret_cast<const cplx *>(v),
+                                   reinterpret_cast<cplx *>(out), n_samples, n_params, dev, st)
+                       : run<double>(O, o, skk, v, out, n_samples, n_params, dev, st);
+    if (dev != cur) cudaSetDevice(cur);
+    return rc;
 }

@@ -1,6 +1,7 @@
 """Generates the committed golden fixtures under tests/golden/.
 
-Run from the repository root:  python tests/golden/make_golden.py [--reference DIR]
+Run from the repository root:  python tests/golden/make_golden.py [--reference DIR] [--only ref|physics|ed]
+(DIR defaults to the environment variable NQES_REFERENCE_DIR.)
 
 1. ref_golden.json — outputs of the reference's own header-only code
    (code/pcg_random.h, code/minresqlp.h, compiled where they lie by
@@ -15,7 +16,9 @@ Run from the repository root:  python tests/golden/make_golden.py [--reference D
    192-239), independently of the C++ oracle. O is checked here against a
    holomorphic finite difference of log det Phi before it is written.
 3. ed_golden.json — the K lowest eigenvalues per site of H (exact
-   diagonalisation, scipy) for the synthetic power-law chains used by tests.
+   diagonalisation, scipy) for the synthetic power-law chains used by tests
+   (N up to 20) and for the reference's own 2D ion-crystal couplings
+   (code/Jmat/Ising2d_N{8,16}_alpha1.0.mat).
 """
 import argparse
 import json
@@ -153,48 +156,79 @@ def make_physics():
     return {"cases": cases}
 
 
+def reference_j(n):
+    """The reference's compiled-in couplings code/Jmat/Ising2d_N{n}_alpha1.0.mat,
+    as extracted to nqes-trapped-ion_gb300/cli/jmat/ (raw float64, row-major)."""
+    path = os.path.join(ROOT, "nqes-trapped-ion_gb300", "cli", "jmat", f"Ising2d_N{n}_alpha1.0.f64")
+    return np.fromfile(path, dtype="<f8").reshape(n, n)
+
+
+# (N, h, K, couplings): "alpha1.2" is the power-law chain above, "ion2d" the
+# reference's 2D ion-crystal J of the same N.
+ED_CASES = [(4, 0.595, 2, "alpha1.2"), (6, 0.595, 2, "alpha1.2"), (8, 0.595, 2, "alpha1.2"), (8, 1.0, 3, "alpha1.2"),
+            (10, 0.595, 2, "alpha1.2"), (12, 0.595, 2, "alpha1.2"), (16, 0.595, 2, "alpha1.2"),
+            (20, 0.595, 2, "alpha1.2"), (8, 0.595, 2, "ion2d"), (16, 0.595, 2, "ion2d")]
+
+
 def make_ed():
-    import scipy.sparse as sp
+    """K lowest eigenvalues per site of H = sum_{i!=j} J_ij sz_i sz_j - h sum_i sx_i
+    (the reference's ising_like_hamiltonian with J(s) = 2 sum_{i>j} J_ij s_i s_j,
+    code/rbm.cc:1011-1062): dense eigvalsh up to 1024 states, else Lanczos
+    (scipy eigsh) on a matrix-free H."""
     import scipy.sparse.linalg as sla
     out = []
-    for (n, h, K) in [(4, 0.595, 2), (6, 0.595, 2), (8, 0.595, 2), (8, 1.0, 3), (10, 0.595, 2), (12, 0.595, 2)]:
-        J = synthetic_j(n)
+    for (n, h, K, kind) in ED_CASES:
+        J = synthetic_j(n) if kind == "alpha1.2" else reference_j(n)
         dim = 1 << n
         idx = np.arange(dim)
-        bits = (idx[:, None] >> np.arange(n)[None, :]) & 1
-        s = 1.0 - 2.0 * bits
-        diag = np.einsum("ai,ij,aj->a", s, J, s) - np.sum(np.diag(J)) * 0.0
-        rows, cols, vals = [idx], [idx], [diag]
+        diag = np.zeros(dim)
         for i in range(n):
-            rows.append(idx)
-            cols.append(idx ^ (1 << i))
-            vals.append(np.full(dim, -h))
-        H = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(dim, dim))
+            si = 1.0 - 2.0 * ((idx >> i) & 1)
+            for j in range(i):
+                sj = 1.0 - 2.0 * ((idx >> j) & 1)
+                diag += 2.0 * J[i, j] * si * sj
+
+        def matvec(x):
+            x = np.asarray(x).ravel()
+            y = diag * x
+            for i in range(n):
+                y -= h * x[idx ^ (1 << i)]
+            return y
+
         if dim <= 1024:
-            ev = np.sort(np.linalg.eigvalsh(H.toarray()))[:K]
+            H = np.stack([matvec(np.eye(dim)[c]) for c in range(dim)], 1)
+            ev = np.sort(np.linalg.eigvalsh(H))[:K]
         else:
-            ev = np.sort(sla.eigsh(H, k=K, which="SA")[0])
-        out.append({"N": n, "h": h, "K": K, "alpha": 1.2, "evals_per_site": (ev / n).tolist()})
+            op = sla.LinearOperator((dim, dim), matvec=matvec, dtype=np.float64)
+            ev = np.sort(sla.eigsh(op, k=K, which="SA", tol=1e-12)[0])
+        case = {"N": n, "h": h, "K": K, "couplings": kind, "evals_per_site": (ev / n).tolist()}
+        if kind == "alpha1.2":
+            case["alpha"] = 1.2
+        out.append(case)
     return {"cases": out}
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("NQES_REFERENCE_DIR"),
+                    help="the reference tree (default: $NQES_REFERENCE_DIR)")
+    ap.add_argument("--only", choices=["ref", "physics", "ed"], help="regenerate one file only")
     args = ap.parse_args()
-    if os.path.isdir(args.reference):
+    if args.only in (None, "ref") and args.reference and os.path.isdir(args.reference):
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={args.reference}"], check=True)
         raw = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_harness")], check=True,
                              capture_output=True, text=True).stdout
         data = json.loads(raw)
         with open(os.path.join(HERE, "ref_golden.json"), "w") as f:
             json.dump(data, f, separators=(",", ":"))
-    else:
+    elif args.only in (None, "ref"):
         print("reference tree absent: ref_golden.json left as committed", file=sys.stderr)
-    with open(os.path.join(HERE, "physics_golden.json"), "w") as f:
-        json.dump(make_physics(), f, separators=(",", ":"))
-    with open(os.path.join(HERE, "ed_golden.json"), "w") as f:
-        json.dump(make_ed(), f, indent=1)
+    if args.only in (None, "physics"):
+        with open(os.path.join(HERE, "physics_golden.json"), "w") as f:
+            json.dump(make_physics(), f, separators=(",", ":"))
+    if args.only in (None, "ed"):
+        with open(os.path.join(HERE, "ed_golden.json"), "w") as f:
+            json.dump(make_ed(), f, indent=1)
 
 
 if __name__ == "__main__":

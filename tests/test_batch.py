@@ -109,3 +109,44 @@ def test_batch_rebuilds_after_a_member_changes_its_hamiltonian(pkg):
     batch.close()
     member.close()
     alone.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_batch_after_a_member_reallocates_its_buffers(pkg, prec):
+    """A solo step at another chain count (or a precision switch with a solo
+    step in between) frees and reallocates a member's step buffers; the next
+    batched step at the original shape must not replay a graph that points at
+    the freed memory. Its results equal a fresh context's through the same
+    steps."""
+    N, M, K = 8, 16, 2
+    w = helpers.random_weights(N, M, K, 0.05, 21, real=True)
+
+    def fresh():
+        c = pkg.Context(N, M, K, synthetic_j(N), 0.7)
+        c.set_weights(*w)
+        c.set_option(pkg.OPT_PRECISION, prec)
+        return c
+
+    member, ref = fresh(), fresh()
+    batch = pkg.Batch([member])
+    args = lambda t: ([40 + 16 * t], [16], [12], [4], [0.1], [5.0], [1e-9], [2000])
+    e_b, _, stats, _ = batch.sr_step(*args(0))
+    e_r, _ = ref.sr_step(40, 16, 12, 4, 0.1, 5.0, 1e-9, 2000)
+    assert stats == [0] and np.array_equal(e_b[0], e_r)
+    # solo step at another chain count: new buffers; then (prec 1) a solo step
+    # in the other precision and back, which reallocates them once more
+    for c in (member, ref):
+        c.sr_step(99, 24, 12, 4, 0.1, 5.0, 1e-9, 2000)
+        if prec:
+            c.set_option(pkg.OPT_PRECISION, 0)
+            c.sr_step(101, 16, 12, 4, 0.1, 5.0, 1e-9, 2000)
+            c.set_option(pkg.OPT_PRECISION, prec)
+    e_b, _, stats, _ = batch.sr_step(*args(1))
+    e_r, _ = ref.sr_step(56, 16, 12, 4, 0.1, 5.0, 1e-9, 2000)
+    assert stats == [0] and np.array_equal(e_b[0], e_r)
+    assert np.array_equal(member.get_samples()[0], ref.get_samples()[0])
+    for x, y in zip(member.get_weights(), ref.get_weights()):
+        assert np.array_equal(x, y)
+    batch.close()
+    member.close()
+    ref.close()

@@ -18,6 +18,15 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 BIN = os.path.join(ROOT, "nqes-trapped-ion_gb300", "bin")
 
 
+JMAT = os.path.join(ROOT, "nqes-trapped-ion_gb300", "cli", "jmat")
+
+
+def reference_j(n):
+    """The couplings the reference compiles into its trapped-ion executables
+    (code/Jmat/Ising2d_N{n}_alpha1.0.mat), as committed beside the CLI."""
+    return np.fromfile(os.path.join(JMAT, f"Ising2d_N{n}_alpha1.0.f64"), dtype="<f8").reshape(n, n)
+
+
 @pytest.fixture(scope="module")
 def exe():
     ge._load_build_module().build_cli([(8, 16, 2)])
@@ -55,6 +64,27 @@ def test_zero_chains_and_unknown_option(exe):
     assert r.returncode == 1
     assert "unrecognised commandline argument: bogus" in r.stderr
     assert "Number of CPU cores cannot be zero." in r.stderr
+
+
+def test_compiled_in_couplings_are_the_reference_jmat(exe, tmp_path):
+    """--model trappedion uses the reference's compiled-in J (code/build.sh:34-41,
+    code/rbm.cc:1011-1031) element for element; --jmat synthetic the power-law
+    chain of the benchmark inputs. --dump-jmat writes the J that nqes_create
+    would receive and exits before touching a device."""
+    sio = pytest.importorskip("scipy.io")
+    base = [exe, "--model", "trappedion", "-h", "0.595", "-n", "1", "-m", "1", "-c", "1", "--correlation-data", "x"]
+    f = str(tmp_path / "j.mat")
+    r = run(base + ["--dump-jmat", f])
+    assert r.returncode == 0, r.stderr
+    J = sio.loadmat(f)["J"]
+    assert np.array_equal(J, reference_j(8))
+    ref = os.environ.get("NQES_REFERENCE_DIR")
+    if ref and os.path.isdir(ref):  # the committed values against the reference's own file
+        want = sio.loadmat(os.path.join(ref, "code", "Jmat", "Ising2d_N8_alpha1.0.mat"))["J"]
+        assert np.array_equal(J, want)
+    r = run(base + ["--jmat", "synthetic", "--dump-jmat", f])
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(sio.loadmat(f)["J"], helpers.synthetic_j(8))
 
 
 @pytest.fixture(scope="module")
@@ -117,7 +147,7 @@ def test_executable_matches_oracle_schedule(exe, tmp_path):
     assert lines[0] == f"Random seed is {seed}"
     got = np.array([[float(v) for v in ln.split()] for ln in lines[1:1 + niters]])
     # oracle through the same schedule (code/rbm.cc:1178-1196)
-    orc = helpers.Oracle(N, M, K, helpers.synthetic_j(N), h)
+    orc = helpers.Oracle(N, M, K, reference_j(N), h)
     orc.set_weights(*w0)
     lr, reglam = 0.1, 5.0
     want = []
@@ -201,7 +231,7 @@ def test_executable_dumps(exe, tmp_path):
     der = sio.loadmat(pre["der"] + suffix)["s"]
     P = K * (N + M + N * M)
     assert st.shape == (2 ** (K * N), K, K) and ham.shape == (2 ** (K * N), K, K) and der.shape == (2 ** (K * N), P)
-    orc = helpers.Oracle(N, M, K, helpers.synthetic_j(N), h)
+    orc = helpers.Oracle(N, M, K, reference_j(N), h)
     orc.set_weights(*w0)
     rng = np.random.default_rng(1)
     for idx in list(rng.integers(0, 2 ** (K * N), size=12)) + [0x1234, 2 ** (K * N) - 2]:
@@ -215,3 +245,24 @@ def test_executable_dumps(exe, tmp_path):
         assert np.max(np.abs(st[idx] - phi)) <= 1e-12 * np.max(np.abs(phi))
         assert np.max(np.abs(ham[idx] - E)) <= 1e-10 * np.max(np.abs(E))
         assert np.max(np.abs(der[idx] - O)) <= 1e-10 * np.max(np.abs(O))
+
+
+@pytest.mark.gpu
+def test_nonfinite_weights_exit_127_with_throw_fperror(exe, tmp_path):
+    """A NaN weight loaded with --load-rbm makes the first SR step non-finite:
+    with --throw-fperror the executable exits with status 127, the code
+    run.sh retries on (code/rbm.cc:1248-1271); without it the run carries on
+    and exits 0, as the reference does with floating-point traps off."""
+    sio = pytest.importorskip("scipy.io")
+    N, M, K = 8, 16, 2
+    a, b, w = helpers.random_weights(N, M, K, 0.05, 8, real=False)
+    w[1, 3, 5] = np.nan
+    wfile = str(tmp_path / "nan.mat")
+    sio.savemat(wfile, {"a": a, "b": b, "w": w})
+    base = [exe, "--model", "trappedion", "-h", "0.595", "-n", "2", "-m", "4", "-c", "2", "--burn-in-steps", "2",
+            "--seed", "3", "--load-rbm", wfile, "--correlation-data", str(tmp_path / "c.mat")]
+    r = run(base + ["--throw-fperror"])
+    assert r.returncode == 127, (r.returncode, r.stderr)
+    assert "Floating point error occured. Exiting." in r.stderr
+    r = run(base)
+    assert r.returncode == 0, (r.returncode, r.stderr)

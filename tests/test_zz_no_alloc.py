@@ -6,10 +6,13 @@ owns and keeps its intermediates in the library's fixed 16 MiB device array.
 
 The test allocates the caller's buffers itself (as such a caller would have
 done up front), calls the entry point through the C ABI twice in a row, and
-checks each result against the context-based nqes_apply_S on the same
-samples, to the 1e-11 relative tolerance of the other S·v parity tests. It
-also checks that a size beyond the array is refused with a message. This file
-is collected last so that a failure here comes after every other test ran."""
+checks each result against the CPU oracle's S·v (the matrix-free operator of
+code/rbm.cc:660-683 over the oracle's own samples, which are the GPU's bit for
+bit) and against the context-based nqes_apply_S, to the 1e-11 relative
+tolerance of the other S·v parity tests. It also checks that sizes beyond the
+array are refused with a message, including sizes whose sum would overflow.
+This file is collected last so that a failure here comes after every other
+test ran."""
 import ctypes
 
 import numpy as np
@@ -36,10 +39,15 @@ def test_static_scratch_sv_matches_apply_S(pkg, real):
     torch = pytest.importorskip("torch")
     N, M, K = 8, 16, 2
     J = helpers.synthetic_j(N)
+    weights = helpers.random_weights(N, M, K, 0.1, 5, real=real)
     ctx = pkg.Context(N, M, K, J, 0.595)
-    ctx.set_weights(*helpers.random_weights(N, M, K, 0.1, 5, real=real))
+    ctx.set_weights(*weights)
+    orc = helpers.Oracle(N, M, K, J, 0.595)
+    orc.set_weights(*weights)
     chains, m = 16, 25
     ctx.sr_step(777, chains, m, 8, 0.1, 2.0, 1e-9, 500)
+    orc.sr_step(777, chains, m, 8, 0.1, 2.0, 1e-9, 500, store_o=True)
+    assert np.array_equal(ctx.get_samples()[0], orc.samples(chains * m)[0])
     ns, P = chains * m, ctx.P
     O = ctx.get_O(0, ns)
     o, skk, _ = ctx.get_moments()
@@ -60,14 +68,22 @@ def test_static_scratch_sv_matches_apply_S(pkg, real):
         assert st == pkg.OK, lib.nqes_last_error(None)
         torch.cuda.synchronize()
         got = out_d.cpu().numpy().view(np.float64 if real else np.complex128)
-        want = ctx.apply_S(v)
-        if real:
-            want = want.real
-        assert rel_err(got, want) < 1e-11, (call, rel_err(got, want))
+        for want in (orc.apply_S(v), ctx.apply_S(v)):
+            if real:
+                want = want.real
+            assert rel_err(got, want) < 1e-11, (call, rel_err(got, want))
     # Sizes beyond the static array are refused, with a description.
     st = lib.nqes_apply_S_static(ctypes.c_void_p(O_d.data_ptr()), ctypes.c_void_p(o_d.data_ptr()),
                                  ctypes.c_void_p(skk_d.data_ptr()), ctypes.c_void_p(v_d.data_ptr()),
                                  ctypes.c_void_p(out_d.data_ptr()), 1 << 40, P, 0, stream)
     assert st == pkg.ERR_INVALID
     assert b"static scratch" in lib.nqes_last_error(None)
+    # n_samples + n_params would wrap around in 64 bits: refused all the same
+    big = (1 << 63) - 1
+    for ns_, p_ in ((big, big), (big, P), (ns, big)):
+        st = lib.nqes_apply_S_static(ctypes.c_void_p(O_d.data_ptr()), ctypes.c_void_p(o_d.data_ptr()),
+                                     ctypes.c_void_p(skk_d.data_ptr()), ctypes.c_void_p(v_d.data_ptr()),
+                                     ctypes.c_void_p(out_d.data_ptr()), ns_, p_, 0, stream)
+        assert st == pkg.ERR_INVALID, (ns_, p_)
+        assert b"static scratch" in lib.nqes_last_error(None)
     ctx.close()
