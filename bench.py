@@ -109,24 +109,6 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def fp64_peak_tflops(torch):
-    """Measured FP64 throughput of this GPU (cuBLAS DGEMM, best of 5)."""
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 1e9
-    for _ in range(5):
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
-        torch.matmul(a, b)
-        e.record()
-        e.synchronize()
-        best = min(best, s.elapsed_time(e))
-    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
-
-
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -209,6 +191,29 @@ def run_form(pkg, J, weights, precision, chains, steps, warmup, seed0, local):
             infos.append(info)
         evals.append(np.sort(np.linalg.eigvals(e / N).real))
     return ctx, infos, evals
+
+
+def mixed_along_fp64(pkg, J, weights, chains, nsteps, seed0, local):
+    """The mixed form's energy error beyond the first step: along the FP64
+    form's trajectory, the mixed context is reset to the FP64 context's
+    weights before every step, so both sample the same Markov chains and the
+    difference is the arithmetic alone. Max over steps of max_k |dE_k|/|E_k|."""
+    f = pkg.Context(N, M, K, J, H, device=local)
+    x = pkg.Context(N, M, K, J, H, device=local)
+    f.set_weights(*weights)
+    x.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+    worst = []
+    for t in range(nsteps):
+        lr, reglam = schedule(t)
+        x.set_weights(*f.get_weights())
+        args = (seed0 + t * chains, chains, SAMPLES, BURN, lr, reglam, RTOL, MAXIT)
+        ef, _ = f.sr_step(*args)
+        em, _ = x.sr_step(*args)
+        vf, vm = (np.sort(np.linalg.eigvals(e / N).real) for e in (ef, em))
+        worst.append(float(np.max(np.abs(vm - vf) / np.abs(vf))))
+    f.close()
+    x.close()
+    return worst
 
 
 def batched_form(pkg, n_solves, chains, samples, steps, local):
@@ -304,22 +309,29 @@ def target_form(pkg, n_solves, local, fp64_sr_steps_per_s, de_rel):
             "target": ">= 10x the plain FP64 form's SR steps/s at |dE| <= 1e-6"}
 
 
-def serving_form(pkg, rate, window_s, local, max_steps=10):
+SERVE_TOL = 1e-3  # the convergence test's tolerance per site for served requests (see serving_form)
+
+
+def serving_form(pkg, rate, window_s, local, max_steps=40, max_requests=48):
     """Config-5 style serving: Poisson arrivals at `rate` per second for
-    `window_s` seconds of solve requests (N log-uniform on [8, 96], M in
-    {N, 2N}, K uniform on 1..4, h ~ U[0, 2], tol 1e-6, 64 chains x 100 samples,
-    MINRES-QLP capped at 200 iterations (the reference's --minres-maxit: with up
-    to 75k parameters and 6400 samples S is rank-deficient), mixed precision, at
-    most max_steps SR steps), admitted by device footprint
-    into the continuous batch. Returns solves/s and the time-to-converged-energy
-    percentiles (submit to completion)."""
+    `window_s` seconds (at most max_requests) of solve requests (N log-uniform
+    on [8, 96], M in {N, 2N}, K uniform on 1..4, h ~ U[0, 2], 64 chains x 100
+    samples, MINRES-QLP capped at 200 iterations (the reference's
+    --minres-maxit: with up to 75k parameters and 6400 samples S is rank
+    deficient), mixed precision, at most max_steps SR steps), admitted by
+    device footprint into the continuous batch. A request converges by the
+    reference's rule (code/rbm.cc:1185-1194) with tol = SERVE_TOL per site:
+    with 6400 samples a step's energies fluctuate by about 1e-4..1e-3 per site,
+    so the configs' tol = 1e-6 is never met (as in the reference's own logs,
+    whose runs stop at -n). Returns solves/s and the time-to-converged-energy
+    percentiles (submit to completion) of the converged requests, and of all."""
     import torch
     rng = np.random.default_rng(SEED + int(rate))
     free, _ = torch.cuda.mem_get_info(local)
     srv = pkg.Server(hbm_budget_bytes=int(0.8 * free), max_active=256, device=local)
     t0 = time.perf_counter()
     t_next, n = 0.0, 0
-    while t_next < window_s:
+    while t_next < window_s and n < max_requests:
         now = time.perf_counter() - t0
         if now < t_next:
             time.sleep(t_next - now)
@@ -328,21 +340,46 @@ def serving_form(pkg, rate, window_s, local, max_steps=10):
         K = int(rng.integers(1, 5))
         srv.submit(N, M, K, pkg.synthetic_j(N), weights=pkg.synthetic_weights(N, M, K, 0.01, SEED + n),
                    h=float(rng.uniform(0.0, 2.0)), seed=SEED + 7919 * n, chains=64, samples_per_chain=100, burn_in=16,
-                   tol=1e-6, max_steps=max_steps, minres_maxit=200, precision=pkg.PRECISION_MIXED)
+                   tol=SERVE_TOL, max_steps=max_steps, minres_maxit=200, precision=pkg.PRECISION_MIXED)
         n += 1
         t_next += rng.exponential(1.0 / rate)
+    t_last_submit = time.perf_counter() - t0
     res = srv.wait_all(n, timeout=900)
     t_end = time.perf_counter() - t0
     phases = srv.times()
     srv.close()
-    lat = np.array([r["t_total"] for r in res if r["status"] == 0])
-    return {"rate_per_s": rate, "window_s": window_s, "submitted": n, "completed": int(len(lat)),
-            "failed": int(sum(r["status"] != 0 for r in res)), "converged": int(sum(r["converged"] for r in res)),
-            "step_capped": int(sum(r["status"] == 0 and not r["converged"] for r in res)),
-            "solves_per_s": len(lat) / t_end, "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
-            "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
+    ok = [r for r in res if r["status"] == 0]
+    conv = np.array([r["t_total"] for r in ok if r["converged"]])
+    lat = np.array([r["t_total"] for r in ok])
+    pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
+    return {"rate_per_s": rate, "window_s": t_last_submit, "submitted": n, "completed": len(ok),
+            "failed": int(sum(r["status"] != 0 for r in res)), "converged": int(len(conv)),
+            "step_capped": int(sum(not r["converged"] for r in ok)),
+            "offered_per_s": n / max(t_last_submit, 1e-9), "solves_per_s": len(ok) / t_end,
+            "p50_converged_s": pct(conv, 50), "p99_converged_s": pct(conv, 99),
+            "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
+            "mean_steps": float(np.mean([r["steps"] for r in ok])) if ok else None,
             "mean_queue_s": float(np.mean([r["t_queued"] for r in res])) if res else None,
-            "max_steps": max_steps, "worker_phases": phases}
+            "max_steps": max_steps, "tol_per_site": SERVE_TOL, "worker_phases": phases}
+
+
+def serving_sweep(pkg, rates, window_s, local):
+    """Serving lines over the arrival rates and the highest rate the server
+    sustains: completions keep up with arrivals (>= 90 %) and p99 stays within
+    3x the lowest rate's."""
+    lines = [serving_form(pkg, r, window_s, local) for r in rates]
+    base = lines[0]["p99_s"] or 0.0
+    sus = None
+    for ln in lines:
+        if ln["p99_s"] is not None and ln["solves_per_s"] >= 0.9 * ln["offered_per_s"] and ln["p99_s"] <= 3 * base:
+            sus = ln
+    summary = {"sustainable_rate_per_s": sus["rate_per_s"] if sus else None,
+               "solves_per_s_at_sustainable": sus["solves_per_s"] if sus else None,
+               "p50_converged_s_at_sustainable": sus["p50_converged_s"] if sus else None,
+               "p99_converged_s_at_sustainable": sus["p99_converged_s"] if sus else None,
+               "p99_s_at_sustainable": sus["p99_s"] if sus else None,
+               "rule": "completions >= 90% of arrivals and p99 within 3x the lowest rate's"}
+    return lines, summary
 
 
 def precision_form(pkg, chains, samples, steps, local):
@@ -409,6 +446,29 @@ def max_over_ranks(x, world):
     return float(tt.item())
 
 
+def peak_tflops(torch, dtype):
+    """Measured dense GEMM throughput of this GPU in `dtype` (cuBLAS, 4096^3,
+    best of 5); FP32 without TF32, i.e. the CUDA-core FP32 pipe."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 4096
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+FORMS = {"certified": 2, "fp64": 0}
+
+
 def run_ours(args):
     import torch
     import __graft_entry__ as ge
@@ -419,10 +479,12 @@ def run_ours(args):
     torch.cuda.set_device(local)
     pkg = ge.load_package()
     chains = args.chains
+    form = FORMS[args.precision]
     J = pkg.synthetic_j(N)
     a0, b0, w0 = pkg.synthetic_weights(N, M, K, 0.01, SEED + rank)
     ctx = pkg.Context(N, M, K, J, H, device=local)
     ctx.set_weights(a0, b0, w0)
+    ctx.set_option(pkg.OPT_PRECISION, form)
     ns = chains * SAMPLES
 
     def barrier():
@@ -452,56 +514,57 @@ def run_ours(args):
 
     # ---- per-kernel timing for the roofline (same data, same stream) ----
     kern = {}
-    for name, kid in [("sample", pkg.KERNEL_SAMPLE), ("sv_rows", pkg.KERNEL_SV_ROWS), ("sv_cols", pkg.KERNEL_SV_COLS),
-                      ("moments", pkg.KERNEL_MOMENTS)]:
+    for name, kid in [("sample", pkg.KERNEL_SAMPLE), ("sv", pkg.KERNEL_SV), ("moments", pkg.KERNEL_MOMENTS)]:
         ms, by = ctx.time_kernel(kid, reps=3 if kid == pkg.KERNEL_SAMPLE else 10)
         kern[name] = {"avg_ms": ms, "bytes": by}
-    # S·v passes per step: the first Lanczos step before the MINRES-QLP loop and
-    # one per loop body (14 kernels outside the loop, 7 per body)
-    passes = [(i["kernel_launches"] - 14) // 7 + 1 for i in infos]
-    share = {
-        "sample": kern["sample"]["avg_ms"],
-        "sv_rows": kern["sv_rows"]["avg_ms"] * float(np.mean(passes)),
-        "sv_cols": kern["sv_cols"]["avg_ms"] * float(np.mean(passes)),
-    }
+    # S·v products per step: the first Lanczos step before the MINRES-QLP loop
+    # and one per loop body (14 kernels outside the loop, 7 per body)
+    passes = float(np.mean([(i["kernel_launches"] - 14) // 7 + 1 for i in infos]))
+    share = {"sample": kern["sample"]["avg_ms"], "sv": kern["sv"]["avg_ms"] * passes}
     dom = max(share, key=share.get)
     hbm, hbm_src = measured_peaks()
     traffic = {}
-    tpath = os.path.join(ROOT, "profiles", "traffic.txt")  # "kernel bytes" lines from an ncu capture
+    tpath = os.path.join(ROOT, "profiles", "traffic.txt")  # "kernel bytes" lines from ncu captures
     if os.path.exists(tpath):
         with open(tpath) as f:
             for line in f:
                 parts = line.split()
                 if len(parts) == 2 and not line.startswith("#"):
                     traffic[parts[0]] = float(parts[1])
-    fp64_tf = fp64_peak_tflops(torch)
+    fp64_tf = peak_tflops(torch, torch.float64)
+    fp32_tf = peak_tflops(torch, torch.float32)
     cmul = 4 if infos[-1]["arith"] == pkg.ARITH_COMPLEX else 1
-    # algorithmic FLOPs per launch: a measured MC sample (its K N proposals and
-    # its local energy) updates 2 K^2 N M hidden units at 2 FLOP each (real;
-    # x4 complex); burn-in sweeps are not counted
+    fused = infos[-1]["arith"] == pkg.ARITH_REAL and ns * ctx.P * 8 <= kern["sv"]["bytes"] < 1.5 * ns * ctx.P * 8
+    # algorithmic FLOPs per sampler launch: a measured MC sample (its K N
+    # proposals and its local energy) updates 2 K^2 N M hidden units at 2 FLOP
+    # each (real; x4 complex); burn-in sweeps are not counted
     sample_flops = ns * 4.0 * K * K * N * M * cmul
-    # S·v: one FMA per stored log-derivative in each of its two passes
-    sv_flops = 2.0 * ns * ctx.P * cmul
-    sv_ms = kern["sv_rows"]["avg_ms"] + kern["sv_cols"]["avg_ms"]
-    sv_gbs = (kern["sv_rows"]["bytes"] + kern["sv_cols"]["bytes"]) / (sv_ms * 1e-3) / 1e9
-    sv_tf = 2.0 * sv_flops / (sv_ms * 1e-3) / 1e12
-    peak_src = "in-run cuBLAS DGEMM 4096^3, best of 5 (MEASURED_PEAKS.json has no FP64 figure)"
     s_ms = kern["sample"]["avg_ms"]
     s_tf = sample_flops / (s_ms * 1e-3) / 1e12
-    roof_sample = {"kernel": "sample", "bound": "fp64", "achieved": s_tf, "peak": fp64_tf, "unit": "TFLOP/s",
-                   "frac": s_tf / fp64_tf, "traffic": traffic.get("sample"), "algorithmic_flops": sample_flops,
-                   "avg_ms": s_ms, "peak_source": peak_src,
-                   "hbm": {"achieved_gbs": kern["sample"]["bytes"] / (s_ms * 1e-3) / 1e9, "peak_gbs": hbm,
-                           "peak_source": hbm_src + " (MEASURED_PEAKS.json hbm_gbs)"},
-                   "note": "the sweep is compute-bound on the FP64 pipe; a chain's proposals are serial, and at "
-                           "128 chains one chain per SM leaves one warp per sub-partition, so the kernel is bound "
-                           "by the latency of each proposal's FP64 instructions (~64 cycles per FP64 warp "
-                           "instruction); profiles/k_sample_fp64_N32M64K2_128chains.md"}
-    roof_sv = {"kernel": "sv_rows+sv_cols", "bound": "fp64", "achieved": sv_tf, "peak": fp64_tf, "unit": "TFLOP/s",
-               "frac": sv_tf / fp64_tf, "traffic": traffic.get("sv"), "avg_ms": sv_ms, "peak_source": peak_src,
-               "hbm": {"achieved_gbs": sv_gbs, "peak_gbs": hbm, "frac": sv_gbs / hbm},
-               "note": "2 FLOP per 8-byte entry per pass (0.25 FLOP/B) lies above the FP64 ridge "
-                       "(DGEMM / HBM ~ 0.16 FLOP/B): FP64-pipe bound"}
+    s_pipe, s_peak = ("fp32", fp32_tf) if form == pkg.PRECISION_CERTIFIED else ("fp64", fp64_tf)
+    roof_sample = {
+        "kernel": "sample", "bound": s_pipe, "achieved": s_tf, "peak": s_peak, "unit": "TFLOP/s",
+        "frac": s_tf / s_peak, "traffic": traffic.get("sample_" + args.precision), "algorithmic_flops": sample_flops,
+        "avg_ms": s_ms,
+        "peak_source": "in-run cuBLAS %s GEMM 4096^3, best of 5 (MEASURED_PEAKS.json has no %s figure)"
+                       % (s_pipe.upper(), s_pipe.upper()),
+        "hbm": {"achieved_gbs": kern["sample"]["bytes"] / (s_ms * 1e-3) / 1e9, "peak_gbs": hbm},
+        "note": ("the proposals' arithmetic runs on the %s pipe; a chain's proposals are serial and at 128 chains "
+                 "one chain per SM leaves the SM's sub-partitions mostly idle: the kernel is bound by the latency "
+                 "of each proposal, not by a pipe's throughput" % s_pipe.upper())}
+    sv_ms = kern["sv"]["avg_ms"]
+    sv_gbs = kern["sv"]["bytes"] / (sv_ms * 1e-3) / 1e9
+    sv_flops = 4.0 * ns * ctx.P * cmul  # u = O v and O^T u: one FMA per entry each
+    roof_sv = {"kernel": "sv_fused" if fused else "sv_rows+sv_cols", "avg_ms": sv_ms, "traffic": traffic.get("sv"),
+               "algorithmic_bytes": kern["sv"]["bytes"], "passes_per_step": passes}
+    if fused:  # one read of O, double-float on the FP32 pipe: HBM-bound
+        roof_sv.update(bound="hbm", achieved=sv_gbs, peak=hbm, unit="GB/s", frac=sv_gbs / hbm,
+                       peak_source=hbm_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                       fp64_equivalent_tflops=sv_flops / (sv_ms * 1e-3) / 1e12)
+    else:  # two FP64 passes: 0.25 FLOP/B, above the FP64 ridge (DGEMM / HBM ~ 0.16 FLOP/B)
+        sv_tf = sv_flops / (sv_ms * 1e-3) / 1e12
+        roof_sv.update(bound="fp64", achieved=sv_tf, peak=fp64_tf, unit="TFLOP/s", frac=sv_tf / fp64_tf,
+                       hbm={"achieved_gbs": sv_gbs, "frac": sv_gbs / hbm})
     roofline = dict(roof_sample if dom == "sample" else roof_sv)
     roofline["other"] = roof_sv if dom == "sample" else roof_sample
 
@@ -534,6 +597,10 @@ def run_ours(args):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
+        "precision": ("certified: FP64 local energies, log-derivatives, moments, S·v (double-float, one read of O), "
+                      "MINRES-QLP and update; accept decisions taken in FP32 only where a rigorous bound proves them "
+                      "equal to FP64's, else in FP64: the FP64 Markov chains" if form == pkg.PRECISION_CERTIFIED
+                      else "FP64 throughout"),
         "data": "synthetic",
         "config": {"workload": "SR step, trapped-ion N=32 M=64 K=2 h=0.595, J=|i-j|^-1.2, real N(0,0.01^2) weights",
                    "chains": chains, "samples_per_chain": SAMPLES, "burn_in": BURN, "minres_rtol": RTOL,
@@ -544,6 +611,7 @@ def run_ours(args):
         "wall_sr_steps_per_s": args.steps / t_wall,
         "minres_iters_mean": float(np.mean([i["minres_iters"] for i in infos])),
         "accept_rate": float(np.mean([i["accepted"] / i["proposals"] for i in infos])),
+        "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for i in infos])),
         "gpu_launches": int(sum(i["kernel_launches"] for i in infos)),
         "kernels": kern,
         "roofline": roofline,
@@ -552,50 +620,51 @@ def run_ours(args):
     if clk:
         out["clocks"] = clk
 
-    # ---- the mixed-precision form on the same weights, seeds and schedule ----
+    # ---- the plain FP64 form and the mixed form on the same weights, seeds and schedule ----
+    seed0 = SEED + (rank << 40)
+    cf, if_, ef = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_FP64, chains, args.steps, args.warmup, seed0, local)
+    ms_f = sum(i["ms_total"] for i in if_) / args.steps
+    ksf, _ = cf.time_kernel(pkg.KERNEL_SAMPLE, reps=3)
+    out["fp64_plain"] = {"value": ns / (ms_f * 1e-3), "unit": "MC samples/s", "ms_per_step": ms_f,
+                         "sr_steps_per_s": 1e3 / ms_f, "sampler_ms": ksf,
+                         "minres_iters_mean": float(np.mean([i["minres_iters"] for i in if_])),
+                         "note": "every quantity in FP64 (FP64 sampler; S·v as the headline's)"}
+    cf.close()
+    if form == pkg.PRECISION_CERTIFIED:
+        # the headline against the plain FP64 form on the same weights and seeds
+        cc, _, ec = run_form(pkg, J, (a0, b0, w0), form, chains, args.steps, args.warmup, seed0, local)
+        cc.close()
+        out["dE_rel_vs_fp64_plain"] = {"first_step": float(np.max(np.abs(ec[0] - ef[0]) / np.abs(ef[0]))),
+                                       "last_step": float(np.max(np.abs(ec[-1] - ef[-1]) / np.abs(ef[-1]))),
+                                       "steps": args.warmup + args.steps}
     if not args.no_mixed:
-        seed0 = SEED + (rank << 40)
-        cf, if_, ef = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_FP64, chains, args.steps, args.warmup, seed0, local)
-        cf.close()
         cm, im, em = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_MIXED, chains, args.steps, args.warmup, seed0, local)
-        ms_f = sum(i["ms_total"] for i in if_) / args.steps
         ms_m = sum(i["ms_total"] for i in im) / args.steps
         ksm, _ = cm.time_kernel(pkg.KERNEL_SAMPLE, reps=3)
+        cm.close()
         # first step: same weights, hence the same Markov chains; the difference
-        # is the FP32 arithmetic alone. Later steps start from weights that
-        # differ by the FP32 solve (~1e-6) and so draw different chains.
-        dE = float(np.max(np.abs(em[0] - ef[0]) / np.abs(ef[0])))
-        dE_last = float(np.max(np.abs(em[-1] - ef[-1]) / np.abs(ef[-1])))
+        # is the FP32 arithmetic alone. Along the FP64 trajectory (the mixed
+        # context reset to the FP64 weights before each step) every step's
+        # difference is again the arithmetic alone.
+        along = mixed_along_fp64(pkg, J, (a0, b0, w0), chains, args.warmup + args.steps, seed0, local)
         out["mixed"] = {
             "value": ns / (ms_m * 1e-3), "unit": "MC samples/s", "ms_per_step": ms_m,
-            "sr_steps_per_s": 1e3 / ms_m, "speedup_vs_fp64": ms_f / ms_m, "fp64_ms_per_step": ms_f,
-            "sampler_ms": ksm, "fp64_sampler_ms": kern["sample"]["avg_ms"],
-            "dE_rel": dE, "dE_note": "max_k |E_k mixed - E_k FP64| / |E_k| per site at the first step: same "
-                                     "weights and seeds, so the same Markov chains",
-            "dE_rel_last_step": dE_last, "dE_last_note": "after %d steps the weights differ by the FP32 solve, so the "
-                                                         "chains differ: Monte Carlo noise, not arithmetic" % (args.warmup + args.steps),
+            "sr_steps_per_s": 1e3 / ms_m, "speedup_vs_fp64_plain": ms_f / ms_m, "sampler_ms": ksm,
+            "dE_rel": float(np.max(np.abs(em[0] - ef[0]) / np.abs(ef[0]))),
+            "dE_note": "max_k |E_k mixed - E_k FP64| / |E_k| per site at the first step: same weights and seeds, so "
+                       "the same Markov chains",
+            "dE_rel_max_over_steps": float(max(along)), "dE_rel_mean_over_steps": float(np.mean(along)),
+            "dE_steps": len(along),
+            "dE_steps_note": "every step of the FP64 trajectory, the mixed context reset to the FP64 weights before "
+                             "it (same chains): the arithmetic's error alone",
             "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for i in im])),
             "dtype": "f32 factors/decisions (certified) + f64 theta, Phi, MINRES-QLP, update",
         }
-        cm.close()
-        # FP64 results from the certified sampler: the FP64 form's chains and
-        # FP64 E, O, moments, S·v, MINRES-QLP and update
-        cc, ic, ec = run_form(pkg, J, (a0, b0, w0), pkg.PRECISION_CERTIFIED, chains, args.steps, args.warmup, seed0, local)
-        ms_c = sum(i["ms_total"] for i in ic) / args.steps
-        ksc, _ = cc.time_kernel(pkg.KERNEL_SAMPLE, reps=3)
-        out["certified"] = {
-            "value": ns / (ms_c * 1e-3), "unit": "MC samples/s", "ms_per_step": ms_c, "speedup_vs_fp64": ms_f / ms_c,
-            "sampler_ms": ksc, "dE_rel_first_step": float(np.max(np.abs(ec[0] - ef[0]) / np.abs(ef[0]))),
-            "dE_rel_last_step": float(np.max(np.abs(ec[-1] - ef[-1]) / np.abs(ef[-1]))),
-            "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for i in ic])),
-            "dtype": "f64 results; accept decisions certified in f32 (identical to f64), exact f64 fallback",
-        }
-        cc.close()
 
     # ---- the 4096-chain sweep (both forms, fewer steps) ----
     if args.sweep_chains:
         sweep = {}
-        for prec, name in ((pkg.PRECISION_FP64, "fp64"), (pkg.PRECISION_MIXED, "mixed")):
+        for prec, name in ((form, args.precision), (pkg.PRECISION_MIXED, "mixed")):
             c4, i4, _ = run_form(pkg, J, (a0, b0, w0), prec, args.sweep_chains, 2, 1, SEED + 7, local)
             ms = sum(i["ms_total"] for i in i4) / len(i4)
             sweep[name] = {"ms_per_step": ms, "value": args.sweep_chains * SAMPLES / (ms * 1e-3),
@@ -612,7 +681,7 @@ def run_ours(args):
     if args.target_solves:
         try:
             de = out.get("mixed", {}).get("dE_rel")
-            out["target"] = target_form(pkg, args.target_solves, local, out["sr_steps_per_s"], de)
+            out["target"] = target_form(pkg, args.target_solves, local, out["fp64_plain"]["sr_steps_per_s"], de)
         except Exception as e:  # reported, never fatal to the headline line
             out["target"] = {"error": f"{type(e).__name__}: {e}"}
 
@@ -620,9 +689,10 @@ def run_ours(args):
     if args.precision_chains:
         out["precision_form"] = precision_form(pkg, args.precision_chains, 64, 1, local)
 
-    # ---- serving loop (config-5 style Poisson arrivals) ----
+    # ---- serving loop (config-5 style Poisson arrivals, rate sweep) ----
     if args.serve_rates:
-        out["serving"] = [serving_form(pkg, float(r), args.serve_window, local) for r in args.serve_rates.split(",")]
+        rates = [float(r) for r in args.serve_rates.split(",")]
+        out["serving"], out["serving_summary"] = serving_sweep(pkg, rates, args.serve_window, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, args.warmup)
     if rank == 0:
@@ -667,9 +737,12 @@ def main():
     ap.add_argument("--batch-solves", type=int, default=64, help="solves of the batched line (0: skip)")
     ap.add_argument("--target-solves", type=int, default=32,
                     help="solves of the headline shape in the batched mixed target line (0: skip)")
-    ap.add_argument("--serve-rates", default="4,16", help="arrival rates (1/s) of the serving lines ('' : skip)")
+    ap.add_argument("--serve-rates", default="1,2,4,8,16,32,64",
+                    help="arrival rates (1/s) of the serving lines ('' : skip)")
+    ap.add_argument("--precision", default="certified", choices=sorted(FORMS),
+                    help="the headline's form: certified (FP64 results, FP32-certified decisions) or fp64")
     ap.add_argument("--precision-chains", type=int, default=16384, help="chains of the precision-form line (0: skip)")
-    ap.add_argument("--serve-window", type=float, default=5.0, help="seconds of arrivals per serving line")
+    ap.add_argument("--serve-window", type=float, default=4.0, help="seconds of arrivals per serving line")
     ap.add_argument("--kernel-case", default="", help="N,M,K,chains,samples: one mixed step, then its kernels timed alone")
     args = ap.parse_args()
     if args.kernel_case:

@@ -64,6 +64,16 @@ extern "C" {
                                       * FP32 accumulation) where the shape allows (N <= 143, M <= 255) and
                                       * pays off (N M >= 4096); 2: wherever the shape allows; 0: FP32
                                       * CUDA cores. All agree to FP32 rounding. */
+#define NQES_OPT_FUSED_SV 9          /* 1 (default): with real arithmetic in the FP64 and CERTIFIED forms,
+                                      * S·v reads the stored O once per product (one persistent kernel:
+                                      * u = O v and O^T u per staged group of rows, double-float
+                                      * arithmetic on the FP32 pipe, within 1e-13 of FP64 sums) where
+                                      * P is even and at most 8192; 0: two FP64 passes. */
+#define NQES_OPT_TEST_STAGE_WAIT 10  /* test hook for the bounded device-side waits: 1 = the decision-warp
+                                      * sampler stages its tables and its wait is for bytes that no copy
+                                      * delivers, with a short poll limit, so the step returns
+                                      * NQES_ERR_TIMEOUT and the context stays usable; 0 (default): off.
+                                      * Only for shapes with that sampler (MIXED / CERTIFIED, real). */
 #define NQES_OPT_MIXED_EXACT 6       /* 1: MIXED takes every accept decision by its exact FP64 path
                                       * (verification of that path); 0 (default): only when the FP32
                                       * bound cannot decide. */
@@ -108,6 +118,7 @@ typedef struct nqes_step_info {
 #define NQES_KERNEL_SV_ROWS 2  /* u = O v over the stored log-derivatives */
 #define NQES_KERNEL_SV_COLS 3  /* y = O^H u over the stored log-derivatives */
 #define NQES_KERNEL_MOMENTS 4  /* o, <|O|^2>, <E conj O> column reductions */
+#define NQES_KERNEL_SV 5       /* the step's S·v passes (the fused kernel where NQES_OPT_FUSED_SV applies) */
 
 /* Create a context for N spins, M hidden units, K states on CUDA `device`,
  * for H = sum_{i!=j} J_ij sz_i sz_j - h sum_i sx_i with the diagonal term

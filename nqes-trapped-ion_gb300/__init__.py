@@ -24,6 +24,7 @@ ERR_CUDA, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_INVALID, ERR_STATE = -1, -2, 
 ARITH_AUTO, ARITH_COMPLEX, ARITH_REAL = 0, 1, 2
 OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP, OPT_PRECISION = 1, 2, 3, 4
 OPT_REJECT_FILTER, OPT_MIXED_EXACT, OPT_AUTOTUNE, OPT_TENSOR_CORES = 5, 6, 7, 8
+OPT_FUSED_SV, OPT_TEST_STAGE_WAIT = 9, 10
 PRECISION_FP64, PRECISION_MIXED, PRECISION_CERTIFIED = 0, 1, 2
 HAM_ISING_LIKE, HAM_HEISENBERG_LIKE = 0, 1
 
@@ -35,7 +36,7 @@ EXPORTS = [
     "nqes_footprint_bytes", "nqes_server_create", "nqes_server_submit", "nqes_server_poll", "nqes_server_status",
     "nqes_server_destroy", "nqes_server_last_error", "nqes_server_times", "nqes_set_hamiltonian",
 ]
-KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS = 1, 2, 3, 4
+KERNEL_SAMPLE, KERNEL_SV_ROWS, KERNEL_SV_COLS, KERNEL_MOMENTS, KERNEL_SV = 1, 2, 3, 4, 5
 
 
 class NqesError(RuntimeError):

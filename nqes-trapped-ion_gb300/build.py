@@ -21,7 +21,8 @@ OBJDIR = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["kernels_sample.cu", "kernels_sample_mixed.cu", "kernels_sample_warp.cu", "kernels_sample_warp_k34.cu",
-           "kernels_solve.cu", "kernels_factored.cu", "kernels_factored_tc.cu", "nqes_api.cu", "sv_static.cu", "nqes_server.cc"]
+           "kernels_solve.cu", "kernels_sv_fused.cu", "kernels_factored.cu", "kernels_factored_tc.cu", "nqes_api.cu",
+           "sv_static.cu", "nqes_server.cc"]
 HEADERS = ["nqes_math.cuh", "pcg64.cuh", "nqes_internal.h", "tma_stage.cuh", "sample_warp.cuh", "tc_util.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -64,7 +65,7 @@ def build_library(verbose=False):
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     lib = os.path.join(LIBDIR, "libnqes.so")
     if _stale(lib, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", lib, *objs, "-lcudart", "-lpthread"]
+        cmd = [nvcc(), *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", lib, *objs, "-lcudart", "-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link of libnqes.so failed:\n{r.stderr}")
@@ -153,6 +154,8 @@ def build_cli(shapes=None):
     lib = build_library()
     os.makedirs(BINDIR, exist_ok=True)
     objs = [_cli_object(s) for s in CLI_SOURCES]
+    for n in sorted({sh[0] for sh in (shapes or DEFAULT_SHAPES)}):
+        jmat_header(n)  # before the parallel links: shapes that share N share the header
     with cf.ThreadPoolExecutor(max_workers=8) as ex:
         return list(ex.map(lambda sh: _cli_binary(sh, objs, lib), shapes or DEFAULT_SHAPES))
 

@@ -61,6 +61,7 @@ template <int JT, int JB, int RB>
 __global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F, const float *__restrict__ v,
                                                                      float *__restrict__ u) {
     extern __shared__ float4 smem4[];
+    if (loop_guard_off(F.guard)) return;
     constexpr int WS = JT * JB, NG = kThreads / JT;
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K, IC = F.ic;
     float *sw = reinterpret_cast<float *>(smem4);  // IC x WS
@@ -194,6 +195,7 @@ __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_g
 template <int IB, int JB>
 __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int gn, const float *__restrict__ w,
                                                      const cplx *__restrict__ E, float *__restrict__ out) {
+    if (loop_guard_off(F.guard)) return;
     constexpr int WS = kJT * JB, kStage = cols_stage(JB);
     extern __shared__ float4 smem4[];
     float *st = reinterpret_cast<float *>(smem4);          // [2][kStage][WS] tanh rows (second factor: [2][kStage][WS])

@@ -51,6 +51,7 @@ RowsTcShape rows_tc_shape(const FactArgs &F) {
 
 // Split image of Wt for every state: [k][split][K-major MN x NP] BF16.
 __global__ void k_rows_bimg(FactArgs F, int NP, int MN, const float *__restrict__ v, uint16_t *__restrict__ img) {
+    if (loop_guard_off(F.guard)) return;
     const int N = F.N, M = F.M, L = N + M + N * M;
     const size_t per = size_t(MN) * NP, total = size_t(F.K) * per;
     for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
@@ -78,6 +79,7 @@ __global__ void __launch_bounds__(kTcThreads) k_frows_tc(FactArgs F, int NP, int
                                                        size_t bbytes, const uint16_t *__restrict__ img,
                                                        float *__restrict__ u, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    if (loop_guard_off(F.guard)) return;  // before any barrier init or tensor-memory allocation
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, MT = F.MT, KK = K * K;
     unsigned char *sA = smem_raw;
     unsigned char *sB = smem_raw + abytes;
@@ -281,6 +283,7 @@ __global__ void __launch_bounds__(kColThreadsTc) k_fcols_tc(FactArgs F, int mode
                                                           const float *__restrict__ w, const cplx *__restrict__ E,
                                                           float *__restrict__ out, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    if (loop_guard_off(F.guard)) return;  // before any barrier init or tensor-memory allocation
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K, P = K * L;
     float *sT = reinterpret_cast<float *>(smem_raw);  // [2][rows][MT]: two batches, or (mode 3) two factors
     unsigned char *sA = smem_raw + tbytes;

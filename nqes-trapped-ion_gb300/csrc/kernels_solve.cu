@@ -160,7 +160,8 @@ __global__ void k_moment_final(int Ns, int P, int rchunks, const StepParams *sp,
 // ---------------- S·v ----------------
 
 // u_s = sum_p O_sp v_p: one warp per row.
-template <class S> __global__ void k_sv_rows(int Ns, int P, const S *O, const S *v, S *u) {
+template <class S> __global__ void k_sv_rows(int Ns, int P, const S *O, const S *v, S *u, const int *guard) {
+    if (loop_guard_off(guard)) return;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= Ns) return;
     const S *row = O + size_t(warp) * P;
@@ -171,7 +172,9 @@ template <class S> __global__ void k_sv_rows(int Ns, int P, const S *O, const S 
 }
 
 // ypart[r][p] = sum_{s in chunk r} conj(O_sp) u_s
-template <class S> __global__ void k_sv_cols(int Ns, int P, int rchunks, const S *O, const S *u, S *ypart) {
+template <class S>
+__global__ void k_sv_cols(int Ns, int P, int rchunks, const S *O, const S *u, S *ypart, const int *guard) {
+    if (loop_guard_off(guard)) return;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int r = blockIdx.y;
     if (p >= P) return;
@@ -215,7 +218,7 @@ template <class S> struct ColSumSmem {
 // form) are summed with two-float accumulators, converted to FP64 once.
 template <class S>
 __device__ S sv_colsum(const SolveBufs<S> &B, int p, int pl, int rg, ColSumSmem<S> &cs) {
-    const int R = B.rchunks, r0 = int(int64_t(R) * rg / kRG), r1 = int(int64_t(R) * (rg + 1) / kRG);
+    const int R = B.fact ? B.rchunks : B.svp, r0 = int(int64_t(R) * rg / kRG), r1 = int(int64_t(R) * (rg + 1) / kRG);
     const bool in = p < B.sh.P;
     S y = zero<S>();
     if (B.fact) {
@@ -236,7 +239,7 @@ __device__ S sv_colsum(const SolveBufs<S> &B, int p, int pl, int rg, ColSumSmem<
         }
     } else {
         if (in)
-            for (int r = r0; r < r1; r++) y = y + B.ypart[size_t(r) * B.sh.P + p];
+            for (int r = r0; r < r1; r++) y = y + B.ysv[size_t(r) * B.sh.P + p];
         cs.y[rg][pl] = y;
         __syncthreads();
         if (rg == 0) {
@@ -359,6 +362,7 @@ template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(
     __shared__ double sh[32];
     __shared__ S ovs;
     __shared__ ColSumSmem<S> cs;
+    if (loop_guard_off(B.guard)) return;
     const LzState &lz = *B.lz;
     const unsigned long long j = lz.j;
     const int nb = mr_blocks(B.sh.P);
@@ -387,6 +391,7 @@ template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(
 template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
     __shared__ double sh[32];
     __shared__ double alfa_s;
+    if (loop_guard_off(B.guard)) return;
     const LzState &lz = *B.lz;
     const unsigned long long j = lz.j;
     const int nb = mr_blocks(B.sh.P);
@@ -417,6 +422,7 @@ template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
     __shared__ double sh[32];
     __shared__ double s_alfa, s_bn2;
     __shared__ int last;
+    if (loop_guard_off(B.guard)) return;
     LzState &lz = *B.lz;
     const unsigned long long j = lz.j;
     const int nb = mr_blocks(B.sh.P);
@@ -739,7 +745,20 @@ __global__ void k_update(Shape sh, const StepParams *sp, const S *x, cplx *a, cp
     }
 }
 
+// The batched MINRES-QLP loop runs while any member's solve runs.
+__global__ void k_batch_cond(const int *const *flags, int n, cudaGraphConditionalHandle cond) {
+    int any = 0;
+    for (int i = threadIdx.x; i < n; i += 32) any |= *reinterpret_cast<const volatile int *>(flags[i]) != 0;
+    any = __any_sync(0xffffffffu, any);
+    if (threadIdx.x == 0) cudaGraphSetConditional(cond, any ? 1u : 0u);
+}
+
 }  // namespace
+
+cudaError_t launch_batch_cond(const int *const *flags, int n, cudaGraphConditionalHandle cond, cudaStream_t st) {
+    k_batch_cond<<<1, 32, 0, st>>>(flags, n, cond);
+    return cudaGetLastError();
+}
 
 template <class S> cudaError_t launch_moments(const SolveBufs<S> &B, cudaStream_t st) {
     const int P = B.sh.P, nb = (P + kVecThreads - 1) / kVecThreads;
@@ -783,8 +802,11 @@ template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, co
         const cudaError_t e = launch_frows(B.F, B.v32, B.u32, st);
         return e != cudaSuccess ? e : launch_fcols(B.F, B.u32, B.ypart32, st);
     }
-    k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u);
-    k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart);
+    if constexpr (std::is_same<S, double>::value) {
+        if (B.fG) return launch_sv_fused(B.Ns, P, B.fG, B.svp, B.O, v, B.ysv, B.err, B.guard, st);
+    }
+    k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u, B.guard);
+    k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart, B.guard);
     return cudaGetLastError();
 }
 
@@ -810,7 +832,7 @@ template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &B, cudaSt
     if (B.fact)
         return launch_frows(B.F, B.v32, B.u32, st);
     else
-        k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O, B.v, B.u);
+        k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.O, B.v, B.u, B.guard);
     return cudaGetLastError();
 }
 
@@ -820,8 +842,12 @@ template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &B, cudaSt
     if (B.fact)
         return launch_fcols(B.F, B.u32, B.ypart32, st);
     else
-        k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O, B.u, B.ypart);
+        k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, B.sh.P, B.rchunks, B.O, B.u, B.ypart, B.guard);
     return cudaGetLastError();
+}
+
+template <class S> cudaError_t launch_sv_only(const SolveBufs<S> &B, cudaStream_t st) {
+    return launch_sv_passes(B, B.v, st);
 }
 
 template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &B, cudaStream_t st) {
@@ -863,6 +889,7 @@ cudaError_t launch_update(const Shape &sh, const StepParams *sp, const S *x, cpl
     template cudaError_t launch_apply_S<S>(const SolveBufs<S> &, const S *, S *, cudaStream_t);          \
     template cudaError_t launch_sv_rows_only<S>(const SolveBufs<S> &, cudaStream_t);                     \
     template cudaError_t launch_sv_cols_only<S>(const SolveBufs<S> &, cudaStream_t);                     \
+    template cudaError_t launch_sv_only<S>(const SolveBufs<S> &, cudaStream_t);                          \
     template cudaError_t launch_moment_part_only<S>(const SolveBufs<S> &, cudaStream_t);                 \
     template cudaError_t launch_update<S>(const Shape &, const StepParams *, const S *, cplx *, cplx *, \
                                           cplx *, cudaStream_t);

@@ -11,6 +11,7 @@
 // count, samples per chain, burn-in, arithmetic or thread shape change.
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -18,11 +19,25 @@
 #include <type_traits>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/nqes.h"
 #include "nqes_internal.h"
 #include "pcg64.cuh"
 
 using namespace nqes;
+
+namespace {
+// NVTX range over a host-side phase of an SR step (visible in Nsight Systems:
+// argument checks and buffer sizing, graph capture, the graph launch, the
+// result read-back). The device phases inside a step run in one CUDA graph.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+}  // namespace
 
 struct nqes_ctx {
     Shape sh{};
@@ -55,6 +70,11 @@ struct nqes_ctx {
     bool autotune = false;
     long long tune_key[5] = {-1, -1, -1, -1, -1};
     int tk_tuned = 0, dw_force_warps = 0, dw_force_stage = 0;
+    // Chains the sampler's launch shape is planned for (0: the step's own).
+    // A batch sets it to the chains of all its members while it builds its
+    // graph: the members' samplers then share the GPU.
+    int plan_chains = 0;
+    int stage_fault = 0;  // NQES_OPT_TEST_STAGE_WAIT
     bool mixed_exact_all = false;  // MIXED: every decision through the exact FP64 path
     bool weights_real = true;
     std::string err;
@@ -78,6 +98,11 @@ struct nqes_ctx {
     void *u = nullptr, *ypart = nullptr, *vecs = nullptr, *ovpart = nullptr;
     double *part = nullptr;
     int rchunks = 1;
+    // fused S·v over the dense FP64 O (real arithmetic): rows per staged
+    // group, CTAs and their partials (fG = 0: the two-pass S·v)
+    int fG = 0, fctas = 0;
+    double *ysv = nullptr;
+    int fused_opt = 1, step_fused_opt = 1;  // NQES_OPT_FUSED_SV, and its value when the buffers were sized
 
     // Generation of the step buffers: bumped whenever they are freed or
     // reallocated, so that a batch graph that baked in the old addresses is
@@ -141,6 +166,8 @@ void free_step_buffers(nqes_ctx *ctx) {
     dfree(ctx->u32);
     dfree(ctx->ypart32);
     dfree(ctx->tcimg);
+    dfree(ctx->ysv);
+    ctx->fG = ctx->fctas = 0;
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
     ctx->exec = nullptr;
     ctx->g_chains = -1;
@@ -152,7 +179,7 @@ void free_step_buffers(nqes_ctx *ctx) {
 
 int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     if (ctx->chains == chains && ctx->m == m && ctx->arith == arith && ctx->step_precision == ctx->precision &&
-        ctx->O)
+        ctx->step_fused_opt == ctx->fused_opt && ctx->O)
         return NQES_OK;
     free_step_buffers(ctx);
     const Shape &sh = ctx->sh;
@@ -191,6 +218,17 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
         return rc;
     }
     ctx->step_precision = ctx->precision;
+    ctx->step_fused_opt = ctx->fused_opt;
+    if (!mixed && arith == NQES_ARITH_REAL && ctx->fused_opt && sv_fused_plan(int(Ns), sh.P, &ctx->fG, &ctx->fctas)) {
+        if ((rc = dalloc(ctx, &ctx->ysv, size_t(ctx->fctas) * P))) return rc;
+        const cudaError_t e = prepare_sv_fused(sh.P);
+        if (e != cudaSuccess) {
+            ctx->err = std::string("fused S·v attributes: ") + cudaGetErrorString(e);
+            return NQES_ERR_CUDA;
+        }
+    } else {
+        ctx->fG = ctx->fctas = 0;
+    }
     if ((rc = dalloc(ctx, &ctx->E, Ns * sh.K * sh.K))) return rc;
     if ((rc = dalloc(ctx, &ctx->spins, Ns * sh.K * sh.NW))) return rc;
     if ((rc = dalloc(ctx, &ctx->accepted, size_t(chains)))) return rc;
@@ -264,6 +302,13 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     B.eloc = ctx->eloc_d;
     B.err = ctx->err_d;
     B.use_cond = 0;
+    B.svp = ctx->rchunks;
+    B.ysv = B.ypart;
+    if (std::is_same<S, double>::value && ctx->fG) {
+        B.fG = ctx->fG;
+        B.svp = ctx->fctas;
+        B.ysv = reinterpret_cast<S *>(ctx->ysv);
+    }
     if (ctx->step_precision == NQES_PRECISION_MIXED) {
         B.O = nullptr;
         B.fact = 1;
@@ -310,6 +355,7 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.G = ctx->dw_G;
     A.U = ctx->dw_U;
     A.MP = ctx->dw_MP;
+    A.stage_fault = ctx->stage_fault;
     A.out64 = ctx->step_precision == NQES_PRECISION_CERTIFIED ? 1 : 0;
     if (A.out64) {
         // dense FP64 O and the FP64 tables of the step (ch, sh, eup, edn)
@@ -351,6 +397,12 @@ void dw_plan(nqes_ctx *ctx, int chains, int *warps, int *stage) {
         *stage = ctx->dw_force_stage;
         return;
     }
+    if (ctx->stage_fault) {  // test hook: a staged plan, so that the staging wait exists
+        *warps = 1;
+        *stage = 1;
+        return;
+    }
+    if (ctx->plan_chains) chains = ctx->plan_chains;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     for (int w = 4; w >= 1; w >>= 1)
@@ -459,20 +511,21 @@ int choose_tk(nqes_ctx *ctx, int chains) {
     } else {
         int dev_sms = 152;
         cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        if (ctx->plan_chains) chains = ctx->plan_chains;
         tk = chains <= dev_sms ? std::min(128, (M + 31) / 32 * 32) : tmin;
     }
     return std::min(std::max(tk, tmin), tmax);
 }
 
-// Appends one SR step of ctx to graph g as three nodes with no dependency on
-// anything else in g: the sampling segment (tables, sampler, moments, MINRES
-// init), a conditional while node running the MINRES-QLP body, the update.
-template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, int m, int burn, int tk) {
+// Captures the sampling segment of one SR step into *out: the error word
+// cleared, the tables, the sampler, the moments, and the MINRES-QLP init with
+// the first Lanczos step. Sets the sampler's shared-memory attribute first
+// (that call is not allowed during a capture).
+template <class S> int capture_sampling(nqes_ctx *ctx, int chains, int m, int burn, int tk, cudaGraph_t *out) {
     SampleArgs<S> A = sample_args<S>(ctx, chains, m, burn, tk);
     SolveBufs<S> B = solve_bufs<S>(ctx);
     const int threads = sample_threads(ctx->sh.K, tk);
     {
-        // the sampler's dynamic shared memory attribute must be set before capture
         const bool mixed = uses_mixed_sampler(ctx);
         const size_t smem = mixed ? mixed_sampler_smem(ctx) : sample_smem_bytes(ctx->sh, threads, sizeof(S) == sizeof(cplx));
         if (smem > 227 * 1024) {
@@ -484,13 +537,6 @@ template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, 
         else
             NQES_CUDA(prepare_sample<S>(ctx->sh));
     }
-    cudaGraph_t gA = nullptr, gC = nullptr;
-    cudaGraphConditionalHandle cond;
-    // Default value 1 on every launch: the body runs at least once, and its
-    // scalar kernel writes 0 as soon as the solve has finished (or was
-    // never needed), so the loop always ends.
-    NQES_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
-
     NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(ctx->err_d, 0, sizeof(int), ctx->st);
     cudaError_t le;
@@ -504,14 +550,47 @@ template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, 
     }
     if (le == cudaSuccess) le = launch_moments<S>(B, ctx->st);
     if (le == cudaSuccess) le = launch_minres_init<S>(B, ctx->st);
-    cudaError_t ce = cudaStreamEndCapture(ctx->st, &gA);
+    const cudaError_t ce = cudaStreamEndCapture(ctx->st, out);
     if (le != cudaSuccess || ce != cudaSuccess) {
-        ctx->err = std::string("capture of the sampling segment: ") +
-                   cudaGetErrorString(le != cudaSuccess ? le : ce);
+        ctx->err = std::string("capture of the sampling segment: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
+        if (ce == cudaSuccess && *out) cudaGraphDestroy(*out);
+        *out = nullptr;
         return NQES_ERR_CUDA;
     }
+    return NQES_OK;
+}
+
+// Captures the update w -= lr x into *out.
+template <class S> int capture_update(nqes_ctx *ctx, cudaGraph_t *out) {
+    SolveBufs<S> B = solve_bufs<S>(ctx);
+    NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    const cudaError_t le = launch_update<S>(ctx->sh, ctx->sp, B.x, ctx->a, ctx->b, ctx->w, ctx->st);
+    const cudaError_t ce = cudaStreamEndCapture(ctx->st, out);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        ctx->err = std::string("capture of the update: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
+        if (ce == cudaSuccess && *out) cudaGraphDestroy(*out);
+        *out = nullptr;
+        return NQES_ERR_CUDA;
+    }
+    return NQES_OK;
+}
+
+// Appends one SR step of ctx to graph g as three nodes with no dependency on
+// anything else in g: the sampling segment (tables, sampler, moments, MINRES
+// init), a conditional while node running the MINRES-QLP body, the update.
+template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, int m, int burn, int tk) {
+    SolveBufs<S> B = solve_bufs<S>(ctx);
+    cudaGraph_t gA = nullptr, gC = nullptr;
+    int rc = capture_sampling<S>(ctx, chains, m, burn, tk, &gA);
+    if (rc) return rc;
+    cudaGraphConditionalHandle cond;
+    // Default value 1 on every launch: the body runs at least once, and its
+    // scalar kernel writes 0 as soon as the solve has finished (or was
+    // never needed), so the loop always ends.
+    NQES_CUDA(cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault));
     cudaGraphNode_t nA, nW, nC;
     NQES_CUDA(cudaGraphAddChildGraphNode(&nA, g, nullptr, 0, gA));
+    cudaGraphDestroy(gA);
     cudaGraphNodeParams cp{};
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = cond;
@@ -525,29 +604,78 @@ template <class S> int add_step_nodes(nqes_ctx *ctx, cudaGraph_t g, int chains, 
     // scalar kernel sets the loop condition) on st_qlp; the first Lanczos step
     // ran before the loop.
     NQES_CUDA(cudaStreamBeginCaptureToGraph(ctx->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    le = cudaEventRecord(ctx->ev_fork, ctx->st);
+    cudaError_t le = cudaEventRecord(ctx->ev_fork, ctx->st);
     if (le == cudaSuccess) le = cudaStreamWaitEvent(ctx->st_qlp, ctx->ev_fork, 0);
     if (le == cudaSuccess) le = launch_qlp_step<S>(B, ctx->st_qlp);
     if (le == cudaSuccess) le = launch_lanczos_step<S>(B, ctx->st);
     if (le == cudaSuccess) le = cudaEventRecord(ctx->ev_join, ctx->st_qlp);
     if (le == cudaSuccess) le = cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0);
-    ce = cudaStreamEndCapture(ctx->st, &body);
+    cudaError_t ce = cudaStreamEndCapture(ctx->st, &body);
     if (le != cudaSuccess || ce != cudaSuccess) {
         ctx->err = std::string("capture of the MINRES-QLP body: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
-        cudaGraphDestroy(gA);
         return NQES_ERR_CUDA;
     }
-    NQES_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
-    le = launch_update<S>(ctx->sh, ctx->sp, B.x, ctx->a, ctx->b, ctx->w, ctx->st);
-    ce = cudaStreamEndCapture(ctx->st, &gC);
-    if (le != cudaSuccess || ce != cudaSuccess) {
-        ctx->err = std::string("capture of the update: ") + cudaGetErrorString(le != cudaSuccess ? le : ce);
-        return NQES_ERR_CUDA;
-    }
+    if ((rc = capture_update<S>(ctx, &gC))) return rc;
     NQES_CUDA(cudaGraphAddChildGraphNode(&nC, g, &nW, 1, gC));
-    cudaGraphDestroy(gA);
     cudaGraphDestroy(gC);
     return NQES_OK;
+}
+
+// ---- pieces of the batch graph (one shared MINRES-QLP loop) ----
+
+// The member's sampling segment as a node of g with no dependencies.
+template <class S>
+int add_member_sampling(nqes_ctx *ctx, cudaGraph_t g, int chains, int m, int burn, int tk, cudaGraphNode_t *node) {
+    cudaGraph_t gA = nullptr;
+    const int rc = capture_sampling<S>(ctx, chains, m, burn, tk, &gA);
+    if (rc) return rc;
+    const cudaError_t e = cudaGraphAddChildGraphNode(node, g, nullptr, 0, gA);
+    cudaGraphDestroy(gA);
+    if (e != cudaSuccess) {
+        ctx->err = std::string("cudaGraphAddChildGraphNode: ") + cudaGetErrorString(e);
+        return NQES_ERR_CUDA;
+    }
+    return NQES_OK;
+}
+
+// The member's update as a node of g after `after`.
+template <class S> int add_member_update(nqes_ctx *ctx, cudaGraph_t g, cudaGraphNode_t after) {
+    cudaGraph_t gC = nullptr;
+    const int rc = capture_update<S>(ctx, &gC);
+    if (rc) return rc;
+    cudaGraphNode_t nC;
+    const cudaError_t e = cudaGraphAddChildGraphNode(&nC, g, &after, 1, gC);
+    cudaGraphDestroy(gC);
+    if (e != cudaSuccess) {
+        ctx->err = std::string("cudaGraphAddChildGraphNode: ") + cudaGetErrorString(e);
+        return NQES_ERR_CUDA;
+    }
+    return NQES_OK;
+}
+
+// Address of the member's QlpState::running in device memory.
+const int *running_flag(const nqes_ctx *ctx) {
+    return reinterpret_cast<const int *>(reinterpret_cast<const char *>(ctx->qs) + offsetof(QlpState, running));
+}
+
+// Captures the member's part of the shared loop body onto the capture that
+// `origin` carries: forked from `fork`, its QLP step j (st_qlp) beside its
+// Lanczos step j + 1 (st), both guarded by its running flag, joined back into
+// origin. The member's kernels are those of its own loop body.
+template <class S> cudaError_t capture_member_body(nqes_ctx *ctx, cudaStream_t origin, cudaEvent_t fork) {
+    SolveBufs<S> B = solve_bufs<S>(ctx);
+    B.use_cond = 0;
+    B.guard = running_flag(ctx);
+    B.F.guard = B.guard;
+    cudaError_t e = cudaStreamWaitEvent(ctx->st, fork, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->st_qlp, fork, 0);
+    if (e == cudaSuccess) e = launch_qlp_step<S>(B, ctx->st_qlp);
+    if (e == cudaSuccess) e = launch_lanczos_step<S>(B, ctx->st);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, ctx->st_qlp);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, ctx->ev_join, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_fork, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, ctx->ev_fork, 0);
+    return e;
 }
 
 template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
@@ -695,6 +823,10 @@ int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t 
         }
     }
     const int e = *ctx->err_host;
+    if (e & kErrTimeout) {  // first: what the step computed after a wait ran out is not meaningful
+        ctx->err = "a bounded device-side wait ran out (bulk staging into shared memory)";
+        return NQES_ERR_TIMEOUT;
+    }
     if (e & (kErrNonFinite | kErrMinresNonFinite)) {
         ctx->err = "non-finite value during the SR step (error bits " + std::to_string(e) + ")";
         return NQES_ERR_NONFINITE;
@@ -702,10 +834,6 @@ int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t 
     if (e & kErrSingular) {
         ctx->err = "a sample was taken at a singular Phi";
         return NQES_ERR_NONFINITE;
-    }
-    if (e & kErrTimeout) {
-        ctx->err = "a bounded device-side wait ran out (staging of the sampler's tables)";
-        return NQES_ERR_TIMEOUT;
     }
     return NQES_OK;
 }
@@ -994,6 +1122,28 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
             ctx->exec = nullptr;
         }
         return NQES_OK;
+    case NQES_OPT_TEST_STAGE_WAIT:
+        if (value != 0 && value != 1) {
+            ctx->err = "option value must be 0 or 1";
+            return NQES_ERR_INVALID;
+        }
+        if (value == 1 && !ctx->dw_U) {
+            ctx->err = "this shape has no staged sampler (the decision-warp form does not apply)";
+            return NQES_ERR_INVALID;
+        }
+        ctx->stage_fault = int(value);
+        if (ctx->exec) {  // the captured step bakes the sampler's arguments in
+            cudaGraphExecDestroy(ctx->exec);
+            ctx->exec = nullptr;
+        }
+        return NQES_OK;
+    case NQES_OPT_FUSED_SV:
+        if (value != 0 && value != 1) {
+            ctx->err = "option value must be 0 or 1";
+            return NQES_ERR_INVALID;
+        }
+        ctx->fused_opt = int(value);  // takes effect at the next step (the buffers are resized then)
+        return NQES_OK;
     case NQES_OPT_REJECT_FILTER:
     case NQES_OPT_MIXED_EXACT:
         if (value != 0 && value != 1) {
@@ -1074,11 +1224,20 @@ int nqes_init_weights(nqes_ctx *ctx, uint64_t seed) {
 int nqes_sr_step(nqes_ctx *ctx, uint64_t seed, int chains, int m, int burn, double lr, double reglam, double rtol,
                  uint64_t maxit, double *e_mat, nqes_step_info *info) {
     if (!ctx) return NQES_ERR_INVALID;
+    NvtxRange r_step("nqes_sr_step");
     int arith = 0;
-    int rc = step_prepare(ctx, seed, chains, m, burn, lr, reglam, rtol, maxit, &arith);
+    int rc;
+    {
+        NvtxRange r("prepare (arguments, buffers, autotune)");
+        rc = step_prepare(ctx, seed, chains, m, burn, lr, reglam, rtol, maxit, &arith);
+    }
     if (rc) return rc;
-    rc = arith == NQES_ARITH_COMPLEX ? sr_step_t<cplx>(ctx, chains, m, burn) : sr_step_t<double>(ctx, chains, m, burn);
+    {
+        NvtxRange r("graph (capture when the shape changed) and launch");
+        rc = arith == NQES_ARITH_COMPLEX ? sr_step_t<cplx>(ctx, chains, m, burn) : sr_step_t<double>(ctx, chains, m, burn);
+    }
     if (rc) return rc;
+    NvtxRange r_wait("device step and read-back");
     rc = step_readback(ctx, ctx->st);
     if (rc) return rc;
     NQES_CUDA(cudaStreamSynchronize(ctx->st));
@@ -1307,6 +1466,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
         }
         case NQES_KERNEL_SV_ROWS: return launch_sv_rows_only<S>(B, ctx->st);
         case NQES_KERNEL_SV_COLS: return launch_sv_cols_only<S>(B, ctx->st);
+        case NQES_KERNEL_SV: return launch_sv_only<S>(B, ctx->st);
         default: return launch_moment_part_only<S>(B, ctx->st);
         }
     };
@@ -1314,6 +1474,10 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
     case NQES_KERNEL_SAMPLE: *bytes = double(Ns) * (P * ss + KK * sizeof(cplx) + ctx->sh.K * ctx->sh.NW * 8); break;
     case NQES_KERNEL_SV_ROWS: *bytes = double(Ns) * P * ss + double(P) * ss + double(Ns) * ss; break;
     case NQES_KERNEL_SV_COLS: *bytes = double(Ns) * P * ss + double(Ns) * ss + double(ctx->rchunks) * P * ss; break;
+    case NQES_KERNEL_SV:  // fused: O once, v, one partial per CTA; two-pass: both passes
+        *bytes = B.fG ? double(Ns) * P * ss + double(P) * ss + double(B.svp) * P * ss
+                      : 2.0 * double(Ns) * P * ss + double(P) * ss + 2.0 * double(Ns) * ss + double(ctx->rchunks) * P * ss;
+        break;
     default: *bytes = double(Ns) * P * ss + double(Ns) * KK * sizeof(cplx) + 3.0 * ctx->rchunks * P * ss; break;
     }
     const bool mixed = ctx->step_precision == NQES_PRECISION_MIXED;
@@ -1324,6 +1488,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
         case NQES_KERNEL_SAMPLE: *bytes = fac + double(Ns) * KK * sizeof(cplx); break;
         case NQES_KERNEL_SV_ROWS: *bytes = fac + double(P) * 4 + double(Ns) * 4; break;
         case NQES_KERNEL_SV_COLS: *bytes = fac + double(Ns) * 4 + double(ctx->rchunks) * P * 4; break;
+        case NQES_KERNEL_SV: *bytes = 2.0 * fac + double(P) * 4 + 2.0 * double(Ns) * 4 + double(ctx->rchunks) * P * 4; break;
         default: *bytes = fac + double(Ns) * KK * sizeof(cplx) + 3.0 * ctx->rchunks * P * 4; break;
         }
         NQES_CUDA(prepare_mixed_sampler(ctx));
@@ -1350,8 +1515,7 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
 extern "C" {
 
 int nqes_time_kernel(nqes_ctx *ctx, int kernel, int reps, double *avg_ms, double *algorithmic_bytes) {
-    if (!ctx || !avg_ms || !algorithmic_bytes || reps < 1 || kernel < NQES_KERNEL_SAMPLE ||
-        kernel > NQES_KERNEL_MOMENTS)
+    if (!ctx || !avg_ms || !algorithmic_bytes || reps < 1 || kernel < NQES_KERNEL_SAMPLE || kernel > NQES_KERNEL_SV)
         return NQES_ERR_INVALID;
     if (!ctx->have_step) {
         ctx->err = "no SR step has run";
@@ -1487,6 +1651,8 @@ struct nqes_batch {
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev_fork = nullptr;      // fork of the members' loop bodies (capture only)
+    const int **flags_d = nullptr;      // device array: each member's QlpState::running
     cudaGraphExec_t exec = nullptr;
     std::vector<std::vector<long long>> keys;  // per member: what its captured nodes depend on (see the step)
     std::string err;
@@ -1525,10 +1691,19 @@ int nqes_batch_create(nqes_ctx *const *members, int count, nqes_batch **out) {
     b->m.assign(members, members + count);
     b->device = members[0]->device;
     if (cudaSetDevice(b->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+        cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess) {
         g_batch_create_error = "stream or event creation failed";
         nqes_batch_destroy(b);
         return NQES_ERR_CUDA;
+    }
+    std::vector<const int *> flags(count);
+    for (int i = 0; i < count; i++) flags[i] = running_flag(members[i]);
+    if (cudaMalloc(reinterpret_cast<void **>(&b->flags_d), sizeof(int *) * count) != cudaSuccess ||
+        cudaMemcpy(b->flags_d, flags.data(), sizeof(int *) * count, cudaMemcpyHostToDevice) != cudaSuccess) {
+        g_batch_create_error = "allocation of the batch's flag table failed";
+        nqes_batch_destroy(b);
+        return NQES_ERR_OOM;
     }
     *out = b;
     return NQES_OK;
@@ -1539,8 +1714,10 @@ int nqes_batch_destroy(nqes_batch *b) {
     cudaSetDevice(b->device);
     if (b->st) cudaStreamSynchronize(b->st);
     if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->flags_d) cudaFree(b->flags_d);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
     return NQES_OK;
@@ -1550,6 +1727,7 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
                        const double *lr, const double *reglam, const double *rtol, const uint64_t *maxit,
                        double *const *e_mats, nqes_step_info *infos, int *statuses, double *ms_total) {
     if (!b || !seeds || !chains || !samples || !burn || !lr || !reglam || !rtol || !maxit) return NQES_ERR_INVALID;
+    NvtxRange r_step("nqes_batch_sr_step");
     const int n = int(b->m.size());
     if (cudaSetDevice(b->device) != cudaSuccess) {
         b->err = "cudaSetDevice failed";
@@ -1559,6 +1737,17 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
     std::vector<std::vector<long long>> keys(n);
     if (statuses)
         for (int i = 0; i < n; i++) statuses[i] = NQES_ERR_STATE;  // not run (yet)
+    // The members' samplers share the GPU: plan their launch shapes for the
+    // chains of the whole batch (reset when this call returns).
+    long long total = 0;
+    for (int i = 0; i < n; i++) total += std::max(0, chains[i]);
+    struct PlanScope {
+        std::vector<nqes_ctx *> &m;
+        ~PlanScope() {
+            for (auto *c : m) c->plan_chains = 0;
+        }
+    } plan_scope{b->m};
+    for (int i = 0; i < n; i++) b->m[i]->plan_chains = int(std::min<long long>(total, 1 << 30));
     for (int i = 0; i < n; i++) {
         nqes_ctx *c = b->m[i];
         const int rc = step_prepare(c, seeds[i], chains[i], samples[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i],
@@ -1570,32 +1759,73 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
         }
         tks[i] = choose_tk(c, chains[i]);
         // everything the captured nodes bake in: counts, arithmetic, launch shape,
-        // precision, local-energy form and the options that select kernels
+        // precision, local-energy form, the options that select kernels, the
+        // planned chains and the generation of the step buffers
         long long delta_bits = 0;
         std::memcpy(&delta_bits, &c->ham_delta, sizeof(delta_bits));
         keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision, c->ham, delta_bits,
                    c->tensor_cores, c->reject_filter ? 1 : 0, c->mixed_exact_all ? 1 : 0, c->dw_force_warps,
-                   c->dw_force_stage, (long long)c->buf_gen};
+                   c->dw_force_stage, (long long)c->buf_gen, total, c->stage_fault};
     }
     if (!b->exec || keys != b->keys) {
+        NvtxRange r_build("batch graph capture");
         if (b->exec) {
             cudaGraphExecDestroy(b->exec);
             b->exec = nullptr;
         }
+        b->keys.clear();
+        // Graph: every member's sampling segment; ONE conditional while node
+        // whose body holds every member's loop body (each guarded by its own
+        // running flag) and then sets the loop condition from all the flags;
+        // every member's update. The loop runs max over members of their
+        // iteration counts, each member's kernels doing exactly the work of
+        // its own loop and skipping once its solve has stopped.
         cudaGraph_t g = nullptr;
         if (cudaGraphCreate(&g, 0) != cudaSuccess) {
             b->err = "cudaGraphCreate failed";
             return NQES_ERR_CUDA;
         }
+        auto fail = [&](int rc, const std::string &msg) {
+            b->err = msg;
+            cudaGraphDestroy(g);
+            return rc;
+        };
+        std::vector<cudaGraphNode_t> nA(n);
         for (int i = 0; i < n; i++) {
             nqes_ctx *c = b->m[i];
-            const int rc = arith[i] == NQES_ARITH_COMPLEX ? add_step_nodes<cplx>(c, g, chains[i], samples[i], burn[i], tks[i])
-                                                          : add_step_nodes<double>(c, g, chains[i], samples[i], burn[i], tks[i]);
-            if (rc) {
-                b->err = "member " + std::to_string(i) + ": " + c->err;
-                cudaGraphDestroy(g);
-                return rc;
-            }
+            const int rc = arith[i] == NQES_ARITH_COMPLEX
+                               ? add_member_sampling<cplx>(c, g, chains[i], samples[i], burn[i], tks[i], &nA[i])
+                               : add_member_sampling<double>(c, g, chains[i], samples[i], burn[i], tks[i], &nA[i]);
+            if (rc) return fail(rc, "member " + std::to_string(i) + ": " + c->err);
+        }
+        cudaGraphConditionalHandle cond;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) return fail(NQES_ERR_CUDA, std::string("cudaGraphConditionalHandleCreate: ") + cudaGetErrorString(e));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t nW;
+        e = cudaGraphAddNode(&nW, g, nA.data(), nullptr, n, &cp);
+        if (e != cudaSuccess) return fail(NQES_ERR_CUDA, std::string("cudaGraphAddNode (while): ") + cudaGetErrorString(e));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(b->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return fail(NQES_ERR_CUDA, std::string("capture of the batched loop body: ") + cudaGetErrorString(e));
+        cudaError_t le = cudaEventRecord(b->ev_fork, b->st);
+        for (int i = 0; i < n && le == cudaSuccess; i++)
+            le = arith[i] == NQES_ARITH_COMPLEX ? capture_member_body<cplx>(b->m[i], b->st, b->ev_fork)
+                                                : capture_member_body<double>(b->m[i], b->st, b->ev_fork);
+        if (le == cudaSuccess) le = launch_batch_cond(b->flags_d, n, cond, b->st);
+        const cudaError_t ce = cudaStreamEndCapture(b->st, &body);
+        if (le != cudaSuccess || ce != cudaSuccess)
+            return fail(NQES_ERR_CUDA, std::string("capture of the batched loop body: ") +
+                                           cudaGetErrorString(le != cudaSuccess ? le : ce));
+        for (int i = 0; i < n; i++) {
+            nqes_ctx *c = b->m[i];
+            const int rc = arith[i] == NQES_ARITH_COMPLEX ? add_member_update<cplx>(c, g, nW)
+                                                          : add_member_update<double>(c, g, nW);
+            if (rc) return fail(rc, "member " + std::to_string(i) + ": " + c->err);
         }
         const cudaError_t ie = cudaGraphInstantiate(&b->exec, g, 0);
         cudaGraphDestroy(g);

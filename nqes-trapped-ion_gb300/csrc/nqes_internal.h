@@ -94,6 +94,7 @@ struct MixedArgs {
     const float *bnd;                    // per (kk, i): float4 bound record, then per kk 2 max_j sum_i |w_ij|
     int G, U, MP;
     int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
+    int stage_fault;                     // test hook (NQES_OPT_TEST_STAGE_WAIT): the staging wait runs out
     // FP64 outputs (NQES_PRECISION_CERTIFIED): E from FP64 flip ratios and the
     // dense FP64 O (P per sample) instead of the FP32 factors
     int out64;
@@ -183,6 +184,7 @@ struct FactArgs {
     int tcc;           // column passes (S·v and moments) on the tensor cores
     uint16_t *tcimg;   // its BF16 split image of the parameter vector
     int *err;
+    const int *guard;  // see loop_guard_off (nullptr: no guard)
 };
 __host__ __device__ inline int fact_mt(int M) { return (M + 3) & ~3; }
 
@@ -239,6 +241,18 @@ template <class S> struct SolveBufs {
     int *err;
     cudaGraphConditionalHandle cond;
     int use_cond;
+    // Loop-body guard of a batched solve (nullptr outside a batch): the
+    // MINRES-QLP loop of a batch runs until every member has stopped, and a
+    // member's loop-body kernels return at entry once *guard (its
+    // QlpState::running) is 0. Its own loop condition is then left alone
+    // (use_cond 0): one kernel after all members' bodies sets the batch's.
+    const int *guard;
+    // Partials of O^H u that the Lanczos epilogue sums over (sv_colsum):
+    // svp rows of P at ysv. The two-pass S·v writes rchunks rows to ypart; the
+    // fused S·v (fG > 0: real arithmetic, kernels_sv_fused.cu) one row per CTA.
+    int svp;
+    S *ysv;
+    int fG;
     // Mixed precision (real arithmetic only, fact = 1): O held as its factors
     // and the two passes of S·v and the moments computed from them in FP32
     // (kernels_factored.cu); v is mirrored into v32 by the kernels that
@@ -247,6 +261,31 @@ template <class S> struct SolveBufs {
     FactArgs F;
     float *v32, *u32, *ypart32;
 };
+
+// Fused S·v over the dense FP64 O (kernels_sv_fused.cu): one read of O,
+// double-float arithmetic on the FP32 pipe. sv_fused_plan gives the rows per
+// staged group and the CTAs (false: the shape needs the two-pass S·v).
+bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out);
+cudaError_t prepare_sv_fused(int P);
+cudaError_t launch_sv_fused(int Ns, int P, int G, int ctas, const double *O, const double *v, double *ypart, int *err,
+                            const int *guard, cudaStream_t st);
+
+// Sets the batched MINRES-QLP loop's condition: 1 while any member's flag
+// (its QlpState::running) is set.
+cudaError_t launch_batch_cond(const int *const *flags, int n, cudaGraphConditionalHandle cond, cudaStream_t st);
+
+// True, uniformly over the block, when a loop-body guard is set and its flag
+// is 0: the kernel then returns at entry (every thread of the block, before
+// any barrier). The flag is read once by thread 0: in the loop body where the
+// member's solve stops, the QLP kernel beside may clear it while blocks of a
+// Lanczos kernel start, and the Lanczos step of that body is never used.
+__device__ __forceinline__ bool loop_guard_off(const int *guard) {
+    if (!guard) return false;
+    __shared__ int s_guard;
+    if (threadIdx.x == 0) s_guard = *reinterpret_cast<const volatile int *>(guard);
+    __syncthreads();
+    return s_guard == 0;
+}
 
 template <class S> cudaError_t launch_moments(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &b, cudaStream_t st);
@@ -258,6 +297,7 @@ template <class S> cudaError_t launch_qlp_step(const SolveBufs<S> &b, cudaStream
 template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &b, const S *v, S *out, cudaStream_t st);
 template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &b, cudaStream_t st);
+template <class S> cudaError_t launch_sv_only(const SolveBufs<S> &b, cudaStream_t st);  // the step's S·v passes
 template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_update(const Shape &sh, const StepParams *sp, const S *x, cplx *a, cplx *b,
                                              cplx *w, cudaStream_t st);

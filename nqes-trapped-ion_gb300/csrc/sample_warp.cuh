@@ -628,11 +628,18 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         if (writer) {
             mbar_init(sm.mbar, 1);
             mbar_expect_tx(sm.mbar, unsigned(4 * tb));
-            bulk_g2s(stc, A.cp, unsigned(tb), sm.mbar);
-            bulk_g2s(sts, A.spp, unsigned(tb), sm.mbar);
-            bulk_g2s(stwh, A.whp, unsigned(tb), sm.mbar);
-            bulk_g2s(stwl, A.wlp, unsigned(tb), sm.mbar);
-            const bool ok = mbar_wait(sm.mbar, 0);
+            bool ok;
+            if (A.stage_fault) {
+                // test hook: the phase waits for bytes that no copy delivers
+                // (nothing is in flight), under a short poll limit
+                ok = mbar_wait(sm.mbar, 0, 4096);
+            } else {
+                bulk_g2s(stc, A.cp, unsigned(tb), sm.mbar);
+                bulk_g2s(sts, A.spp, unsigned(tb), sm.mbar);
+                bulk_g2s(stwh, A.whp, unsigned(tb), sm.mbar);
+                bulk_g2s(stwl, A.wlp, unsigned(tb), sm.mbar);
+                ok = mbar_wait(sm.mbar, 0);
+            }
             sm.flag[2] = ok ? 1 : 0;
             if (!ok) atomicOr(A.err, kErrTimeout);
         }

@@ -34,9 +34,10 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
         : "memory");
 }
 
-// Bounded wait for phase `parity` of the mbarrier; false when it ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, unsigned parity) {
-    for (long long it = 0; it < kStageSpin; it++) {
+// Bounded wait for phase `parity` of the mbarrier: at most `polls` polls;
+// false when it ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mbar, unsigned parity, long long polls = kStageSpin) {
+    for (long long it = 0; it < polls; it++) {
         unsigned done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"

@@ -247,3 +247,36 @@ def test_evaluate_singular_phi_uses_the_pseudo_inverse(pkg, N, M, K, rows):
     Eref = np.linalg.pinv(Phi) @ HPhi
     assert rel_err(E[0], Eref) < 1e-10
     assert np.max(np.abs(O)) <= 1e-12 * max(1.0, np.max(np.abs(Phi)))
+
+
+def test_staging_wait_runs_out_and_reports_timeout(pkg):
+    """A bounded device-side wait that runs out is reported, not hung: with the
+    test hook, the sampler's table staging waits for bytes that no copy
+    delivers (nothing is in flight), gives up after its poll limit, and the
+    step returns NQES_ERR_TIMEOUT. The context stays usable: with the hook off
+    its next step equals a fresh context's."""
+    N, M, K = 32, 64, 2
+    w = pkg.synthetic_weights(N, M, K, 0.01, 5)
+
+    def make():
+        c = pkg.Context(N, M, K, synthetic_j(N), 0.595)
+        c.set_weights(*w)
+        c.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+        c.set_option(pkg.OPT_MINRES_CAP, 5)
+        return c
+
+    ctx = make()
+    ctx.set_option(pkg.OPT_TEST_STAGE_WAIT, 1)
+    with pytest.raises(pkg.NqesError) as e:
+        ctx.sr_step(7, 16, 4, 2, 0.0, 5.0, 1e-9, 100)
+    assert e.value.status == pkg.ERR_TIMEOUT
+    assert "wait ran out" in str(e.value)
+    ctx.set_option(pkg.OPT_TEST_STAGE_WAIT, 0)
+    ctx.set_weights(*w)
+    got, _ = ctx.sr_step(9, 16, 4, 2, 0.1, 5.0, 1e-9, 100)
+    ref = make()
+    want, _ = ref.sr_step(9, 16, 4, 2, 0.1, 5.0, 1e-9, 100)
+    assert np.array_equal(got, want)
+    assert np.array_equal(ctx.get_samples()[0], ref.get_samples()[0])
+    ctx.close()
+    ref.close()

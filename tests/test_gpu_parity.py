@@ -338,3 +338,34 @@ def test_certified_matches_fp64(pkg, N, M, K, chains, m):
         assert rel_err(a, b) < 1e-10
     assert rel_err(c["sv"], f["sv"]) < 1e-10
     assert rel_err(c["w"], f["w"]) < 1e-6
+
+
+@pytest.mark.parametrize("N,M,K,prec", [(8, 16, 2, 0), (32, 64, 2, 0), (32, 64, 2, 2), (12, 20, 3, 0)])
+def test_fused_sv_matches_two_pass(pkg, N, M, K, prec):
+    """The fused S·v (one read of the FP64 O per product, double-float
+    arithmetic on the FP32 pipe) against the two FP64 passes on the same
+    samples: S·v within 1e-13 relative, and a whole SR step (MINRES-QLP
+    iterations, flag, e_mat, updated weights) agreeing to the solver's
+    rounding."""
+    out = {}
+    for fused in (0, 1):
+        ctx = pkg.Context(N, M, K, synthetic_j(N), 0.595)
+        ctx.set_weights(*pkg.synthetic_weights(N, M, K, 0.02, 3))
+        ctx.set_option(pkg.OPT_PRECISION, prec)
+        ctx.set_option(pkg.OPT_FUSED_SV, fused)
+        e, info = ctx.sr_step(71, 64, 50, 16, 0.1, 10.0, 1e-9, 100000)
+        rng = np.random.default_rng(9)
+        vs = [rng.normal(size=ctx.P) for _ in range(3)]
+        out[fused] = dict(e=e, info=info, sv=[ctx.apply_S(v) for v in vs], w=ctx.get_weights(),
+                          spins=ctx.get_samples()[0])
+        ctx.close()
+    a, b = out[0], out[1]
+    assert np.array_equal(a["spins"], b["spins"])
+    for x, y in zip(a["sv"], b["sv"]):
+        assert rel_err(y, x) < 1e-13, rel_err(y, x)
+    assert a["info"]["minres_flag"] == b["info"]["minres_flag"]
+    assert abs(int(a["info"]["minres_iters"]) - int(b["info"]["minres_iters"])) <= 1
+    assert rel_err(b["e"], a["e"]) < 1e-13
+    wa = np.concatenate([z.ravel() for z in a["w"]])
+    wb = np.concatenate([z.ravel() for z in b["w"]])
+    assert rel_err(wb, wa) < 1e-6  # the solves agree to the rtol scale

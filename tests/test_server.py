@@ -121,3 +121,46 @@ def test_turnover_rebuilds_the_batch(pkg):
         alone.close()
         assert res[rid]["status"] == 0 and ares[aid]["status"] == 0
         assert res[rid]["energies"] == ares[aid]["energies"]
+
+
+@pytest.mark.gpu
+def test_request_arriving_during_a_step_equals_running_alone(pkg):
+    """A request submitted while another solve's batched steps are running on
+    the device joins the batch at the next step; both results equal those of
+    running each alone, bit for bit."""
+    import time
+    big = dict(n=32, m=64, k=2, h=0.6, prec=1, seed=51)
+    small = dict(n=12, m=24, k=2, h=0.9, prec=0, seed=53)
+
+    def submit(srv, s, steps, chains, m):
+        w = helpers.random_weights(s["n"], s["m"], s["k"], 0.05, s["seed"], real=True)
+        return srv.submit(s["n"], s["m"], s["k"], synthetic_j(s["n"]), weights=w, h=s["h"], seed=s["seed"],
+                          chains=chains, samples_per_chain=m, burn_in=8, reglam0=5.0, tol=1e-12, max_steps=steps,
+                          precision=s["prec"])
+
+    alone = {}
+    for s, args in ((big, (12, 128, 100)), (small, (3, 16, 20))):
+        srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+        submit(srv, s, *args)
+        (r,) = srv.wait_all(1)
+        srv.close()
+        assert r["status"] == 0
+        alone[s["seed"]] = r
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+    t0 = time.perf_counter()
+    id_big = submit(srv, big, 12, 128, 100)
+    # wait until the big solve's batched steps are under way, then submit
+    deadline = time.perf_counter() + 60
+    while srv.times()["steps"] < 2 and time.perf_counter() < deadline:
+        time.sleep(0.001)
+    t_small = time.perf_counter() - t0
+    id_small = submit(srv, small, 3, 16, 20)
+    res = {r["id"]: r for r in srv.wait_all(2)}
+    srv.close()
+    rb, rs = res[id_big], res[id_small]
+    assert rb["status"] == 0 and rs["status"] == 0
+    # the small solve was admitted while the big one was still stepping
+    assert t_small + rs["t_queued"] < rb["t_total"], (t_small, rs["t_queued"], rb["t_total"])
+    for r, s in ((rb, big), (rs, small)):
+        a = alone[s["seed"]]
+        assert r["steps"] == a["steps"] and r["energies"] == a["energies"] and r["best"] == a["best"]
