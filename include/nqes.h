@@ -64,11 +64,11 @@ extern "C" {
                                       * FP32 accumulation) where the shape allows (N <= 143, M <= 255) and
                                       * pays off (N M >= 4096); 2: wherever the shape allows; 0: FP32
                                       * CUDA cores. All agree to FP32 rounding. */
-#define NQES_OPT_FUSED_SV 9          /* 1 (default): with real arithmetic in the FP64 and CERTIFIED forms,
-                                      * S·v reads the stored O once per product (one persistent kernel:
-                                      * u = O v and O^T u per staged group of rows, double-float
-                                      * arithmetic on the FP32 pipe, within 1e-13 of FP64 sums) where
-                                      * P is even and at most 8192; 0: two FP64 passes. */
+#define NQES_OPT_FUSED_SV 9          /* 1: with real arithmetic in the FP64 and CERTIFIED forms, S·v reads
+                                      * the stored O once per product (one persistent kernel: u = O v and
+                                      * O^T u per staged group of rows, double-float arithmetic on the FP32
+                                      * pipe, within 1e-13 of FP64 sums) where P is even and at most 8192;
+                                      * 0: two FP64 passes; -1 (default): on in CERTIFIED, off in FP64. */
 #define NQES_OPT_TEST_STAGE_WAIT 10  /* test hook for the bounded device-side waits: 1 = the decision-warp
                                       * sampler stages its tables and its wait is for bytes that no copy
                                       * delivers, with a short poll limit, so the step returns

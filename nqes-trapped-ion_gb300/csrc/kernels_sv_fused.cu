@@ -7,8 +7,9 @@
 // FP64 pipe retires about two FMAs per SM per clock: 0.41 ms at N32 M64 K2.
 //
 // Here a persistent CTA per SM owns a contiguous range of rows and streams
-// them through shared memory in groups of G rows, double-buffered by bulk
-// copies (cp.async.bulk on an mbarrier, bounded waits). For each staged group
+// them through shared memory in groups of G rows (as many as two buffers of
+// shared memory hold, at most 16), double-buffered by bulk copies
+// (cp.async.bulk on an mbarrier, bounded waits). For each staged group
 //   pass 1: u_r = O_r . v for the group's rows, block-wide, and
 //   pass 2: y_p += O_rp u_r into the CTA's partial of O^T u (registers),
 // both from shared memory, so O leaves HBM once per S·v. The arithmetic is
@@ -19,8 +20,8 @@
 // The relative error of u and of the partials against FP64 sums of the same
 // terms is a few 2^-48 per term of sum |O v| (about 1e-14 at these sizes),
 // inside the 1e-12 parity bound. Entries below 2^-126 in magnitude count as
-// zero (absolute error under 1e-38); an entry of magnitude 2^127 or more, or a
-// non-finite one, sets kErrNonFinite.
+// zero (absolute error under 1e-38); an entry of O of magnitude 2^127 or
+// more, or a non-finite one, sets kErrNonFinite.
 //
 // Each CTA writes its partial y (converted to FP64) to ypart[cta]; the
 // Lanczos epilogue sums the partials over CTAs in a fixed order, so results
@@ -32,10 +33,6 @@
 
 namespace nqes {
 namespace {
-
-constexpr int kFsThreads = 512;  // 16 warps
-constexpr int kFsWarps = kFsThreads / 32;
-constexpr int kFsMaxG = 8;       // rows per staged group (registers per thread: 2 per row)
 
 // hi + lo = d to 2^-48 relative (see the file comment); returns false when
 // |d| >= 2^127 or d is not finite.
@@ -93,28 +90,33 @@ struct FusedSvArgs {
     const int *guard;
 };
 
-// Block: kFsThreads threads; thread t owns columns p = t + c kFsThreads
-// (c < C), holding v's split and its partial of O^T u for them in registers.
-template <int C>
-__global__ void __launch_bounds__(kFsThreads, 1) k_sv_fused(FusedSvArgs a) {
+constexpr int kFsMaxThreads = 1024;
+constexpr int kFsMaxWarps = kFsMaxThreads / 32;
+
+// Block: T = blockDim.x threads (a multiple of 32, T C >= P); thread t owns
+// columns p = t + c T (c < C), holding v's split and its partial of O^T u for
+// them in registers. Rows of a staged group are walked one at a time, so no
+// per-row state lives in registers.
+template <int C, int MaxT>
+__global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     extern __shared__ __align__(16) unsigned char fs_smem[];
     if (loop_guard_off(a.guard)) return;
-    const int P = a.P, G = a.G, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int P = a.P, G = a.G, T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
     double *buf0 = reinterpret_cast<double *>(fs_smem);
     double *buf1 = buf0 + size_t(G) * P;
-    float2 *red = reinterpret_cast<float2 *>(buf1 + size_t(G) * P);  // [kFsWarps][G]
-    float2 *us = red + kFsWarps * G;                                  // [G]
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(us + kFsMaxG);      // [2] (8-byte aligned: G, P even or 8-byte sized)
+    float2 *red = reinterpret_cast<float2 *>(buf1 + size_t(G) * P);  // [G][warps]
+    float2 *us = red + size_t(G) * kFsMaxWarps;                       // [G]
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(us + G + (G & 1));  // [2], 8-byte aligned
     const int r0 = int(int64_t(a.Ns) * blockIdx.x / gridDim.x), r1 = int(int64_t(a.Ns) * (blockIdx.x + 1) / gridDim.x);
     const int ngroups = (r1 - r0 + G - 1) / G;
 
     float vh[C], vl[C], yh[C], yl[C];
-    bool range_ok = true;
+    bool range_ok = true;  // of the O entries (v is not checked: a solve that never starts has v = 0/0)
 #pragma unroll
     for (int c = 0; c < C; c++) {
-        const int p = tid + c * kFsThreads;
+        const int p = tid + c * T;
         vh[c] = vl[c] = yh[c] = yl[c] = 0.f;
-        if (p < P) range_ok &= split_d(a.v[p], vh[c], vl[c]);
+        if (p < P) split_d(a.v[p], vh[c], vl[c]);
     }
     auto issue = [&](int g) {  // thread 0: group g into buffer g & 1
         const int rs = r0 + g * G, nr = min(G, r1 - rs);
@@ -142,59 +144,53 @@ __global__ void __launch_bounds__(kFsThreads, 1) k_sv_fused(FusedSvArgs a) {
             timed_out = true;
             break;
         }
-        // pass 1: split the staged entries in place (each thread its own
-        // columns, read back only by itself) and form the rows' dot products
-        float sh[kFsMaxG], sl[kFsMaxG];
+        // pass 1, row by row: split the staged entries in place (each thread
+        // its own columns, read back only by itself), the row's dot product
+        // with v, its warp sum to red[r][warp]
+        for (int r = 0; r < nr; r++) {
+            double *row = buf + size_t(r) * P;
+            // two accumulators (even and odd columns) for two independent chains
+            float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
 #pragma unroll
-        for (int r = 0; r < kFsMaxG; r++) sh[r] = sl[r] = 0.f;
-#pragma unroll
-        for (int c = 0; c < C; c++) {
-            const int p = tid + c * kFsThreads;
-            if (p < P) {
-#pragma unroll
-                for (int r = 0; r < kFsMaxG; r++) {
-                    if (r < nr) {
-                        double *at = buf + size_t(r) * P + p;
-                        float oh, ol;
-                        range_ok &= split_d(*at, oh, ol);
-                        *reinterpret_cast<float2 *>(at) = make_float2(oh, ol);
-                        df_mac(sh[r], sl[r], oh, ol, vh[c], vl[c]);
-                    }
+            for (int c = 0; c < C; c++) {
+                const int p = tid + c * T;
+                if (p < P) {
+                    float oh, ol;
+                    range_ok &= split_d(row[p], oh, ol);
+                    *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
+                    if (c & 1)
+                        df_mac(h2, l2, oh, ol, vh[c], vl[c]);
+                    else
+                        df_mac(h, l, oh, ol, vh[c], vl[c]);
                 }
             }
-        }
-        // block sums of the rows: warp shuffles, then the warps in order
+            df_add(h, l, h2, l2);
 #pragma unroll
-        for (int r = 0; r < kFsMaxG; r++) {
-            if (r < nr) {
-                float h = sh[r], l = sl[r];
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
-                    df_add(h, l, oh, ol);
-                }
-                if (lane == 0) red[warp * G + r] = make_float2(h, l);
+            for (int off = 16; off > 0; off >>= 1) {
+                const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
+                df_add(h, l, oh, ol);
             }
+            if (lane == 0) red[r * kFsMaxWarps + warp] = make_float2(h, l);
         }
         __syncthreads();
-        if (tid < nr) {
+        // u_r: the warps' sums in warp order, one warp per row
+        for (int r = warp; r < nr; r += nw) {
             float h = 0.f, l = 0.f;
-            for (int w = 0; w < kFsWarps; w++) df_add(h, l, red[w * G + tid].x, red[w * G + tid].y);
-            us[tid] = make_float2(h, l);
+            if (lane == 0)
+                for (int w = 0; w < nw; w++) df_add(h, l, red[r * kFsMaxWarps + w].x, red[r * kFsMaxWarps + w].y);
+            if (lane == 0) us[r] = make_float2(h, l);
         }
         __syncthreads();
         // pass 2: y_p += O_rp u_r over the group's rows
+        for (int r = 0; r < nr; r++) {
+            const float2 u = us[r];
+            const double *row = buf + size_t(r) * P;
 #pragma unroll
-        for (int r = 0; r < kFsMaxG; r++) {
-            if (r < nr) {
-                const float2 u = us[r];
-#pragma unroll
-                for (int c = 0; c < C; c++) {
-                    const int p = tid + c * kFsThreads;
-                    if (p < P) {
-                        const float2 o = *reinterpret_cast<const float2 *>(buf + size_t(r) * P + p);
-                        df_mac(yh[c], yl[c], o.x, o.y, u.x, u.y);
-                    }
+            for (int c = 0; c < C; c++) {
+                const int p = tid + c * T;
+                if (p < P) {
+                    const float2 o = *reinterpret_cast<const float2 *>(row + p);
+                    df_mac(yh[c], yl[c], o.x, o.y, u.x, u.y);
                 }
             }
         }
@@ -215,62 +211,96 @@ __global__ void __launch_bounds__(kFsThreads, 1) k_sv_fused(FusedSvArgs a) {
     if (!range_ok) atomicOr(a.err, kErrNonFinite);
 #pragma unroll
     for (int c = 0; c < C; c++) {
-        const int p = tid + c * kFsThreads;
+        const int p = tid + c * T;
         if (p < P) a.ypart[size_t(blockIdx.x) * P + p] = double(yh[c]) + double(yl[c]);
     }
 }
 
-template <int C> const void *fused_fn() { return reinterpret_cast<const void *>(k_sv_fused<C>); }
+// Columns per thread C and threads per block T (whole warps, T C >= P): the
+// fewest columns whose block fits its register budget: C = 1, 2, 4 with up to
+// 1024 threads (64 registers), 8 with up to 768, 16 with up to 512.
+constexpr int kFsShapes[5][2] = {{1, 1024}, {2, 1024}, {4, 1024}, {8, 768}, {16, 512}};
+bool fused_shape(int P, int *C, int *T) {
+    for (const auto &sh : kFsShapes) {
+        const int t = 32 * ((P + 32 * sh[0] - 1) / (32 * sh[0]));
+        if (t <= sh[1]) {
+            *C = sh[0];
+            *T = t;
+            return true;
+        }
+    }
+    return false;
+}
 
-int fused_cols(int P) {
-    const int c = (P + kFsThreads - 1) / kFsThreads;
-    return c <= 1 ? 1 : c <= 2 ? 2 : c <= 4 ? 4 : c <= 8 ? 8 : c <= 12 ? 12 : 16;
+template <class F> cudaError_t fused_dispatch(int C, F &&f) {
+    switch (C) {
+    case 1: return f(k_sv_fused<1, 1024>);
+    case 2: return f(k_sv_fused<2, 1024>);
+    case 4: return f(k_sv_fused<4, 1024>);
+    case 8: return f(k_sv_fused<8, 768>);
+    default: return f(k_sv_fused<16, 512>);
+    }
 }
 
 size_t fused_smem(int P, int G) {
-    return size_t(2) * G * P * sizeof(double) + (size_t(kFsWarps) * G + kFsMaxG) * sizeof(float2) + 2 * sizeof(uint64_t);
+    return size_t(2) * G * P * sizeof(double) + (size_t(G) * kFsMaxWarps + G + 1) * sizeof(float2) +
+           2 * sizeof(uint64_t);
 }
+
+constexpr int kFsMaxG = 16;
 
 }  // namespace
 
+cudaError_t prepare_sv_fused(int P) {
+    int C, T;
+    if (!fused_shape(P, &C, &T)) return cudaErrorInvalidValue;
+    return fused_dispatch(C, [](auto fn) { return allow_max_dynamic_smem(reinterpret_cast<const void *>(fn)); });
+}
+
+// Rows per staged group G and the grid: the G that keeps the most threads
+// resident per SM (blocks per SM from the occupancy calculator, which counts
+// the two buffers of G rows), the largest such G (fewer barriers per row);
+// the grid fills every SM with that many blocks.
 bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out) {
-    if (P % 2 || P > 16 * kFsThreads || Ns < 1) return false;  // rows 16-byte aligned; columns in registers
+    int C, T;
+    if (P % 2 || Ns < 1 || !fused_shape(P, &C, &T)) return false;  // rows 16-byte aligned; columns in registers
     int dev = 0, sms = 152, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    int G = kFsMaxG;
-    while (G > 1 && fused_smem(P, G) > size_t(optin) - 1024) G--;
-    if (fused_smem(P, G) > size_t(optin) - 1024) return false;
-    *G_out = G;
-    *ctas_out = std::max(1, std::min(sms, (Ns + G - 1) / G));
-    return true;
-}
-
-cudaError_t prepare_sv_fused(int P) {
-    switch (fused_cols(P)) {
-    case 1: return allow_max_dynamic_smem(fused_fn<1>());
-    case 2: return allow_max_dynamic_smem(fused_fn<2>());
-    case 4: return allow_max_dynamic_smem(fused_fn<4>());
-    case 8: return allow_max_dynamic_smem(fused_fn<8>());
-    case 12: return allow_max_dynamic_smem(fused_fn<12>());
-    default: return allow_max_dynamic_smem(fused_fn<16>());
+    if (prepare_sv_fused(P) != cudaSuccess) return false;
+    int best_G = 0, best_blocks = 0, best_threads = 0;
+    for (int G = 1; G <= kFsMaxG; G++) {
+        const size_t smem = fused_smem(P, G);
+        if (smem > size_t(optin) - 1024) break;
+        int blocks = 0;
+        const cudaError_t e = fused_dispatch(C, [&](auto fn) {
+            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, T, smem);
+        });
+        if (e != cudaSuccess || blocks < 1) break;
+        const int threads = std::min(blocks * T, 2048);
+        if (threads >= best_threads) {
+            best_threads = threads;
+            best_G = G;
+            best_blocks = blocks;
+        }
     }
+    if (!best_G) return false;
+    *G_out = best_G;
+    *ctas_out = std::max(1, std::min(sms * best_blocks, (Ns + best_G - 1) / best_G));
+    return true;
 }
 
 cudaError_t launch_sv_fused(int Ns, int P, int G, int ctas, const double *O, const double *v, double *ypart, int *err,
                             const int *guard, cudaStream_t st) {
     FusedSvArgs a{Ns, P, G, O, v, ypart, err, guard};
     const size_t smem = fused_smem(P, G);
-    switch (fused_cols(P)) {
-    case 1: k_sv_fused<1><<<ctas, kFsThreads, smem, st>>>(a); break;
-    case 2: k_sv_fused<2><<<ctas, kFsThreads, smem, st>>>(a); break;
-    case 4: k_sv_fused<4><<<ctas, kFsThreads, smem, st>>>(a); break;
-    case 8: k_sv_fused<8><<<ctas, kFsThreads, smem, st>>>(a); break;
-    case 12: k_sv_fused<12><<<ctas, kFsThreads, smem, st>>>(a); break;
-    default: k_sv_fused<16><<<ctas, kFsThreads, smem, st>>>(a); break;
-    }
-    return cudaGetLastError();
+    int C, T;
+    if (!fused_shape(P, &C, &T)) return cudaErrorInvalidValue;
+    return fused_dispatch(C, [&](auto fn) {
+        fn<<<ctas, T, smem, st>>>(a);
+        return cudaGetLastError();
+    });
 }
 
 }  // namespace nqes

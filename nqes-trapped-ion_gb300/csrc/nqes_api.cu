@@ -102,7 +102,7 @@ struct nqes_ctx {
     // group, CTAs and their partials (fG = 0: the two-pass S·v)
     int fG = 0, fctas = 0;
     double *ysv = nullptr;
-    int fused_opt = 1, step_fused_opt = 1;  // NQES_OPT_FUSED_SV, and its value when the buffers were sized
+    int fused_opt = -1, step_fused_opt = -1;  // NQES_OPT_FUSED_SV, and its value when the buffers were sized
 
     // Generation of the step buffers: bumped whenever they are freed or
     // reallocated, so that a batch graph that baked in the old addresses is
@@ -219,7 +219,10 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     }
     ctx->step_precision = ctx->precision;
     ctx->step_fused_opt = ctx->fused_opt;
-    if (!mixed && arith == NQES_ARITH_REAL && ctx->fused_opt && sv_fused_plan(int(Ns), sh.P, &ctx->fG, &ctx->fctas)) {
+    // the fused S·v: by default in the certified form (FP64-grade results);
+    // the FP64 form keeps IEEE FP64 arithmetic unless asked
+    const bool fused = ctx->fused_opt < 0 ? ctx->precision == NQES_PRECISION_CERTIFIED : ctx->fused_opt == 1;
+    if (!mixed && arith == NQES_ARITH_REAL && fused && sv_fused_plan(int(Ns), sh.P, &ctx->fG, &ctx->fctas)) {
         if ((rc = dalloc(ctx, &ctx->ysv, size_t(ctx->fctas) * P))) return rc;
         const cudaError_t e = prepare_sv_fused(sh.P);
         if (e != cudaSuccess) {
@@ -1138,8 +1141,8 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         }
         return NQES_OK;
     case NQES_OPT_FUSED_SV:
-        if (value != 0 && value != 1) {
-            ctx->err = "option value must be 0 or 1";
+        if (value != -1 && value != 0 && value != 1) {
+            ctx->err = "option value must be -1 (by precision), 0 or 1";
             return NQES_ERR_INVALID;
         }
         ctx->fused_opt = int(value);  // takes effect at the next step (the buffers are resized then)

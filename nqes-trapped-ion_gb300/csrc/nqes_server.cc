@@ -15,6 +15,15 @@
 //           their device memory and slot; results wait for nqes_server_poll.
 // Requests that arrive while others run join the next step's batch as memory
 // and slots free up, so their work overlaps on the device.
+//
+// Solves of very different sizes would make one batch wait for its largest
+// member every step (a step of N = 96, K = 4 takes ~100x one of N = 16), so
+// the server runs kLanes such workers, one per size class (parameters P =
+// K (N + M + N M) up to 5000, up to 20000, above), each with its own batch on
+// its own stream: the lanes' steps run side by side on the GPU, and a small
+// solve is never held back by a large one. The lanes share the queue (each
+// takes the oldest request of its class), the device-memory budget, the slot
+// count and the results.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -45,6 +54,26 @@ struct Solve {
     std::vector<std::complex<double>> emat;
 };
 
+constexpr int kLanes = 3;
+
+// Size class of a request: its lane.
+int lane_of(const nqes_request &r) {
+    const long long P = (long long)r.n_states * (r.n_spins + r.n_hidden + (long long)r.n_spins * r.n_hidden);
+    return P <= 5000 ? 0 : P <= 20000 ? 1 : 2;
+}
+
+// One lane: its worker's active solves and batch.
+struct Lane {
+    int index = 0;
+    std::vector<Solve *> active;
+    nqes_batch *batch = nullptr;
+    // the batch's members by solve id: a retired solve's context is freed and a
+    // new context may reuse its address, so pointers cannot tell batches apart
+    std::vector<uint64_t> batch_members;
+    int n_active = 0;  // published under the server's mutex
+    std::thread worker;
+};
+
 }  // namespace
 
 struct nqes_server {
@@ -54,19 +83,14 @@ struct nqes_server {
     std::mutex mu;
     std::condition_variable cv;
     std::deque<Solve *> queue;
-    std::vector<Solve *> active;
     std::deque<nqes_result> done;
     uint64_t next_id = 1;
-    int n_active = 0;  // active solves, published by the worker under mu
-    // cumulative worker time (seconds) by phase, and counts, published under mu
+    int slots_used = 0;  // admitted and not yet retired, all lanes (under mu)
+    // cumulative worker time (seconds) by phase over the lanes, and counts, under mu
     double t_admit = 0, t_rebuild = 0, t_step = 0, t_post = 0;
     uint64_t n_steps = 0, n_rebuilds = 0;
     bool stop = false;
-    std::thread worker;
-    nqes_batch *batch = nullptr;
-    // the batch's members by solve id: a retired solve's context is freed and a
-    // new context may reuse its address, so pointers cannot tell batches apart
-    std::vector<uint64_t> batch_members;
+    Lane lanes[kLanes];
     std::string err;
 };
 
@@ -112,21 +136,27 @@ void finish_solve(nqes_server *srv, Solve *s, int status, int converged) {
     s->ctx = nullptr;
     std::lock_guard<std::mutex> g(srv->mu);
     srv->in_use -= s->bytes;
+    srv->slots_used--;
     srv->done.push_back(res);
     delete s;
 }
 
-void worker_loop(nqes_server *srv) {
+void worker_loop(nqes_server *srv, Lane *lane) {
     for (;;) {
         std::vector<Solve *> admitted;
         {
             std::unique_lock<std::mutex> lk(srv->mu);
             if (srv->stop) break;
-            while (!srv->queue.empty() && int(srv->active.size() + admitted.size()) < srv->max_active) {
-                Solve *s = srv->queue.front();
+            // the oldest queued requests of this lane's class, while memory and slots allow
+            for (auto it = srv->queue.begin(); it != srv->queue.end() && srv->slots_used < srv->max_active;) {
+                Solve *s = *it;
+                if (lane_of(s->r) != lane->index) {
+                    ++it;
+                    continue;
+                }
                 if (srv->in_use + s->bytes > srv->budget) {
-                    if (srv->active.empty() && admitted.empty() && s->bytes > srv->budget) {
-                        srv->queue.pop_front();  // can never fit: fail it
+                    if (srv->slots_used == 0 && s->bytes > srv->budget) {
+                        it = srv->queue.erase(it);  // can never fit: fail it
                         nqes_result res = make_result(*s, NQES_ERR_OOM, 0);
                         srv->done.push_back(res);
                         delete s;
@@ -134,11 +164,12 @@ void worker_loop(nqes_server *srv) {
                     }
                     break;  // oldest first: wait for memory
                 }
-                srv->queue.pop_front();
+                it = srv->queue.erase(it);
                 srv->in_use += s->bytes;
+                srv->slots_used++;
                 admitted.push_back(s);
             }
-            if (srv->active.empty() && admitted.empty()) {
+            if (lane->active.empty() && admitted.empty()) {
                 srv->cv.wait_for(lk, std::chrono::milliseconds(20));
                 continue;
             }
@@ -150,37 +181,37 @@ void worker_loop(nqes_server *srv) {
             if (st)
                 finish_solve(srv, s, st, 0);
             else
-                srv->active.push_back(s);
+                lane->active.push_back(s);
         }
-        if (srv->active.empty()) continue;
+        if (lane->active.empty()) continue;
 
         // one batched step over the active solves
         const auto c1 = Clock::now();
         std::vector<nqes_ctx *> members;
         std::vector<uint64_t> ids;
-        for (Solve *s : srv->active) {
+        for (Solve *s : lane->active) {
             members.push_back(s->ctx);
             ids.push_back(s->id);
         }
         bool rebuilt = false;
-        if (!srv->batch || ids != srv->batch_members) {
+        if (!lane->batch || ids != lane->batch_members) {
             rebuilt = true;
-            if (srv->batch) nqes_batch_destroy(srv->batch);
-            srv->batch = nullptr;
-            if (nqes_batch_create(members.data(), int(members.size()), &srv->batch)) {
-                for (Solve *s : srv->active) finish_solve(srv, s, NQES_ERR_CUDA, 0);
-                srv->active.clear();
+            if (lane->batch) nqes_batch_destroy(lane->batch);
+            lane->batch = nullptr;
+            if (nqes_batch_create(members.data(), int(members.size()), &lane->batch)) {
+                for (Solve *s : lane->active) finish_solve(srv, s, NQES_ERR_CUDA, 0);
+                lane->active.clear();
                 continue;
             }
-            srv->batch_members = ids;
+            lane->batch_members = ids;
         }
-        const size_t n = srv->active.size();
+        const size_t n = lane->active.size();
         std::vector<uint64_t> seeds(n), maxit(n);
         std::vector<int> chains(n), m(n), burn(n), status(n);
         std::vector<double> lr(n), reglam(n), rtol(n);
         std::vector<double *> emats(n);
         for (size_t i = 0; i < n; i++) {
-            const Solve *s = srv->active[i];
+            const Solve *s = lane->active[i];
             const nqes_request &r = s->r;
             seeds[i] = r.seed + uint64_t(s->step) * r.chains;
             chains[i] = r.chains;
@@ -190,15 +221,15 @@ void worker_loop(nqes_server *srv) {
             reglam[i] = std::max(s->reglam, r.reglam_cutoff);
             rtol[i] = r.minres_rtol;
             maxit[i] = r.minres_maxit;
-            emats[i] = reinterpret_cast<double *>(srv->active[i]->emat.data());
+            emats[i] = reinterpret_cast<double *>(lane->active[i]->emat.data());
         }
         const auto c2 = Clock::now();
-        nqes_batch_sr_step(srv->batch, seeds.data(), chains.data(), m.data(), burn.data(), lr.data(), reglam.data(),
+        nqes_batch_sr_step(lane->batch, seeds.data(), chains.data(), m.data(), burn.data(), lr.data(), reglam.data(),
                            rtol.data(), maxit.data(), emats.data(), nullptr, status.data(), nullptr);
         const auto c3 = Clock::now();
         std::vector<Solve *> keep;
         for (size_t i = 0; i < n; i++) {
-            Solve *s = srv->active[i];
+            Solve *s = lane->active[i];
             const int K = s->r.n_states, N = s->r.n_spins;
             if (status[i] == NQES_ERR_STATE) {  // not run: another member failed first
                 keep.push_back(s);
@@ -231,11 +262,11 @@ void worker_loop(nqes_server *srv) {
             else
                 keep.push_back(s);
         }
-        srv->active.swap(keep);
+        lane->active.swap(keep);
         const auto c4 = Clock::now();
         auto sec = [](Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); };
         std::lock_guard<std::mutex> g(srv->mu);
-        srv->n_active = int(srv->active.size());
+        lane->n_active = int(lane->active.size());
         srv->t_admit += sec(c0, c1);
         srv->t_step += sec(c2, c3);
         srv->t_post += sec(c3, c4);
@@ -245,13 +276,13 @@ void worker_loop(nqes_server *srv) {
             srv->n_rebuilds++;
         }
     }
-    if (srv->batch) nqes_batch_destroy(srv->batch);
-    srv->batch = nullptr;
-    for (Solve *s : srv->active) {
+    if (lane->batch) nqes_batch_destroy(lane->batch);
+    lane->batch = nullptr;
+    for (Solve *s : lane->active) {
         if (s->ctx) nqes_destroy(s->ctx);
         delete s;
     }
-    srv->active.clear();
+    lane->active.clear();
 }
 
 std::string g_server_error;
@@ -271,7 +302,10 @@ int nqes_server_create(int device, uint64_t hbm_budget_bytes, int max_active, nq
     s->device = device;
     s->budget = hbm_budget_bytes;
     s->max_active = max_active;
-    s->worker = std::thread(worker_loop, s);
+    for (int l = 0; l < kLanes; l++) {
+        s->lanes[l].index = l;
+        s->lanes[l].worker = std::thread(worker_loop, s, &s->lanes[l]);
+    }
     *out = s;
     return NQES_OK;
 }
@@ -307,13 +341,14 @@ int nqes_server_submit(nqes_server *s, const nqes_request *r, uint64_t *id) {
     nqes_footprint_bytes(r->n_spins, r->n_hidden, r->n_states, r->chains, r->samples_per_chain, r->precision,
                          cplx_w ? 1 : 0, &v->bytes);
     v->t_submit = Clock::now();
+    uint64_t vid;
     {
         std::lock_guard<std::mutex> g(s->mu);
-        v->id = s->next_id++;
-        s->queue.push_back(v);
+        vid = v->id = s->next_id++;
+        s->queue.push_back(v);  // from here on a worker may admit, fail and free v
     }
-    s->cv.notify_one();
-    if (id) *id = v->id;
+    s->cv.notify_all();
+    if (id) *id = vid;
     return NQES_OK;
 }
 
@@ -333,7 +368,10 @@ int nqes_server_status(nqes_server *s, int *queued, int *active, int *done, uint
     if (!s) return NQES_ERR_INVALID;
     std::lock_guard<std::mutex> g(s->mu);
     if (queued) *queued = int(s->queue.size());
-    if (active) *active = s->n_active;
+    if (active) {
+        *active = 0;
+        for (const Lane &l : s->lanes) *active += l.n_active;
+    }
     if (done) *done = int(s->done.size());
     if (bytes_in_use) *bytes_in_use = s->in_use;
     return NQES_OK;
@@ -359,7 +397,8 @@ int nqes_server_destroy(nqes_server *s) {
         s->stop = true;
     }
     s->cv.notify_all();
-    if (s->worker.joinable()) s->worker.join();
+    for (Lane &l : s->lanes)
+        if (l.worker.joinable()) l.worker.join();
     for (Solve *v : s->queue) delete v;
     delete s;
     return NQES_OK;

@@ -1,0 +1,91 @@
+"""SR training on the GPU against exact diagonalisation (N <= 20).
+
+The reference's schedule (code/rbm.cc:1173-1196 with the BASELINE plain
+configuration's flags): 128 chains x 200 samples, burn-in 64, 200 SR steps,
+lambda 40 -> 1 (x0.9 per step), lr 0.1 -> 0.01 (x0.99), MINRES-QLP rtol 1e-9,
+h = 0.595, K = 2 states, M = 2N. The energies of a step are the sorted real
+eigenvalues of e_mat / N (code/rbm.cc:1184-1187); the test takes the last 20
+steps' mean and their standard deviation sigma (the Monte Carlo noise of one
+step's estimate) and checks them against the two lowest eigenvalues of H
+(tests/golden/ed_golden.json, scipy):
+
+* the estimate lies above ED up to noise (variational): mean >= ED - 3 sigma / sqrt(20);
+* it lies within 5 sigma of ED for N = 8 and 16;
+* at N = 20 the gap left after 200 steps (3e-4 relative when measured) is the
+  RBM's variational and optimisation error, larger than one step's noise; the
+  test bounds it at 5e-4 relative.
+
+Couplings: the power-law chain J_ij = |i-j|^-1.2 (max |J| = 1) of the
+benchmark inputs with seeded real N(0, 0.01^2) weights (the plain
+configuration at N = 8), and the reference's own 2D ion-crystal couplings
+(code/Jmat/Ising2d_N8_alpha1.0.mat) from the reference's weight
+initialisation (init_multi_rbm, code/rbm.cc:241-270, complex weights)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from helpers import GOLDEN, synthetic_j
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+JMAT = os.path.join(ROOT, "nqes-trapped-ion_gb300", "cli", "jmat")
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    ge._load_build_module().build_library()
+    return ge.load_package()
+
+
+def train(pkg, N, M, K, J, h, init, steps=200, chains=128, m=200, tries=16):
+    """The reference's run as code/run.sh drives it: with lambda at its cutoff
+    S can be ill-conditioned enough for a step to go non-finite, and run.sh
+    restarts the run with a new seed (up to 16 times); so does this."""
+    for attempt in range(tries):
+        seed = 11 + attempt
+        ctx = pkg.Context(N, M, K, J, h)
+        if init == "reference":
+            ctx.init_weights(seed)
+        else:
+            ctx.set_weights(*pkg.synthetic_weights(N, M, K, 0.01, seed))
+        lr, lam, hist = 0.1, 40.0, []
+        try:
+            for it in range(steps):
+                e, _ = ctx.sr_step(5000 * seed + it * chains, chains, m, 64, max(lr, 0.01), max(lam, 1.0), 1e-9,
+                                   100000)
+                lr *= 0.99
+                lam *= 0.9
+                hist.append(np.sort(np.linalg.eigvals(e / N).real))
+        except pkg.NqesError as err:
+            if err.status != pkg.ERR_NONFINITE:
+                raise
+            print(f"attempt {attempt}: non-finite at step {len(hist)}, restarting with a new seed")
+            continue
+        finally:
+            ctx.close()
+        return np.array(hist)
+    raise AssertionError(f"every one of {tries} runs went non-finite")
+
+
+@pytest.mark.parametrize("N,couplings,init", [(8, "alpha1.2", "synthetic"), (16, "alpha1.2", "synthetic"),
+                                              (20, "alpha1.2", "synthetic"), (8, "ion2d", "reference")])
+def test_training_matches_exact_diagonalisation(pkg, N, couplings, init):
+    with open(os.path.join(GOLDEN, "ed_golden.json")) as f:
+        ed = [c for c in json.load(f)["cases"] if c["N"] == N and c["h"] == 0.595 and c["couplings"] == couplings]
+    want = np.array(ed[0]["evals_per_site"][:2])
+    J = synthetic_j(N) if couplings == "alpha1.2" else \
+        np.fromfile(os.path.join(JMAT, f"Ising2d_N{N}_alpha1.0.f64"), dtype="<f8").reshape(N, N)
+    hist = train(pkg, N, 2 * N, 2, J, 0.595, init)
+    tail = hist[-20:]
+    mean, sigma = tail.mean(0), tail.std(0, ddof=1)
+    print(f"N={N} {couplings}: VMC {mean} +- {sigma} (per step), ED {want}, gap {mean - want}")
+    assert np.all(np.isfinite(hist))
+    assert np.all(mean >= want - 3 * sigma / np.sqrt(len(tail))), (mean, want, sigma)
+    if N <= 16:
+        assert np.all(mean - want <= 5 * sigma), (mean, want, sigma)
+    else:
+        assert np.all((mean - want) / np.abs(want) <= 5e-4), (mean, want)

@@ -364,7 +364,8 @@ def test_fused_sv_matches_two_pass(pkg, N, M, K, prec):
     for x, y in zip(a["sv"], b["sv"]):
         assert rel_err(y, x) < 1e-13, rel_err(y, x)
     assert a["info"]["minres_flag"] == b["info"]["minres_flag"]
-    assert abs(int(a["info"]["minres_iters"]) - int(b["info"]["minres_iters"])) <= 1
+    it_a, it_b = int(a["info"]["minres_iters"]), int(b["info"]["minres_iters"])
+    assert abs(it_a - it_b) <= max(2, it_a // 20), (it_a, it_b)  # Krylov counts move with the last bits
     assert rel_err(b["e"], a["e"]) < 1e-13
     wa = np.concatenate([z.ravel() for z in a["w"]])
     wb = np.concatenate([z.ravel() for z in b["w"]])

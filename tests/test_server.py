@@ -1,5 +1,5 @@
-"""Serving loop: admission by device footprint, continuous batching, results
-independent of what else runs."""
+"""Serving loop: admission by device footprint, continuous batching in lanes
+by size class, results independent of what else runs."""
 import numpy as np
 import pytest
 
@@ -126,10 +126,11 @@ def test_turnover_rebuilds_the_batch(pkg):
 @pytest.mark.gpu
 def test_request_arriving_during_a_step_equals_running_alone(pkg):
     """A request submitted while another solve's batched steps are running on
-    the device joins the batch at the next step; both results equal those of
-    running each alone, bit for bit."""
+    the device joins that batch at its next step (both are of the same size
+    class, so they share a lane); both results equal those of running each
+    alone, bit for bit."""
     import time
-    big = dict(n=32, m=64, k=2, h=0.6, prec=1, seed=51)
+    big = dict(n=24, m=48, k=2, h=0.6, prec=1, seed=51)
     small = dict(n=12, m=24, k=2, h=0.9, prec=0, seed=53)
 
     def submit(srv, s, steps, chains, m):
@@ -164,3 +165,40 @@ def test_request_arriving_during_a_step_equals_running_alone(pkg):
     for r, s in ((rb, big), (rs, small)):
         a = alone[s["seed"]]
         assert r["steps"] == a["steps"] and r["energies"] == a["energies"] and r["best"] == a["best"]
+
+
+@pytest.mark.gpu
+def test_size_classes_run_side_by_side(pkg):
+    """A small solve submitted after a large one (another size class) is not
+    held back by the large one's steps: it finishes first, and both results
+    equal running each alone."""
+    big = dict(n=64, m=128, k=2, h=0.6, prec=1, seed=61)     # P = 16768: the middle lane
+    small = dict(n=10, m=20, k=2, h=0.9, prec=0, seed=63)    # P = 440: the first lane
+
+    def submit(srv, s, steps, chains, m):
+        w = helpers.random_weights(s["n"], s["m"], s["k"], 0.05, s["seed"], real=True)
+        return srv.submit(s["n"], s["m"], s["k"], synthetic_j(s["n"]), weights=w, h=s["h"], seed=s["seed"],
+                          chains=chains, samples_per_chain=m, burn_in=8, reglam0=5.0, tol=1e-12, max_steps=steps,
+                          precision=s["prec"])
+
+    alone = {}
+    for s, args in ((big, (6, 256, 100)), (small, (6, 16, 20))):
+        srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+        submit(srv, s, *args)
+        (r,) = srv.wait_all(1)
+        srv.close()
+        assert r["status"] == 0
+        alone[s["seed"]] = r
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+    id_big = submit(srv, big, 6, 256, 100)
+    id_small = submit(srv, small, 6, 16, 20)
+    order = [r["id"] for r in srv.wait_all(2)]
+    srv.close()
+    assert order == [id_small, id_big], order
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+    ids = [submit(srv, big, 6, 256, 100), submit(srv, small, 6, 16, 20)]
+    res = {r["id"]: r for r in srv.wait_all(2)}
+    srv.close()
+    for rid, s in zip(ids, (big, small)):
+        a = alone[s["seed"]]
+        assert res[rid]["energies"] == a["energies"] and res[rid]["steps"] == a["steps"]
