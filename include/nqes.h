@@ -69,6 +69,10 @@ extern "C" {
                                       * O^T u per staged group of rows, double-float arithmetic on the FP32
                                       * pipe, within 1e-13 of FP64 sums) where P is even and at most 8192;
                                       * 0: two FP64 passes; -1 (default): on in CERTIFIED, off in FP64. */
+#define NQES_OPT_MIXED_ENERGY64 11   /* 1 (default): in the MIXED form the decision-warp sampler forms the
+                                      * local energies in FP64 (the N single-flip ratios from tanh of the
+                                      * exact theta and the FP64 tables, as the CERTIFIED form does) and
+                                      * keeps O as its FP32 factors; 0: FP32 ratio products. */
 #define NQES_OPT_TEST_STAGE_WAIT 10  /* test hook for the bounded device-side waits: 1 = the decision-warp
                                       * sampler stages its tables and its wait is for bytes that no copy
                                       * delivers, with a short poll limit, so the step returns
@@ -83,7 +87,8 @@ extern "C" {
  * MIXED (real weights only): factors, ratio products and accept decisions
  *   in FP32 with a certified error bound and an exact FP64 decision whenever
  *   the bound cannot decide, so the Markov chains are the FP64 chains;
- *   theta, Phi, local-energy sums, moments, MINRES-QLP and the update in FP64;
+ *   theta, Phi, local energies (NQES_OPT_MIXED_ENERGY64), moments' sums,
+ *   MINRES-QLP and the update in FP64;
  *   log-derivatives stored as their FP32 factors (tanh rows, Phi coefficients)
  *   and S·v and the moments computed from them in FP32. */
 #define NQES_PRECISION_FP64 0

@@ -62,7 +62,7 @@ cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_
 }
 
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st) {
-    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K, a.stage != 0, a.out64 != 0);
+    const size_t smem = dsmem_bytes(a.sh.N, a.MP, a.sh.K, a.stage != 0, a.out64 != 0 || a.e64 != 0);
     const DwKernel fn = dw_kernel(a.sh.K, a.U);
     if (!fn || warps < 1 || warps > 8 || a.sh.NW > 2 || a.G * a.U != a.MP) return cudaErrorInvalidConfiguration;
     fn<<<a.chains, 32 * warps, smem, st>>>(a);

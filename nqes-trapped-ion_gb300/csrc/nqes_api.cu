@@ -75,6 +75,7 @@ struct nqes_ctx {
     // graph: the members' samplers then share the GPU.
     int plan_chains = 0;
     int stage_fault = 0;  // NQES_OPT_TEST_STAGE_WAIT
+    bool mixed_e64 = true;  // NQES_OPT_MIXED_ENERGY64
     bool mixed_exact_all = false;  // MIXED: every decision through the exact FP64 path
     bool weights_real = true;
     std::string err;
@@ -323,6 +324,8 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     return B;
 }
 
+bool dw_energy64(const nqes_ctx *ctx);
+
 MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     MixedArgs A{};
     A.sh = ctx->sh;
@@ -360,6 +363,15 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.MP = ctx->dw_MP;
     A.stage_fault = ctx->stage_fault;
     A.out64 = ctx->step_precision == NQES_PRECISION_CERTIFIED ? 1 : 0;
+    A.e64 = !A.out64 && dw_energy64(ctx) ? 1 : 0;
+    if (A.e64) {  // the FP64 tables for the local energies; O stays as FP32 factors
+        const size_t nw = size_t(ctx->sh.K) * ctx->sh.N * ctx->sh.M, na = size_t(ctx->sh.K) * ctx->sh.N;
+        const double *t = static_cast<const double *>(ctx->tab);
+        A.c64 = t;
+        A.s64 = t + nw;
+        A.eup64 = t + 2 * nw;
+        A.edn64 = t + 2 * nw + na;
+    }
     if (A.out64) {
         // dense FP64 O and the FP64 tables of the step (ch, sh, eup, edn)
         const size_t nw = size_t(ctx->sh.K) * ctx->sh.N * ctx->sh.M, na = size_t(ctx->sh.K) * ctx->sh.N;
@@ -382,6 +394,12 @@ bool certified_dw(const nqes_ctx *ctx) {
 }
 bool uses_mixed_sampler(const nqes_ctx *ctx) {
     return ctx->step_precision == NQES_PRECISION_MIXED || certified_dw(ctx);
+}
+// The decision-warp sampler forms its local energies in FP64 (the certified
+// form; the mixed form unless NQES_OPT_MIXED_ENERGY64 is 0): it then needs the
+// FP64 tables and room for FP64 tanh rows.
+bool dw_energy64(const nqes_ctx *ctx) {
+    return certified_dw(ctx) || (ctx->step_precision == NQES_PRECISION_MIXED && ctx->dw_U && ctx->mixed_e64);
 }
 
 cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
@@ -410,7 +428,7 @@ void dw_plan(nqes_ctx *ctx, int chains, int *warps, int *stage) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
     for (int w = 4; w >= 1; w >>= 1)
         for (int st = 1; st >= 0; st--) {
-            const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1, certified_dw(ctx));
+            const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1, dw_energy64(ctx));
             if (smem > 227 * 1024) continue;
             int per_sm = 0;
             if (dw_occupancy(ctx->sh, 32 * w, smem, &per_sm) == cudaSuccess && per_sm * sms >= chains) {
@@ -433,7 +451,7 @@ cudaError_t launch_mixed_tables(nqes_ctx *ctx) {
     return e;
 }
 size_t mixed_sampler_smem(nqes_ctx *ctx) {
-    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP, false, certified_dw(ctx)) : mixed_smem_bytes(ctx->sh);
+    return ctx->dw_U ? dw_smem_bytes(ctx->sh, ctx->dw_MP, false, dw_energy64(ctx)) : mixed_smem_bytes(ctx->sh);
 }
 // The mixed sampler's and the factored S·v's shared-memory limits.
 cudaError_t prepare_mixed_sampler(nqes_ctx *ctx) {
@@ -545,7 +563,7 @@ template <class S> int capture_sampling(nqes_ctx *ctx, int chains, int m, int bu
     cudaError_t le;
     if (uses_mixed_sampler(ctx)) {
         le = launch_mixed_tables(ctx);
-        if (le == cudaSuccess && certified_dw(ctx)) le = launch_tables_ctx<S>(ctx);  // the FP64 outputs' tables
+        if (le == cudaSuccess && dw_energy64(ctx)) le = launch_tables_ctx<S>(ctx);  // the FP64 energies' tables
         if (le == cudaSuccess) le = launch_mixed_sampler(ctx, chains, m, burn, tk);
     } else {
         le = launch_tables_ctx<S>(ctx);
@@ -851,7 +869,7 @@ template <class S> int tune_sampler(nqes_ctx *ctx, int chains, int m, int burn) 
     const bool mixed = uses_mixed_sampler(ctx);
     NQES_CUDA(cudaMemcpyAsync(ctx->sp, ctx->sp_host, sizeof(StepParams), cudaMemcpyHostToDevice, ctx->st));
     if (mixed) NQES_CUDA(launch_mixed_tables(ctx));
-    if (!mixed || certified_dw(ctx)) NQES_CUDA(launch_tables_ctx<S>(ctx));
+    if (!mixed || dw_energy64(ctx)) NQES_CUDA(launch_tables_ctx<S>(ctx));
     auto time_one = [&](auto &&launch, float *ms) -> cudaError_t {
         cudaError_t e = launch();  // warm-up
         if (e != cudaSuccess) return e;
@@ -868,7 +886,7 @@ template <class S> int tune_sampler(nqes_ctx *ctx, int chains, int m, int burn) 
         int bw = 0, bs = 0;
         for (int w = 1; w <= 4; w <<= 1)
             for (int st = 0; st <= 1; st++) {
-                if (dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1) > 227 * 1024) continue;
+                if (dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1, dw_energy64(ctx)) > 227 * 1024) continue;
                 ctx->dw_force_warps = w;
                 ctx->dw_force_stage = st;
                 float ms = 0;
@@ -1121,6 +1139,17 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         }
         ctx->tensor_cores = int(value);
         if (ctx->exec) {  // the captured step bakes the S·v kernels in
+            cudaGraphExecDestroy(ctx->exec);
+            ctx->exec = nullptr;
+        }
+        return NQES_OK;
+    case NQES_OPT_MIXED_ENERGY64:
+        if (value != 0 && value != 1) {
+            ctx->err = "option value must be 0 or 1";
+            return NQES_ERR_INVALID;
+        }
+        ctx->mixed_e64 = value == 1;
+        if (ctx->exec) {  // the captured step bakes the sampler's arguments in
             cudaGraphExecDestroy(ctx->exec);
             ctx->exec = nullptr;
         }
@@ -1768,7 +1797,7 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
         std::memcpy(&delta_bits, &c->ham_delta, sizeof(delta_bits));
         keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision, c->ham, delta_bits,
                    c->tensor_cores, c->reject_filter ? 1 : 0, c->mixed_exact_all ? 1 : 0, c->dw_force_warps,
-                   c->dw_force_stage, (long long)c->buf_gen, total, c->stage_fault};
+                   c->dw_force_stage, (long long)c->buf_gen, total, c->stage_fault, c->mixed_e64 ? 1 : 0};
     }
     if (!b->exec || keys != b->keys) {
         NvtxRange r_build("batch graph capture");

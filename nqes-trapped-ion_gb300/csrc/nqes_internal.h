@@ -100,6 +100,9 @@ struct MixedArgs {
     int out64;
     double *O64;
     const double *c64, *s64, *eup64, *edn64;  // FP64 tables [kk][i][j], [kk][i]
+    // FP64 local energies with the FP32 factor outputs (MIXED, NQES_OPT_MIXED_ENERGY64):
+    // E from tanh of the exact theta and the FP64 tables as with out64, O as factors
+    int e64;
 };
 size_t mixed_smem_bytes(const Shape &sh);
 int dw_units(const Shape &sh, int *G_out);  // U of the decision-warp form, 0 if it does not apply

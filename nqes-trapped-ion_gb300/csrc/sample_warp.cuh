@@ -619,7 +619,8 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
     const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int c = blockIdx.x;
-    DSmem sm = dcarve(smem_raw, N, MP, K, A.out64 != 0);
+    const bool e64 = A.out64 || A.e64;  // FP64 local energies (tanh of the exact theta, FP64 tables)
+    DSmem sm = dcarve(smem_raw, N, MP, K, e64);
     const bool writer = tid == 0;
     const size_t tb = dw_table_bytes(N, MP, K);
     if (A.stage) {
@@ -726,7 +727,7 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
                 if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
             }
         }
-        if (A.out64) {
+        if (e64) {
             for (int e = tid; e < KK * MP; e += T) {
                 const int j = e % MP;
                 sm.t64[e] = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
@@ -781,7 +782,7 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         __syncthreads();
         for (int q = warp; q < KK; q += nwarp) {
             double acc = 0.0;
-            if (A.out64) {
+            if (e64) {
                 const double *rat64 = reinterpret_cast<const double *>(sm.rat);
                 for (int i = lane; i < N; i += 32) acc += rat64[q * N + i];
                 acc = warp_sum(acc);

@@ -370,3 +370,34 @@ def test_fused_sv_matches_two_pass(pkg, N, M, K, prec):
     wa = np.concatenate([z.ravel() for z in a["w"]])
     wb = np.concatenate([z.ravel() for z in b["w"]])
     assert rel_err(wb, wa) < 1e-6  # the solves agree to the rtol scale
+
+
+def test_mixed_energies_along_the_fp64_trajectory(pkg):
+    """The mixed form's energy error beyond the first step, at the plain
+    configuration N8 M16 K2 (128 chains x 200 samples, burn-in 64, the
+    reference schedule lambda 40 -> 1, lr 0.1 -> 0.01): before every step the
+    mixed context takes the FP64 context's weights, so both sample the same
+    Markov chains and the difference is the arithmetic alone. Max over 40
+    steps of the per-site energies' relative difference <= 1e-6 (the stated
+    target); with the FP64 local energies of NQES_OPT_MIXED_ENERGY64 it is at
+    the FP64 rounding level."""
+    N, M, K, chains = 8, 16, 2, 128
+    J = synthetic_j(N)
+    f = pkg.Context(N, M, K, J, 0.595)
+    x = pkg.Context(N, M, K, J, 0.595)
+    f.set_weights(*pkg.synthetic_weights(N, M, K, 0.01, 20240601))
+    x.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+    worst = 0.0
+    for t in range(40):
+        lr, lam = max(0.1 * 0.99 ** t, 0.01), max(40.0 * 0.9 ** t, 1.0)
+        x.set_weights(*f.get_weights())
+        args = (777 + t * chains, chains, 200, 64, lr, lam, 1e-9, 100000)
+        ef, _ = f.sr_step(*args)
+        em, _ = x.sr_step(*args)
+        assert np.array_equal(f.get_samples()[0], x.get_samples()[0])
+        vf, vm = (np.sort(np.linalg.eigvals(e / N).real) for e in (ef, em))
+        worst = max(worst, float(np.max(np.abs(vm - vf) / np.abs(vf))))
+    print("max relative energy difference over 40 steps:", worst)
+    assert worst <= 1e-6
+    f.close()
+    x.close()
