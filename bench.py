@@ -359,26 +359,32 @@ def serving_form(pkg, rate, window_s, local, max_steps=40, max_requests=48):
             "p50_converged_s": pct(conv, 50), "p99_converged_s": pct(conv, 99),
             "p50_s": pct(lat, 50), "p99_s": pct(lat, 99),
             "mean_steps": float(np.mean([r["steps"] for r in ok])) if ok else None,
+            "restarts": int(sum(r["restarts"] for r in res)),
+            "failed_statuses": sorted({int(r["status"]) for r in res if r["status"] != 0}),
             "mean_queue_s": float(np.mean([r["t_queued"] for r in res])) if res else None,
             "max_steps": max_steps, "tol_per_site": SERVE_TOL, "worker_phases": phases}
 
 
 def serving_sweep(pkg, rates, window_s, local):
-    """Serving lines over the arrival rates and the highest rate the server
-    sustains: completions keep up with arrivals (>= 90 %) and p99 stays within
-    3x the lowest rate's."""
+    """Serving lines over the arrival rates, the server's capacity (the most
+    solves per second any line completed) and the highest arrival rate it
+    sustains: at most that capacity, no failed solve, and p99 latency within
+    2x the lowest rate's (arrivals beyond capacity queue, so p99 then grows
+    with the window instead of staying bounded)."""
     lines = [serving_form(pkg, r, window_s, local) for r in rates]
     base = lines[0]["p99_s"] or 0.0
+    capacity = max(ln["solves_per_s"] for ln in lines)
     sus = None
     for ln in lines:
-        if ln["p99_s"] is not None and ln["solves_per_s"] >= 0.9 * ln["offered_per_s"] and ln["p99_s"] <= 3 * base:
+        if (ln["p99_s"] is not None and ln["rate_per_s"] <= capacity and not ln["failed"]
+                and ln["p99_s"] <= 2 * base):
             sus = ln
-    summary = {"sustainable_rate_per_s": sus["rate_per_s"] if sus else None,
-               "solves_per_s_at_sustainable": sus["solves_per_s"] if sus else None,
+    summary = {"capacity_solves_per_s": capacity,
+               "sustainable_rate_per_s": sus["rate_per_s"] if sus else None,
                "p50_converged_s_at_sustainable": sus["p50_converged_s"] if sus else None,
                "p99_converged_s_at_sustainable": sus["p99_converged_s"] if sus else None,
                "p99_s_at_sustainable": sus["p99_s"] if sus else None,
-               "rule": "completions >= 90% of arrivals and p99 within 3x the lowest rate's"}
+               "rule": "arrival rate <= capacity, no failures, p99 within 2x the lowest rate's"}
     return lines, summary
 
 

@@ -271,9 +271,12 @@ int nqes_batch_sr_step(nqes_batch *batch, const uint64_t *seeds, const int *chai
  * the reference's schedules (code/rbm.cc:1173-1183); applies the reference's
  * convergence test to each (sorted real eigenvalues of e_mat/N; converged at
  * step t > 0 when |evals - best| < tol, best = lowest-sum evals so far,
- * code/rbm.cc:1185-1194); and retires a solve when it converges, reaches
- * max_steps or fails. Solves submitted while others run join the next step.
- * A solve's numbers equal those of running it alone. */
+ * code/rbm.cc:1185-1194); restarts a solve whose step goes non-finite from
+ * its initial weights with a new seed, up to 16 runs (code/run.sh); and
+ * retires a solve when it converges, reaches max_steps or fails. Solves
+ * submitted while others run join the next step. Three workers (lanes) by
+ * size class, P up to 5000, up to 20000 and beyond, each batch their solves
+ * side by side on the GPU. A solve's numbers equal those of running it alone. */
 typedef struct nqes_server nqes_server;
 typedef struct nqes_request {
     int n_spins, n_hidden, n_states;
@@ -299,6 +302,7 @@ typedef struct nqes_result {
     double best[4];                  /* lowest-sum energies seen */
     double t_queued, t_total;        /* seconds from submit to admission and to completion */
     uint64_t footprint;              /* device bytes reserved for the solve */
+    int restarts;                    /* runs restarted after a non-finite step (new seed, as code/run.sh) */
 } nqes_result;
 int nqes_server_create(int device, uint64_t hbm_budget_bytes, int max_active, nqes_server **out);
 /* Copies the request; returns at once with its id. Thread-safe. */

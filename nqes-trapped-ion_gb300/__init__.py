@@ -81,13 +81,13 @@ class Result(ctypes.Structure):
     _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_int), ("converged", ctypes.c_int),
                 ("steps", ctypes.c_int), ("n_states", ctypes.c_int), ("energies", ctypes.c_double * 4),
                 ("best", ctypes.c_double * 4), ("t_queued", ctypes.c_double), ("t_total", ctypes.c_double),
-                ("footprint", ctypes.c_uint64)]
+                ("footprint", ctypes.c_uint64), ("restarts", ctypes.c_int)]
 
     def as_dict(self):
         k = self.n_states
         return {"id": self.id, "status": self.status, "converged": bool(self.converged), "steps": self.steps,
                 "energies": list(self.energies[:k]), "best": list(self.best[:k]), "t_queued": self.t_queued,
-                "t_total": self.t_total, "footprint": self.footprint}
+                "t_total": self.t_total, "footprint": self.footprint, "restarts": self.restarts}
 _dp = ctypes.POINTER(ctypes.c_double)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 

@@ -133,6 +133,48 @@ __global__ void __launch_bounds__(kVecThreads) k_moment_part(int Ns, int P, int 
     pf[size_t(r) * P + p] = f;
 }
 
+// The same partial column sums over O stored as double-float pairs (hi, lo)
+// in its FP64 slots (real arithmetic): o, |O|^2 and E_loc O accumulated in
+// double-float on the FP32 pipe (products with their FMA error terms, sums
+// TwoSum-compensated: a few 2^-48 of the sums of |terms|), converted to FP64
+// once per partial.
+__global__ void __launch_bounds__(kVecThreads) k_moment_part_split(int Ns, int P, int K, int rchunks, const float2 *O,
+                                                                   const cplx *E, double *po, double *ps2, double *pf) {
+    __shared__ float2 els[kVecThreads];
+    const int p = blockIdx.x * kVecThreads + threadIdx.x;
+    const int r = blockIdx.y;
+    const int s0 = int(int64_t(Ns) * r / rchunks), s1 = int(int64_t(Ns) * (r + 1) / rchunks);
+    const int KK = K * K;
+    float oh = 0.f, ol = 0.f, qh = 0.f, ql = 0.f, fh = 0.f, fl = 0.f;
+    for (int t0 = s0; t0 < s1; t0 += kVecThreads) {
+        const int nt = min(kVecThreads, s1 - t0);
+        if (int(threadIdx.x) < nt) {
+            const size_t s = size_t(t0) + threadIdx.x;
+            double el = 0.0;
+            for (int k = 0; k < K; k++) el += E[s * KK + k * K + k].re;
+            float eh, elo;
+            df_split(el, eh, elo);
+            els[threadIdx.x] = make_float2(eh, elo);
+        }
+        __syncthreads();
+        if (p < P) {
+            const float2 *col = O + size_t(t0) * P + p;
+            for (int q = 0; q < nt; q++) {
+                const float2 v = col[size_t(q) * P];
+                const float2 e = els[q];
+                df_acc(oh, ol, v.x, v.y);
+                df_fma(qh, ql, v.x, v.y, v.x, v.y);
+                df_fma(fh, fl, v.x, v.y, e.x, e.y);  // real: conj(O) E = O E
+            }
+        }
+        __syncthreads();
+    }
+    if (p >= P) return;
+    po[size_t(r) * P + p] = double(oh) + double(ol);
+    ps2[size_t(r) * P + p] = double(qh) + double(ql);
+    pf[size_t(r) * P + p] = double(fh) + double(fl);
+}
+
 template <class S>
 __global__ void k_moment_final(int Ns, int P, int rchunks, const StepParams *sp, const S *po, const double *ps2,
                                const S *pf, const cplx *eloc, S *o, S *skk, S *f, int *err) {
@@ -776,6 +818,13 @@ template <class S> cudaError_t launch_moments(const SolveBufs<S> &B, cudaStream_
                 e = launch_fmoment_final(B.F, B.sp, fo, ff, fs, B.eloc, B.o, B.skk, B.f, B.err, st);
             return e;
         }
+        if (B.o_split) {
+            k_moment_part_split<<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks,
+                                                           reinterpret_cast<const float2 *>(B.O), B.E, po, ps2, pf);
+            k_moment_final<S><<<nb, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.sp, po, ps2, pf, B.eloc, B.o, B.skk,
+                                                           B.f, B.err);
+            return cudaGetLastError();
+        }
     }
     k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
     k_moment_final<S><<<nb, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.sp, po, ps2, pf, B.eloc, B.o, B.skk, B.f,
@@ -803,7 +852,7 @@ template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, co
         return e != cudaSuccess ? e : launch_fcols(B.F, B.u32, B.ypart32, st);
     }
     if constexpr (std::is_same<S, double>::value) {
-        if (B.fG) return launch_sv_fused(B.Ns, P, B.fG, B.svp, B.O, v, B.ysv, B.err, B.guard, st);
+        if (B.fG) return launch_sv_fused(B.Ns, P, B.fG, B.svp, B.O, v, B.ysv, B.err, B.guard, st, B.o_split != 0);
     }
     k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u, B.guard);
     k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart, B.guard);
@@ -859,6 +908,13 @@ template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &B, cu
     if (B.fact) {
         float *fo = B.ypart32, *ff = fo + size_t(B.rchunks) * P, *fs = ff + size_t(B.rchunks) * P;
         return launch_fmoments(B.F, B.E, fo, ff, fs, st);
+    }
+    if constexpr (std::is_same<S, double>::value) {
+        if (B.o_split) {
+            k_moment_part_split<<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks,
+                                                           reinterpret_cast<const float2 *>(B.O), B.E, po, ps2, pf);
+            return cudaGetLastError();
+        }
     }
     k_moment_part<S, S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks, B.O, B.E, po, ps2, pf);
     return cudaGetLastError();

@@ -15,8 +15,11 @@
 // both from shared memory, so O leaves HBM once per S·v. The arithmetic is
 // double-float on the FP32 pipe: each FP64 entry d is split exactly-enough
 // into hi + lo floats by integer operations (hi = d cut to 24 significant
-// bits, lo = the remaining 29 bits rounded to 24: |d - hi - lo| <= 2^-48 |d|),
-// products are formed with their FMA error terms, sums are TwoSum-compensated.
+// bits, lo = the remaining 29 bits rounded to 24: |d - hi - lo| <= 2^-48 |d|,
+// nqes_math.cuh), products are formed with their FMA error terms, sums are
+// TwoSum-compensated. The certified sampler stores O already split (the
+// pairs in the FP64 slots), which saves the split here; O written as FP64
+// (the FP64 sampler) is split in shared memory on its first read.
 // The relative error of u and of the partials against FP64 sums of the same
 // terms is a few 2^-48 per term of sum |O v| (about 1e-14 at these sizes),
 // inside the 1e-12 parity bound. Entries below 2^-126 in magnitude count as
@@ -34,56 +37,13 @@
 namespace nqes {
 namespace {
 
-// hi + lo = d to 2^-48 relative (see the file comment); returns false when
-// |d| >= 2^127 or d is not finite.
-__device__ __forceinline__ bool split_d(double d, float &hi, float &lo) {
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
-    const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
-    const unsigned ax = hw & 0x7fffffffu, sgn = hw & 0x80000000u;
-    // biased exponent e = ax >> 20; hi is representable as a normal float for
-    // 897 <= e <= 1150: exponent e - 896, mantissa the top 23 of d's 52 bits
-    const bool nrm = ax >= 0x38100000u;
-    const unsigned hb = __funnelshift_l(lw, ax - 0x38000000u, 3);
-    hi = __uint_as_float(nrm ? (hb | sgn) : sgn);
-    // lo = sign * r * 2^(e - 1075) with r the low 29 mantissa bits; the scale
-    // is a normal float for e >= 949 (below, |lo| < 2^-149 |...|: dropped)
-    const unsigned e = ax >> 20;
-    const float sc = __uint_as_float((e - 948u) << 23);
-    const float l = __uint2float_rn(lw & 0x1fffffffu) * sc;
-    lo = e >= 949u ? __uint_as_float(__float_as_uint(l) | sgn) : 0.f;
-    return ax < 0x47f00000u;
-}
-
-// (sh, sl) += (ah + al) (bh + bl): the product to 2^-48 relative (its FMA
-// error term and the two cross terms), added with TwoSum into sh and the
-// rounding error and low terms into sl.
-__device__ __forceinline__ void df_mac(float &sh, float &sl, float ah, float al, float bh, float bl) {
-    const float p = ah * bh;
-    float e = __fmaf_rn(ah, bh, -p);
-    e = __fmaf_rn(ah, bl, e);
-    e = __fmaf_rn(al, bh, e);
-    const float s = __fadd_rn(sh, p);
-    const float bb = __fsub_rn(s, sh);
-    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    sh = s;
-    sl = __fadd_rn(sl, __fadd_rn(err, e));
-}
-
-// (ah, al) += (bh, bl)
-__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl) {
-    const float s = __fadd_rn(ah, bh);
-    const float bb = __fsub_rn(s, ah);
-    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
-    ah = s;
-    al = __fadd_rn(al, __fadd_rn(err, bl));
-}
-
 __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 struct FusedSvArgs {
     int Ns, P, G;
+    int o_split;  // O already stored as (hi, lo) pairs
     const double *O, *v;
     double *ypart;  // gridDim.x × P
     int *err;
@@ -97,7 +57,7 @@ constexpr int kFsMaxWarps = kFsMaxThreads / 32;
 // columns p = t + c T (c < C), holding v's split and its partial of O^T u for
 // them in registers. Rows of a staged group are walked one at a time, so no
 // per-row state lives in registers.
-template <int C, int MaxT>
+template <int C, int MaxT, bool PRE>
 __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     extern __shared__ __align__(16) unsigned char fs_smem[];
     if (loop_guard_off(a.guard)) return;
@@ -116,7 +76,7 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     for (int c = 0; c < C; c++) {
         const int p = tid + c * T;
         vh[c] = vl[c] = yh[c] = yl[c] = 0.f;
-        if (p < P) split_d(a.v[p], vh[c], vl[c]);
+        if (p < P) df_split(a.v[p], vh[c], vl[c]);
     }
     auto issue = [&](int g) {  // thread 0: group g into buffer g & 1
         const int rs = r0 + g * G, nr = min(G, r1 - rs);
@@ -156,19 +116,25 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
                 const int p = tid + c * T;
                 if (p < P) {
                     float oh, ol;
-                    range_ok &= split_d(row[p], oh, ol);
-                    *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
+                    if (PRE) {  // split when it was written
+                        const float2 o = *reinterpret_cast<const float2 *>(row + p);
+                        oh = o.x;
+                        ol = o.y;
+                    } else {
+                        range_ok &= df_split(row[p], oh, ol);
+                        *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
+                    }
                     if (c & 1)
-                        df_mac(h2, l2, oh, ol, vh[c], vl[c]);
+                        df_fma(h2, l2, oh, ol, vh[c], vl[c]);
                     else
-                        df_mac(h, l, oh, ol, vh[c], vl[c]);
+                        df_fma(h, l, oh, ol, vh[c], vl[c]);
                 }
             }
-            df_add(h, l, h2, l2);
+            df_acc(h, l, h2, l2);
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {
                 const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
-                df_add(h, l, oh, ol);
+                df_acc(h, l, oh, ol);
             }
             if (lane == 0) red[r * kFsMaxWarps + warp] = make_float2(h, l);
         }
@@ -177,7 +143,7 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
         for (int r = warp; r < nr; r += nw) {
             float h = 0.f, l = 0.f;
             if (lane == 0)
-                for (int w = 0; w < nw; w++) df_add(h, l, red[r * kFsMaxWarps + w].x, red[r * kFsMaxWarps + w].y);
+                for (int w = 0; w < nw; w++) df_acc(h, l, red[r * kFsMaxWarps + w].x, red[r * kFsMaxWarps + w].y);
             if (lane == 0) us[r] = make_float2(h, l);
         }
         __syncthreads();
@@ -190,7 +156,7 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
                 const int p = tid + c * T;
                 if (p < P) {
                     const float2 o = *reinterpret_cast<const float2 *>(row + p);
-                    df_mac(yh[c], yl[c], o.x, o.y, u.x, u.y);
+                    df_fma(yh[c], yl[c], o.x, o.y, u.x, u.y);
                 }
             }
         }
@@ -232,14 +198,17 @@ bool fused_shape(int P, int *C, int *T) {
     return false;
 }
 
-template <class F> cudaError_t fused_dispatch(int C, F &&f) {
+template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
     switch (C) {
-    case 1: return f(k_sv_fused<1, 1024>);
-    case 2: return f(k_sv_fused<2, 1024>);
-    case 4: return f(k_sv_fused<4, 1024>);
-    case 8: return f(k_sv_fused<8, 768>);
-    default: return f(k_sv_fused<16, 512>);
+    case 1: return f(k_sv_fused<1, 1024, PRE>);
+    case 2: return f(k_sv_fused<2, 1024, PRE>);
+    case 4: return f(k_sv_fused<4, 1024, PRE>);
+    case 8: return f(k_sv_fused<8, 768, PRE>);
+    default: return f(k_sv_fused<16, 512, PRE>);
     }
+}
+template <class F> cudaError_t fused_dispatch(int C, F &&f, bool pre = false) {
+    return pre ? fused_dispatch_p<true>(C, f) : fused_dispatch_p<false>(C, f);
 }
 
 size_t fused_smem(int P, int G) {
@@ -254,7 +223,9 @@ constexpr int kFsMaxG = 16;
 cudaError_t prepare_sv_fused(int P) {
     int C, T;
     if (!fused_shape(P, &C, &T)) return cudaErrorInvalidValue;
-    return fused_dispatch(C, [](auto fn) { return allow_max_dynamic_smem(reinterpret_cast<const void *>(fn)); });
+    auto set = [](auto fn) { return allow_max_dynamic_smem(reinterpret_cast<const void *>(fn)); };
+    const cudaError_t e = fused_dispatch(C, set, false);
+    return e != cudaSuccess ? e : fused_dispatch(C, set, true);
 }
 
 // Rows per staged group G and the grid: the G that keeps the most threads
@@ -292,15 +263,18 @@ bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out) {
 }
 
 cudaError_t launch_sv_fused(int Ns, int P, int G, int ctas, const double *O, const double *v, double *ypart, int *err,
-                            const int *guard, cudaStream_t st) {
-    FusedSvArgs a{Ns, P, G, O, v, ypart, err, guard};
+                            const int *guard, cudaStream_t st, bool o_split) {
+    FusedSvArgs a{Ns, P, G, o_split ? 1 : 0, O, v, ypart, err, guard};
     const size_t smem = fused_smem(P, G);
     int C, T;
     if (!fused_shape(P, &C, &T)) return cudaErrorInvalidValue;
-    return fused_dispatch(C, [&](auto fn) {
-        fn<<<ctas, T, smem, st>>>(a);
-        return cudaGetLastError();
-    });
+    return fused_dispatch(
+        C,
+        [&](auto fn) {
+            fn<<<ctas, T, smem, st>>>(a);
+            return cudaGetLastError();
+        },
+        o_split);
 }
 
 }  // namespace nqes

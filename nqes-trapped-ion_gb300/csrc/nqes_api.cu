@@ -273,6 +273,11 @@ FactArgs fact_args(nqes_ctx *ctx) {
     return F;
 }
 
+bool certified_dw(const nqes_ctx *ctx);
+// The certified decision-warp sampler stores O as double-float pairs when the
+// fused S·v reads it (NQES_OPT_FUSED_SV).
+bool o_split(const nqes_ctx *ctx) { return ctx->fG > 0 && certified_dw(ctx); }
+
 template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     SolveBufs<S> B{};
     const size_t P = ctx->sh.P;
@@ -312,6 +317,7 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
         B.fG = ctx->fG;
         B.svp = ctx->fctas;
         B.ysv = reinterpret_cast<S *>(ctx->ysv);
+        B.o_split = o_split(ctx) ? 1 : 0;
     }
     if (ctx->step_precision == NQES_PRECISION_MIXED) {
         B.O = nullptr;
@@ -362,6 +368,7 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.U = ctx->dw_U;
     A.MP = ctx->dw_MP;
     A.stage_fault = ctx->stage_fault;
+    A.o_split = o_split(ctx) ? 1 : 0;
     A.out64 = ctx->step_precision == NQES_PRECISION_CERTIFIED ? 1 : 0;
     A.e64 = !A.out64 && dw_energy64(ctx) ? 1 : 0;
     if (A.e64) {  // the FP64 tables for the local energies; O stays as FP32 factors
@@ -1415,6 +1422,16 @@ int nqes_get_O(nqes_ctx *ctx, int first, int count, double *O) {
         return NQES_OK;
     }
     const unsigned char *src = static_cast<const unsigned char *>(ctx->O) + size_t(first) * P * ssize(ctx->arith);
+    if (o_split(ctx)) {  // stored as double-float pairs: hi + lo
+        std::vector<float> tmp(2 * size_t(count) * P);
+        NQES_CUDA(cudaMemcpyAsync(tmp.data(), src, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
+        NQES_CUDA(cudaStreamSynchronize(ctx->st));
+        for (size_t t = 0; t < size_t(count) * P; t++) {
+            O[2 * t] = double(tmp[2 * t]) + double(tmp[2 * t + 1]);
+            O[2 * t + 1] = 0.0;
+        }
+        return NQES_OK;
+    }
     return copy_out_c(ctx, src, size_t(count) * P, O);
 }
 
@@ -1496,8 +1513,10 @@ template <class S> int time_kernel_t(nqes_ctx *ctx, int kernel, int reps, double
             SampleArgs<S> A = sample_args<S>(ctx, ctx->chains, ctx->m, ctx->last_burn, ctx->last_tk);
             return launch_sample<S>(A, sample_threads(ctx->sh.K, ctx->last_tk), ctx->st);
         }
-        case NQES_KERNEL_SV_ROWS: return launch_sv_rows_only<S>(B, ctx->st);
-        case NQES_KERNEL_SV_COLS: return launch_sv_cols_only<S>(B, ctx->st);
+        case NQES_KERNEL_SV_ROWS:
+        case NQES_KERNEL_SV_COLS:
+            if (B.o_split) return cudaErrorNotSupported;  // the two-pass kernels read FP64 entries
+            return kernel == NQES_KERNEL_SV_ROWS ? launch_sv_rows_only<S>(B, ctx->st) : launch_sv_cols_only<S>(B, ctx->st);
         case NQES_KERNEL_SV: return launch_sv_only<S>(B, ctx->st);
         default: return launch_moment_part_only<S>(B, ctx->st);
         }

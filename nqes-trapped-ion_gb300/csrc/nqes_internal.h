@@ -99,6 +99,7 @@ struct MixedArgs {
     // dense FP64 O (P per sample) instead of the FP32 factors
     int out64;
     double *O64;
+    int o_split;  // out64: each entry of O64 stored as its double-float split (hi, lo) for the fused S·v
     const double *c64, *s64, *eup64, *edn64;  // FP64 tables [kk][i][j], [kk][i]
     // FP64 local energies with the FP32 factor outputs (MIXED, NQES_OPT_MIXED_ENERGY64):
     // E from tanh of the exact theta and the FP64 tables as with out64, O as factors
@@ -256,6 +257,10 @@ template <class S> struct SolveBufs {
     int svp;
     S *ysv;
     int fG;
+    // O stored as double-float (hi, lo) pairs in its FP64 slots (the certified
+    // sampler writes it so when the fused S·v runs): the fused S·v and the
+    // moments read the pairs directly
+    int o_split;
     // Mixed precision (real arithmetic only, fact = 1): O held as its factors
     // and the two passes of S·v and the moments computed from them in FP32
     // (kernels_factored.cu); v is mirrored into v32 by the kernels that
@@ -271,7 +276,7 @@ template <class S> struct SolveBufs {
 bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out);
 cudaError_t prepare_sv_fused(int P);
 cudaError_t launch_sv_fused(int Ns, int P, int G, int ctas, const double *O, const double *v, double *ypart, int *err,
-                            const int *guard, cudaStream_t st);
+                            const int *guard, cudaStream_t st, bool o_split = false);
 
 // Sets the batched MINRES-QLP loop's condition: 1 while any member's flag
 // (its QlpState::running) is set.

@@ -279,4 +279,53 @@ template <class S> __host__ __device__ inline int small_pinv(const S *a, S *out,
     return r;
 }
 
+// ---- double-float (hi + lo FP32 pairs) on the FP32 pipe ----
+
+// d as hi + lo: hi = d cut to 24 significant bits, lo = the remaining 29
+// bits rounded to 24, by integer operations (no FP64 instruction), so that
+// |d - hi - lo| <= 2^-48 |d|; |d| < 2^-126 gives 0. Returns false when
+// |d| >= 2^127 or d is not finite.
+__device__ __forceinline__ bool df_split(double d, float &hi, float &lo) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
+    const unsigned hw = unsigned(b >> 32), lw = unsigned(b);
+    const unsigned ax = hw & 0x7fffffffu, sgn = hw & 0x80000000u;
+    // biased exponent e = ax >> 20; hi is representable as a normal float for
+    // 897 <= e <= 1150: exponent e - 896, mantissa the top 23 of d's 52 bits
+    const bool nrm = ax >= 0x38100000u;
+    const unsigned hb = __funnelshift_l(lw, ax - 0x38000000u, 3);
+    hi = __uint_as_float(nrm ? (hb | sgn) : sgn);
+    // lo = sign * r * 2^(e - 1075) with r the low 29 mantissa bits; the scale
+    // is a normal float for e >= 949 (below, |lo| < 2^-149 |...|: dropped)
+    const unsigned e = ax >> 20;
+    const float sc = __uint_as_float((e - 948u) << 23);
+    const float l = __uint2float_rn(lw & 0x1fffffffu) * sc;
+    lo = e >= 949u ? __uint_as_float(__float_as_uint(l) | sgn) : 0.f;
+    return ax < 0x47f00000u;
+}
+
+// (sh, sl) += (ah + al) (bh + bl): the product to 2^-48 relative (its FMA
+// error term and the two cross terms), added with TwoSum into sh and the
+// rounding error and low terms into sl.
+__device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(err, e));
+}
+
+// (ah, al) += (bh, bl)
+__device__ __forceinline__ void df_acc(float &ah, float &al, float bh, float bl) {
+    const float s = __fadd_rn(ah, bh);
+    const float bb = __fsub_rn(s, ah);
+    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    ah = s;
+    al = __fadd_rn(al, __fadd_rn(err, bl));
+}
+
+
 }  // namespace nqes

@@ -13,6 +13,9 @@
 //           |evals - best| < tol, best = the lowest-sum evals so far;
 //   retire  converged solves, solves at max_steps and failed ones, freeing
 //           their device memory and slot; results wait for nqes_server_poll.
+//           A step that goes non-finite restarts the solve's run from its
+//           initial weights with a new seed, up to 16 runs, as code/run.sh
+//           does with the reference's exit code 127.
 // Requests that arrive while others run join the next step's batch as memory
 // and slots free up, so their work overlaps on the device.
 //
@@ -49,12 +52,15 @@ struct Solve {
     nqes_ctx *ctx = nullptr;
     uint64_t bytes = 0;
     int step = 0;
+    int restarts = 0;     // restarts after a non-finite step (code/run.sh)
+    uint64_t seed = 0;    // the current run's seed: the request's, moved on at each restart
     double lr = 0, reglam = 0;
     std::vector<double> evals, best;
     std::vector<std::complex<double>> emat;
 };
 
 constexpr int kLanes = 3;
+constexpr int kMaxTries = 16;  // runs per solve, as code/run.sh's MAX_TRIES
 
 // Size class of a request: its lane.
 int lane_of(const nqes_request &r) {
@@ -111,7 +117,22 @@ nqes_result make_result(const Solve &s, int status, int converged) {
     res.t_queued = std::chrono::duration<double>(s.t_admit - s.t_submit).count();
     res.t_total = std::chrono::duration<double>(now - s.t_submit).count();
     res.footprint = s.bytes;
+    res.restarts = s.restarts;
     return res;
+}
+
+// (Re)starts the solve's run from its initial weights with its current seed:
+// the request's weights, else the reference initialisation from that seed.
+int begin_run(Solve *s) {
+    const nqes_request &r = s->r;
+    const int st = !s->a.empty() ? nqes_set_weights(s->ctx, s->a.data(), s->b.data(), s->w.data())
+                                 : nqes_init_weights(s->ctx, s->seed);
+    s->step = 0;
+    s->lr = r.lr0;
+    s->reglam = r.reglam0;
+    s->evals.clear();
+    s->best.clear();
+    return st;
 }
 
 // Creates the solve's context (worker thread). Returns the status.
@@ -119,13 +140,9 @@ int start_solve(nqes_server *srv, Solve *s) {
     const nqes_request &r = s->r;
     int st = nqes_create(r.n_spins, r.n_hidden, r.n_states, s->J.data(), r.h, srv->device, &s->ctx);
     if (st) return st;
-    if (!s->a.empty())
-        st = nqes_set_weights(s->ctx, s->a.data(), s->b.data(), s->w.data());
-    else
-        st = nqes_init_weights(s->ctx, r.seed);
+    s->seed = r.seed;
+    st = begin_run(s);
     if (!st) st = nqes_set_option(s->ctx, NQES_OPT_PRECISION, r.precision);
-    s->lr = r.lr0;
-    s->reglam = r.reglam0;
     s->emat.assign(size_t(r.n_states) * r.n_states, 0.0);
     return st;
 }
@@ -213,7 +230,7 @@ void worker_loop(nqes_server *srv, Lane *lane) {
         for (size_t i = 0; i < n; i++) {
             const Solve *s = lane->active[i];
             const nqes_request &r = s->r;
-            seeds[i] = r.seed + uint64_t(s->step) * r.chains;
+            seeds[i] = s->seed + uint64_t(s->step) * r.chains;
             chains[i] = r.chains;
             m[i] = r.samples_per_chain;
             burn[i] = r.burn_in;
@@ -234,6 +251,16 @@ void worker_loop(nqes_server *srv, Lane *lane) {
             if (status[i] == NQES_ERR_STATE) {  // not run: another member failed first
                 keep.push_back(s);
                 continue;
+            }
+            if (status[i] == NQES_ERR_NONFINITE && s->restarts + 1 < kMaxTries) {
+                // as code/run.sh does after a floating-point error: the run
+                // again from the start with a new seed
+                s->restarts++;
+                s->seed = s->r.seed + (uint64_t(s->restarts) << 40);
+                if (begin_run(s) == NQES_OK) {
+                    keep.push_back(s);
+                    continue;
+                }
             }
             if (status[i]) {
                 finish_solve(srv, s, status[i], 0);

@@ -830,6 +830,7 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
             if (tid < KK) sm.Dm[tid] = sm.pinv[(tid / K) * K + tid % K] * sm.phi[(tid % K) * K + tid / K];
             __syncthreads();
             double *orow = A.O64 + s * size_t(A.sh.P);
+            bool split_ok = true;
             for (int e = tid; e < K * L; e += T) {
                 const int k = e / L, p = e - k * L;
                 double v = 0.0;
@@ -845,8 +846,15 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
 #pragma unroll
                     for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
                 }
-                orow[e] = v;
+                if (A.o_split) {  // as hi + lo for the fused S·v (nqes_math.cuh: df_split)
+                    float hi, lo;
+                    split_ok &= df_split(v, hi, lo);
+                    reinterpret_cast<float2 *>(orow)[e] = make_float2(hi, lo);
+                } else {
+                    orow[e] = v;
+                }
             }
+            if (!split_ok) atomicOr(A.err, kErrNonFinite);
         } else {
             const int MT = fact_mt(M);
             float *ft = A.FT + s * size_t(KK) * MT;
