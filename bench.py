@@ -347,6 +347,7 @@ def serving_form(pkg, rate, window_s, local, max_steps=40, max_requests=48):
     res = srv.wait_all(n, timeout=900)
     t_end = time.perf_counter() - t0
     phases = srv.times()
+    err = srv.last_error()
     srv.close()
     ok = [r for r in res if r["status"] == 0]
     conv = np.array([r["t_total"] for r in ok if r["converged"]])
@@ -362,7 +363,7 @@ def serving_form(pkg, rate, window_s, local, max_steps=40, max_requests=48):
             "restarts": int(sum(r["restarts"] for r in res)),
             "failed_statuses": sorted({int(r["status"]) for r in res if r["status"] != 0}),
             "mean_queue_s": float(np.mean([r["t_queued"] for r in res])) if res else None,
-            "max_steps": max_steps, "tol_per_site": SERVE_TOL, "worker_phases": phases}
+            "max_steps": max_steps, "tol_per_site": SERVE_TOL, "worker_phases": phases, "server_error": err or None}
 
 
 def serving_sweep(pkg, rates, window_s, local):
@@ -386,6 +387,33 @@ def serving_sweep(pkg, rates, window_s, local):
                "p99_s_at_sustainable": sus["p99_s"] if sus else None,
                "rule": "arrival rate <= capacity, no failures, p99 within 2x the lowest rate's"}
     return lines, summary
+
+
+def serving_in_child(rates, window_s, local):
+    """The serving sweep in a child process of this script (same device): its
+    requests run on three worker threads of their own, and a failure there is
+    reported in the line instead of ending the other measurements."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--serving-only", "--serve-rates", rates, "--serve-window",
+           str(window_s), "--serving-device", str(local)]
+    try:
+        p = subprocess.run(cmd, capture_output=True, text=True, timeout=3600)
+    except subprocess.TimeoutExpired:
+        return {"error": "serving sweep did not finish within 3600 s"}, None
+    for line in reversed(p.stdout.strip().split("\n")):
+        if line.startswith("{"):
+            d = json.loads(line)
+            return d["serving"], d["serving_summary"]
+    return {"error": "serving sweep exited %d: %s" % (p.returncode, " | ".join(p.stderr.strip().split("\n")[-4:]))}, None
+
+
+def serving_only(args):
+    """--serving-only: the serving sweep alone, one JSON line (serving_in_child)."""
+    import torch  # noqa: F401  (initialises the device as the other legs do)
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    lines, summary = serving_sweep(pkg, rates, args.serve_window, args.serving_device)
+    print(json.dumps({"serving": lines, "serving_summary": summary}))
 
 
 def precision_form(pkg, chains, samples, steps, local):
@@ -696,9 +724,8 @@ def run_ours(args):
         out["precision_form"] = precision_form(pkg, args.precision_chains, 64, 1, local)
 
     # ---- serving loop (config-5 style Poisson arrivals, rate sweep) ----
-    if args.serve_rates:
-        rates = [float(r) for r in args.serve_rates.split(",")]
-        out["serving"], out["serving_summary"] = serving_sweep(pkg, rates, args.serve_window, local)
+    if args.serve_rates and rank == 0:
+        out["serving"], out["serving_summary"] = serving_in_child(args.serve_rates, args.serve_window, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, args.warmup)
     if rank == 0:
@@ -730,6 +757,27 @@ def kernel_case(spec):
     print(json.dumps(out))
 
 
+def sv_case(reps):
+    """One certified SR step of the headline shape (N32 M64 K2, 128 chains x 200
+    samples), then its S·v timed alone with the fused kernel and with the two
+    FP64 passes (the launches a profiler can attribute; the step's own run
+    inside a CUDA graph with a conditional node)."""
+    import torch  # noqa: F401  (initialises the device as the other legs do)
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    out = {}
+    for fused in (1, 0):
+        c = pkg.Context(N, M, K, pkg.synthetic_j(N), H, device=0)
+        c.set_weights(*pkg.synthetic_weights(N, M, K, 0.01, SEED))
+        c.set_option(pkg.OPT_PRECISION, pkg.PRECISION_CERTIFIED)
+        c.set_option(pkg.OPT_FUSED_SV, fused)
+        c.sr_step(SEED, 128, SAMPLES, BURN, 0.1, 40.0, RTOL, MAXIT)
+        ms, by = c.time_kernel(pkg.KERNEL_SV, reps=reps)
+        out["fused" if fused else "two_pass"] = {"ms": ms, "bytes": by, "GB_per_s": by / ms / 1e6}
+        c.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -750,8 +798,16 @@ def main():
     ap.add_argument("--precision-chains", type=int, default=16384, help="chains of the precision-form line (0: skip)")
     ap.add_argument("--serve-window", type=float, default=4.0, help="seconds of arrivals per serving line")
     ap.add_argument("--kernel-case", default="", help="N,M,K,chains,samples: one mixed step, then its kernels timed alone")
+    ap.add_argument("--sv-case", type=int, default=0,
+                    help="REPS: one certified headline step, then its S·v (fused and two-pass) timed alone")
+    ap.add_argument("--serving-only", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--serving-device", type=int, default=0, help=argparse.SUPPRESS)
     args = ap.parse_args()
-    if args.kernel_case:
+    if args.serving_only:
+        serving_only(args)
+    elif args.sv_case:
+        sv_case(args.sv_case)
+    elif args.kernel_case:
         kernel_case(args.kernel_case)
     elif args.impl == "reference":
         run_reference(args)

@@ -133,8 +133,9 @@ typedef struct nqes_step_info {
  * Limits: 1 <= K <= 4, 1 <= N <= 128, 1 <= M <= 512. */
 int nqes_create(int n_spins, int n_hidden, int n_states, const double *J, double h, int device, nqes_ctx **out);
 int nqes_destroy(nqes_ctx *ctx);
-/* Description of the last failure on ctx (or of the last failed nqes_create
- * when ctx is NULL). Valid until the next call on the same context. */
+/* Description of the last failure on ctx (or of the calling thread's last
+ * failed nqes_create when ctx is NULL). Valid until the next call on the same
+ * context (in the same thread). */
 const char *nqes_last_error(const nqes_ctx *ctx);
 int nqes_set_option(nqes_ctx *ctx, int option, int64_t value);
 
@@ -255,9 +256,11 @@ int nqes_batch_destroy(nqes_batch *batch);
 const char *nqes_batch_last_error(const nqes_batch *batch);
 /* One SR step of every member; every array has `count` entries in member
  * order, with nqes_sr_step's meaning. e_mats (or an entry) and infos may be
- * NULL; statuses (may be NULL) receives each member's status, NQES_ERR_STATE for
- * members not run because an earlier member's arguments failed; ms_total (may
- * be NULL) the device time of the batched launch. Returns the first member error. */
+ * NULL; statuses (may be NULL) receives each member's status: NQES_ERR_STATE for
+ * every other member when one member's arguments or buffers failed (none ran),
+ * the error itself for every member when the capture, launch or wait failed;
+ * ms_total (may be NULL) the device time of the batched launch. Returns the
+ * first member error. */
 int nqes_batch_sr_step(nqes_batch *batch, const uint64_t *seeds, const int *chains, const int *samples_per_chain,
                        const int *burn_in, const double *lr, const double *reglam, const double *rtol,
                        const uint64_t *maxit, double *const *e_mats, nqes_step_info *infos, int *statuses,
@@ -319,6 +322,9 @@ int nqes_server_times(nqes_server *server, double *admit_s, double *rebuild_s, d
                       uint64_t *steps, uint64_t *rebuilds);
 /* Stops the worker after its current step; unfinished solves are dropped. */
 int nqes_server_destroy(nqes_server *server);
+/* The last error: of a rejected submit, or of a batched step that failed
+ * (its lane and the batch's message; the members carry the status). Valid in
+ * the calling thread until its next call. NULL: the last failed create. */
 const char *nqes_server_last_error(const nqes_server *server);
 
 #ifdef __cplusplus

@@ -421,6 +421,10 @@ class Server:
         self.lib.nqes_server_status(self._h, ctypes.byref(q), ctypes.byref(a), ctypes.byref(d), ctypes.byref(b))
         return {"queued": q.value, "active": a.value, "done": d.value, "bytes_in_use": b.value}
 
+    def last_error(self):
+        """The last rejected submit's or failed batched step's message ('' if none)."""
+        return self.lib.nqes_server_last_error(self._h).decode()
+
     def times(self):
         """Cumulative worker seconds by phase and the step / batch-rebuild counts."""
         v = [ctypes.c_double() for _ in range(4)]

@@ -64,6 +64,10 @@ __global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F,
     if (loop_guard_off(F.guard)) return;
     constexpr int WS = JT * JB, NG = kThreads / JT;
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K, IC = F.ic;
+    if (!dyn_smem_covers((size_t(IC) * WS + ((N + 3) & ~3) + WS + NG * RB) * sizeof(float)) || NW > 2) {
+        if (threadIdx.x == 0) atomicOr(F.err, kErrLaunch);
+        return;
+    }
     float *sw = reinterpret_cast<float *>(smem4);  // IC x WS
     float *sva = sw + IC * WS;                     // N (rounded to 4)
     float *svb = sva + ((N + 3) & ~3);             // WS
@@ -178,6 +182,14 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// Staging buffers, then weights and sign words; with row sets the staging
+// buffers must also hold every thread's IB JB + IB + JB sums.
+template <int IB, int JB> __host__ __device__ constexpr size_t cols_smem(bool sets) {
+    constexpr size_t st = cols_stage(JB);
+    constexpr size_t stage = size_t(2) * 2 * st * kJT * JB, red = size_t(kThreads) * (IB * JB + IB + JB);
+    return ((sets && red > stage ? red : stage) + 2 * st) * sizeof(float) + size_t(2) * st * 2 * 8;
+}
+
 // Column-type partial sums over chunk blockIdx.x of the rows of state
 // k = blockIdx.y, grid rows i in block blockIdx.z (kGroups * IB of them).
 //   mode 0: w_r = u_s B          (the O^T u pass of S·v)
@@ -206,6 +218,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int
     const int c = blockIdx.x, k = blockIdx.y;
     const int tj = threadIdx.x & (kJT - 1), ig = threadIdx.x / kJT;
     const int nset = kGroups / gn, set = ig / gn, igl = ig - set * gn;
+    if (!dyn_smem_covers(cols_smem<IB, JB>(nset > 1)) || NW > 2 || MT > WS) {
+        if (threadIdx.x == 0) atomicOr(F.err, kErrLaunch);
+        return;
+    }
     const int ibase = blockIdx.z * (gn * IB) + igl * IB;
     const int vpr = mode == 3 ? K * (K + 1) / 2 : K;  // (virtual) rows per sample
     const size_t nrows = size_t(F.Ns) * vpr;
@@ -494,13 +510,6 @@ cudaError_t rows_dispatch(const FactArgs &F, const float *v, float *u, cudaStrea
     return rows_launch<8, 64>(F, v, u, st, prepare);
 }
 
-// Staging buffers, then weights and sign words; with row sets the staging
-// buffers must also hold every thread's IB JB + IB + JB sums.
-template <int IB, int JB> constexpr size_t cols_smem(bool sets) {
-    constexpr size_t st = cols_stage(JB);
-    constexpr size_t stage = size_t(2) * 2 * st * kJT * JB, red = size_t(kThreads) * (IB * JB + IB + JB);
-    return ((sets && red > stage ? red : stage) + 2 * st) * sizeof(float) + size_t(2) * st * 2 * 8;
-}
 template <int IB, int JB>
 cudaError_t cols_launch(const FactArgs &F, int mode, const float *w, const cplx *E, float *out, cudaStream_t st,
                         bool prepare) {

@@ -80,6 +80,11 @@ __global__ void __launch_bounds__(kTcThreads) k_frows_tc(FactArgs F, int NP, int
                                                        float *__restrict__ u, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     if (loop_guard_off(F.guard)) return;  // before any barrier init or tensor-memory allocation
+    if (!dyn_smem_covers(abytes + bbytes + 64 + kTcThreads * sizeof(float)) || unsigned(MN) > tcols || tcols > 512 ||
+        F.NW > 2) {
+        if (threadIdx.x == 0) atomicOr(err, kErrLaunch);
+        return;
+    }
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, MT = F.MT, KK = K * K;
     unsigned char *sA = smem_raw;
     unsigned char *sB = smem_raw + abytes;
@@ -284,6 +289,11 @@ __global__ void __launch_bounds__(kColThreadsTc) k_fcols_tc(FactArgs F, int mode
                                                           float *__restrict__ out, int *err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     if (loop_guard_off(F.guard)) return;  // before any barrier init or tensor-memory allocation
+    if (!dyn_smem_covers(tbytes + abytes + bbytes + 2 * kColRows * (4 + 16) + 16) || unsigned(MN) > tcols ||
+        tcols > 512 || F.NW > 2) {
+        if (threadIdx.x == 0) atomicOr(err, kErrLaunch);
+        return;
+    }
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K, P = K * L;
     float *sT = reinterpret_cast<float *>(smem_raw);  // [2][rows][MT]: two batches, or (mode 3) two factors
     unsigned char *sA = smem_raw + tbytes;

@@ -325,6 +325,10 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample(const SampleArgs<S> 
     const int TK = A.tk, WK = TK >> 5;
     const int my_kk = tid / TK, my_jl = tid - (tid / TK) * TK;
     const int c = blockIdx.x;
+    if (!dyn_smem_covers(smem_bytes(N, M, K, sizeof(S))) || K * NW > kMaxSpinWords) {
+        if (tid == 0) atomicOr(A.err, kErrLaunch);
+        return;
+    }
     Smem<S> sm = carve<S>(smem_raw, N, M, K);
 
     // Every thread advances an identical copy of the chain's pcg64 stream, so

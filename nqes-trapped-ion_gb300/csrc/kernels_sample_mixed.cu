@@ -181,6 +181,10 @@ __global__ void __maxnreg__(UMAX >= 4 ? 255 : 128) k_sample_mixed(const MixedArg
     const int TK = A.tk, WK = TK >> 5;
     const int my_kk = tid / TK, my_jl = tid - (tid / TK) * TK;
     const int c = blockIdx.x;
+    if (!dyn_smem_covers(msmem_bytes(N, M, K)) || K * NW > kMaxSpinWords) {
+        if (tid == 0) atomicOr(A.err, kErrLaunch);
+        return;
+    }
     MSmem sm = mcarve(smem_raw, N, M, K);
     const bool writer = tid == 0;
 

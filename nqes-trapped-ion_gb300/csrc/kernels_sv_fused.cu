@@ -57,11 +57,22 @@ constexpr int kFsMaxWarps = kFsMaxThreads / 32;
 // columns p = t + c T (c < C), holding v's split and its partial of O^T u for
 // them in registers. Rows of a staged group are walked one at a time, so no
 // per-row state lives in registers.
+// Dynamic shared memory of a launch: two staged groups of G rows, the
+// per-warp partials of u, u itself, two mbarriers.
+__host__ __device__ inline size_t fused_smem(int P, int G) {
+    return size_t(2) * G * P * sizeof(double) + (size_t(G) * kFsMaxWarps + G + 1) * sizeof(float2) +
+           2 * sizeof(uint64_t);
+}
+
 template <int C, int MaxT, bool PRE>
 __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     extern __shared__ __align__(16) unsigned char fs_smem[];
     if (loop_guard_off(a.guard)) return;
     const int P = a.P, G = a.G, T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
+    if (!dyn_smem_covers(fused_smem(P, G)) || nw > kFsMaxWarps || T * C < P) {
+        if (tid == 0) atomicOr(a.err, kErrLaunch);
+        return;
+    }
     double *buf0 = reinterpret_cast<double *>(fs_smem);
     double *buf1 = buf0 + size_t(G) * P;
     float2 *red = reinterpret_cast<float2 *>(buf1 + size_t(G) * P);  // [G][warps]
@@ -209,11 +220,6 @@ template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
 }
 template <class F> cudaError_t fused_dispatch(int C, F &&f, bool pre = false) {
     return pre ? fused_dispatch_p<true>(C, f) : fused_dispatch_p<false>(C, f);
-}
-
-size_t fused_smem(int P, int G) {
-    return size_t(2) * G * P * sizeof(double) + (size_t(G) * kFsMaxWarps + G + 1) * sizeof(float2) +
-           2 * sizeof(uint64_t);
 }
 
 constexpr int kFsMaxG = 16;

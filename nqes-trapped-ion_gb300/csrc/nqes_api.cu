@@ -117,9 +117,10 @@ struct nqes_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
-static std::string g_create_error;
+// Error text for calls that have no context (reported by nqes_last_error(NULL)),
+// per calling thread: the serving loop's workers create contexts concurrently.
+thread_local std::string g_create_error;
 
-// Error text for calls that have no context (reported by nqes_last_error(NULL)).
 namespace nqes {
 void set_global_error(const std::string &msg) { g_create_error = msg; }
 }  // namespace nqes
@@ -851,7 +852,11 @@ int step_finish(nqes_ctx *ctx, int chains, int m, int burn, int arith, uint64_t 
         }
     }
     const int e = *ctx->err_host;
-    if (e & kErrTimeout) {  // first: what the step computed after a wait ran out is not meaningful
+    if (e & kErrLaunch) {  // a kernel returned at entry: the step's results are not meaningful
+        ctx->err = "a kernel was launched with less dynamic shared memory than its layout needs (launch check)";
+        return NQES_ERR_CUDA;
+    }
+    if (e & kErrTimeout) {  // what the step computed after a wait ran out is not meaningful
         ctx->err = "a bounded device-side wait ran out (bulk staging into shared memory)";
         return NQES_ERR_TIMEOUT;
     }
@@ -1710,7 +1715,7 @@ struct nqes_batch {
 };
 
 namespace {
-std::string g_batch_create_error;
+thread_local std::string g_batch_create_error;
 }
 
 extern "C" {
@@ -1803,8 +1808,8 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
         nqes_ctx *c = b->m[i];
         const int rc = step_prepare(c, seeds[i], chains[i], samples[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i],
                                     &arith[i]);
-        if (statuses) statuses[i] = rc;
-        if (rc) {
+        if (rc) {  // this member's error; the others stay NQES_ERR_STATE (not run)
+            if (statuses) statuses[i] = rc;
             b->err = "member " + std::to_string(i) + ": " + c->err;
             return rc;
         }
@@ -1818,6 +1823,9 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
                    c->tensor_cores, c->reject_filter ? 1 : 0, c->mixed_exact_all ? 1 : 0, c->dw_force_warps,
                    c->dw_force_stage, (long long)c->buf_gen, total, c->stage_fault, c->mixed_e64 ? 1 : 0};
     }
+    // Capture (when the members changed), launch and wait. A failure here
+    // means no member's step ran: each member's status becomes the error.
+    auto capture_and_run = [&]() -> int {
     if (!b->exec || keys != b->keys) {
         NvtxRange r_build("batch graph capture");
         if (b->exec) {
@@ -1903,6 +1911,14 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
     if (le != cudaSuccess) {
         b->err = std::string("batched step: ") + cudaGetErrorString(le);
         return NQES_ERR_CUDA;
+    }
+    return NQES_OK;
+    };
+    const int rc_run = capture_and_run();
+    if (rc_run) {
+        if (statuses)
+            for (int i = 0; i < n; i++) statuses[i] = rc_run;
+        return rc_run;
     }
     float ms = 0;
     cudaEventElapsedTime(&ms, b->ev0, b->ev1);

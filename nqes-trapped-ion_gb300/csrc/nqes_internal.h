@@ -124,7 +124,18 @@ enum : int {
     kErrMinresNonFinite = 4,
     kErrMinresCap = 8,      // MINRES-QLP stopped at the device-side iteration cap
     kErrTimeout = 16,       // a bounded device-side wait ran out
+    kErrLaunch = 32,        // a kernel got less dynamic shared memory than its layout needs
 };
+
+// True when the launch's dynamic shared memory holds `need` bytes. Kernels
+// that carve their dynamic shared memory check this at entry (uniformly over
+// the block) and return with kErrLaunch instead of addressing past the
+// allocation, should a host-side size ever disagree with the device layout.
+__device__ __forceinline__ bool dyn_smem_covers(size_t need) {
+    unsigned have;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(have));
+    return need <= size_t(have);
+}
 
 size_t sample_smem_bytes(const Shape &sh, int threads, bool complex_arith);
 int sample_threads(int K, int tk);  // K*tk threads per chain

@@ -241,8 +241,14 @@ void worker_loop(nqes_server *srv, Lane *lane) {
             emats[i] = reinterpret_cast<double *>(lane->active[i]->emat.data());
         }
         const auto c2 = Clock::now();
-        nqes_batch_sr_step(lane->batch, seeds.data(), chains.data(), m.data(), burn.data(), lr.data(), reglam.data(),
-                           rtol.data(), maxit.data(), emats.data(), nullptr, status.data(), nullptr);
+        const int step_rc = nqes_batch_sr_step(lane->batch, seeds.data(), chains.data(), m.data(), burn.data(),
+                                               lr.data(), reglam.data(), rtol.data(), maxit.data(), emats.data(),
+                                               nullptr, status.data(), nullptr);
+        if (step_rc != NQES_OK && step_rc != NQES_ERR_NONFINITE) {
+            // kept for nqes_server_last_error: the failed members carry the status
+            std::lock_guard<std::mutex> g(srv->mu);
+            srv->err = "lane " + std::to_string(lane->index) + ": " + nqes_batch_last_error(lane->batch);
+        }
         const auto c3 = Clock::now();
         std::vector<Solve *> keep;
         for (size_t i = 0; i < n; i++) {
@@ -312,13 +318,19 @@ void worker_loop(nqes_server *srv, Lane *lane) {
     lane->active.clear();
 }
 
-std::string g_server_error;
+thread_local std::string g_server_error;
 
 }  // namespace
 
 extern "C" {
 
-const char *nqes_server_last_error(const nqes_server *s) { return s ? s->err.c_str() : g_server_error.c_str(); }
+const char *nqes_server_last_error(const nqes_server *s) {
+    if (!s) return g_server_error.c_str();
+    thread_local std::string copy;  // the workers may set err meanwhile
+    std::lock_guard<std::mutex> g(const_cast<nqes_server *>(s)->mu);
+    copy = s->err;
+    return copy.c_str();
+}
 
 int nqes_server_create(int device, uint64_t hbm_budget_bytes, int max_active, nqes_server **out) {
     if (!out || max_active < 1 || hbm_budget_bytes == 0) {

@@ -620,6 +620,10 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int c = blockIdx.x;
     const bool e64 = A.out64 || A.e64;  // FP64 local energies (tanh of the exact theta, FP64 tables)
+    if (!dyn_smem_covers(dsmem_bytes(N, MP, K, A.stage != 0, e64)) || K * NW > kMaxSpinWords || A.G * A.U != MP) {
+        if (tid == 0) atomicOr(A.err, kErrLaunch);
+        return;
+    }
     DSmem sm = dcarve(smem_raw, N, MP, K, e64);
     const bool writer = tid == 0;
     const size_t tb = dw_table_bytes(N, MP, K);

@@ -183,11 +183,15 @@ def test_correlations_match_oracle(pkg, N, M, K, real):
 
 
 @pytest.mark.parametrize("N,M,K,chains,m", [(8, 16, 2, 16, 30), (32, 64, 2, 32, 20), (12, 24, 3, 8, 20),
-                                            (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (10, 300, 4, 4, 6)])
+                                            (20, 40, 1, 8, 10), (64, 128, 4, 4, 6), (10, 300, 4, 4, 6),
+                                            (19, 19, 3, 8, 10), (72, 144, 4, 4, 6), (68, 136, 3, 4, 6),
+                                            (86, 172, 1, 8, 6), (96, 192, 4, 4, 6)])
 def test_mixed_precision_keeps_fp64_chains(pkg, N, M, K, chains, m):
     """MIXED: FP32 decisions with a certified bound and an exact FP64 fallback
-    give the FP64 chains bit for bit (decision-warp form for up to 16 hidden
-    units per lane, block form beyond: M=300, K=4); energies within 1e-6 relative, FP32
+    give the FP64 chains bit for bit (decision-warp form for up to 32 hidden
+    units per lane, block form beyond: M=300, K=4; the serving loop's shapes:
+    M = N odd, 32 units per lane at K = 3, 4, N > 64 up to N96 M192 K4, the
+    largest request it serves); energies within 1e-6 relative, FP32
     log-derivatives, moments and S·v (factored FP32 passes) within 1e-5 / 1e-4,
     the updated weights within 5e-5 (2e-4 where 24 samples meet P > 10^4)."""
     J = synthetic_j(N)

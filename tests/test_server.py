@@ -202,3 +202,38 @@ def test_size_classes_run_side_by_side(pkg):
     for rid, s in zip(ids, (big, small)):
         a = alone[s["seed"]]
         assert res[rid]["energies"] == a["energies"] and res[rid]["steps"] == a["steps"]
+
+
+@pytest.mark.gpu
+def test_nonfinite_solve_restarts_then_fails_beside_a_healthy_one(pkg):
+    """A solve whose weights hold a NaN goes non-finite at every step: the
+    server restarts its run with a new seed 15 times (16 runs, as code/run.sh)
+    and then fails it with NQES_ERR_NONFINITE, while a solve of another size
+    class that runs at the same time (MIXED, the decision-warp sampler) is
+    unaffected: its result equals running it alone."""
+    bad = dict(n=20, m=40, k=3, h=0.8, prec=1, seed=71)
+    good = dict(n=48, m=96, k=2, h=0.7, prec=1, seed=73)  # P = 9408: another lane
+
+    def submit(srv, s, nan):
+        a, b, w = helpers.random_weights(s["n"], s["m"], s["k"], 0.05, s["seed"], real=True)
+        if nan:
+            w[0, 1, 2] = np.nan
+        return srv.submit(s["n"], s["m"], s["k"], synthetic_j(s["n"]), weights=(a, b, w), h=s["h"], seed=s["seed"],
+                          chains=32, samples_per_chain=20, burn_in=8, reglam0=5.0, tol=1e-12, max_steps=4,
+                          precision=s["prec"])
+
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+    submit(srv, good, False)
+    (alone,) = srv.wait_all(1)
+    srv.close()
+    assert alone["status"] == 0
+    srv = pkg.Server(hbm_budget_bytes=1 << 36, max_active=4)
+    id_bad = submit(srv, bad, True)
+    id_good = submit(srv, good, False)
+    res = {r["id"]: r for r in srv.wait_all(2)}
+    err = srv.last_error()
+    srv.close()
+    rb, rg = res[id_bad], res[id_good]
+    assert rb["status"] == pkg.ERR_NONFINITE and rb["restarts"] == 15, (rb, err)
+    assert rg["status"] == 0 and rg["restarts"] == 0
+    assert rg["energies"] == alone["energies"] and rg["steps"] == alone["steps"]
