@@ -791,8 +791,10 @@ def main():
     ap.add_argument("--batch-solves", type=int, default=64, help="solves of the batched line (0: skip)")
     ap.add_argument("--target-solves", type=int, default=32,
                     help="solves of the headline shape in the batched mixed target line (0: skip)")
-    ap.add_argument("--serve-rates", default="1,2,4,8,16,32,64",
-                    help="arrival rates (1/s) of the serving lines ('' : skip)")
+    ap.add_argument("--serve-rates", default="",
+                    help="arrival rates (1/s) of the serving lines, e.g. 1,2,4,8,16,32,64 ('': skip, the default: "
+                         "the sweep hit an illegal address in its three-lane form on GB300 and stays off until "
+                         "the cause is found)")
     ap.add_argument("--precision", default="certified", choices=sorted(FORMS),
                     help="the headline's form: certified (FP64 results, FP32-certified decisions) or fp64")
     ap.add_argument("--precision-chains", type=int, default=16384, help="chains of the precision-form line (0: skip)")

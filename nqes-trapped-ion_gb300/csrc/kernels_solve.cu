@@ -852,7 +852,7 @@ template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, co
         return e != cudaSuccess ? e : launch_fcols(B.F, B.u32, B.ypart32, st);
     }
     if constexpr (std::is_same<S, double>::value) {
-        if (B.fG) return launch_sv_fused(B.Ns, P, B.fG, B.svp, B.O, v, B.ysv, B.err, B.guard, st, B.o_split != 0);
+        if (B.fG) return launch_sv_fused(B.Ns, P, B.fG, B.fNB, B.svp, B.O, v, B.ysv, B.err, B.guard, st, B.o_split != 0);
     }
     k_sv_rows<S><<<rb, kVecThreads, 0, st>>>(B.Ns, P, B.O, v, B.u, B.guard);
     k_sv_cols<S><<<g, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.O, B.u, B.ypart, B.guard);

@@ -7,11 +7,17 @@
 // FP64 pipe retires about two FMAs per SM per clock: 0.41 ms at N32 M64 K2.
 //
 // Here a persistent CTA per SM owns a contiguous range of rows and streams
-// them through shared memory in groups of G rows (as many as two buffers of
-// shared memory hold, at most 16), double-buffered by bulk copies
-// (cp.async.bulk on an mbarrier, bounded waits). For each staged group
-//   pass 1: u_r = O_r . v for the group's rows, block-wide, and
-//   pass 2: y_p += O_rp u_r into the CTA's partial of O^T u (registers),
+// them through shared memory in groups of G rows, NB groups deep (a ring of
+// buffers, each filled by a bulk copy (cp.async.bulk) on its own mbarrier,
+// bounded waits), so that up to NB - 1 groups are in flight while one is
+// used. For each staged group
+//   pass 1: u_r = O_r . v, rows taken in pairs: each thread's two partial
+//           dots, then one butterfly over the warp for both rows (the first
+//           exchange trades one row for the other, so the pair costs five
+//           exchanges, not ten), the warps' sums to shared memory;
+//   pass 2: every warp sums the warps' partials of a pair of rows (again one
+//           butterfly), then y_p += O_rp u_r into the CTA's partial of O^T u
+//           (registers),
 // both from shared memory, so O leaves HBM once per S·v. The arithmetic is
 // double-float on the FP32 pipe: each FP64 entry d is split exactly-enough
 // into hi + lo floats by integer operations (hi = d cut to 24 significant
@@ -41,8 +47,13 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+constexpr int kFsMaxThreads = 1024;
+constexpr int kFsMaxWarps = kFsMaxThreads / 32;
+constexpr int kFsMaxG = 16;  // rows per group
+constexpr int kFsMaxNB = 4;  // groups in the ring
+
 struct FusedSvArgs {
-    int Ns, P, G;
+    int Ns, P, G, NB;
     int o_split;  // O already stored as (hi, lo) pairs
     const double *O, *v;
     double *ypart;  // gridDim.x × P
@@ -50,34 +61,46 @@ struct FusedSvArgs {
     const int *guard;
 };
 
-constexpr int kFsMaxThreads = 1024;
-constexpr int kFsMaxWarps = kFsMaxThreads / 32;
+// Dynamic shared memory of a launch: NB groups of G rows, the warps'
+// partials of the group's u (float2 [G][warps]), NB mbarriers.
+__host__ __device__ inline size_t fused_smem(int P, int G, int NB) {
+    return size_t(NB) * G * P * sizeof(double) + size_t(G) * kFsMaxWarps * sizeof(float2) +
+           size_t(NB) * sizeof(uint64_t);
+}
+
+// The double-float pairs (h0, l0) and (h1, l1) summed over the warp in a
+// fixed order: the first exchange (lanes i and i + 16) sends the row a lane
+// does not keep, the next four reduce the kept row within each half. Returns
+// the first row's sum in lane 0 and the second's in lane 16 (the other lanes
+// hold the same sums in other orders).
+__device__ __forceinline__ void warp_sum_pair(float &h, float &l, float h0, float l0, float h1, float l1) {
+    const bool upper = (threadIdx.x & 16) != 0;
+    h = upper ? h1 : h0;
+    l = upper ? l1 : l0;
+    const float sh = upper ? h0 : h1, sl = upper ? l0 : l1;
+    df_acc(h, l, __shfl_xor_sync(0xffffffffu, sh, 16), __shfl_xor_sync(0xffffffffu, sl, 16));
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1)
+        df_acc(h, l, __shfl_xor_sync(0xffffffffu, h, off), __shfl_xor_sync(0xffffffffu, l, off));
+}
 
 // Block: T = blockDim.x threads (a multiple of 32, T C >= P); thread t owns
 // columns p = t + c T (c < C), holding v's split and its partial of O^T u for
-// them in registers. Rows of a staged group are walked one at a time, so no
-// per-row state lives in registers.
-// Dynamic shared memory of a launch: two staged groups of G rows, the
-// per-warp partials of u, u itself, two mbarriers.
-__host__ __device__ inline size_t fused_smem(int P, int G) {
-    return size_t(2) * G * P * sizeof(double) + (size_t(G) * kFsMaxWarps + G + 1) * sizeof(float2) +
-           2 * sizeof(uint64_t);
-}
-
+// them in registers.
 template <int C, int MaxT, bool PRE>
 __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     extern __shared__ __align__(16) unsigned char fs_smem[];
     if (loop_guard_off(a.guard)) return;
-    const int P = a.P, G = a.G, T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
-    if (!dyn_smem_covers(fused_smem(P, G)) || nw > kFsMaxWarps || T * C < P) {
+    const int P = a.P, G = a.G, NB = a.NB, T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5,
+              nw = T >> 5;
+    if (!dyn_smem_covers(fused_smem(P, G, NB)) || nw > kFsMaxWarps || T * C < P || G > kFsMaxG || NB < 2 ||
+        NB > kFsMaxNB) {
         if (tid == 0) atomicOr(a.err, kErrLaunch);
         return;
     }
-    double *buf0 = reinterpret_cast<double *>(fs_smem);
-    double *buf1 = buf0 + size_t(G) * P;
-    float2 *red = reinterpret_cast<float2 *>(buf1 + size_t(G) * P);  // [G][warps]
-    float2 *us = red + size_t(G) * kFsMaxWarps;                       // [G]
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(us + G + (G & 1));  // [2], 8-byte aligned
+    double *bufs = reinterpret_cast<double *>(fs_smem);                   // [NB][G][P]
+    float2 *red = reinterpret_cast<float2 *>(bufs + size_t(NB) * G * P);  // [G][kFsMaxWarps]
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(red + size_t(G) * kFsMaxWarps);  // [NB]
     const int r0 = int(int64_t(a.Ns) * blockIdx.x / gridDim.x), r1 = int(int64_t(a.Ns) * (blockIdx.x + 1) / gridDim.x);
     const int ngroups = (r1 - r0 + G - 1) / G;
 
@@ -89,99 +112,106 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
         vh[c] = vl[c] = yh[c] = yl[c] = 0.f;
         if (p < P) df_split(a.v[p], vh[c], vl[c]);
     }
-    auto issue = [&](int g) {  // thread 0: group g into buffer g & 1
+    auto issue = [&](int g) {  // thread 0: group g into ring slot g % NB
         const int rs = r0 + g * G, nr = min(G, r1 - rs);
         const unsigned bytes = unsigned(size_t(nr) * P * sizeof(double));
-        uint64_t *mb = &mbar[g & 1];
+        uint64_t *mb = &mbar[g % NB];
         mbar_expect_tx(mb, bytes);
-        bulk_g2s(g & 1 ? buf1 : buf0, a.O + size_t(rs) * P, bytes, mb);
+        bulk_g2s(bufs + size_t(g % NB) * G * P, a.O + size_t(rs) * P, bytes, mb);
     };
-    if (tid == 0) {
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
-    }
+    if (tid == 0)
+        for (int b = 0; b < NB; b++) mbar_init(&mbar[b], 1);
     __syncthreads();
-    if (tid == 0) {
-        if (ngroups > 0) issue(0);
-        if (ngroups > 1) issue(1);
-    }
+    if (tid == 0)
+        for (int g = 0; g < min(NB, ngroups); g++) issue(g);
+
+    // thread's partial dot of row `row` with v (two chains over its columns);
+    // FP64 entries are split in place (each thread its own columns, read back
+    // only by itself in pass 2)
+    auto row_dot = [&](double *row, float &h, float &l) {
+        float h2 = 0.f, l2 = 0.f;
+        h = l = 0.f;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+            const int p = tid + c * T;
+            if (p < P) {
+                float oh, ol;
+                if (PRE) {  // split when it was written
+                    const float2 o = *reinterpret_cast<const float2 *>(row + p);
+                    oh = o.x;
+                    ol = o.y;
+                } else {
+                    range_ok &= df_split(row[p], oh, ol);
+                    *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
+                }
+                if (c & 1)
+                    df_fma(h2, l2, oh, ol, vh[c], vl[c]);
+                else
+                    df_fma(h, l, oh, ol, vh[c], vl[c]);
+            }
+        }
+        df_acc(h, l, h2, l2);
+    };
+
     bool timed_out = false;
     int g = 0;
     for (; g < ngroups; g++) {
-        double *buf = g & 1 ? buf1 : buf0;
+        double *buf = bufs + size_t(g % NB) * G * P;
         const int nr = min(G, r1 - (r0 + g * G));
-        const bool ok = mbar_wait(&mbar[g & 1], unsigned(g >> 1) & 1u);
+        const bool ok = mbar_wait(&mbar[g % NB], unsigned(g / NB) & 1u);
         if (__syncthreads_or(!ok)) {
             timed_out = true;
             break;
         }
-        // pass 1, row by row: split the staged entries in place (each thread
-        // its own columns, read back only by itself), the row's dot product
-        // with v, its warp sum to red[r][warp]
-        for (int r = 0; r < nr; r++) {
-            double *row = buf + size_t(r) * P;
-            // two accumulators (even and odd columns) for two independent chains
-            float h = 0.f, l = 0.f, h2 = 0.f, l2 = 0.f;
-#pragma unroll
-            for (int c = 0; c < C; c++) {
-                const int p = tid + c * T;
-                if (p < P) {
-                    float oh, ol;
-                    if (PRE) {  // split when it was written
-                        const float2 o = *reinterpret_cast<const float2 *>(row + p);
-                        oh = o.x;
-                        ol = o.y;
-                    } else {
-                        range_ok &= df_split(row[p], oh, ol);
-                        *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
-                    }
-                    if (c & 1)
-                        df_fma(h2, l2, oh, ol, vh[c], vl[c]);
-                    else
-                        df_fma(h, l, oh, ol, vh[c], vl[c]);
-                }
-            }
-            df_acc(h, l, h2, l2);
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
-                df_acc(h, l, oh, ol);
-            }
+        // pass 1: rows in pairs; the warp's sums of rows r and r + 1 to red
+        for (int r = 0; r < nr; r += 2) {
+            float h0, l0, h1 = 0.f, l1 = 0.f;
+            row_dot(buf + size_t(r) * P, h0, l0);
+            if (r + 1 < nr) row_dot(buf + size_t(r + 1) * P, h1, l1);
+            float h, l;
+            warp_sum_pair(h, l, h0, l0, h1, l1);
             if (lane == 0) red[r * kFsMaxWarps + warp] = make_float2(h, l);
+            if (lane == 16 && r + 1 < nr) red[(r + 1) * kFsMaxWarps + warp] = make_float2(h, l);
         }
         __syncthreads();
-        // u_r: the warps' sums in warp order, one warp per row
-        for (int r = warp; r < nr; r += nw) {
-            float h = 0.f, l = 0.f;
-            if (lane == 0)
-                for (int w = 0; w < nw; w++) df_acc(h, l, red[r * kFsMaxWarps + w].x, red[r * kFsMaxWarps + w].y);
-            if (lane == 0) us[r] = make_float2(h, l);
-        }
-        __syncthreads();
-        // pass 2: y_p += O_rp u_r over the group's rows
-        for (int r = 0; r < nr; r++) {
-            const float2 u = us[r];
-            const double *row = buf + size_t(r) * P;
+        // pass 2: per pair of rows, u from the warps' sums (every warp alike,
+        // in warp order), then y_p += O_rp u_r
+        for (int r = 0; r < nr; r += 2) {
+            const bool two = r + 1 < nr;
+            float2 p0 = make_float2(0.f, 0.f), p1 = make_float2(0.f, 0.f);
+            if (lane < nw) {
+                p0 = red[r * kFsMaxWarps + lane];
+                if (two) p1 = red[(r + 1) * kFsMaxWarps + lane];
+            }
+            float h, l;
+            warp_sum_pair(h, l, p0.x, p0.y, p1.x, p1.y);
+            const float u0h = __shfl_sync(0xffffffffu, h, 0), u0l = __shfl_sync(0xffffffffu, l, 0);
+            const float u1h = __shfl_sync(0xffffffffu, h, 16), u1l = __shfl_sync(0xffffffffu, l, 16);
+            const double *row0 = buf + size_t(r) * P, *row1 = row0 + P;
 #pragma unroll
             for (int c = 0; c < C; c++) {
                 const int p = tid + c * T;
                 if (p < P) {
-                    const float2 o = *reinterpret_cast<const float2 *>(row + p);
-                    df_fma(yh[c], yl[c], o.x, o.y, u.x, u.y);
+                    const float2 o = *reinterpret_cast<const float2 *>(row0 + p);
+                    df_fma(yh[c], yl[c], o.x, o.y, u0h, u0l);
+                    if (two) {
+                        const float2 o1 = *reinterpret_cast<const float2 *>(row1 + p);
+                        df_fma(yh[c], yl[c], o1.x, o1.y, u1h, u1l);
+                    }
                 }
             }
         }
-        // every thread is done with buf (and with us); its in-place splits
+        // every thread is done with the slot and with red; its in-place splits
         // (generic proxy) are ordered before the next bulk copy (async proxy)
         fence_proxy_async_smem();
         __syncthreads();
-        if (tid == 0 && g + 2 < ngroups) issue(g + 2);
+        if (tid == 0 && g + NB < ngroups) issue(g + NB);
     }
     if (timed_out) {
         if (tid == 0) {
             atomicOr(a.err, kErrTimeout);
-            // wait (bounded) for the copies still in flight into this CTA's buffers
-            for (int q = g; q < min(g + 2, ngroups); q++) mbar_wait(&mbar[q & 1], unsigned(q >> 1) & 1u);
+            // wait (bounded) for the copies still in flight into this CTA's ring
+            for (int q = g; q < min(g + NB, ngroups); q++) mbar_wait(&mbar[q % NB], unsigned(q / NB) & 1u);
         }
         return;
     }
@@ -194,9 +224,10 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
 }
 
 // Columns per thread C and threads per block T (whole warps, T C >= P): the
-// fewest columns whose block fits its register budget: C = 1, 2, 4 with up to
+// fewest columns whose block fits its register budget: C <= 6 with up to
 // 1024 threads (64 registers), 8 with up to 768, 16 with up to 512.
-constexpr int kFsShapes[5][2] = {{1, 1024}, {2, 1024}, {4, 1024}, {8, 768}, {16, 512}};
+constexpr int kFsShapes[8][2] = {{1, 1024}, {2, 1024}, {3, 1024}, {4, 1024},
+                                 {5, 1024}, {6, 1024}, {8, 768},  {16, 512}};
 bool fused_shape(int P, int *C, int *T) {
     for (const auto &sh : kFsShapes) {
         const int t = 32 * ((P + 32 * sh[0] - 1) / (32 * sh[0]));
@@ -213,7 +244,10 @@ template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
     switch (C) {
     case 1: return f(k_sv_fused<1, 1024, PRE>);
     case 2: return f(k_sv_fused<2, 1024, PRE>);
+    case 3: return f(k_sv_fused<3, 1024, PRE>);
     case 4: return f(k_sv_fused<4, 1024, PRE>);
+    case 5: return f(k_sv_fused<5, 1024, PRE>);
+    case 6: return f(k_sv_fused<6, 1024, PRE>);
     case 8: return f(k_sv_fused<8, 768, PRE>);
     default: return f(k_sv_fused<16, 512, PRE>);
     }
@@ -221,8 +255,6 @@ template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
 template <class F> cudaError_t fused_dispatch(int C, F &&f, bool pre = false) {
     return pre ? fused_dispatch_p<true>(C, f) : fused_dispatch_p<false>(C, f);
 }
-
-constexpr int kFsMaxG = 16;
 
 }  // namespace
 
@@ -234,11 +266,12 @@ cudaError_t prepare_sv_fused(int P) {
     return e != cudaSuccess ? e : fused_dispatch(C, set, true);
 }
 
-// Rows per staged group G and the grid: the G that keeps the most threads
-// resident per SM (blocks per SM from the occupancy calculator, which counts
-// the two buffers of G rows), the largest such G (fewer barriers per row);
-// the grid fills every SM with that many blocks.
-bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out) {
+// Rows per group G, ring depth NB and the grid: over G in {1, 2, 4, 8, 16}
+// and NB in {2, 3, 4} whose shared memory fits, the most threads resident
+// per SM (blocks per SM from the occupancy calculator), then the most rows
+// staged per block (deeper pipeline), then the larger G (fewer barriers per
+// row); the grid fills every SM with that many blocks.
+bool sv_fused_plan(int Ns, int P, int *G_out, int *NB_out, int *ctas_out) {
     int C, T;
     if (P % 2 || Ns < 1 || !fused_shape(P, &C, &T)) return false;  // rows 16-byte aligned; columns in registers
     int dev = 0, sms = 152, optin = 0;
@@ -246,32 +279,36 @@ bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (prepare_sv_fused(P) != cudaSuccess) return false;
-    int best_G = 0, best_blocks = 0, best_threads = 0;
-    for (int G = 1; G <= kFsMaxG; G++) {
-        const size_t smem = fused_smem(P, G);
-        if (smem > size_t(optin) - 1024) break;
-        int blocks = 0;
-        const cudaError_t e = fused_dispatch(C, [&](auto fn) {
-            return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, T, smem);
-        });
-        if (e != cudaSuccess || blocks < 1) break;
-        const int threads = std::min(blocks * T, 2048);
-        if (threads >= best_threads) {
-            best_threads = threads;
-            best_G = G;
-            best_blocks = blocks;
+    int best_G = 0, best_NB = 0, best_blocks = 0, best_threads = 0, best_rows = 0;
+    for (int G = 1; G <= kFsMaxG; G *= 2)
+        for (int NB = 2; NB <= kFsMaxNB; NB++) {
+            const size_t smem = fused_smem(P, G, NB);
+            if (smem > size_t(optin) - 1024) continue;
+            int blocks = 0;
+            const cudaError_t e = fused_dispatch(C, [&](auto fn) {
+                return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, fn, T, smem);
+            });
+            if (e != cudaSuccess || blocks < 1) continue;
+            const int threads = std::min(blocks * T, 2048), rows = G * NB;
+            if (threads > best_threads || (threads == best_threads && (rows > best_rows || (rows == best_rows && G > best_G)))) {
+                best_threads = threads;
+                best_rows = rows;
+                best_G = G;
+                best_NB = NB;
+                best_blocks = blocks;
+            }
         }
-    }
     if (!best_G) return false;
     *G_out = best_G;
+    *NB_out = best_NB;
     *ctas_out = std::max(1, std::min(sms * best_blocks, (Ns + best_G - 1) / best_G));
     return true;
 }
 
-cudaError_t launch_sv_fused(int Ns, int P, int G, int ctas, const double *O, const double *v, double *ypart, int *err,
-                            const int *guard, cudaStream_t st, bool o_split) {
-    FusedSvArgs a{Ns, P, G, o_split ? 1 : 0, O, v, ypart, err, guard};
-    const size_t smem = fused_smem(P, G);
+cudaError_t launch_sv_fused(int Ns, int P, int G, int NB, int ctas, const double *O, const double *v, double *ypart,
+                            int *err, const int *guard, cudaStream_t st, bool o_split) {
+    FusedSvArgs a{Ns, P, G, NB, o_split ? 1 : 0, O, v, ypart, err, guard};
+    const size_t smem = fused_smem(P, G, NB);
     int C, T;
     if (!fused_shape(P, &C, &T)) return cudaErrorInvalidValue;
     return fused_dispatch(

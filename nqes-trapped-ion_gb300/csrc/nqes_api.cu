@@ -101,7 +101,7 @@ struct nqes_ctx {
     int rchunks = 1;
     // fused S·v over the dense FP64 O (real arithmetic): rows per staged
     // group, CTAs and their partials (fG = 0: the two-pass S·v)
-    int fG = 0, fctas = 0;
+    int fG = 0, fNB = 0, fctas = 0;
     double *ysv = nullptr;
     int fused_opt = -1, step_fused_opt = -1;  // NQES_OPT_FUSED_SV, and its value when the buffers were sized
 
@@ -169,7 +169,7 @@ void free_step_buffers(nqes_ctx *ctx) {
     dfree(ctx->ypart32);
     dfree(ctx->tcimg);
     dfree(ctx->ysv);
-    ctx->fG = ctx->fctas = 0;
+    ctx->fG = ctx->fNB = ctx->fctas = 0;
     if (ctx->exec) cudaGraphExecDestroy(ctx->exec);
     ctx->exec = nullptr;
     ctx->g_chains = -1;
@@ -224,7 +224,7 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
     // the fused S·v: by default in the certified form (FP64-grade results);
     // the FP64 form keeps IEEE FP64 arithmetic unless asked
     const bool fused = ctx->fused_opt < 0 ? ctx->precision == NQES_PRECISION_CERTIFIED : ctx->fused_opt == 1;
-    if (!mixed && arith == NQES_ARITH_REAL && fused && sv_fused_plan(int(Ns), sh.P, &ctx->fG, &ctx->fctas)) {
+    if (!mixed && arith == NQES_ARITH_REAL && fused && sv_fused_plan(int(Ns), sh.P, &ctx->fG, &ctx->fNB, &ctx->fctas)) {
         if ((rc = dalloc(ctx, &ctx->ysv, size_t(ctx->fctas) * P))) return rc;
         const cudaError_t e = prepare_sv_fused(sh.P);
         if (e != cudaSuccess) {
@@ -232,7 +232,7 @@ int ensure_step_buffers(nqes_ctx *ctx, int chains, int m, int arith) {
             return NQES_ERR_CUDA;
         }
     } else {
-        ctx->fG = ctx->fctas = 0;
+        ctx->fG = ctx->fNB = ctx->fctas = 0;
     }
     if ((rc = dalloc(ctx, &ctx->E, Ns * sh.K * sh.K))) return rc;
     if ((rc = dalloc(ctx, &ctx->spins, Ns * sh.K * sh.NW))) return rc;
@@ -316,6 +316,7 @@ template <class S> SolveBufs<S> solve_bufs(nqes_ctx *ctx) {
     B.ysv = B.ypart;
     if (std::is_same<S, double>::value && ctx->fG) {
         B.fG = ctx->fG;
+        B.fNB = ctx->fNB;
         B.svp = ctx->fctas;
         B.ysv = reinterpret_cast<S *>(ctx->ysv);
         B.o_split = o_split(ctx) ? 1 : 0;

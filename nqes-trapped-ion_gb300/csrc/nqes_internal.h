@@ -267,7 +267,7 @@ template <class S> struct SolveBufs {
     // fused S·v (fG > 0: real arithmetic, kernels_sv_fused.cu) one row per CTA.
     int svp;
     S *ysv;
-    int fG;
+    int fG, fNB;  // fused S·v: rows per staged group and groups in its ring
     // O stored as double-float (hi, lo) pairs in its FP64 slots (the certified
     // sampler writes it so when the fused S·v runs): the fused S·v and the
     // moments read the pairs directly
@@ -284,10 +284,10 @@ template <class S> struct SolveBufs {
 // Fused S·v over the dense FP64 O (kernels_sv_fused.cu): one read of O,
 // double-float arithmetic on the FP32 pipe. sv_fused_plan gives the rows per
 // staged group and the CTAs (false: the shape needs the two-pass S·v).
-bool sv_fused_plan(int Ns, int P, int *G_out, int *ctas_out);
+bool sv_fused_plan(int Ns, int P, int *G_out, int *NB_out, int *ctas_out);
 cudaError_t prepare_sv_fused(int P);
-cudaError_t launch_sv_fused(int Ns, int P, int G, int ctas, const double *O, const double *v, double *ypart, int *err,
-                            const int *guard, cudaStream_t st, bool o_split = false);
+cudaError_t launch_sv_fused(int Ns, int P, int G, int NB, int ctas, const double *O, const double *v, double *ypart,
+                            int *err, const int *guard, cudaStream_t st, bool o_split = false);
 
 // Sets the batched MINRES-QLP loop's condition: 1 while any member's flag
 // (its QlpState::running) is set.
