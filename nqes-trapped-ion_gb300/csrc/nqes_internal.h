@@ -281,6 +281,13 @@ template <class S> struct SolveBufs {
     float *v32, *u32, *ypart32;
 };
 
+// O stored split (the certified sampler with the fused S·v): each row's FP64
+// slots hold double-float pairs, per pair of columns (2q, 2q + 1) the 16
+// bytes (hi_2q, hi_2q+1, lo_2q, lo_2q+1), so that one 16-byte load gives
+// both columns' hi and lo parts as packed FP32 pairs. Float index of column
+// p's hi part within its row; its lo part is two floats further.
+__host__ __device__ inline size_t osplit_hi(size_t p) { return 4 * (p >> 1) + (p & 1); }
+
 // Fused S·v over the dense FP64 O (kernels_sv_fused.cu): one read of O,
 // double-float arithmetic on the FP32 pipe. sv_fused_plan gives the rows per
 // staged group and the CTAs (false: the shape needs the two-pass S·v).

@@ -328,4 +328,53 @@ __device__ __forceinline__ void df_acc(float &ah, float &al, float bh, float bl)
 }
 
 
+// Two double-float lanes at once with the packed FP32 instructions of sm_100
+// and later (add/sub/mul/fma .f32x2 on 64-bit register pairs): one
+// instruction does a lane's operation for both, with per-lane round to
+// nearest, so results equal two scalar evaluations bit for bit.
+__device__ __forceinline__ uint64_t f2_pack(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t r, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// df_fma on two lanes: (sh, sl) += (ah + al)(bh + bl), with bn = -bh given
+// (the products' negations are exact, so no negation instruction is needed):
+// -p = ah bn, the product's error fma(ah, bh, -p), the cross terms, TwoSum of
+// sh + p from the negated product.
+__device__ __forceinline__ void df_fma2(uint64_t &sh, uint64_t &sl, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
+                                        uint64_t bn) {
+    const uint64_t pn = f2_mul(ah, bn);
+    uint64_t e = f2_fma(ah, bh, pn);
+    e = f2_fma(ah, bl, e);
+    e = f2_fma(al, bh, e);
+    const uint64_t s = f2_sub(sh, pn);
+    const uint64_t bb = f2_sub(s, sh);
+    const uint64_t err = f2_sub(f2_sub(sh, f2_sub(s, bb)), f2_add(pn, bb));
+    sh = s;
+    sl = f2_add(sl, f2_add(err, e));
+}
+
 }  // namespace nqes

@@ -850,10 +850,12 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
 #pragma unroll
                     for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
                 }
-                if (A.o_split) {  // as hi + lo for the fused S·v (nqes_math.cuh: df_split)
+                if (A.o_split) {  // as hi + lo for the fused S·v (df_split; layout: osplit_hi)
                     float hi, lo;
                     split_ok &= df_split(v, hi, lo);
-                    reinterpret_cast<float2 *>(orow)[e] = make_float2(hi, lo);
+                    float *of = reinterpret_cast<float *>(orow);
+                    of[osplit_hi(e)] = hi;
+                    of[osplit_hi(e) + 2] = lo;
                 } else {
                     orow[e] = v;
                 }
