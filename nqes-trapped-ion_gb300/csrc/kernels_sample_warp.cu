@@ -70,12 +70,13 @@ cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st) {
 }
 
 cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
-                             float *wlp, float *bh, float *bl, float *bnd, cudaStream_t st) {
+                             float *wlp, float *bh, float *bl, float *bnd, float *cpl, float *spl, cudaStream_t st) {
     const size_t n = size_t(sh.K) * sh.N * MP;
     const int blocks = int(std::min<size_t>((n + 255) / 256, 4096));
     const cudaError_t e = cudaMemsetAsync(bnd + 4 * size_t(sh.K) * sh.N, 0, sizeof(float) * sh.K, st);
     if (e != cudaSuccess) return e;
-    k_tables_dw<<<blocks, 256, 0, st>>>(sh, MP, b, w, cp, spp, whp, wlp, bh, bl, reinterpret_cast<float4 *>(bnd));
+    k_tables_dw<<<blocks, 256, 0, st>>>(sh, MP, b, w, cp, spp, whp, wlp, bh, bl, reinterpret_cast<float4 *>(bnd), cpl,
+                                        spl);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,7 @@ struct nqes_ctx {
     // decision-warp form of the mixed sampler (dw_U = 0: block form)
     int dw_G = 0, dw_U = 0, dw_MP = 0;
     float *dcp = nullptr, *dsp = nullptr, *dwh = nullptr, *dwl = nullptr, *dbh = nullptr, *dbl = nullptr;
+    float *dcpl = nullptr, *dspl = nullptr;  // remainders of the FP32 cosh / sinh tables (double-float ratios)
     float *dbnd = nullptr;  // K·N float4 bound records, then K row-sum maxima
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
     uint16_t *tcimg = nullptr;  // BF16 split image of v for the tensor-core rows pass
@@ -360,6 +361,8 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.err = ctx->err_d;
     A.exact_all = ctx->mixed_exact_all ? 1 : 0;
     A.cp = ctx->dcp;
+    A.cpl = ctx->dcpl;
+    A.spl = ctx->dspl;
     A.spp = ctx->dsp;
     A.whp = ctx->dwh;
     A.wlp = ctx->dwl;
@@ -456,7 +459,7 @@ cudaError_t launch_mixed_tables(nqes_ctx *ctx) {
     cudaError_t e = launch_tables_mixed_ctx(ctx);
     if (e == cudaSuccess && ctx->dw_U)
         e = launch_tables_dw(ctx->sh, ctx->dw_MP, ctx->b, ctx->w, ctx->dcp, ctx->dsp, ctx->dwh, ctx->dwl, ctx->dbh,
-                             ctx->dbl, ctx->dbnd, ctx->st);
+                             ctx->dbl, ctx->dbnd, ctx->dcpl, ctx->dspl, ctx->st);
     return e;
 }
 size_t mixed_sampler_smem(nqes_ctx *ctx) {
@@ -1016,6 +1019,7 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
         ctx->dw_MP = ctx->dw_G * ctx->dw_U;
         const size_t np = size_t(K) * N * ctx->dw_MP, nb = size_t(K) * ctx->dw_MP;
         if ((rc = dalloc(ctx, &ctx->dcp, np)) || (rc = dalloc(ctx, &ctx->dsp, np)) || (rc = dalloc(ctx, &ctx->dwh, np)) ||
+            (rc = dalloc(ctx, &ctx->dcpl, np)) || (rc = dalloc(ctx, &ctx->dspl, np)) ||
             (rc = dalloc(ctx, &ctx->dwl, np)) || (rc = dalloc(ctx, &ctx->dbh, nb)) || (rc = dalloc(ctx, &ctx->dbl, nb)) ||
             (rc = dalloc(ctx, &ctx->dbnd, 4 * size_t(K) * N + 4 * size_t(K))))
             return fail(rc);
@@ -1056,6 +1060,8 @@ int nqes_destroy(nqes_ctx *ctx) {
     dfree(ctx->ma);
     dfree(ctx->mb);
     dfree(ctx->dcp);
+    dfree(ctx->dcpl);
+    dfree(ctx->dspl);
     dfree(ctx->dsp);
     dfree(ctx->dwh);
     dfree(ctx->dwl);
@@ -1698,7 +1704,7 @@ extern "C" int nqes_footprint_bytes(int n_spins, int n_hidden, int n_states, int
     if (mixed) b += P * 4 + Ns * 4 + 3 * 256 * P * 4;
     b += (3 * nw + 2 * na + K * M) * 16 + N * N * 8;  // weights, FP64 tables (complex-sized), J
     b += nw * 4 * 2 + na * 4 * 2 + (nw + na + K * M) * 8;  // FP32 tables and FP64 copies of the real weights
-    b += 4 * K * N * 512 * 4 + 6 * K * 512 * 4 + (4 * K * N + 4 * K) * 4;  // decision-warp tables (upper bound)
+    b += 6 * K * N * 512 * 4 + 6 * K * 512 * 4 + (4 * K * N + 4 * K) * 4;  // decision-warp tables (upper bound)
     *bytes = b + (uint64_t(4) << 20);                        // small buffers and allocation rounding
     return NQES_OK;
 }

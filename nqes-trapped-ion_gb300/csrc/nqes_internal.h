@@ -91,6 +91,7 @@ struct MixedArgs {
     // lane, tables padded to MP = G*U units per (kk, i) row: FP32 cosh(2w),
     // sinh(2w) and w as hi + lo [kk][i][MP]; b as hi + lo [kk][MP].
     const float *cp, *spp, *whp, *wlp, *bh, *bl;
+    const float *cpl, *spl;              // the roundings' remainders: cosh(2w) - cp, sinh(2w) - spp [kk][i][MP]
     const float *bnd;                    // per (kk, i): float4 bound record, then per kk 2 max_j sum_i |w_ij|
     int G, U, MP;
     int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
@@ -102,7 +103,8 @@ struct MixedArgs {
     int o_split;  // out64: each entry of O64 stored as its double-float split (hi, lo) for the fused S·v
     const double *c64, *s64, *eup64, *edn64;  // FP64 tables [kk][i][j], [kk][i]
     // FP64 local energies with the FP32 factor outputs (MIXED, NQES_OPT_MIXED_ENERGY64):
-    // E from tanh of the exact theta and the FP64 tables as with out64, O as factors
+    // E from tanh of the exact theta (FP64) and the flip ratios as double-float
+    // products over (cp + cpl, spp + spl) on the FP32 pipe, O as factors
     int e64;
 };
 size_t mixed_smem_bytes(const Shape &sh);
@@ -112,7 +114,7 @@ cudaError_t prepare_sample_dw(const Shape &sh, int MP);
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st);
 cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm);
 cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
-                             float *wlp, float *bh, float *bl, float *bnd, cudaStream_t st);
+                             float *wlp, float *bh, float *bl, float *bnd, float *cpl, float *spl, cudaStream_t st);
 cudaError_t prepare_sample_mixed(const Shape &sh);
 cudaError_t launch_sample_mixed(const MixedArgs &a, cudaStream_t st);
 cudaError_t launch_tables_mixed(const Shape &sh, const cplx *a, const cplx *b, const cplx *w, float *ch, float *sh32,

@@ -731,7 +731,62 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
                 if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
             }
         }
-        if (e64) {
+        if (e64 && !A.out64) {
+            // MIXED: tanh of the exact theta in FP64, kept as double-float in the
+            // t64 space (layout osplit_hi per row of MP units); each flip ratio
+            // prod_j (c_j + sigma t_j s_j) as a double-float product on the FP32
+            // pipe, two units per packed instruction (padded units are exactly
+            // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor
+            for (int e = tid; e < KK * MP; e += T) {
+                const int q = e / MP, j = e - q * MP;
+                const double tv = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
+                float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + osplit_hi(j);
+                const float th = float(tv);
+                tf[0] = th;
+                tf[2] = float(tv - double(th));
+            }
+            __syncthreads();
+            double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
+            constexpr uint64_t kSign2 = 0x8000000080000000ULL;
+            for (int it = tid; it < KK * N; it += T) {
+                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+                const bool down = down_bit(sm.spin + k * NW, i);
+                const uint64_t sg = down ? 0ULL : kSign2;  // sigma t = t (spin down) or -t
+                const size_t o = (size_t(kk) * N + i) * MP;
+                const float *crow = sm.tc + o, *srow = sm.ts + o, *clrow = A.cpl + o, *slrow = A.spl + o;
+                const float *trow = reinterpret_cast<const float *>(sm.t64) + size_t(q) * 2 * MP;
+                uint64_t Ph = f2_pack(1.f, 1.f), Pl = 0;
+                for (int j = 0; j < MP; j += 2) {
+                    const uint64_t ch = *reinterpret_cast<const uint64_t *>(crow + j);
+                    const uint64_t sh = *reinterpret_cast<const uint64_t *>(srow + j);
+                    const uint64_t cl = __ldg(reinterpret_cast<const unsigned long long *>(clrow + j));
+                    const uint64_t sl = __ldg(reinterpret_cast<const unsigned long long *>(slrow + j));
+                    const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(trow + 2 * j);
+                    const uint64_t a = tt.x ^ sg, al = tt.y ^ sg;
+                    // f = c + a s (double-float, not renormalised)
+                    const uint64_t p = f2_mul(a, sh);
+                    uint64_t e = f2_fma(a, sh, p ^ kSign2);
+                    e = f2_fma(a, sl, e);
+                    e = f2_fma(al, sh, e);
+                    const uint64_t fs = f2_add(ch, p);
+                    const uint64_t bb = f2_sub(fs, ch);
+                    const uint64_t err = f2_add(f2_sub(ch, f2_sub(fs, bb)), f2_sub(p, bb));
+                    const uint64_t fl = f2_add(cl, f2_add(err, e));
+                    // P *= f, renormalised
+                    const uint64_t ph = f2_mul(Ph, fs);
+                    uint64_t pe = f2_fma(Ph, fs, ph ^ kSign2);
+                    pe = f2_fma(Ph, fl, pe);
+                    pe = f2_fma(Pl, fs, pe);
+                    Ph = f2_add(ph, pe);
+                    Pl = f2_sub(pe, f2_sub(Ph, ph));
+                }
+                float h0, h1, l0, l1;
+                f2_unpack(Ph, h0, h1);
+                f2_unpack(Pl, l0, l1);
+                rat64[it] = ((double(h0) + double(l0)) * (double(h1) + double(l1))) *
+                            (down ? A.edn64 : A.eup64)[kk * N + i];
+            }
+        } else if (e64) {
             for (int e = tid; e < KK * MP; e += T) {
                 const int j = e % MP;
                 sm.t64[e] = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
@@ -886,7 +941,7 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
 // rounded up; after the K*N records, per RBM 2 max_j sum_i |w_ij| (float bits,
 // rounded up, maximised with atomicMax over a zeroed slot).
 __global__ void k_tables_dw(Shape sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
-                            float *wlp, float *bh, float *bl, float4 *bnd) {
+                            float *wlp, float *bh, float *bl, float4 *bnd, float *cpl, float *spl) {
     const size_t nr = size_t(sh.K) * sh.N;
     for (size_t r = blockIdx.x * size_t(blockDim.x) + threadIdx.x; r < nr; r += size_t(gridDim.x) * blockDim.x) {
         double sc = 0.0, s1 = 0.0, f2 = 0.0, qm = 0.0;
@@ -914,16 +969,21 @@ __global__ void k_tables_dw(Shape sh, int MP, const cplx *b, const cplx *w, floa
     for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
         const int j = int(t % MP);
         const size_t ki = t / MP;  // kk*N + i
-        float c = 1.f, s = 0.f, h = 0.f, l = 0.f;
+        float c = 1.f, s = 0.f, h = 0.f, l = 0.f, cl = 0.f, sl = 0.f;
         if (j < sh.M) {
             const double wv = w[ki * sh.M + j].re;
-            c = float(cosh(2.0 * wv));
-            s = float(sinh(2.0 * wv));
+            const double cd = cosh(2.0 * wv), sd = sinh(2.0 * wv);
+            c = float(cd);
+            s = float(sd);
+            cl = float(cd - double(c));
+            sl = float(sd - double(s));
             h = float(wv);
             l = float(wv - double(h));
         }
         cp[t] = c;
         spp[t] = s;
+        cpl[t] = cl;
+        spl[t] = sl;
         whp[t] = h;
         wlp[t] = l;
         if (t < size_t(sh.K) * MP) {
