@@ -133,12 +133,12 @@ __global__ void __launch_bounds__(kVecThreads) k_moment_part(int Ns, int P, int 
     pf[size_t(r) * P + p] = f;
 }
 
-// The same partial column sums over O stored as double-float pairs in its
-// FP64 slots (real arithmetic, layout osplit_hi): o, |O|^2 and E_loc O accumulated in
+// The same partial column sums over O stored as double-float pairs (hi, lo)
+// in its FP64 slots (real arithmetic): o, |O|^2 and E_loc O accumulated in
 // double-float on the FP32 pipe (products with their FMA error terms, sums
 // TwoSum-compensated: a few 2^-48 of the sums of |terms|), converted to FP64
 // once per partial.
-__global__ void __launch_bounds__(kVecThreads) k_moment_part_split(int Ns, int P, int K, int rchunks, const float *O,
+__global__ void __launch_bounds__(kVecThreads) k_moment_part_split(int Ns, int P, int K, int rchunks, const float2 *O,
                                                                    const cplx *E, double *po, double *ps2, double *pf) {
     __shared__ float2 els[kVecThreads];
     const int p = blockIdx.x * kVecThreads + threadIdx.x;
@@ -158,9 +158,9 @@ __global__ void __launch_bounds__(kVecThreads) k_moment_part_split(int Ns, int P
         }
         __syncthreads();
         if (p < P) {
-            const float *col = O + size_t(t0) * 2 * P + osplit_hi(p);
+            const float2 *col = O + size_t(t0) * P + p;
             for (int q = 0; q < nt; q++) {
-                const float2 v = make_float2(col[size_t(q) * 2 * P], col[size_t(q) * 2 * P + 2]);
+                const float2 v = col[size_t(q) * P];
                 const float2 e = els[q];
                 df_acc(oh, ol, v.x, v.y);
                 df_fma(qh, ql, v.x, v.y, v.x, v.y);
@@ -820,7 +820,7 @@ template <class S> cudaError_t launch_moments(const SolveBufs<S> &B, cudaStream_
         }
         if (B.o_split) {
             k_moment_part_split<<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks,
-                                                           reinterpret_cast<const float *>(B.O), B.E, po, ps2, pf);
+                                                           reinterpret_cast<const float2 *>(B.O), B.E, po, ps2, pf);
             k_moment_final<S><<<nb, kVecThreads, 0, st>>>(B.Ns, P, B.rchunks, B.sp, po, ps2, pf, B.eloc, B.o, B.skk,
                                                            B.f, B.err);
             return cudaGetLastError();
@@ -912,7 +912,7 @@ template <class S> cudaError_t launch_moment_part_only(const SolveBufs<S> &B, cu
     if constexpr (std::is_same<S, double>::value) {
         if (B.o_split) {
             k_moment_part_split<<<g, kVecThreads, 0, st>>>(B.Ns, P, B.sh.K, B.rchunks,
-                                                           reinterpret_cast<const float *>(B.O), B.E, po, ps2, pf);
+                                                           reinterpret_cast<const float2 *>(B.O), B.E, po, ps2, pf);
             return cudaGetLastError();
         }
     }

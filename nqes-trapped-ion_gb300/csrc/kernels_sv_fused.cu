@@ -84,21 +84,17 @@ __device__ __forceinline__ void warp_sum_pair(float &h, float &l, float h0, floa
         df_acc(h, l, __shfl_xor_sync(0xffffffffu, h, off), __shfl_xor_sync(0xffffffffu, l, off));
 }
 
-// Block: T = blockDim.x threads (a multiple of 32, T CP >= P / 2); thread t
-// owns the column pairs q = t + c T (c < CP), i.e. columns 2q and 2q + 1,
-// holding v's split and its partial of O^T u for them as packed FP32 pairs
-// (one .f32x2 instruction per double-float operation of both columns). A
-// staged row is in the split layout (osplit_hi), so one 16-byte load gives a
-// pair's hi parts and lo parts as packed operands; O written in FP64 is split
-// into that layout in place on its first read.
-template <int CP, int MaxT, bool PRE>
+// Block: T = blockDim.x threads (a multiple of 32, T C >= P); thread t owns
+// columns p = t + c T (c < C), holding v's split and its partial of O^T u for
+// them in registers.
+template <int C, int MaxT, bool PRE>
 __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     extern __shared__ __align__(16) unsigned char fs_smem[];
     if (loop_guard_off(a.guard)) return;
-    const int P = a.P, P2 = P >> 1, G = a.G, NB = a.NB, T = blockDim.x, tid = threadIdx.x, lane = tid & 31,
-              warp = tid >> 5, nw = T >> 5;
-    if (!dyn_smem_covers(fused_smem(P, G, NB)) || nw > kFsMaxWarps || T * CP < P2 || (P & 1) || G > kFsMaxG ||
-        NB < 2 || NB > kFsMaxNB) {
+    const int P = a.P, G = a.G, NB = a.NB, T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5,
+              nw = T >> 5;
+    if (!dyn_smem_covers(fused_smem(P, G, NB)) || nw > kFsMaxWarps || T * C < P || G > kFsMaxG || NB < 2 ||
+        NB > kFsMaxNB) {
         if (tid == 0) atomicOr(a.err, kErrLaunch);
         return;
     }
@@ -108,21 +104,13 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     const int r0 = int(int64_t(a.Ns) * blockIdx.x / gridDim.x), r1 = int(int64_t(a.Ns) * (blockIdx.x + 1) / gridDim.x);
     const int ngroups = (r1 - r0 + G - 1) / G;
 
-    // v as packed hi, lo and -hi per column pair; the partials of O^T u
-    uint64_t vhh[CP], vll[CP], vhn[CP], yhh[CP], yll[CP];
+    float vh[C], vl[C], yh[C], yl[C];
     bool range_ok = true;  // of the O entries (v is not checked: a solve that never starts has v = 0/0)
 #pragma unroll
-    for (int c = 0; c < CP; c++) {
-        const int q = tid + c * T;
-        float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
-        if (q < P2) {
-            df_split(a.v[2 * q], h0, l0);
-            df_split(a.v[2 * q + 1], h1, l1);
-        }
-        vhh[c] = f2_pack(h0, h1);
-        vll[c] = f2_pack(l0, l1);
-        vhn[c] = f2_pack(-h0, -h1);
-        yhh[c] = yll[c] = 0;
+    for (int c = 0; c < C; c++) {
+        const int p = tid + c * T;
+        vh[c] = vl[c] = yh[c] = yl[c] = 0.f;
+        if (p < P) df_split(a.v[p], vh[c], vl[c]);
     }
     auto issue = [&](int g) {  // thread 0: group g into ring slot g % NB
         const int rs = r0 + g * G, nr = min(G, r1 - rs);
@@ -137,51 +125,32 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     if (tid == 0)
         for (int g = 0; g < min(NB, ngroups); g++) issue(g);
 
-    // column pair q of a staged row as packed (hi, hi) and (lo, lo); an FP64
-    // row is split here and written back in the split layout (each thread its
-    // own pairs, read back only by itself in pass 2)
-    auto load_pair = [&](double *row, int q, uint64_t &ohh, uint64_t &oll) {
-        ulonglong2 *slot = reinterpret_cast<ulonglong2 *>(row + 2 * q);
-        if (PRE) {
-            const ulonglong2 w = *slot;
-            ohh = w.x;
-            oll = w.y;
-        } else {
-            const double2 d = *reinterpret_cast<const double2 *>(slot);
-            float h0, l0, h1, l1;
-            range_ok &= df_split(d.x, h0, l0);
-            range_ok &= df_split(d.y, h1, l1);
-            ohh = f2_pack(h0, h1);
-            oll = f2_pack(l0, l1);
-            *slot = make_ulonglong2(ohh, oll);
-        }
-    };
-    // the thread's partial dot of a row with v (two packed chains), as one
-    // double-float (h, l)
+    // thread's partial dot of row `row` with v (two chains over its columns);
+    // FP64 entries are split in place (each thread its own columns, read back
+    // only by itself in pass 2)
     auto row_dot = [&](double *row, float &h, float &l) {
-        uint64_t sh = 0, sl = 0, sh2 = 0, sl2 = 0;
+        float h2 = 0.f, l2 = 0.f;
+        h = l = 0.f;
 #pragma unroll
-        for (int c = 0; c < CP; c++) {
-            const int q = tid + c * T;
-            if (q < P2) {
-                uint64_t ohh, oll;
-                load_pair(row, q, ohh, oll);
+        for (int c = 0; c < C; c++) {
+            const int p = tid + c * T;
+            if (p < P) {
+                float oh, ol;
+                if (PRE) {  // split when it was written
+                    const float2 o = *reinterpret_cast<const float2 *>(row + p);
+                    oh = o.x;
+                    ol = o.y;
+                } else {
+                    range_ok &= df_split(row[p], oh, ol);
+                    *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
+                }
                 if (c & 1)
-                    df_fma2(sh2, sl2, ohh, oll, vhh[c], vll[c], vhn[c]);
+                    df_fma(h2, l2, oh, ol, vh[c], vl[c]);
                 else
-                    df_fma2(sh, sl, ohh, oll, vhh[c], vll[c], vhn[c]);
+                    df_fma(h, l, oh, ol, vh[c], vl[c]);
             }
         }
-        float a0, a1, b0, b1, c0, c1, d0, d1;
-        f2_unpack(sh, a0, a1);
-        f2_unpack(sl, b0, b1);
-        f2_unpack(sh2, c0, c1);
-        f2_unpack(sl2, d0, d1);
-        df_acc(a0, b0, a1, b1);
-        df_acc(c0, d0, c1, d1);
-        df_acc(a0, b0, c0, d0);
-        h = a0;
-        l = b0;
+        df_acc(h, l, h2, l2);
     };
 
     bool timed_out = false;
@@ -218,18 +187,16 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
             warp_sum_pair(h, l, p0.x, p0.y, p1.x, p1.y);
             const float u0h = __shfl_sync(0xffffffffu, h, 0), u0l = __shfl_sync(0xffffffffu, l, 0);
             const float u1h = __shfl_sync(0xffffffffu, h, 16), u1l = __shfl_sync(0xffffffffu, l, 16);
-            const uint64_t U0h = f2_pack(u0h, u0h), U0l = f2_pack(u0l, u0l), U0n = f2_pack(-u0h, -u0h);
-            const uint64_t U1h = f2_pack(u1h, u1h), U1l = f2_pack(u1l, u1l), U1n = f2_pack(-u1h, -u1h);
-            double *row0 = buf + size_t(r) * P, *row1 = row0 + P;
+            const double *row0 = buf + size_t(r) * P, *row1 = row0 + P;
 #pragma unroll
-            for (int c = 0; c < CP; c++) {
-                const int q = tid + c * T;
-                if (q < P2) {
-                    const ulonglong2 o0 = *reinterpret_cast<const ulonglong2 *>(row0 + 2 * q);
-                    df_fma2(yhh[c], yll[c], o0.x, o0.y, U0h, U0l, U0n);
+            for (int c = 0; c < C; c++) {
+                const int p = tid + c * T;
+                if (p < P) {
+                    const float2 o = *reinterpret_cast<const float2 *>(row0 + p);
+                    df_fma(yh[c], yl[c], o.x, o.y, u0h, u0l);
                     if (two) {
-                        const ulonglong2 o1 = *reinterpret_cast<const ulonglong2 *>(row1 + 2 * q);
-                        df_fma2(yhh[c], yll[c], o1.x, o1.y, U1h, U1l, U1n);
+                        const float2 o1 = *reinterpret_cast<const float2 *>(row1 + p);
+                        df_fma(yh[c], yl[c], o1.x, o1.y, u1h, u1l);
                     }
                 }
             }
@@ -250,27 +217,20 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     }
     if (!range_ok) atomicOr(a.err, kErrNonFinite);
 #pragma unroll
-    for (int c = 0; c < CP; c++) {
-        const int q = tid + c * T;
-        if (q < P2) {
-            float h0, h1, l0, l1;
-            f2_unpack(yhh[c], h0, h1);
-            f2_unpack(yll[c], l0, l1);
-            *reinterpret_cast<double2 *>(a.ypart + size_t(blockIdx.x) * P + 2 * q) =
-                make_double2(double(h0) + double(l0), double(h1) + double(l1));
-        }
+    for (int c = 0; c < C; c++) {
+        const int p = tid + c * T;
+        if (p < P) a.ypart[size_t(blockIdx.x) * P + p] = double(yh[c]) + double(yl[c]);
     }
 }
 
-// Column pairs per thread CP and threads per block T (whole warps,
-// T CP >= P / 2): the fewest pairs whose block fits its register budget:
-// CP <= 3 with up to 1024 threads (64 registers), 4 with up to 768, 8 with
-// up to 512.
-constexpr int kFsShapes[5][2] = {{1, 1024}, {2, 1024}, {3, 1024}, {4, 768}, {8, 512}};
+// Columns per thread C and threads per block T (whole warps, T C >= P): the
+// fewest columns whose block fits its register budget: C <= 6 with up to
+// 1024 threads (64 registers), 8 with up to 768, 16 with up to 512.
+constexpr int kFsShapes[8][2] = {{1, 1024}, {2, 1024}, {3, 1024}, {4, 1024},
+                                 {5, 1024}, {6, 1024}, {8, 768},  {16, 512}};
 bool fused_shape(int P, int *C, int *T) {
-    const int pairs = P / 2;
     for (const auto &sh : kFsShapes) {
-        const int t = 32 * ((pairs + 32 * sh[0] - 1) / (32 * sh[0]));
+        const int t = 32 * ((P + 32 * sh[0] - 1) / (32 * sh[0]));
         if (t <= sh[1]) {
             *C = sh[0];
             *T = t;
@@ -280,13 +240,16 @@ bool fused_shape(int P, int *C, int *T) {
     return false;
 }
 
-template <bool PRE, class F> cudaError_t fused_dispatch_p(int CP, F &&f) {
-    switch (CP) {
+template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
+    switch (C) {
     case 1: return f(k_sv_fused<1, 1024, PRE>);
     case 2: return f(k_sv_fused<2, 1024, PRE>);
     case 3: return f(k_sv_fused<3, 1024, PRE>);
-    case 4: return f(k_sv_fused<4, 768, PRE>);
-    default: return f(k_sv_fused<8, 512, PRE>);
+    case 4: return f(k_sv_fused<4, 1024, PRE>);
+    case 5: return f(k_sv_fused<5, 1024, PRE>);
+    case 6: return f(k_sv_fused<6, 1024, PRE>);
+    case 8: return f(k_sv_fused<8, 768, PRE>);
+    default: return f(k_sv_fused<16, 512, PRE>);
     }
 }
 template <class F> cudaError_t fused_dispatch(int C, F &&f, bool pre = false) {

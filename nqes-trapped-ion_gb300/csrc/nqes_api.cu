@@ -1434,16 +1434,14 @@ int nqes_get_O(nqes_ctx *ctx, int first, int count, double *O) {
         return NQES_OK;
     }
     const unsigned char *src = static_cast<const unsigned char *>(ctx->O) + size_t(first) * P * ssize(ctx->arith);
-    if (o_split(ctx)) {  // stored as double-float pairs (layout osplit_hi): hi + lo
+    if (o_split(ctx)) {  // stored as double-float pairs: hi + lo
         std::vector<float> tmp(2 * size_t(count) * P);
         NQES_CUDA(cudaMemcpyAsync(tmp.data(), src, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->st));
         NQES_CUDA(cudaStreamSynchronize(ctx->st));
-        for (size_t r = 0; r < size_t(count); r++)
-            for (size_t p = 0; p < P; p++) {
-                const float *row = tmp.data() + r * 2 * P;
-                O[2 * (r * P + p)] = double(row[osplit_hi(p)]) + double(row[osplit_hi(p) + 2]);
-                O[2 * (r * P + p) + 1] = 0.0;
-            }
+        for (size_t t = 0; t < size_t(count) * P; t++) {
+            O[2 * t] = double(tmp[2 * t]) + double(tmp[2 * t + 1]);
+            O[2 * t + 1] = 0.0;
+        }
         return NQES_OK;
     }
     return copy_out_c(ctx, src, size_t(count) * P, O);

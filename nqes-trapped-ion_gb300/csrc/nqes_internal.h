@@ -283,12 +283,11 @@ template <class S> struct SolveBufs {
     float *v32, *u32, *ypart32;
 };
 
-// O stored split (the certified sampler with the fused S·v): each row's FP64
-// slots hold double-float pairs, per pair of columns (2q, 2q + 1) the 16
-// bytes (hi_2q, hi_2q+1, lo_2q, lo_2q+1), so that one 16-byte load gives
-// both columns' hi and lo parts as packed FP32 pairs. Float index of column
-// p's hi part within its row; its lo part is two floats further.
-__host__ __device__ inline size_t osplit_hi(size_t p) { return 4 * (p >> 1) + (p & 1); }
+// Pair-interleaved double-float rows: per pair of entries (2q, 2q + 1) the 16
+// bytes (hi_2q, hi_2q+1, lo_2q, lo_2q+1), so that one 16-byte load gives both
+// entries' hi and lo parts as packed FP32 pairs (nqes_math.cuh f2_*). Float
+// index of entry p's hi part within its row; its lo part is two floats further.
+__host__ __device__ inline size_t dfpair_hi(size_t p) { return 4 * (p >> 1) + (p & 1); }
 
 // Fused S·v over the dense FP64 O (kernels_sv_fused.cu): one read of O,
 // double-float arithmetic on the FP32 pipe. sv_fused_plan gives the rows per

@@ -733,14 +733,14 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
         }
         if (e64 && !A.out64) {
             // MIXED: tanh of the exact theta in FP64, kept as double-float in the
-            // t64 space (layout osplit_hi per row of MP units); each flip ratio
+            // t64 space (layout dfpair_hi per row of MP units); each flip ratio
             // prod_j (c_j + sigma t_j s_j) as a double-float product on the FP32
             // pipe, two units per packed instruction (padded units are exactly
             // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor
             for (int e = tid; e < KK * MP; e += T) {
                 const int q = e / MP, j = e - q * MP;
                 const double tv = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
-                float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + osplit_hi(j);
+                float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + dfpair_hi(j);
                 const float th = float(tv);
                 tf[0] = th;
                 tf[2] = float(tv - double(th));
@@ -905,12 +905,10 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
 #pragma unroll
                     for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
                 }
-                if (A.o_split) {  // as hi + lo for the fused S·v (df_split; layout: osplit_hi)
+                if (A.o_split) {  // as hi + lo for the fused S·v (nqes_math.cuh: df_split)
                     float hi, lo;
                     split_ok &= df_split(v, hi, lo);
-                    float *of = reinterpret_cast<float *>(orow);
-                    of[osplit_hi(e)] = hi;
-                    of[osplit_hi(e) + 2] = lo;
+                    reinterpret_cast<float2 *>(orow)[e] = make_float2(hi, lo);
                 } else {
                     orow[e] = v;
                 }
