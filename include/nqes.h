@@ -69,10 +69,11 @@ extern "C" {
                                       * O^T u per staged group of rows, double-float arithmetic on the FP32
                                       * pipe, within 1e-13 of FP64 sums) where P is even and at most 8192;
                                       * 0: two FP64 passes; -1 (default): on in CERTIFIED, off in FP64. */
-#define NQES_OPT_MIXED_ENERGY64 11   /* 1 (default): in the MIXED form the decision-warp sampler forms the
-                                      * local energies in FP64 (the N single-flip ratios from tanh of the
-                                      * exact theta and the FP64 tables, as the CERTIFIED form does) and
-                                      * keeps O as its FP32 factors; 0: FP32 ratio products. */
+#define NQES_OPT_MIXED_ENERGY64 11   /* local energies of the MIXED form's decision-warp sampler (O stays
+                                      * as its FP32 factors): the N single-flip ratios as double-float
+                                      * products of the tables on the FP32 pipe, with tanh of the exact
+                                      * theta from its FP32 value plus the first-order term of theta's
+                                      * low part (2, default) or in FP64 (1); 0: FP32 ratio products. */
 #define NQES_OPT_TEST_STAGE_WAIT 10  /* test hook for the bounded device-side waits: 1 = the decision-warp
                                       * sampler stages its tables and its wait is for bytes that no copy
                                       * delivers, with a short poll limit, so the step returns

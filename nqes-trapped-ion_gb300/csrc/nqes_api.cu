@@ -76,7 +76,7 @@ struct nqes_ctx {
     // graph: the members' samplers then share the GPU.
     int plan_chains = 0;
     int stage_fault = 0;  // NQES_OPT_TEST_STAGE_WAIT
-    bool mixed_e64 = true;  // NQES_OPT_MIXED_ENERGY64
+    int mixed_e64 = 2;  // NQES_OPT_MIXED_ENERGY64: 0, 1 or 2
     bool mixed_exact_all = false;  // MIXED: every decision through the exact FP64 path
     bool weights_real = true;
     std::string err;
@@ -375,7 +375,7 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.stage_fault = ctx->stage_fault;
     A.o_split = o_split(ctx) ? 1 : 0;
     A.out64 = ctx->step_precision == NQES_PRECISION_CERTIFIED ? 1 : 0;
-    A.e64 = !A.out64 && dw_energy64(ctx) ? 1 : 0;
+    A.e64 = !A.out64 && dw_energy64(ctx) ? ctx->mixed_e64 : 0;
     if (A.e64) {  // the FP64 tables for the local energies; O stays as FP32 factors
         const size_t nw = size_t(ctx->sh.K) * ctx->sh.N * ctx->sh.M, na = size_t(ctx->sh.K) * ctx->sh.N;
         const double *t = static_cast<const double *>(ctx->tab);
@@ -411,7 +411,7 @@ bool uses_mixed_sampler(const nqes_ctx *ctx) {
 // form; the mixed form unless NQES_OPT_MIXED_ENERGY64 is 0): it then needs the
 // FP64 tables and room for FP64 tanh rows.
 bool dw_energy64(const nqes_ctx *ctx) {
-    return certified_dw(ctx) || (ctx->step_precision == NQES_PRECISION_MIXED && ctx->dw_U && ctx->mixed_e64);
+    return certified_dw(ctx) || (ctx->step_precision == NQES_PRECISION_MIXED && ctx->dw_U && ctx->mixed_e64 != 0);
 }
 
 cudaError_t launch_tables_mixed_ctx(nqes_ctx *ctx) {
@@ -1163,11 +1163,11 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         }
         return NQES_OK;
     case NQES_OPT_MIXED_ENERGY64:
-        if (value != 0 && value != 1) {
-            ctx->err = "option value must be 0 or 1";
+        if (value < 0 || value > 2) {
+            ctx->err = "option value must be 0, 1 or 2";
             return NQES_ERR_INVALID;
         }
-        ctx->mixed_e64 = value == 1;
+        ctx->mixed_e64 = int(value);
         if (ctx->exec) {  // the captured step bakes the sampler's arguments in
             cudaGraphExecDestroy(ctx->exec);
             ctx->exec = nullptr;
@@ -1828,7 +1828,7 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
         std::memcpy(&delta_bits, &c->ham_delta, sizeof(delta_bits));
         keys[i] = {chains[i], samples[i], burn[i], arith[i], tks[i], c->step_precision, c->ham, delta_bits,
                    c->tensor_cores, c->reject_filter ? 1 : 0, c->mixed_exact_all ? 1 : 0, c->dw_force_warps,
-                   c->dw_force_stage, (long long)c->buf_gen, total, c->stage_fault, c->mixed_e64 ? 1 : 0};
+                   c->dw_force_stage, (long long)c->buf_gen, total, c->stage_fault, c->mixed_e64};
     }
     // Capture (when the members changed), launch and wait. A failure here
     // means no member's step ran: each member's status becomes the error.

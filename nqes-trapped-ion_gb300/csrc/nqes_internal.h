@@ -103,8 +103,9 @@ struct MixedArgs {
     int o_split;  // out64: each entry of O64 stored as its double-float split (hi, lo) for the fused S·v
     const double *c64, *s64, *eup64, *edn64;  // FP64 tables [kk][i][j], [kk][i]
     // FP64 local energies with the FP32 factor outputs (MIXED, NQES_OPT_MIXED_ENERGY64):
-    // E from tanh of the exact theta (FP64) and the flip ratios as double-float
-    // products over (cp + cpl, spp + spl) on the FP32 pipe, O as factors
+    // the flip ratios as double-float products over (cp + cpl, spp + spl) on
+    // the FP32 pipe with tanh of the exact theta in FP64 (1) or from its FP32
+    // value and the low part of theta (2); O as factors; 0: FP32 ratios
     int e64;
 };
 size_t mixed_smem_bytes(const Shape &sh);

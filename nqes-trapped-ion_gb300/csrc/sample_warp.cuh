@@ -732,18 +732,27 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
             }
         }
         if (e64 && !A.out64) {
-            // MIXED: tanh of the exact theta in FP64, kept as double-float in the
-            // t64 space (layout dfpair_hi per row of MP units); each flip ratio
-            // prod_j (c_j + sigma t_j s_j) as a double-float product on the FP32
+            // MIXED: tanh of the exact theta as double-float in the t64 space
+            // (layout dfpair_hi per row of MP units): in FP64 (e64 = 1), or
+            // (e64 = 2) the row's tanhf(theta_hi) (rebuild_row) plus the
+            // first-order term of theta's low part, (1 - t^2) theta_lo, which
+            // leaves tanhf's own error (a few 2^-24). Each flip ratio
+            // prod_j (c_j + sigma t_j s_j) is a double-float product on the FP32
             // pipe, two units per packed instruction (padded units are exactly
-            // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor
+            // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor.
             for (int e = tid; e < KK * MP; e += T) {
                 const int q = e / MP, j = e - q * MP;
-                const double tv = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
                 float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + dfpair_hi(j);
-                const float th = float(tv);
-                tf[0] = th;
-                tf[2] = float(tv - double(th));
+                if (A.e64 == 2) {
+                    const float t = sm.t[e];  // 0 in the padding
+                    tf[0] = t;
+                    tf[2] = j < M ? fmaf(-t, t, 1.f) * sm.th_lo[e] : 0.f;
+                } else {
+                    const double tv = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
+                    const float th = float(tv);
+                    tf[0] = th;
+                    tf[2] = float(tv - double(th));
+                }
             }
             __syncthreads();
             double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles

@@ -376,21 +376,23 @@ def test_fused_sv_matches_two_pass(pkg, N, M, K, prec):
     assert rel_err(wb, wa) < 1e-6  # the solves agree to the rtol scale
 
 
-def test_mixed_energies_along_the_fp64_trajectory(pkg):
+@pytest.mark.parametrize("mode", [2, 1])
+def test_mixed_energies_along_the_fp64_trajectory(pkg, mode):
     """The mixed form's energy error beyond the first step, at the plain
     configuration N8 M16 K2 (128 chains x 200 samples, burn-in 64, the
     reference schedule lambda 40 -> 1, lr 0.1 -> 0.01): before every step the
     mixed context takes the FP64 context's weights, so both sample the same
     Markov chains and the difference is the arithmetic alone. Max over 40
-    steps of the per-site energies' relative difference <= 1e-6 (the stated
-    target); with the FP64 local energies of NQES_OPT_MIXED_ENERGY64 it is at
-    the FP64 rounding level."""
+    steps of the per-site energies' relative difference: <= 1e-6 (the stated
+    target) with the default energies (NQES_OPT_MIXED_ENERGY64 = 2: tanh from
+    FP32, double-float ratio products), <= 1e-10 with tanh in FP64 (1)."""
     N, M, K, chains = 8, 16, 2, 128
     J = synthetic_j(N)
     f = pkg.Context(N, M, K, J, 0.595)
     x = pkg.Context(N, M, K, J, 0.595)
     f.set_weights(*pkg.synthetic_weights(N, M, K, 0.01, 20240601))
     x.set_option(pkg.OPT_PRECISION, pkg.PRECISION_MIXED)
+    x.set_option(pkg.OPT_MIXED_ENERGY64, mode)
     worst = 0.0
     for t in range(40):
         lr, lam = max(0.1 * 0.99 ** t, 0.01), max(40.0 * 0.9 ** t, 1.0)
@@ -401,7 +403,7 @@ def test_mixed_energies_along_the_fp64_trajectory(pkg):
         assert np.array_equal(f.get_samples()[0], x.get_samples()[0])
         vf, vm = (np.sort(np.linalg.eigvals(e / N).real) for e in (ef, em))
         worst = max(worst, float(np.max(np.abs(vm - vf) / np.abs(vf))))
-    print("max relative energy difference over 40 steps:", worst)
-    assert worst <= 1e-6
+    print(f"energy mode {mode}: max relative energy difference over 40 steps:", worst)
+    assert worst <= (1e-6 if mode == 2 else 1e-10)
     f.close()
     x.close()
