@@ -318,6 +318,16 @@ __device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al,
     sl = __fadd_rn(sl, __fadd_rn(err, e));
 }
 
+// (ah, al) *= (bh, bl): the product to a few 2^-48, renormalised
+__device__ __forceinline__ void df_mul(float &ah, float &al, float bh, float bl) {
+    const float p = ah * bh;
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    ah = __fadd_rn(p, e);
+    al = __fsub_rn(e, __fsub_rn(ah, p));
+}
+
 // (ah, al) += (bh, bl)
 __device__ __forceinline__ void df_acc(float &ah, float &al, float bh, float bl) {
     const float s = __fadd_rn(ah, bh);

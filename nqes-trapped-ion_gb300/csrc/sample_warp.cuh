@@ -757,43 +757,76 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
             __syncthreads();
             double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
             constexpr uint64_t kSign2 = 0x8000000080000000ULL;
-            for (int it = tid; it < KK * N; it += T) {
+            // one row's tables, tanh row and sign
+            struct RatRow {
+                const float *c, *s, *cl, *sl, *t;
+                uint64_t sg;
+            };
+            auto rat_row = [&](int it) {
                 const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
                 const bool down = down_bit(sm.spin + k * NW, i);
-                const uint64_t sg = down ? 0ULL : kSign2;  // sigma t = t (spin down) or -t
                 const size_t o = (size_t(kk) * N + i) * MP;
-                const float *crow = sm.tc + o, *srow = sm.ts + o, *clrow = A.cpl + o, *slrow = A.spl + o;
-                const float *trow = reinterpret_cast<const float *>(sm.t64) + size_t(q) * 2 * MP;
-                uint64_t Ph = f2_pack(1.f, 1.f), Pl = 0;
-                for (int j = 0; j < MP; j += 2) {
-                    const uint64_t ch = *reinterpret_cast<const uint64_t *>(crow + j);
-                    const uint64_t sh = *reinterpret_cast<const uint64_t *>(srow + j);
-                    const uint64_t cl = __ldg(reinterpret_cast<const unsigned long long *>(clrow + j));
-                    const uint64_t sl = __ldg(reinterpret_cast<const unsigned long long *>(slrow + j));
-                    const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(trow + 2 * j);
-                    const uint64_t a = tt.x ^ sg, al = tt.y ^ sg;
-                    // f = c + a s (double-float, not renormalised)
-                    const uint64_t p = f2_mul(a, sh);
-                    uint64_t e = f2_fma(a, sh, p ^ kSign2);
-                    e = f2_fma(a, sl, e);
-                    e = f2_fma(al, sh, e);
-                    const uint64_t fs = f2_add(ch, p);
-                    const uint64_t bb = f2_sub(fs, ch);
-                    const uint64_t err = f2_add(f2_sub(ch, f2_sub(fs, bb)), f2_sub(p, bb));
-                    const uint64_t fl = f2_add(cl, f2_add(err, e));
-                    // P *= f, renormalised
-                    const uint64_t ph = f2_mul(Ph, fs);
-                    uint64_t pe = f2_fma(Ph, fs, ph ^ kSign2);
-                    pe = f2_fma(Ph, fl, pe);
-                    pe = f2_fma(Pl, fs, pe);
-                    Ph = f2_add(ph, pe);
-                    Pl = f2_sub(pe, f2_sub(Ph, ph));
+                return RatRow{sm.tc + o, sm.ts + o, A.cpl + o, A.spl + o,
+                              reinterpret_cast<const float *>(sm.t64) + size_t(q) * 2 * MP,
+                              down ? 0ULL : kSign2};  // sigma t = t (spin down) or -t
+            };
+            // P *= f_j f_j+1 for units j, j + 1 (packed lanes), f = c + sigma t s
+            auto rat_step = [&](uint64_t &Ph, uint64_t &Pl, const RatRow &r, int j) {
+                const uint64_t ch = *reinterpret_cast<const uint64_t *>(r.c + j);
+                const uint64_t sh = *reinterpret_cast<const uint64_t *>(r.s + j);
+                const uint64_t cl = __ldg(reinterpret_cast<const unsigned long long *>(r.cl + j));
+                const uint64_t sl = __ldg(reinterpret_cast<const unsigned long long *>(r.sl + j));
+                const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(r.t + 2 * j);
+                const uint64_t a = tt.x ^ r.sg, al = tt.y ^ r.sg;
+                // f = c + a s (double-float, not renormalised)
+                const uint64_t p = f2_mul(a, sh);
+                uint64_t e = f2_fma(a, sh, p ^ kSign2);
+                e = f2_fma(a, sl, e);
+                e = f2_fma(al, sh, e);
+                const uint64_t fs = f2_add(ch, p);
+                const uint64_t bb = f2_sub(fs, ch);
+                const uint64_t err = f2_add(f2_sub(ch, f2_sub(fs, bb)), f2_sub(p, bb));
+                const uint64_t fl = f2_add(cl, f2_add(err, e));
+                // P *= f, renormalised
+                const uint64_t ph = f2_mul(Ph, fs);
+                uint64_t pe = f2_fma(Ph, fs, ph ^ kSign2);
+                pe = f2_fma(Ph, fl, pe);
+                pe = f2_fma(Pl, fs, pe);
+                Ph = f2_add(ph, pe);
+                Pl = f2_sub(pe, f2_sub(Ph, ph));
+            };
+            // the four lane products of a row (two chains x two lanes) as one
+            // double-float, times e^{-+2 sigma a} in FP64
+            auto rat_out = [&](int it, uint64_t Ah, uint64_t Al, uint64_t Bh, uint64_t Bl) {
+                float h[4], l[4];
+                f2_unpack(Ah, h[0], h[1]);
+                f2_unpack(Al, l[0], l[1]);
+                f2_unpack(Bh, h[2], h[3]);
+                f2_unpack(Bl, l[2], l[3]);
+                df_mul(h[0], l[0], h[1], l[1]);
+                df_mul(h[2], l[2], h[3], l[3]);
+                df_mul(h[0], l[0], h[2], l[2]);
+                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+                const bool down = down_bit(sm.spin + k * NW, i);
+                rat64[it] = (double(h[0]) + double(l[0])) * (down ? A.edn64 : A.eup64)[kk * N + i];
+            };
+            // two rows per pass, each as two independent half products: four
+            // packed chains in flight (MP / 2 is even: MP is a multiple of 8)
+            const int half = MP / 2;
+            for (int it0 = tid; it0 < KK * N; it0 += 2 * T) {
+                const int it1 = it0 + T;
+                const bool two = it1 < KK * N;
+                const RatRow r0 = rat_row(it0), r1 = rat_row(two ? it1 : it0);
+                const uint64_t one = f2_pack(1.f, 1.f);
+                uint64_t A0h = one, A0l = 0, B0h = one, B0l = 0, A1h = one, A1l = 0, B1h = one, B1l = 0;
+                for (int j = 0; j < half; j += 2) {
+                    rat_step(A0h, A0l, r0, j);
+                    rat_step(B0h, B0l, r0, j + half);
+                    rat_step(A1h, A1l, r1, j);
+                    rat_step(B1h, B1l, r1, j + half);
                 }
-                float h0, h1, l0, l1;
-                f2_unpack(Ph, h0, h1);
-                f2_unpack(Pl, l0, l1);
-                rat64[it] = ((double(h0) + double(l0)) * (double(h1) + double(l1))) *
-                            (down ? A.edn64 : A.eup64)[kk * N + i];
+                rat_out(it0, A0h, A0l, B0h, B0l);
+                if (two) rat_out(it1, A1h, A1l, B1h, B1l);
             }
         } else if (e64) {
             for (int e = tid; e < KK * MP; e += T) {
