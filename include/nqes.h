@@ -82,6 +82,10 @@ extern "C" {
 #define NQES_OPT_MIXED_EXACT 6       /* 1: MIXED takes every accept decision by its exact FP64 path
                                       * (verification of that path); 0 (default): only when the FP32
                                       * bound cannot decide. */
+#define NQES_OPT_SAMPLER_PLAN 12     /* launch plan of the decision-warp sampler (MIXED, CERTIFIED real):
+                                      * 0 (default): planned from the chains (and the autotuner when on);
+                                      * else the warps per chain (1, 2 or 4), plus 16 to stage the step's
+                                      * tables in shared memory. Results do not depend on the plan. */
 
 /* Precision of the SR step (nqes_set_option NQES_OPT_PRECISION).
  * FP64: every quantity in FP64, as the reference.

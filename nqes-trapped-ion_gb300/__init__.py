@@ -24,7 +24,7 @@ ERR_CUDA, ERR_OOM, ERR_NONFINITE, ERR_TIMEOUT, ERR_INVALID, ERR_STATE = -1, -2, 
 ARITH_AUTO, ARITH_COMPLEX, ARITH_REAL = 0, 1, 2
 OPT_ARITH, OPT_THREADS_PER_BLOCK, OPT_MINRES_CAP, OPT_PRECISION = 1, 2, 3, 4
 OPT_REJECT_FILTER, OPT_MIXED_EXACT, OPT_AUTOTUNE, OPT_TENSOR_CORES = 5, 6, 7, 8
-OPT_FUSED_SV, OPT_TEST_STAGE_WAIT, OPT_MIXED_ENERGY64 = 9, 10, 11
+OPT_FUSED_SV, OPT_TEST_STAGE_WAIT, OPT_MIXED_ENERGY64, OPT_SAMPLER_PLAN = 9, 10, 11, 12
 PRECISION_FP64, PRECISION_MIXED, PRECISION_CERTIFIED = 0, 1, 2
 HAM_ISING_LIKE, HAM_HEISENBERG_LIKE = 0, 1
 

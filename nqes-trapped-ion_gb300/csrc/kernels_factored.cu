@@ -58,8 +58,8 @@ __device__ __forceinline__ float sgn(uint64_t b0, uint64_t b1, int i) {
 // consecutive 16-byte pieces of a staged row: no bank conflicts). W_k is
 // staged in chunks of F.ic rows of JT JB floats (zero beyond M).
 template <int JT, int JB, int RB>
-__global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F, const float *__restrict__ v,
-                                                                     float *__restrict__ u) {
+__device__ __forceinline__ void frows_body(const FactArgs &F, const float *__restrict__ v, float *__restrict__ u,
+                                           const int bid) {
     extern __shared__ float4 smem4[];
     if (loop_guard_off(F.guard)) return;
     constexpr int WS = JT * JB, NG = kThreads / JT;
@@ -74,9 +74,9 @@ __global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F,
     float *surow = svb + WS;                       // NG * RB
     const int tj = threadIdx.x & (JT - 1), rg = threadIdx.x / JT;
     const int spb = (NG * RB) / K;                 // samples per block
-    const int rows_here = min(spb, F.Ns - int(blockIdx.x) * spb) * K;
+    const int rows_here = min(spb, F.Ns - bid * spb) * K;
     const int rl0 = rg * RB;                       // first local row of the group
-    const size_t rbase = size_t(blockIdx.x) * spb * K;
+    const size_t rbase = size_t(bid) * spb * K;
     uint64_t b0[RB], b1[RB];
 #pragma unroll
     for (int rb = 0; rb < RB; rb++) {
@@ -171,8 +171,21 @@ __global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F,
     for (int sl = threadIdx.x; sl * K < rows_here; sl += kThreads) {
         float acc = 0.f;
         for (int kk = 0; kk < K; kk++) acc += surow[sl * K + kk];
-        u[size_t(blockIdx.x) * spb + sl] = acc;
+        u[size_t(bid) * spb + sl] = acc;
     }
+}
+template <int JT, int JB, int RB>
+__global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows(FactArgs F, const float *__restrict__ v,
+                                                                     float *__restrict__ u) {
+    frows_body<JT, JB, RB>(F, v, u, blockIdx.x);
+}
+// The rows pass of a group of solves (one launch; group_member maps blocks to solves).
+template <int JT, int JB, int RB>
+__global__ void __launch_bounds__(kThreads, RB <= 2 ? 3 : 2) k_frows_g(const FactMember *__restrict__ tab,
+                                                                       const int *__restrict__ first, int n) {
+    const int m = group_member(first, n, blockIdx.x);
+    const FactMember &fm = tab[m];
+    frows_body<JT, JB, RB>(fm.F, fm.v32, fm.u32, int(blockIdx.x) - __ldg(first + m));
 }
 
 __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
@@ -205,8 +218,9 @@ template <int IB, int JB> __host__ __device__ constexpr size_t cols_smem(bool se
 // gn groups instead of kGroups, and the sets' sums meet in shared memory at the
 // end (in set order).
 template <int IB, int JB>
-__global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int gn, const float *__restrict__ w,
-                                                     const cplx *__restrict__ E, float *__restrict__ out) {
+__device__ __forceinline__ void fcols_body(const FactArgs &F, int mode, int gn, const float *__restrict__ w,
+                                           const cplx *__restrict__ E, float *__restrict__ out, const int bx,
+                                           const int by, const int bz) {
     if (loop_guard_off(F.guard)) return;
     constexpr int WS = kJT * JB, kStage = cols_stage(JB);
     extern __shared__ float4 smem4[];
@@ -215,14 +229,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int
     uint64_t *sb = reinterpret_cast<uint64_t *>(sw1 + 2 * kStage);  // [2][kStage][2]
     const int N = F.N, M = F.M, K = F.K, NW = F.NW, L = N + M + N * M, MT = F.MT, KK = K * K;
     const int P = K * L;
-    const int c = blockIdx.x, k = blockIdx.y;
+    const int c = bx, k = by;
     const int tj = threadIdx.x & (kJT - 1), ig = threadIdx.x / kJT;
     const int nset = kGroups / gn, set = ig / gn, igl = ig - set * gn;
     if (!dyn_smem_covers(cols_smem<IB, JB>(nset > 1)) || NW > 2 || MT > WS) {
         if (threadIdx.x == 0) atomicOr(F.err, kErrLaunch);
         return;
     }
-    const int ibase = blockIdx.z * (gn * IB) + igl * IB;
+    const int ibase = bz * (gn * IB) + igl * IB;
     const int vpr = mode == 3 ? K * (K + 1) / 2 : K;  // (virtual) rows per sample
     const size_t nrows = size_t(F.Ns) * vpr;
     const size_t r0 = nrows * c / F.rchunks, r1 = nrows * (c + 1) / F.rchunks;
@@ -297,7 +311,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int
     }
 #pragma unroll
     for (int jb = 0; jb < JB; jb++) accb[jb] = 0.f;
-    const bool bgroup = blockIdx.z == 0 && igl == 0;
+    const bool bgroup = bz == 0 && igl == 0;
     // the thread's IB grid rows share one 32-bit half of the sign words (IB | 32):
     // a sign is that word shifted so the row's bit is the top bit, XORed into the weight
     const uint32_t *sb32 = reinterpret_cast<const uint32_t *>(sb);
@@ -414,6 +428,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int
             if (j < M) o[N + j] = accb[jb];
         }
     }
+}
+template <int IB, int JB>
+__global__ void __launch_bounds__(kThreads, 2) k_fcols(FactArgs F, int mode, int gn, const float *__restrict__ w,
+                                                     const cplx *__restrict__ E, float *__restrict__ out) {
+    fcols_body<IB, JB>(F, mode, gn, w, E, out, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+// The O^T u pass (mode 0) of a group of solves: solve m's blocks in the order
+// of its own (rchunks, K, i blocks) grid.
+template <int IB, int JB>
+__global__ void __launch_bounds__(kThreads, 2) k_fcols_g(const FactMember *__restrict__ tab,
+                                                       const int *__restrict__ first, int n) {
+    const int m = group_member(first, n, blockIdx.x);
+    const FactMember &fm = tab[m];
+    const int lin = int(blockIdx.x) - __ldg(first + m), X = fm.F.rchunks, Y = fm.F.K;
+    fcols_body<IB, JB>(fm.F, 0, fm.gn, fm.u32, nullptr, fm.ypart32, lin % X, (lin / X) % Y, lin / (X * Y));
 }
 
 // o, skk = reglam (<O^2> - o^2), f = <E_loc O> - eloc o from the chunk partials.
@@ -544,7 +573,112 @@ cudaError_t cols_dispatch(const FactArgs &F, int mode, const float *w, const cpl
     }
 }
 
+// Grouped launches: variant ids. Rows: the case of rows_dispatch (by M);
+// columns: 10 JB + IB.
+template <int JT, int JB, int RB0 = 0>
+cudaError_t rows_group(const FactMember *tab, const int *first, int n, int blocks, size_t smem, cudaStream_t st,
+                       bool prepare) {
+    constexpr int RB = RB0 ? RB0 : JB >= 16 ? 64 / JB : 32 / JB;
+    if (prepare) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_frows_g<JT, JB, RB>));
+    k_frows_g<JT, JB, RB><<<blocks, kThreads, smem, st>>>(tab, first, n);
+    return cudaGetLastError();
+}
+cudaError_t rows_group_dispatch(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
+                                cudaStream_t st, bool prepare) {
+    switch (variant) {
+    case 0: return rows_group<4, 4>(tab, first, n, blocks, smem, st, prepare);
+    case 1: return rows_group<4, 8>(tab, first, n, blocks, smem, st, prepare);
+    case 2: return rows_group<4, 16, 2>(tab, first, n, blocks, smem, st, prepare);
+    case 3: return rows_group<8, 16>(tab, first, n, blocks, smem, st, prepare);
+    case 4: return rows_group<8, 32>(tab, first, n, blocks, smem, st, prepare);
+    case 5: return rows_group<8, 64>(tab, first, n, blocks, smem, st, prepare);
+    default: return cudaErrorInvalidValue;
+    }
+}
+template <int IB, int JB>
+cudaError_t cols_group(const FactMember *tab, const int *first, int n, int blocks, size_t smem, cudaStream_t st,
+                       bool prepare) {
+    if (prepare) return allow_max_dynamic_smem(reinterpret_cast<const void *>(k_fcols_g<IB, JB>));
+    k_fcols_g<IB, JB><<<blocks, kThreads, smem, st>>>(tab, first, n);
+    return cudaGetLastError();
+}
+cudaError_t cols_group_dispatch(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
+                                cudaStream_t st, bool prepare) {
+    switch (variant) {
+    case 41: return cols_group<1, 4>(tab, first, n, blocks, smem, st, prepare);
+    case 42: return cols_group<2, 4>(tab, first, n, blocks, smem, st, prepare);
+    case 44: return cols_group<4, 4>(tab, first, n, blocks, smem, st, prepare);
+    case 81: return cols_group<1, 8>(tab, first, n, blocks, smem, st, prepare);
+    case 82: return cols_group<2, 8>(tab, first, n, blocks, smem, st, prepare);
+    case 84: return cols_group<4, 8>(tab, first, n, blocks, smem, st, prepare);
+    case 161: return cols_group<1, 16>(tab, first, n, blocks, smem, st, prepare);
+    case 162: return cols_group<2, 16>(tab, first, n, blocks, smem, st, prepare);
+    case 164: return cols_group<4, 16>(tab, first, n, blocks, smem, st, prepare);
+    case 321: return cols_group<1, 32>(tab, first, n, blocks, smem, st, prepare);
+    case 641: return cols_group<1, 64>(tab, first, n, blocks, smem, st, prepare);
+    default: return cudaErrorInvalidValue;
+    }
+}
+// Shared memory of the column kernel for (IB, JB) with or without row sets.
+size_t cols_smem_of(int IB, int JB, bool sets) {
+    switch (JB) {
+    case 4: return IB == 1 ? cols_smem<1, 4>(sets) : IB == 2 ? cols_smem<2, 4>(sets) : cols_smem<4, 4>(sets);
+    case 8: return IB == 1 ? cols_smem<1, 8>(sets) : IB == 2 ? cols_smem<2, 8>(sets) : cols_smem<4, 8>(sets);
+    case 16: return IB == 1 ? cols_smem<1, 16>(sets) : IB == 2 ? cols_smem<2, 16>(sets) : cols_smem<4, 16>(sets);
+    case 32: return cols_smem<1, 32>(sets);
+    default: return cols_smem<1, 64>(sets);
+    }
+}
+
 }  // namespace
+
+FactGroupPlan fact_group_plan(const FactArgs &F) {
+    FactGroupPlan g{};
+    const int M = F.M;
+    int JT, JB, RB;
+    if (M <= 16) {
+        g.rows_variant = 0; JT = 4; JB = 4; RB = 32 / 4;
+    } else if (M <= 32) {
+        g.rows_variant = 1; JT = 4; JB = 8; RB = 32 / 8;
+    } else if (M <= 64) {
+        g.rows_variant = 2; JT = 4; JB = 16; RB = 2;
+    } else if (M <= 128) {
+        g.rows_variant = 3; JT = 8; JB = 16; RB = 64 / 16;
+    } else if (M <= 256) {
+        g.rows_variant = 4; JT = 8; JB = 32; RB = 64 / 32;
+    } else {
+        g.rows_variant = 5; JT = 8; JB = 64; RB = 64 / 64;
+    }
+    // as rows_launch
+    const int WS = JT * JB, NG = kThreads / JT;
+    g.ic = std::max(1, std::min(F.N, (48 * 1024 / 4) / WS));
+    g.rows_smem = (size_t(g.ic) * WS + ((F.N + 3) & ~3) + WS + NG * RB) * sizeof(float);
+    const int spb = (NG * RB) / F.K;
+    g.rows_blocks = (F.Ns + spb - 1) / spb;
+    // as cols_dispatch / cols_launch
+    const int cjb = pick_jb(F.M), cib = pick_ib(F.N, cjb);
+    g.cols_variant = 10 * cjb + cib;
+    g.gn = pick_gn(F.N, cib, cjb);
+    g.cols_smem = cols_smem_of(cib, cjb, g.gn < kGroups);
+    g.zg = (F.N + g.gn * cib - 1) / (g.gn * cib);
+    g.cols_blocks = F.rchunks * F.K * g.zg;
+    return g;
+}
+
+cudaError_t prepare_fact_group(const FactGroupPlan &g) {
+    cudaError_t e = rows_group_dispatch(g.rows_variant, nullptr, nullptr, 0, 0, 0, nullptr, true);
+    return e != cudaSuccess ? e : cols_group_dispatch(g.cols_variant, nullptr, nullptr, 0, 0, 0, nullptr, true);
+}
+
+cudaError_t launch_frows_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
+                               cudaStream_t st) {
+    return rows_group_dispatch(variant, tab, first, n, blocks, smem, st, false);
+}
+
+cudaError_t launch_fcols_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
+                               cudaStream_t st) {
+    return cols_group_dispatch(variant, tab, first, n, blocks, smem, st, false);
+}
 
 // Sets the rows and column kernels' shared-memory limits; call outside stream capture.
 cudaError_t prepare_frows(const FactArgs &F) {

@@ -69,6 +69,18 @@ cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+namespace {
+__global__ void k_exp_table(double *tab) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < kExpTabN) tab[n] = exp(-double(n) / 64.0);
+}
+}  // namespace
+
+cudaError_t launch_exp_table(double *tab, cudaStream_t st) {
+    k_exp_table<<<(kExpTabN + 255) / 256, 256, 0, st>>>(tab);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
                              float *wlp, float *bh, float *bl, float *bnd, float *cpl, float *spl, cudaStream_t st) {
     const size_t n = size_t(sh.K) * sh.N * MP;

@@ -400,7 +400,7 @@ template <class S> __global__ void k_minres_first_v(SolveBufs<S> B) {
 // Lanczos part 1 of step j: r3 = S v_j - (beta_j / beta_{j-1}) r1; partials
 // of Re(r3^H v_j). The Lanczos chain runs whether or not the QLP chain beside
 // it ends the solve (a step past the end only costs its time).
-template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(SolveBufs<S> B) {
+template <class S> __device__ __forceinline__ void lanczos_a_body(const SolveBufs<S> &B, const int bid) {
     __shared__ double sh[32];
     __shared__ S ovs;
     __shared__ ColSumSmem<S> cs;
@@ -413,7 +413,7 @@ template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(
         if (threadIdx.x == 0) ovs = ov;
     }
     const int P = B.sh.P, pl = threadIdx.x % kMrThreads, rg = threadIdx.x / kMrThreads;
-    const int p = blockIdx.x * kMrThreads + pl;
+    const int p = bid * kMrThreads + pl;
     const S y = sv_colsum(B, p, pl, rg, cs);  // its barrier also publishes ovs
     const bool first = j == 1;
     const double c1 = first ? 0.0 : lz.beta[j % 3] / lz.beta[(j - 1) % 3];  // beta_new / betal_new
@@ -425,12 +425,15 @@ template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(
         t = re_dot(r3, B.v[p]);
     }
     t = block_sum(t, sh);
-    if (threadIdx.x == 0) B.part[blockIdx.x] = t;
+    if (threadIdx.x == 0) B.part[bid] = t;
+}
+template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(SolveBufs<S> B) {
+    lanczos_a_body(B, blockIdx.x);
 }
 
 // Lanczos part 2 of step j: r3 -= (alfa_j / beta_j) r2; r1 = r2; r2 = r3;
 // partials of |r3|^2.
-template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
+template <class S> __device__ __forceinline__ void lanczos_b_body(const SolveBufs<S> &B, const int bid) {
     __shared__ double sh[32];
     __shared__ double alfa_s;
     if (loop_guard_off(B.guard)) return;
@@ -442,7 +445,7 @@ template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
         if (threadIdx.x == 0) alfa_s = a;
     }
     __syncthreads();
-    const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = B.sh.P, p = bid * blockDim.x + threadIdx.x;
     const double c2 = alfa_s / lz.beta[j % 3];  // alfa / beta_new
     double t = 0.0;
     if (p < P) {
@@ -453,14 +456,15 @@ template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
         t = norm2(r3);
     }
     t = block_sum(t, sh);
-    if (threadIdx.x == 0) B.part[kPartStride + blockIdx.x] = t;
+    if (threadIdx.x == 0) B.part[kPartStride + bid] = t;
 }
+template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) { lanczos_b_body(B, blockIdx.x); }
 
 // Lanczos part 3 of step j: beta_{j+1} = |r3|, v_{j+1} = r3 / beta_{j+1} (into
 // v, its FP32 mirror and the QLP chain's slot), o·v_{j+1} partials; the last
 // block to finish publishes alfa_j, |r3_j|^2 and beta_{j+1} and advances j
 // (every block read j before any block arrived).
-template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
+template <class S> __device__ __forceinline__ void lanczos_next_body(const SolveBufs<S> &B, const int bid) {
     __shared__ double sh[32];
     __shared__ double s_alfa, s_bn2;
     __shared__ int last;
@@ -478,7 +482,7 @@ template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
     }
     __syncthreads();
     const double betan = sqrt(s_bn2);
-    const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = B.sh.P, p = bid * blockDim.x + threadIdx.x;
     S *vq = B.vq + size_t((j + 1) % 3) * P;
     S ovt = zero<S>();
     if (p < P) {
@@ -490,9 +494,9 @@ template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
     }
     S s = block_sum_s(ovt, sh);
     if (threadIdx.x == 0) {
-        B.ovpart[blockIdx.x] = s;
+        B.ovpart[bid] = s;
         __threadfence();
-        last = atomicAdd(&lz.arrived, 1u) == gridDim.x - 1;
+        last = atomicAdd(&lz.arrived, 1u) == unsigned(nb) - 1;  // nb blocks per solve
     }
     __syncthreads();
     if (last && threadIdx.x == 0) {
@@ -504,6 +508,7 @@ template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
         __threadfence();
     }
 }
+template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) { lanczos_next_body(B, blockIdx.x); }
 
 __device__ __forceinline__ double sgn(double a) { return copysign(1.0, a); }
 __device__ void givens(double a, double b, double &c, double &s, double &r) {
@@ -697,7 +702,7 @@ __device__ __forceinline__ void qlp_scalar_step(const SolveBufs<S> &B, QlpState 
     if (B.use_cond) cudaGraphSetConditional(B.cond, q.running);
 }
 
-template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) {
+template <class S> __device__ __forceinline__ void qlp_scalar_body(const SolveBufs<S> &B) {
     QlpState &gq = *B.qs;
     if (threadIdx.x == 0) gq.bodies++;
     if (!gq.running) {
@@ -716,12 +721,13 @@ template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) {
     qlp_scalar_step(B, q, alfa, bn2);
     gq = q;
 }
+template <class S> __global__ void k_qlp_scalar(SolveBufs<S> B) { qlp_scalar_body(B); }
 
 // Vector part: w / x updates (code/minresqlp.h:253-299) with v_j from the
 // QLP chain's slot.
-template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
+template <class S> __device__ __forceinline__ void qlp_vectors_body(const SolveBufs<S> &B, const int bid) {
     const QlpState &q = *B.qs;
-    const int P = B.sh.P, p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int P = B.sh.P, p = bid * blockDim.x + threadIdx.x;
     if (q.mode == 0 && !q.running) return;
     if (p < P) {
         const S v = B.vq[size_t(q.iters_snapshot % 3) * P + p];
@@ -769,6 +775,7 @@ template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
         B.xl2[p] = xl2;
     }
 }
+template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) { qlp_vectors_body(B, blockIdx.x); }
 
 // w -= lr x in the reference layout (code/rbm.cc:699-717).
 template <class S>
@@ -795,7 +802,52 @@ __global__ void k_batch_cond(const int *const *flags, int n, cudaGraphConditiona
     if (threadIdx.x == 0) cudaGraphSetConditional(cond, any ? 1u : 0u);
 }
 
+// ---- grouped launches (the loop body of a batch) ----
+// One launch runs the same kernel for every solve of a group: block b belongs
+// to solve m with first[m] <= b < first[m + 1] and runs as that solve's block
+// b - first[m] with the solve's own buffers, so every solve does exactly the
+// arithmetic of its own launch, in the same order.
+template <class S>
+__global__ void __launch_bounds__(kMrColThreads)
+    k_lanczos_a_g(const SolveBufs<S> *__restrict__ tab, const int *__restrict__ first, int n) {
+    const int m = group_member(first, n, blockIdx.x);
+    lanczos_a_body(tab[m], int(blockIdx.x) - __ldg(first + m));
+}
+template <class S>
+__global__ void k_lanczos_b_g(const SolveBufs<S> *__restrict__ tab, const int *__restrict__ first, int n) {
+    const int m = group_member(first, n, blockIdx.x);
+    lanczos_b_body(tab[m], int(blockIdx.x) - __ldg(first + m));
+}
+template <class S>
+__global__ void k_lanczos_next_g(const SolveBufs<S> *__restrict__ tab, const int *__restrict__ first, int n) {
+    const int m = group_member(first, n, blockIdx.x);
+    lanczos_next_body(tab[m], int(blockIdx.x) - __ldg(first + m));
+}
+template <class S> __global__ void k_qlp_scalar_g(const SolveBufs<S> *__restrict__ tab) { qlp_scalar_body(tab[blockIdx.x]); }
+template <class S>
+__global__ void k_qlp_vectors_g(const SolveBufs<S> *__restrict__ tab, const int *__restrict__ first, int n) {
+    const int m = group_member(first, n, blockIdx.x);
+    qlp_vectors_body(tab[m], int(blockIdx.x) - __ldg(first + m));
+}
+
 }  // namespace
+
+int minres_vector_blocks(int P) { return mr_blocks(P); }
+
+template <class S>
+cudaError_t launch_lanczos_group(const SolveBufs<S> *tab, const int *first, int n, int blocks, cudaStream_t st) {
+    k_lanczos_a_g<S><<<blocks, kMrColThreads, 0, st>>>(tab, first, n);
+    k_lanczos_b_g<S><<<blocks, kMrThreads, 0, st>>>(tab, first, n);
+    k_lanczos_next_g<S><<<blocks, kMrThreads, 0, st>>>(tab, first, n);
+    return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_qlp_group(const SolveBufs<S> *tab, const int *first, int n, int blocks, cudaStream_t st) {
+    k_qlp_scalar_g<S><<<n, 32, 0, st>>>(tab);
+    k_qlp_vectors_g<S><<<blocks, kMrThreads, 0, st>>>(tab, first, n);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_batch_cond(const int *const *flags, int n, cudaGraphConditionalHandle cond, cudaStream_t st) {
     k_batch_cond<<<1, 32, 0, st>>>(flags, n, cond);
@@ -948,7 +1000,9 @@ cudaError_t launch_update(const Shape &sh, const StepParams *sp, const S *x, cpl
     template cudaError_t launch_sv_only<S>(const SolveBufs<S> &, cudaStream_t);                          \
     template cudaError_t launch_moment_part_only<S>(const SolveBufs<S> &, cudaStream_t);                 \
     template cudaError_t launch_update<S>(const Shape &, const StepParams *, const S *, cplx *, cplx *, \
-                                          cplx *, cudaStream_t);
+                                          cplx *, cudaStream_t);                                         \
+    template cudaError_t launch_lanczos_group<S>(const SolveBufs<S> *, const int *, int, int, cudaStream_t); \
+    template cudaError_t launch_qlp_group<S>(const SolveBufs<S> *, const int *, int, int, cudaStream_t);
 NQES_INST(double)
 NQES_INST(cplx)
 

@@ -57,6 +57,7 @@ struct nqes_ctx {
     float *dcp = nullptr, *dsp = nullptr, *dwh = nullptr, *dwl = nullptr, *dbh = nullptr, *dbl = nullptr;
     float *dcpl = nullptr, *dspl = nullptr;  // remainders of the FP32 cosh / sinh tables (double-float ratios)
     float *dbnd = nullptr;  // K·N float4 bound records, then K row-sum maxima
+    double *etab = nullptr; // e^{-n/64} for the row rebuilds (exp_neg_tab)
     float *v32 = nullptr, *u32 = nullptr, *ypart32 = nullptr;
     uint16_t *tcimg = nullptr;  // BF16 split image of v for the tensor-core rows pass
     int tensor_cores = 1;       // NQES_OPT_TENSOR_CORES: 0 off, 1 where it pays off, 2 wherever it fits
@@ -369,6 +370,7 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.bh = ctx->dbh;
     A.bl = ctx->dbl;
     A.bnd = ctx->dbnd;
+    A.etab = ctx->etab;
     A.G = ctx->dw_G;
     A.U = ctx->dw_U;
     A.MP = ctx->dw_MP;
@@ -691,26 +693,6 @@ const int *running_flag(const nqes_ctx *ctx) {
     return reinterpret_cast<const int *>(reinterpret_cast<const char *>(ctx->qs) + offsetof(QlpState, running));
 }
 
-// Captures the member's part of the shared loop body onto the capture that
-// `origin` carries: forked from `fork`, its QLP step j (st_qlp) beside its
-// Lanczos step j + 1 (st), both guarded by its running flag, joined back into
-// origin. The member's kernels are those of its own loop body.
-template <class S> cudaError_t capture_member_body(nqes_ctx *ctx, cudaStream_t origin, cudaEvent_t fork) {
-    SolveBufs<S> B = solve_bufs<S>(ctx);
-    B.use_cond = 0;
-    B.guard = running_flag(ctx);
-    B.F.guard = B.guard;
-    cudaError_t e = cudaStreamWaitEvent(ctx->st, fork, 0);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->st_qlp, fork, 0);
-    if (e == cudaSuccess) e = launch_qlp_step<S>(B, ctx->st_qlp);
-    if (e == cudaSuccess) e = launch_lanczos_step<S>(B, ctx->st);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, ctx->st_qlp);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, ctx->ev_join, 0);
-    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_fork, ctx->st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(origin, ctx->ev_fork, 0);
-    return e;
-}
-
 template <class S> int build_graph(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     if (ctx->exec) {
         cudaGraphExecDestroy(ctx->exec);
@@ -1021,8 +1003,13 @@ int nqes_create(int N, int M, int K, const double *J, double h, int device, nqes
         if ((rc = dalloc(ctx, &ctx->dcp, np)) || (rc = dalloc(ctx, &ctx->dsp, np)) || (rc = dalloc(ctx, &ctx->dwh, np)) ||
             (rc = dalloc(ctx, &ctx->dcpl, np)) || (rc = dalloc(ctx, &ctx->dspl, np)) ||
             (rc = dalloc(ctx, &ctx->dwl, np)) || (rc = dalloc(ctx, &ctx->dbh, nb)) || (rc = dalloc(ctx, &ctx->dbl, nb)) ||
-            (rc = dalloc(ctx, &ctx->dbnd, 4 * size_t(K) * N + 4 * size_t(K))))
+            (rc = dalloc(ctx, &ctx->dbnd, 4 * size_t(K) * N + 4 * size_t(K))) ||
+            (rc = dalloc(ctx, &ctx->etab, size_t(kExpTabN))))
             return fail(rc);
+        if (launch_exp_table(ctx->etab, ctx->st) != cudaSuccess || cudaStreamSynchronize(ctx->st) != cudaSuccess) {
+            ctx->err = "exp table kernel failed";
+            return fail(NQES_ERR_CUDA);
+        }
     }
     if (cudaMallocHost(&ctx->sp_host, sizeof(StepParams)) != cudaSuccess ||
         cudaMallocHost(&ctx->qs_host, sizeof(QlpState)) != cudaSuccess ||
@@ -1068,6 +1055,7 @@ int nqes_destroy(nqes_ctx *ctx) {
     dfree(ctx->dbh);
     dfree(ctx->dbl);
     dfree(ctx->dbnd);
+    dfree(ctx->etab);
     dfree(ctx->sp);
     dfree(ctx->qs);
     dfree(ctx->lz);
@@ -1195,6 +1183,21 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         }
         ctx->fused_opt = int(value);  // takes effect at the next step (the buffers are resized then)
         return NQES_OK;
+    case NQES_OPT_SAMPLER_PLAN: {
+        const int w = int(value & 15);
+        if (value < 0 || value > 31 || (value != 0 && w != 1 && w != 2 && w != 4)) {
+            ctx->err = "sampler plan must be 0, or 1, 2 or 4 warps plus 16 for staged tables";
+            return NQES_ERR_INVALID;
+        }
+        ctx->autotune = false;
+        ctx->dw_force_warps = w;
+        ctx->dw_force_stage = value >= 16 ? 1 : 0;
+        if (ctx->exec) {  // the captured step bakes the sampler's launch in
+            cudaGraphExecDestroy(ctx->exec);
+            ctx->exec = nullptr;
+        }
+        return NQES_OK;
+    }
     case NQES_OPT_REJECT_FILTER:
     case NQES_OPT_MIXED_EXACT:
         if (value != 0 && value != 1) {
@@ -1713,9 +1716,12 @@ struct nqes_batch {
     std::vector<nqes_ctx *> m;
     int device = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t sq = nullptr;          // the loop body's QLP branch (capture only)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    cudaEvent_t ev_fork = nullptr;      // fork of the members' loop bodies (capture only)
+    cudaEvent_t ev_fork = nullptr;      // fork of the loop body's branches (capture only)
+    cudaEvent_t ev_qjoin = nullptr;     // join of the QLP branch (capture only)
     const int **flags_d = nullptr;      // device array: each member's QlpState::running
+    void *groups_d = nullptr;           // the loop body's grouped-launch tables (see the capture)
     cudaGraphExec_t exec = nullptr;
     std::vector<std::vector<long long>> keys;  // per member: what its captured nodes depend on (see the step)
     std::string err;
@@ -1723,7 +1729,213 @@ struct nqes_batch {
 
 namespace {
 thread_local std::string g_batch_create_error;
+
+// The loop body of a batch as grouped launches (one launch per kernel for all
+// the members it covers, kernels_solve.cu / kernels_factored.cu): the members'
+// buffers as device tables, in member order per arithmetic, and the factored
+// S·v passes of the MIXED members grouped by kernel variant. Members whose S·v
+// has no grouped form (two-pass or fused FP64 S·v, tensor-core passes) run it
+// with their own launches on their own streams. Each member's arithmetic is
+// that of its own loop body.
+struct FactGroup {
+    int variant = 0, blocks = 0;
+    size_t smem = 0;
+    std::vector<FactMember> mem;
+    std::vector<int> first{0};
+    size_t off_tab = 0, off_first = 0;  // byte offsets in groups_d
+};
+struct BodyGroups {
+    std::vector<SolveBufs<double>> tabd;
+    std::vector<SolveBufs<cplx>> tabc;
+    std::vector<int> firstd{0}, firstc{0};
+    size_t off_tabd = 0, off_tabc = 0, off_firstd = 0, off_firstc = 0;
+    std::vector<FactGroup> rows, cols;
+    std::vector<int> own_rows;  // members that run their rows pass (or whole S·v) on their own stream
+    std::vector<int> own_cols;  // MIXED members that run their column pass on their own stream
+};
+
+size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+FactGroup &group_of(std::vector<FactGroup> &v, int variant) {
+    for (auto &g : v)
+        if (g.variant == variant) return g;
+    v.emplace_back();
+    v.back().variant = variant;
+    return v.back();
 }
+
+// Builds the tables (host side), uploads them to b->groups_d and sets the
+// grouped kernels' shared-memory limits (not allowed during a capture).
+int plan_body_groups(nqes_batch *b, const std::vector<int> &arith, BodyGroups &g) {
+    const int n = int(b->m.size());
+    for (int i = 0; i < n; i++) {
+        nqes_ctx *c = b->m[i];
+        const int *guard = running_flag(c);
+        if (arith[i] == NQES_ARITH_COMPLEX) {
+            SolveBufs<cplx> B = solve_bufs<cplx>(c);
+            B.use_cond = 0;
+            B.guard = guard;
+            g.tabc.push_back(B);
+            g.firstc.push_back(g.firstc.back() + minres_vector_blocks(c->sh.P));
+            g.own_rows.push_back(i);
+            continue;
+        }
+        SolveBufs<double> B = solve_bufs<double>(c);
+        B.use_cond = 0;
+        B.guard = guard;
+        B.F.guard = guard;
+        g.tabd.push_back(B);
+        g.firstd.push_back(g.firstd.back() + minres_vector_blocks(c->sh.P));
+        if (!B.fact) {
+            g.own_rows.push_back(i);
+            continue;
+        }
+        const FactGroupPlan pl = fact_group_plan(B.F);
+        FactMember fm{};
+        fm.F = B.F;
+        fm.F.ic = pl.ic;
+        fm.v32 = B.v32;
+        fm.u32 = B.u32;
+        fm.ypart32 = B.ypart32;
+        fm.gn = pl.gn;
+        fm.zg = pl.zg;
+        const cudaError_t pe = prepare_fact_group(pl);
+        if (pe != cudaSuccess) {
+            b->err = std::string("grouped S·v kernels: ") + cudaGetErrorString(pe);
+            return NQES_ERR_CUDA;
+        }
+        if (B.F.tc) {
+            g.own_rows.push_back(i);
+        } else {
+            FactGroup &r = group_of(g.rows, pl.rows_variant);
+            r.mem.push_back(fm);
+            r.blocks += pl.rows_blocks;
+            r.first.push_back(r.blocks);
+            r.smem = std::max(r.smem, pl.rows_smem);
+        }
+        if (B.F.tcc) {
+            g.own_cols.push_back(i);
+        } else {
+            FactGroup &q = group_of(g.cols, pl.cols_variant);
+            q.mem.push_back(fm);
+            q.blocks += pl.cols_blocks;
+            q.first.push_back(q.blocks);
+            q.smem = std::max(q.smem, pl.cols_smem);
+        }
+    }
+    // one device buffer for every table
+    size_t off = 0;
+    auto place = [&](size_t bytes) {
+        const size_t o = off;
+        off = align_up(off + bytes);
+        return o;
+    };
+    g.off_tabd = place(g.tabd.size() * sizeof(SolveBufs<double>));
+    g.off_tabc = place(g.tabc.size() * sizeof(SolveBufs<cplx>));
+    g.off_firstd = place(g.firstd.size() * sizeof(int));
+    g.off_firstc = place(g.firstc.size() * sizeof(int));
+    for (auto *v : {&g.rows, &g.cols})
+        for (auto &fg : *v) {
+            fg.off_tab = place(fg.mem.size() * sizeof(FactMember));
+            fg.off_first = place(fg.first.size() * sizeof(int));
+        }
+    std::vector<unsigned char> host(std::max<size_t>(off, 256));
+    auto put = [&](size_t o, const void *src, size_t bytes) {
+        if (bytes) std::memcpy(host.data() + o, src, bytes);
+    };
+    put(g.off_tabd, g.tabd.data(), g.tabd.size() * sizeof(SolveBufs<double>));
+    put(g.off_tabc, g.tabc.data(), g.tabc.size() * sizeof(SolveBufs<cplx>));
+    put(g.off_firstd, g.firstd.data(), g.firstd.size() * sizeof(int));
+    put(g.off_firstc, g.firstc.data(), g.firstc.size() * sizeof(int));
+    for (auto *v : {&g.rows, &g.cols})
+        for (auto &fg : *v) {
+            put(fg.off_tab, fg.mem.data(), fg.mem.size() * sizeof(FactMember));
+            put(fg.off_first, fg.first.data(), fg.first.size() * sizeof(int));
+        }
+    if (b->groups_d) {  // the previous graph, which used it, is destroyed and idle
+        cudaFree(b->groups_d);
+        b->groups_d = nullptr;
+    }
+    if (cudaMalloc(&b->groups_d, host.size()) != cudaSuccess ||
+        cudaMemcpy(b->groups_d, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        b->err = "allocation of the batch's launch tables failed";
+        return NQES_ERR_OOM;
+    }
+    return NQES_OK;
+}
+
+// Captures the loop body onto b->st (in capture): the QLP branch of every
+// member (grouped, on b->sq) beside the Lanczos branch (the S·v passes, then
+// the grouped Lanczos kernels), joined on b->st.
+cudaError_t capture_grouped_body(nqes_batch *b, const BodyGroups &g) {
+    unsigned char *base = static_cast<unsigned char *>(b->groups_d);
+    const auto *tabd = reinterpret_cast<const SolveBufs<double> *>(base + g.off_tabd);
+    const auto *tabc = reinterpret_cast<const SolveBufs<cplx> *>(base + g.off_tabc);
+    const int *firstd = reinterpret_cast<const int *>(base + g.off_firstd);
+    const int *firstc = reinterpret_cast<const int *>(base + g.off_firstc);
+    const int nd = int(g.tabd.size()), nc = int(g.tabc.size());
+    cudaError_t e = cudaEventRecord(b->ev_fork, b->st);
+    // QLP branch
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->sq, b->ev_fork, 0);
+    if (e == cudaSuccess && nd) e = launch_qlp_group<double>(tabd, firstd, nd, g.firstd.back(), b->sq);
+    if (e == cudaSuccess && nc) e = launch_qlp_group<cplx>(tabc, firstc, nc, g.firstc.back(), b->sq);
+    if (e == cudaSuccess) e = cudaEventRecord(b->ev_qjoin, b->sq);
+    // Lanczos branch: members with their own S·v launches on their own streams
+    for (int i : g.own_rows) {
+        if (e != cudaSuccess) break;
+        nqes_ctx *c = b->m[i];
+        e = cudaStreamWaitEvent(c->st, b->ev_fork, 0);
+        if (e != cudaSuccess) break;
+        if (c->arith == NQES_ARITH_COMPLEX) {
+            SolveBufs<cplx> B = solve_bufs<cplx>(c);
+            B.use_cond = 0;
+            B.guard = running_flag(c);
+            e = launch_sv_only<cplx>(B, c->st);
+        } else {
+            SolveBufs<double> B = solve_bufs<double>(c);
+            B.use_cond = 0;
+            B.guard = running_flag(c);
+            B.F.guard = B.guard;
+            e = B.fact ? launch_sv_rows_only<double>(B, c->st) : launch_sv_only<double>(B, c->st);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->st);
+    }
+    for (const FactGroup &fg : g.rows) {
+        if (e != cudaSuccess) break;
+        e = launch_frows_group(fg.variant, reinterpret_cast<const FactMember *>(base + fg.off_tab),
+                               reinterpret_cast<const int *>(base + fg.off_first), int(fg.mem.size()), fg.blocks,
+                               fg.smem, b->st);
+    }
+    for (int i : g.own_rows)
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->m[i]->ev_join, 0);
+    // column passes after every rows pass (a member's rows may have run on its own stream)
+    for (int i : g.own_cols) {
+        if (e != cudaSuccess) break;
+        nqes_ctx *c = b->m[i];
+        SolveBufs<double> B = solve_bufs<double>(c);
+        B.use_cond = 0;
+        B.guard = running_flag(c);
+        B.F.guard = B.guard;
+        e = cudaEventRecord(c->ev_fork, b->st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c->st, c->ev_fork, 0);
+        if (e == cudaSuccess) e = launch_sv_cols_only<double>(B, c->st);
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->st);
+    }
+    for (const FactGroup &fg : g.cols) {
+        if (e != cudaSuccess) break;
+        e = launch_fcols_group(fg.variant, reinterpret_cast<const FactMember *>(base + fg.off_tab),
+                               reinterpret_cast<const int *>(base + fg.off_first), int(fg.mem.size()), fg.blocks,
+                               fg.smem, b->st);
+    }
+    for (int i : g.own_cols)
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->m[i]->ev_join, 0);
+    // the Lanczos kernels of every member, then the join of the QLP branch
+    if (e == cudaSuccess && nd) e = launch_lanczos_group<double>(tabd, firstd, nd, g.firstd.back(), b->st);
+    if (e == cudaSuccess && nc) e = launch_lanczos_group<cplx>(tabc, firstc, nc, g.firstc.back(), b->st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->ev_qjoin, 0);
+    return e;
+}
+}  // namespace
 
 extern "C" {
 
@@ -1754,8 +1966,10 @@ int nqes_batch_create(nqes_ctx *const *members, int count, nqes_batch **out) {
     b->m.assign(members, members + count);
     b->device = members[0]->device;
     if (cudaSetDevice(b->device) != cudaSuccess || cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->sq, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_qjoin, cudaEventDisableTiming) != cudaSuccess) {
         g_batch_create_error = "stream or event creation failed";
         nqes_batch_destroy(b);
         return NQES_ERR_CUDA;
@@ -1778,9 +1992,12 @@ int nqes_batch_destroy(nqes_batch *b) {
     if (b->st) cudaStreamSynchronize(b->st);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->flags_d) cudaFree(b->flags_d);
+    if (b->groups_d) cudaFree(b->groups_d);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_qjoin) cudaEventDestroy(b->ev_qjoin);
+    if (b->sq) cudaStreamDestroy(b->sq);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
     return NQES_OK;
@@ -1876,12 +2093,12 @@ int nqes_batch_sr_step(nqes_batch *b, const uint64_t *seeds, const int *chains, 
         e = cudaGraphAddNode(&nW, g, nA.data(), nullptr, n, &cp);
         if (e != cudaSuccess) return fail(NQES_ERR_CUDA, std::string("cudaGraphAddNode (while): ") + cudaGetErrorString(e));
         cudaGraph_t body = cp.conditional.phGraph_out[0];
+        BodyGroups grp;
+        const int grc = plan_body_groups(b, arith, grp);
+        if (grc) return fail(grc, b->err);
         e = cudaStreamBeginCaptureToGraph(b->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return fail(NQES_ERR_CUDA, std::string("capture of the batched loop body: ") + cudaGetErrorString(e));
-        cudaError_t le = cudaEventRecord(b->ev_fork, b->st);
-        for (int i = 0; i < n && le == cudaSuccess; i++)
-            le = arith[i] == NQES_ARITH_COMPLEX ? capture_member_body<cplx>(b->m[i], b->st, b->ev_fork)
-                                                : capture_member_body<double>(b->m[i], b->st, b->ev_fork);
+        cudaError_t le = capture_grouped_body(b, grp);
         if (le == cudaSuccess) le = launch_batch_cond(b->flags_d, n, cond, b->st);
         const cudaError_t ce = cudaStreamEndCapture(b->st, &body);
         if (le != cudaSuccess || ce != cudaSuccess)

@@ -93,6 +93,7 @@ struct MixedArgs {
     const float *cp, *spp, *whp, *wlp, *bh, *bl;
     const float *cpl, *spl;              // the roundings' remainders: cosh(2w) - cp, sinh(2w) - spp [kk][i][MP]
     const float *bnd;                    // per (kk, i): float4 bound record, then per kk 2 max_j sum_i |w_ij|
+    const double *etab;                  // e^{-n/64}, n < kExpTabN (nqes_math.cuh exp_neg_tab)
     int G, U, MP;
     int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
     int stage_fault;                     // test hook (NQES_OPT_TEST_STAGE_WAIT): the staging wait runs out
@@ -113,6 +114,7 @@ int dw_units(const Shape &sh, int *G_out);  // U of the decision-warp form, 0 if
 size_t dw_smem_bytes(const Shape &sh, int MP, bool staged, bool out64 = false);
 cudaError_t prepare_sample_dw(const Shape &sh, int MP);
 cudaError_t launch_sample_dw(const MixedArgs &a, int warps, cudaStream_t st);
+cudaError_t launch_exp_table(double *tab, cudaStream_t st);  // tab[n] = e^{-n/64}, n < kExpTabN
 cudaError_t dw_occupancy(const Shape &sh, int threads, size_t smem, int *blocks_per_sm);
 cudaError_t launch_tables_dw(const Shape &sh, int MP, const cplx *b, const cplx *w, float *cp, float *spp, float *whp,
                              float *wlp, float *bh, float *bl, float *bnd, float *cpl, float *spl, cudaStream_t st);
@@ -205,6 +207,43 @@ struct FactArgs {
     const int *guard;  // see loop_guard_off (nullptr: no guard)
 };
 __host__ __device__ inline int fact_mt(int M) { return (M + 3) & ~3; }
+
+// A solve's factored S·v passes as a member of a grouped launch (a batch's
+// loop body): its factors, v (FP32 mirror), u = O v and the O^T u partials.
+struct FactMember {
+    FactArgs F;  // F.ic set as its own rows pass would
+    const float *v32;
+    float *u32, *ypart32;
+    int gn, zg;  // column pass: i groups per row set and i blocks
+};
+// Kernel variants, shared memory and blocks of a solve's rows and column
+// passes; solves of one variant can share a launch (the launch takes the
+// largest shared memory of its solves).
+struct FactGroupPlan {
+    int rows_variant, rows_blocks, ic;
+    size_t rows_smem;
+    int cols_variant, cols_blocks, gn, zg;
+    size_t cols_smem;
+};
+FactGroupPlan fact_group_plan(const FactArgs &F);
+cudaError_t prepare_fact_group(const FactGroupPlan &g);  // outside stream capture
+cudaError_t launch_frows_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
+                               cudaStream_t st);
+cudaError_t launch_fcols_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
+                               cudaStream_t st);
+
+// Solve m of a grouped launch owns blocks first[m] .. first[m + 1] - 1.
+__device__ __forceinline__ int group_member(const int *__restrict__ first, int n, int b) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(first + mid) <= b)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
 
 // Lets kernel `fn` take as much dynamic shared memory as the device allows.
 // The limit is a per-kernel global: set to one context's need, it would cap
@@ -323,6 +362,16 @@ template <class S> cudaError_t launch_minres_init(const SolveBufs<S> &b, cudaStr
 template <class S> cudaError_t launch_lanczos_step(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_qlp_step(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_apply_S(const SolveBufs<S> &b, const S *v, S *out, cudaStream_t st);
+// The MINRES-QLP vector kernels of a group of solves (a batch's loop body), one
+// launch per kernel: tab (device memory) holds the solves' buffers, first[m] the
+// first block of solve m (first[0] = 0, first[n] = blocks), each solve taking
+// minres_vector_blocks(P) blocks. The Lanczos part (r3, alfa, beta, v_{j+1})
+// follows the group's S·v passes; the QLP part runs beside it.
+int minres_vector_blocks(int P);
+template <class S>
+cudaError_t launch_lanczos_group(const SolveBufs<S> *tab, const int *first, int n, int blocks, cudaStream_t st);
+template <class S>
+cudaError_t launch_qlp_group(const SolveBufs<S> *tab, const int *first, int n, int blocks, cudaStream_t st);
 template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_sv_cols_only(const SolveBufs<S> &b, cudaStream_t st);
 template <class S> cudaError_t launch_sv_only(const SolveBufs<S> &b, cudaStream_t st);  // the step's S·v passes

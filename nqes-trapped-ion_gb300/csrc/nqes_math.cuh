@@ -279,6 +279,33 @@ template <class S> __host__ __device__ inline int small_pinv(const S *a, S *out,
     return r;
 }
 
+// ---- e^{-x}, x >= 0, from a table (the Phi row rebuilds of the decision-warp sampler) ----
+// x = n/64 + r with n = rint(64 x) and |r| <= 1/128, so e^{-x} = T[n] e^{-r}
+// with T[n] = e^{-n/64} (a table of kExpTabN entries built with exp() when a
+// context is created) and e^{-r} from its Taylor polynomial of degree 6
+// (truncation below (1/128)^7 / 7! < 2^-58). r = x - n/64 is exact (n = 0, or
+// n/64 within 1/128 of x >= 1/128). About 1.5 ulp, ten FP64 operations
+// against the ~25 of exp(). Beyond the table (x > 40) e^{-x} < 2^-57, under
+// half an ulp of the 1 it is added to, and 0 is returned; NaN stays NaN.
+constexpr int kExpTabN = 2561;
+__device__ __forceinline__ double exp_neg_tab(double x, const double *__restrict__ tab) {
+    const double t = x * 64.0;
+    if (!(t < 2560.0)) return t >= 2560.0 ? 0.0 : x;  // x is NaN in the second case
+    // rint(t) by the 1.5 * 2^52 shift (t in [0, 2560)): the integer in the low word
+    const double sh = t + 6755399441055744.0;
+    const int n = __double2loint(sh);
+    const double r = fma(sh - 6755399441055744.0, -0.015625, x);
+    const double q = -r;
+    double p = 1.0 / 720.0;
+    p = fma(p, q, 1.0 / 120.0);
+    p = fma(p, q, 1.0 / 24.0);
+    p = fma(p, q, 1.0 / 6.0);
+    p = fma(p, q, 0.5);
+    p = fma(p, q, 1.0);
+    p = fma(p, q, 1.0);
+    return __ldg(tab + n) * p;
+}
+
 // ---- double-float (hi + lo FP32 pairs) on the FP32 pipe ----
 
 // d as hi + lo: hi = d cut to 24 significant bits, lo = the remaining 29

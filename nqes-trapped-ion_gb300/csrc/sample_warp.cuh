@@ -42,6 +42,11 @@ namespace {
 constexpr float kU = 5.9604645e-8f;  // FP32 unit roundoff 2^-24
 constexpr int kMaxSpinWords = 8;
 
+// Register cap of the decision-warp kernel below 16 units per lane.
+#ifndef NQES_DW_MAXNREG
+#define NQES_DW_MAXNREG 128
+#endif
+
 __device__ __forceinline__ bool down_bit(const uint64_t *s, int i) { return (s[i >> 6] >> (i & 63)) & 1ULL; }
 __device__ __forceinline__ int expo32(float x) {
     const int b = (__float_as_int(x) >> 23) & 0xff;
@@ -156,7 +161,8 @@ __device__ void cofactor_abs(const double *m, int K, int r, int c, double &cof, 
 // row's largest entry near 1:
 //   Phi[k][kk] ~ P_kk exp(A_kk - max A),  A_kk = sum_i sigma_i a_i + sum_j |theta_j|,
 //   P_kk = prod_j (1 + e^{-2|theta_j|})  (each factor in (1, 2]),
-// one exp per hidden unit and per entry. Block-wide; ends with a barrier.
+// e^{-2|theta|} per hidden unit from the exp table (exp_neg_tab) and one exp
+// per entry. Block-wide; ends with a barrier.
 __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
     const int N = A.sh.N, M = A.sh.M, K = A.sh.K, NW = A.sh.NW, MP = A.MP;
     const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
@@ -199,7 +205,7 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
         for (int j = lane + 32 * part; j < M; j += 32 * wpk) {
             const double th = double(sm.th_hi[q * MP + j]) + double(sm.th_lo[q * MP + j]);
             lin += fabs(th);
-            pr *= 1.0 + exp(-2.0 * fabs(th));
+            pr *= 1.0 + exp_neg_tab(2.0 * fabs(th), A.etab);
         }
         if (part == 0)
             for (int i = lane; i < N; i += 32) lin += down_bit(sk, i) ? -A.a64[kk * N + i] : A.a64[kk * N + i];
@@ -472,9 +478,9 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
                         const double w = A.w64[(size_t(kkl) * N + i) * M + j];
                         const double t2 = down ? tt + 2.0 * w : tt - 2.0 * w;
                         lin += fabs(tt);
-                        pr *= 1.0 + exp(-2.0 * fabs(tt));
+                        pr *= 1.0 + exp_neg_tab(2.0 * fabs(tt), A.etab);
                         lin2 += fabs(t2);
-                        pr2 *= 1.0 + exp(-2.0 * fabs(t2));
+                        pr2 *= 1.0 + exp_neg_tab(2.0 * fabs(t2), A.etab);
                     }
                 }
             }
@@ -613,7 +619,7 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
 }
 
 template <int K_, int U>
-__global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArgs A) {
+__global__ void __maxnreg__(U * K_ >= 16 ? 255 : NQES_DW_MAXNREG) k_sample_dw(const MixedArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int K = K_, KK = K * K;
     const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
@@ -778,22 +784,25 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : 168) k_sample_dw(const MixedArg
                 const uint64_t sl = __ldg(reinterpret_cast<const unsigned long long *>(r.sl + j));
                 const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(r.t + 2 * j);
                 const uint64_t a = tt.x ^ r.sg, al = tt.y ^ r.sg;
-                // f = c + a s (double-float, not renormalised)
+                // f = c + a s as fs + fl (not renormalised): the product a s_hi with its
+                // exact error and the cross terms, then ch + p by Fast2Sum, which is exact
+                // here because |p| <= |s_hi| <= c_hi (|t| <= 1, sinh 2w < cosh 2w, and
+                // rounding keeps the order)
                 const uint64_t p = f2_mul(a, sh);
                 uint64_t e = f2_fma(a, sh, p ^ kSign2);
                 e = f2_fma(a, sl, e);
                 e = f2_fma(al, sh, e);
                 const uint64_t fs = f2_add(ch, p);
-                const uint64_t bb = f2_sub(fs, ch);
-                const uint64_t err = f2_add(f2_sub(ch, f2_sub(fs, bb)), f2_sub(p, bb));
+                const uint64_t err = f2_sub(p, f2_sub(fs, ch));
                 const uint64_t fl = f2_add(cl, f2_add(err, e));
-                // P *= f, renormalised
+                // compensated product (Graillat's CompProd, with a double-float
+                // factor): Ph *= fs rounded; Pl gathers each product's exact error
+                // and the low part's term, scaled along by the later factors
                 const uint64_t ph = f2_mul(Ph, fs);
                 uint64_t pe = f2_fma(Ph, fs, ph ^ kSign2);
                 pe = f2_fma(Ph, fl, pe);
-                pe = f2_fma(Pl, fs, pe);
-                Ph = f2_add(ph, pe);
-                Pl = f2_sub(pe, f2_sub(Ph, ph));
+                Pl = f2_fma(Pl, fs, pe);
+                Ph = ph;
             };
             // the four lane products of a row (two chains x two lanes) as one
             // double-float, times e^{-+2 sigma a} in FP64

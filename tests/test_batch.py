@@ -63,6 +63,38 @@ def test_batch_equals_individual_steps(pkg):
         c.close()
 
 
+# grouped loop body: three MIXED members of one S·v kernel variant, a MIXED
+# member of another, one whose rows pass runs on the tensor cores (N M = 4096:
+# its own launches), a CERTIFIED member (fused FP64 S·v: its own launches)
+GROUPED = [(16, 32, 2, 0.5, 1.2, 1, True), (16, 32, 2, 0.9, 1.0, 1, True), (16, 32, 2, 0.7, 1.4, 1, True),
+           (20, 40, 3, 0.6, 1.1, 1, True), (64, 64, 2, 0.8, 1.2, 1, True), (12, 24, 2, 0.4, 1.3, 2, True)]
+
+
+def test_grouped_loop_body_equals_individual_steps(pkg):
+    """The batch's loop body launches each MINRES-QLP kernel once for all its
+    members (grouped by S·v kernel variant; members without a grouped S·v run
+    it on their own streams): every member's e_mat, iterations, samples and
+    updated weights equal nqes_sr_step on it, bit for bit, over two steps."""
+    alone = [make(pkg, i, s) for i, s in enumerate(GROUPED)]
+    mixed = [make(pkg, i, s) for i, s in enumerate(GROUPED)]
+    batch = pkg.Batch(mixed)
+    n = len(GROUPED)
+    for t in range(2):
+        seeds, chains, m, burn, lr, reglam, rtol, maxit = step_args(t, n)
+        emats, infos, stats, ms = batch.sr_step(seeds, chains, m, burn, lr, reglam, rtol, maxit)
+        assert stats == [0] * n and ms > 0
+        for i, c in enumerate(alone):
+            e, info = c.sr_step(seeds[i], chains[i], m[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i])
+            assert np.array_equal(e, emats[i]), (t, i)
+            assert info["minres_iters"] == infos[i]["minres_iters"], (t, i)
+            assert np.array_equal(c.get_samples()[0], mixed[i].get_samples()[0])
+            for x, y in zip(c.get_weights(), mixed[i].get_weights()):
+                assert np.array_equal(x, y), (t, i)
+    batch.close()
+    for c in alone + mixed:
+        c.close()
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_autotune_keeps_the_chains(pkg, prec):
     """The autotuner only changes launch shapes: the chains are the same and

@@ -341,7 +341,11 @@ def test_certified_matches_fp64(pkg, N, M, K, chains, m):
     for a, b in zip(c["mom"], f["mom"]):
         assert rel_err(a, b) < 1e-10
     assert rel_err(c["sv"], f["sv"]) < 1e-10
-    assert rel_err(c["w"], f["w"]) < 1e-6
+    # the update: MINRES-QLP stops at rtol 1e-9, so two solves whose operators
+    # differ by rounding (1e-13 here) agree to the solver's tolerance times the
+    # conditioning of S, not to rounding; with 24 samples for P > 10^4
+    # parameters S is the regulariser plus a rank-24 term
+    assert rel_err(c["w"], f["w"]) < (1e-6 if P < 10000 else 5e-6)
 
 
 @pytest.mark.parametrize("N,M,K,prec", [(8, 16, 2, 0), (32, 64, 2, 0), (32, 64, 2, 2), (12, 20, 3, 0)])
