@@ -68,7 +68,7 @@ __device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl)
 struct DSmem {
     double *phi, *pinv, *Dm, *jk, *lsum, *jpart;
     float *th_hi, *th_lo, *t, *rat, *bsig, *Bm;
-    uint64_t *spin, *mbar;
+    uint64_t *spin, *spin_snap, *mbar;
     int *flag;
     double *t64;  // FP64 outputs: tanh of the exact theta [K*K][MP]
     float *tabs;  // staged tables (cosh 2w, sinh 2w, w hi, w lo), 4 * K*N*MP floats
@@ -83,7 +83,7 @@ __host__ __device__ inline size_t dsmem_bytes(int N, int MP, int K, bool staged,
     const size_t KK = size_t(K) * K;
     const size_t nd = 3 * KK + 4 + 32 + 32 * 4;
     const size_t nf = 3 * KK * MP + 2 * KK * N + KK;
-    size_t base = nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 8 * kMaxSpinWords + 8 + 4 * 4;  // 16: alignment pad
+    size_t base = nd * 8 + 16 + ((nf * 4 + 15) / 16) * 16 + 16 * kMaxSpinWords + 8 + 4 * 4;  // 16: alignment pad
     if (out64) base += 16 + KK * MP * 8;
     return staged ? base + 16 + 4 * dw_table_bytes(N, MP, K) : base;
 }
@@ -111,7 +111,8 @@ __device__ inline DSmem dcarve(unsigned char *base, int N, int MP, int K, bool o
     unsigned char *p = reinterpret_cast<unsigned char *>(f);
     p += (8 - (reinterpret_cast<uintptr_t>(p) & 7)) & 7;
     s.spin = reinterpret_cast<uint64_t *>(p);
-    s.mbar = s.spin + kMaxSpinWords;
+    s.spin_snap = s.spin + kMaxSpinWords;
+    s.mbar = s.spin_snap + kMaxSpinWords;
     s.flag = reinterpret_cast<int *>(s.mbar + 1);
     unsigned char *tb = reinterpret_cast<unsigned char *>(s.flag + 4);
     tb += (16 - (reinterpret_cast<uintptr_t>(tb) & 15)) & 15;
@@ -618,11 +619,371 @@ __device__ bool run_row(const MixedArgs &A, DSmem &sm, int k, Pcg64 &rng, unsign
     return changed;
 }
 
+// One sample (code/rbm.cc:574-657 per sample: local energy and
+// log-derivatives) from the chain's current rows of Phi, theta and tanh and the
+// configurations `spin`, computed by the threads htid = 0 .. HT - 1 of the
+// block, which `sync` synchronises (all of the block's threads, or only the
+// helper warps while warp 0 sweeps on).
+template <int K, class Sync>
+__device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, const size_t s, const uint64_t *spin,
+                                             const int htid, const int HT, Sync sync) {
+    constexpr int KK = K * K;
+    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
+    const int lane = htid & 31, hw = htid >> 5, nhw = HT >> 5;
+    const bool writer = htid == 0;
+    const bool e64 = A.out64 || A.e64;
+
+    // ---- sample: local energy and log-derivatives. Mixed form: FP32 flip
+    // ratios combined in FP64, O as its FP32 factors. FP64 outputs: tanh of
+    // the exact theta, flip ratios over the FP64 tables, the dense FP64 O row
+    // (what the FP64 sampler produces from the same configurations). ----
+    if (writer) {
+        double pinv[16];
+        if (!small_inv(sm.phi, pinv, K)) {
+            atomicOr(A.err, kErrSingular);
+            for (int t = 0; t < KK; t++) pinv[t] = 0.0;
+        }
+        for (int t = 0; t < KK; t++) sm.pinv[t] = pinv[t];
+    }
+    sync();
+    {
+        // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031): the
+        // N x N grid strided over the threads, partial sums per warp, then the
+        // warps' partials in order (deterministic)
+        double acc[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] = 0.0;
+        int i = htid / N, j = htid - (htid / N) * N;
+        const int di = HT / N, dj = HT - (HT / N) * N;
+        while (i < N) {
+            if (j < i) {
+                const double p = A.J[size_t(i) * N + j];
+#pragma unroll
+                for (int k = 0; k < K; k++) acc[k] += (down_bit(spin + k * NW, i) ^ down_bit(spin + k * NW, j)) ? -p : p;
+            }
+            j += dj;
+            i += di;
+            if (j >= N) {
+                j -= N;
+                i++;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            acc[k] = warp_sum(acc[k]);
+            if (lane == 0) sm.jpart[hw * 4 + k] = acc[k];
+        }
+    }
+    if (e64 && !A.out64) {
+        // MIXED: tanh of the exact theta as double-float in the t64 space
+        // (layout dfpair_hi per row of MP units): in FP64 (e64 = 1), or
+        // (e64 = 2) the row's tanhf(theta_hi) (rebuild_row) plus the
+        // first-order term of theta's low part, (1 - t^2) theta_lo, which
+        // leaves tanhf's own error (a few 2^-24). Each flip ratio
+        // prod_j (c_j + sigma t_j s_j) is a double-float product on the FP32
+        // pipe, two units per packed instruction (padded units are exactly
+        // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor.
+        for (int e = htid; e < KK * MP; e += HT) {
+            const int q = e / MP, j = e - q * MP;
+            float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + dfpair_hi(j);
+            if (A.e64 == 2) {
+                const float t = sm.t[e];  // 0 in the padding
+                tf[0] = t;
+                tf[2] = j < M ? fmaf(-t, t, 1.f) * sm.th_lo[e] : 0.f;
+            } else {
+                const double tv = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
+                const float th = float(tv);
+                tf[0] = th;
+                tf[2] = float(tv - double(th));
+            }
+        }
+        sync();
+        double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
+        constexpr uint64_t kSign2 = 0x8000000080000000ULL;
+        // one row's tables, tanh row and sign
+        struct RatRow {
+            const float *c, *s, *cl, *sl, *t;
+            uint64_t sg;
+        };
+        auto rat_row = [&](int it) {
+            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const bool down = down_bit(spin + k * NW, i);
+            const size_t o = (size_t(kk) * N + i) * MP;
+            return RatRow{sm.tc + o, sm.ts + o, A.cpl + o, A.spl + o,
+                          reinterpret_cast<const float *>(sm.t64) + size_t(q) * 2 * MP,
+                          down ? 0ULL : kSign2};  // sigma t = t (spin down) or -t
+        };
+        // P *= f_j f_j+1 for units j, j + 1 (packed lanes), f = c + sigma t s
+        auto rat_step = [&](uint64_t &Ph, uint64_t &Pl, const RatRow &r, int j) {
+            const uint64_t ch = *reinterpret_cast<const uint64_t *>(r.c + j);
+            const uint64_t sh = *reinterpret_cast<const uint64_t *>(r.s + j);
+            const uint64_t cl = __ldg(reinterpret_cast<const unsigned long long *>(r.cl + j));
+            const uint64_t sl = __ldg(reinterpret_cast<const unsigned long long *>(r.sl + j));
+            const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(r.t + 2 * j);
+            const uint64_t a = tt.x ^ r.sg, al = tt.y ^ r.sg;
+            // f = c + a s as fs + fl (not renormalised): the product a s_hi with its
+            // exact error and the cross terms, then ch + p by Fast2Sum, which is exact
+            // here because |p| <= |s_hi| <= c_hi (|t| <= 1, sinh 2w < cosh 2w, and
+            // rounding keeps the order)
+            const uint64_t p = f2_mul(a, sh);
+            uint64_t e = f2_fma(a, sh, p ^ kSign2);
+            e = f2_fma(a, sl, e);
+            e = f2_fma(al, sh, e);
+            const uint64_t fs = f2_add(ch, p);
+            const uint64_t err = f2_sub(p, f2_sub(fs, ch));
+            const uint64_t fl = f2_add(cl, f2_add(err, e));
+            // compensated product (Graillat's CompProd, with a double-float
+            // factor): Ph *= fs rounded; Pl gathers each product's exact error
+            // and the low part's term, scaled along by the later factors
+            const uint64_t ph = f2_mul(Ph, fs);
+            uint64_t pe = f2_fma(Ph, fs, ph ^ kSign2);
+            pe = f2_fma(Ph, fl, pe);
+            Pl = f2_fma(Pl, fs, pe);
+            Ph = ph;
+        };
+        // the four lane products of a row (two chains x two lanes) as one
+        // double-float, times e^{-+2 sigma a} in FP64
+        auto rat_out = [&](int it, uint64_t Ah, uint64_t Al, uint64_t Bh, uint64_t Bl) {
+            float h[4], l[4];
+            f2_unpack(Ah, h[0], h[1]);
+            f2_unpack(Al, l[0], l[1]);
+            f2_unpack(Bh, h[2], h[3]);
+            f2_unpack(Bl, l[2], l[3]);
+            df_mul(h[0], l[0], h[1], l[1]);
+            df_mul(h[2], l[2], h[3], l[3]);
+            df_mul(h[0], l[0], h[2], l[2]);
+            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const bool down = down_bit(spin + k * NW, i);
+            rat64[it] = (double(h[0]) + double(l[0])) * (down ? A.edn64 : A.eup64)[kk * N + i];
+        };
+        // two rows per pass, each as two independent half products: four
+        // packed chains in flight (MP / 2 is even: MP is a multiple of 8)
+        const int half = MP / 2;
+        for (int it0 = htid; it0 < KK * N; it0 += 2 * HT) {
+            const int it1 = it0 + HT;
+            const bool two = it1 < KK * N;
+            const RatRow r0 = rat_row(it0), r1 = rat_row(two ? it1 : it0);
+            const uint64_t one = f2_pack(1.f, 1.f);
+            uint64_t A0h = one, A0l = 0, B0h = one, B0l = 0, A1h = one, A1l = 0, B1h = one, B1l = 0;
+            for (int j = 0; j < half; j += 2) {
+                rat_step(A0h, A0l, r0, j);
+                rat_step(B0h, B0l, r0, j + half);
+                rat_step(A1h, A1l, r1, j);
+                rat_step(B1h, B1l, r1, j + half);
+            }
+            rat_out(it0, A0h, A0l, B0h, B0l);
+            if (two) rat_out(it1, A1h, A1l, B1h, B1l);
+        }
+    } else if (e64) {
+        for (int e = htid; e < KK * MP; e += HT) {
+            const int j = e % MP;
+            sm.t64[e] = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
+        }
+        sync();
+        double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
+        for (int it = htid; it < KK * N; it += HT) {
+            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const bool down = down_bit(spin + k * NW, i);
+            // sigma t = t (spin down) or -t: the sign by an integer XOR, so that a
+            // factor costs one FMA and one multiply on the FP64 pipe
+            const long long sgbit = down ? 0LL : (long long)0x8000000000000000ULL;
+            const double *crow = A.c64 + (size_t(kk) * N + i) * M, *srow = A.s64 + (size_t(kk) * N + i) * M;
+            const double *trow = sm.t64 + q * MP;
+            auto st = [&](int j) { return __longlong_as_double(__double_as_longlong(trow[j]) ^ sgbit); };
+            double p0 = 1.0, p1 = 1.0;
+            int j = 0;
+            for (; j + 1 < M; j += 2) {
+                p0 *= fma(st(j), srow[j], crow[j]);
+                p1 *= fma(st(j + 1), srow[j + 1], crow[j + 1]);
+            }
+            if (j < M) p0 *= fma(st(j), srow[j], crow[j]);
+            rat64[it] = (p0 * p1) * (down ? A.edn64 : A.eup64)[kk * N + i];
+        }
+    } else {
+        for (int it = htid; it < KK * N; it += HT) {
+            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const bool down = down_bit(spin + k * NW, i);
+            const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
+            const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
+            const float *trow = sm.t + q * MP;
+            // four independent partial products over 16-byte loads; padded units
+            // (t = 0, c = 1, s = 0) contribute exactly 1, so MP needs no tail
+            const float sg = down ? 1.f : -1.f;
+            float p0 = 1.f, p1 = 1.f, p2 = 1.f, p3 = 1.f;
+            for (int j = 0; j < MP; j += 4) {
+                const float4 tt = *reinterpret_cast<const float4 *>(trow + j);
+                const float4 ss = *reinterpret_cast<const float4 *>(srow + j);
+                const float4 cc = *reinterpret_cast<const float4 *>(crow + j);
+                p0 *= fmaf(sg * tt.x, ss.x, cc.x);
+                p1 *= fmaf(sg * tt.y, ss.y, cc.y);
+                p2 *= fmaf(sg * tt.z, ss.z, cc.z);
+                p3 *= fmaf(sg * tt.w, ss.w, cc.w);
+            }
+            const float p = (p0 * p1) * (p2 * p3);
+            sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
+        }
+    }
+    sync();
+    if (htid < K) {
+        double jt = 0.0;
+        for (int w2 = 0; w2 < nhw; w2++) jt += sm.jpart[w2 * 4 + htid];
+        sm.jk[htid] = 2.0 * jt;
+    }
+    sync();
+    for (int q = hw; q < KK; q += nhw) {
+        double acc = 0.0;
+        if (e64) {
+            const double *rat64 = reinterpret_cast<const double *>(sm.rat);
+            for (int i = lane; i < N; i += 32) acc += rat64[q * N + i];
+            acc = warp_sum(acc);
+        } else {
+            float a32 = 0.f;
+            for (int i = lane; i < N; i += 32) a32 += sm.rat[q * N + i];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) a32 += __shfl_xor_sync(0xffffffffu, a32, o);
+            acc = double(a32);
+        }
+        if (lane == 0) sm.Dm[q] = sm.jk[q / K] - A.h * acc;
+    }
+    sync();
+    if (writer) {
+        bool ok = true;
+        for (int r = 0; r < K; r++)
+            for (int cc = 0; cc < K; cc++) {
+                double e = 0.0;
+                for (int t = 0; t < K; t++) e = fma(sm.pinv[r * K + t], sm.Dm[t * K + cc] * sm.phi[t * K + cc], e);
+                ok = ok && isfinite(e);
+                A.E[s * KK + r * K + cc] = cplx{e, 0.0};
+            }
+        for (int k = 0; k < K; k++)
+            for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
+        if (!ok) atomicOr(A.err, kErrNonFinite);
+    }
+    for (int t = htid; t < K * NW; t += HT) A.spins[s * K * NW + t] = spin[t];
+    sync();
+    // the factors of the O row (code/rbm.cc:199-239 in closed form): tanh rows
+    // T[s][k][kk][j] = tanh theta_j of configuration kk under RBM k, and
+    // B[s][k][kk] = (Phi^-1)_{k,kk} Phi_{kk,k}; the signs come from the spins
+    if (A.out64) {
+        // O_{k,p} = sum_kk (Phi^-1)_{k,kk} Phi_{kk,k} d_p(configuration kk) in FP64, layout
+        // [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239). The coefficients
+        // times the spin signs, bs[k][kk][i], go to the ratio space (free once
+        // Dm is formed) and the coefficients themselves to Dm (free once E is
+        // formed): K FMAs per entry.
+        const int L = N + M + N * M;
+        if (A.o_split) {
+            // O stored as double-float pairs for the fused S·v: the same sums
+            // formed in double-float on the FP32 pipe (products with their FMA
+            // error and cross terms, TwoSum-compensated sums; ~2^-46 relative)
+            // from double-float splits of the coefficients and of tanh, made once
+            // per sample, instead of K FP64 FMAs per entry. The splits take the
+            // ratio space (bs2), the Dm space (Dm2) and t64 in place (t2).
+            float2 *bs2 = reinterpret_cast<float2 *>(sm.rat);  // K*K*N: the rat and bsig space
+            float2 *t2 = reinterpret_cast<float2 *>(sm.t64);   // K*K*MP, each in its own FP64 slot
+            float2 *Dm2 = reinterpret_cast<float2 *>(sm.Dm);   // K*K
+            bool ok = true;
+            for (int e = htid; e < KK * N; e += HT) {
+                const int q = e / N, i = e - q * N, k = q / K, kk = q - k * K;
+                const double b = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
+                float h, l;
+                ok &= df_split(down_bit(spin + kk * NW, i) ? -b : b, h, l);
+                bs2[e] = make_float2(h, l);
+            }
+            for (int e = htid; e < KK * MP; e += HT) {  // in place: a thread converts the slots it reads
+                float h, l;
+                ok &= df_split(sm.t64[e], h, l);
+                t2[e] = make_float2(h, l);
+            }
+            if (htid < KK) {  // E, the last reader of Dm, was formed before the last barrier
+                float h, l;
+                ok &= df_split(sm.pinv[(htid / K) * K + htid % K] * sm.phi[(htid % K) * K + htid / K], h, l);
+                Dm2[htid] = make_float2(h, l);
+            }
+            sync();
+            float2 *orow2 = reinterpret_cast<float2 *>(A.O64 + s * size_t(A.sh.P));
+            for (int e = htid; e < K * L; e += HT) {
+                const int k = e / L, p = e - k * L;
+                float sh = 0.f, sl = 0.f;
+                if (p < N) {
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) {
+                        const float2 b = bs2[(k * K + kk) * N + p];
+                        df_acc(sh, sl, b.x, b.y);
+                    }
+                } else if (p < N + M) {
+                    const int j = p - N;
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) {
+                        const float2 d = Dm2[k * K + kk], t = t2[(kk * K + k) * MP + j];
+                        df_fma(sh, sl, d.x, d.y, t.x, t.y);
+                    }
+                } else {
+                    const int i = (p - N - M) / M, j = (p - N - M) - i * M;
+#pragma unroll
+                    for (int kk = 0; kk < K; kk++) {
+                        const float2 b = bs2[(k * K + kk) * N + i], t = t2[(kk * K + k) * MP + j];
+                        df_fma(sh, sl, b.x, b.y, t.x, t.y);
+                    }
+                }
+                const float hi = sh + sl;
+                orow2[e] = make_float2(hi, sl - (hi - sh));
+                ok &= isfinite(hi);
+            }
+            if (!ok) atomicOr(A.err, kErrNonFinite);
+            sync();
+            return;
+        }
+        double *bs = reinterpret_cast<double *>(sm.rat);  // K*K*N doubles: the rat and bsig space
+        for (int e = htid; e < KK * N; e += HT) {
+            const int q = e / N, i = e - q * N, k = q / K, kk = q - k * K;
+            const double b = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
+            bs[e] = down_bit(spin + kk * NW, i) ? -b : b;
+        }
+        if (htid < KK) sm.Dm[htid] = sm.pinv[(htid / K) * K + htid % K] * sm.phi[(htid % K) * K + htid / K];
+        sync();
+        double *orow = A.O64 + s * size_t(A.sh.P);
+        bool split_ok = true;
+        for (int e = htid; e < K * L; e += HT) {
+            const int k = e / L, p = e - k * L;
+            double v = 0.0;
+            if (p < N) {
+#pragma unroll
+                for (int kk = 0; kk < K; kk++) v += bs[(k * K + kk) * N + p];
+            } else if (p < N + M) {
+                const int j = p - N;
+#pragma unroll
+                for (int kk = 0; kk < K; kk++) v = fma(sm.Dm[k * K + kk], sm.t64[(kk * K + k) * MP + j], v);
+            } else {
+                const int i = (p - N - M) / M, j = (p - N - M) - i * M;
+#pragma unroll
+                for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
+            }
+            if (A.o_split) {  // as hi + lo for the fused S·v (nqes_math.cuh: df_split)
+                float hi, lo;
+                split_ok &= df_split(v, hi, lo);
+                reinterpret_cast<float2 *>(orow)[e] = make_float2(hi, lo);
+            } else {
+                orow[e] = v;
+            }
+        }
+        if (!split_ok) atomicOr(A.err, kErrNonFinite);
+    } else {
+        const int MT = fact_mt(M);
+        float *ft = A.FT + s * size_t(KK) * MT;
+        for (int e = htid; e < KK * MT; e += HT) {
+            const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
+            ft[e] = j < M ? sm.t[(kk * K + k) * MP + j] : 0.f;
+        }
+        if (htid < KK) A.FB[s * KK + htid] = sm.Bm[htid];
+    }
+    sync();
+}
+
 template <int K_, int U>
 __global__ void __maxnreg__(U * K_ >= 16 ? 255 : NQES_DW_MAXNREG) k_sample_dw(const MixedArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    constexpr int K = K_, KK = K * K;
-    const int N = A.sh.N, M = A.sh.M, NW = A.sh.NW, MP = A.MP;
+    constexpr int K = K_;
+    const int N = A.sh.N, NW = A.sh.NW, MP = A.MP;
     const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = T >> 5;
     const int c = blockIdx.x;
     const bool e64 = A.out64 || A.e64;  // FP64 local energies (tanh of the exact theta, FP64 tables)
@@ -684,298 +1045,40 @@ __global__ void __maxnreg__(U * K_ >= 16 ? 255 : NQES_DW_MAXNREG) k_sample_dw(co
     unsigned long long nacc = 0, nexact = 0;
     int rowctr = 0;
     const int total = A.burn + A.m;
+    // With helper warps, a sweep's sample is formed by warps 1.. while warp 0
+    // runs the first row of the next sweep (named barrier 1 among the helpers);
+    // pending: that sample's index, -1 when none waits.
+    const bool overlap = nwarp >= 2;
+    const int HTn = T - 32;
+    auto helper_sync = [HTn] { asm volatile("bar.sync 1, %0;" ::"r"(HTn) : "memory"); };
+    long long pending = -1;
     for (int sw = 0; sw < total; sw++) {
         for (int k = 0; k < K; k++, rowctr++) {
             if (warp == 0) {
                 const bool ch = run_row<K_, U>(A, sm, k, rng, nacc, nexact);
                 if (lane == 0) sm.flag[rowctr & 1] = ch ? 1 : 0;
+            } else if (pending >= 0) {
+                sample_phase<K_>(A, sm, size_t(pending), sm.spin_snap, tid - 32, T - 32, helper_sync);
+                pending = -1;
             }
             __syncthreads();
             if (sm.flag[rowctr & 1]) rebuild_row(A, sm, k);  // uniform after the barrier
         }
         if (sw < A.burn) continue;
-
-        // ---- sample: local energy and log-derivatives. Mixed form: FP32 flip
-        // ratios combined in FP64, O as its FP32 factors. FP64 outputs: tanh of
-        // the exact theta, flip ratios over the FP64 tables, the dense FP64 O row
-        // (what the FP64 sampler produces from the same configurations). ----
         const size_t s = size_t(c) * A.m + (sw - A.burn);
-        if (writer) {
-            double pinv[16];
-            if (!small_inv(sm.phi, pinv, K)) {
-                atomicOr(A.err, kErrSingular);
-                for (int t = 0; t < KK; t++) pinv[t] = 0.0;
-            }
-            for (int t = 0; t < KK; t++) sm.pinv[t] = pinv[t];
-        }
-        __syncthreads();
-        {
-            // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031): the
-            // N x N grid strided over the block, partial sums per warp, then the
-            // warps' partials in order (deterministic)
-            double acc[K];
-#pragma unroll
-            for (int k = 0; k < K; k++) acc[k] = 0.0;
-            int i = tid / N, j = tid - (tid / N) * N;
-            const int di = T / N, dj = T - (T / N) * N;
-            while (i < N) {
-                if (j < i) {
-                    const double p = A.J[size_t(i) * N + j];
-#pragma unroll
-                    for (int k = 0; k < K; k++) acc[k] += (down_bit(sm.spin + k * NW, i) ^ down_bit(sm.spin + k * NW, j)) ? -p : p;
-                }
-                j += dj;
-                i += di;
-                if (j >= N) {
-                    j -= N;
-                    i++;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < K; k++) {
-                acc[k] = warp_sum(acc[k]);
-                if (lane == 0) sm.jpart[warp * 4 + k] = acc[k];
-            }
-        }
-        if (e64 && !A.out64) {
-            // MIXED: tanh of the exact theta as double-float in the t64 space
-            // (layout dfpair_hi per row of MP units): in FP64 (e64 = 1), or
-            // (e64 = 2) the row's tanhf(theta_hi) (rebuild_row) plus the
-            // first-order term of theta's low part, (1 - t^2) theta_lo, which
-            // leaves tanhf's own error (a few 2^-24). Each flip ratio
-            // prod_j (c_j + sigma t_j s_j) is a double-float product on the FP32
-            // pipe, two units per packed instruction (padded units are exactly
-            // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor.
-            for (int e = tid; e < KK * MP; e += T) {
-                const int q = e / MP, j = e - q * MP;
-                float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + dfpair_hi(j);
-                if (A.e64 == 2) {
-                    const float t = sm.t[e];  // 0 in the padding
-                    tf[0] = t;
-                    tf[2] = j < M ? fmaf(-t, t, 1.f) * sm.th_lo[e] : 0.f;
-                } else {
-                    const double tv = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
-                    const float th = float(tv);
-                    tf[0] = th;
-                    tf[2] = float(tv - double(th));
-                }
-            }
+        if (overlap) {
+            // the helpers take this sample while warp 0 sweeps the next row: the
+            // rows of Phi, theta and tanh stay as they are until that row's
+            // rebuild (after the row barrier); the configurations are copied
+            if (tid < K * NW) sm.spin_snap[tid] = sm.spin[tid];
             __syncthreads();
-            double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
-            constexpr uint64_t kSign2 = 0x8000000080000000ULL;
-            // one row's tables, tanh row and sign
-            struct RatRow {
-                const float *c, *s, *cl, *sl, *t;
-                uint64_t sg;
-            };
-            auto rat_row = [&](int it) {
-                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-                const bool down = down_bit(sm.spin + k * NW, i);
-                const size_t o = (size_t(kk) * N + i) * MP;
-                return RatRow{sm.tc + o, sm.ts + o, A.cpl + o, A.spl + o,
-                              reinterpret_cast<const float *>(sm.t64) + size_t(q) * 2 * MP,
-                              down ? 0ULL : kSign2};  // sigma t = t (spin down) or -t
-            };
-            // P *= f_j f_j+1 for units j, j + 1 (packed lanes), f = c + sigma t s
-            auto rat_step = [&](uint64_t &Ph, uint64_t &Pl, const RatRow &r, int j) {
-                const uint64_t ch = *reinterpret_cast<const uint64_t *>(r.c + j);
-                const uint64_t sh = *reinterpret_cast<const uint64_t *>(r.s + j);
-                const uint64_t cl = __ldg(reinterpret_cast<const unsigned long long *>(r.cl + j));
-                const uint64_t sl = __ldg(reinterpret_cast<const unsigned long long *>(r.sl + j));
-                const ulonglong2 tt = *reinterpret_cast<const ulonglong2 *>(r.t + 2 * j);
-                const uint64_t a = tt.x ^ r.sg, al = tt.y ^ r.sg;
-                // f = c + a s as fs + fl (not renormalised): the product a s_hi with its
-                // exact error and the cross terms, then ch + p by Fast2Sum, which is exact
-                // here because |p| <= |s_hi| <= c_hi (|t| <= 1, sinh 2w < cosh 2w, and
-                // rounding keeps the order)
-                const uint64_t p = f2_mul(a, sh);
-                uint64_t e = f2_fma(a, sh, p ^ kSign2);
-                e = f2_fma(a, sl, e);
-                e = f2_fma(al, sh, e);
-                const uint64_t fs = f2_add(ch, p);
-                const uint64_t err = f2_sub(p, f2_sub(fs, ch));
-                const uint64_t fl = f2_add(cl, f2_add(err, e));
-                // compensated product (Graillat's CompProd, with a double-float
-                // factor): Ph *= fs rounded; Pl gathers each product's exact error
-                // and the low part's term, scaled along by the later factors
-                const uint64_t ph = f2_mul(Ph, fs);
-                uint64_t pe = f2_fma(Ph, fs, ph ^ kSign2);
-                pe = f2_fma(Ph, fl, pe);
-                Pl = f2_fma(Pl, fs, pe);
-                Ph = ph;
-            };
-            // the four lane products of a row (two chains x two lanes) as one
-            // double-float, times e^{-+2 sigma a} in FP64
-            auto rat_out = [&](int it, uint64_t Ah, uint64_t Al, uint64_t Bh, uint64_t Bl) {
-                float h[4], l[4];
-                f2_unpack(Ah, h[0], h[1]);
-                f2_unpack(Al, l[0], l[1]);
-                f2_unpack(Bh, h[2], h[3]);
-                f2_unpack(Bl, l[2], l[3]);
-                df_mul(h[0], l[0], h[1], l[1]);
-                df_mul(h[2], l[2], h[3], l[3]);
-                df_mul(h[0], l[0], h[2], l[2]);
-                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-                const bool down = down_bit(sm.spin + k * NW, i);
-                rat64[it] = (double(h[0]) + double(l[0])) * (down ? A.edn64 : A.eup64)[kk * N + i];
-            };
-            // two rows per pass, each as two independent half products: four
-            // packed chains in flight (MP / 2 is even: MP is a multiple of 8)
-            const int half = MP / 2;
-            for (int it0 = tid; it0 < KK * N; it0 += 2 * T) {
-                const int it1 = it0 + T;
-                const bool two = it1 < KK * N;
-                const RatRow r0 = rat_row(it0), r1 = rat_row(two ? it1 : it0);
-                const uint64_t one = f2_pack(1.f, 1.f);
-                uint64_t A0h = one, A0l = 0, B0h = one, B0l = 0, A1h = one, A1l = 0, B1h = one, B1l = 0;
-                for (int j = 0; j < half; j += 2) {
-                    rat_step(A0h, A0l, r0, j);
-                    rat_step(B0h, B0l, r0, j + half);
-                    rat_step(A1h, A1l, r1, j);
-                    rat_step(B1h, B1l, r1, j + half);
-                }
-                rat_out(it0, A0h, A0l, B0h, B0l);
-                if (two) rat_out(it1, A1h, A1l, B1h, B1l);
-            }
-        } else if (e64) {
-            for (int e = tid; e < KK * MP; e += T) {
-                const int j = e % MP;
-                sm.t64[e] = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
-            }
-            __syncthreads();
-            double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
-            for (int it = tid; it < KK * N; it += T) {
-                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-                const bool down = down_bit(sm.spin + k * NW, i);
-                const double sg = down ? 1.0 : -1.0;
-                const double *crow = A.c64 + (size_t(kk) * N + i) * M, *srow = A.s64 + (size_t(kk) * N + i) * M;
-                const double *trow = sm.t64 + q * MP;
-                double p0 = 1.0, p1 = 1.0;
-                int j = 0;
-                for (; j + 1 < M; j += 2) {
-                    p0 *= fma(sg * trow[j], srow[j], crow[j]);
-                    p1 *= fma(sg * trow[j + 1], srow[j + 1], crow[j + 1]);
-                }
-                if (j < M) p0 *= fma(sg * trow[j], srow[j], crow[j]);
-                rat64[it] = (p0 * p1) * (down ? A.edn64 : A.eup64)[kk * N + i];
-            }
+            pending = (long long)s;
         } else {
-            for (int it = tid; it < KK * N; it += T) {
-                const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
-                const bool down = down_bit(sm.spin + k * NW, i);
-                const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
-                const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
-                const float *trow = sm.t + q * MP;
-                // four independent partial products over 16-byte loads; padded units
-                // (t = 0, c = 1, s = 0) contribute exactly 1, so MP needs no tail
-                const float sg = down ? 1.f : -1.f;
-                float p0 = 1.f, p1 = 1.f, p2 = 1.f, p3 = 1.f;
-                for (int j = 0; j < MP; j += 4) {
-                    const float4 tt = *reinterpret_cast<const float4 *>(trow + j);
-                    const float4 ss = *reinterpret_cast<const float4 *>(srow + j);
-                    const float4 cc = *reinterpret_cast<const float4 *>(crow + j);
-                    p0 *= fmaf(sg * tt.x, ss.x, cc.x);
-                    p1 *= fmaf(sg * tt.y, ss.y, cc.y);
-                    p2 *= fmaf(sg * tt.z, ss.z, cc.z);
-                    p3 *= fmaf(sg * tt.w, ss.w, cc.w);
-                }
-                const float p = (p0 * p1) * (p2 * p3);
-                sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
-            }
+            sample_phase<K_>(A, sm, s, sm.spin, tid, T, [] { __syncthreads(); });
         }
-        __syncthreads();
-        if (tid < K) {
-            double jt = 0.0;
-            for (int w2 = 0; w2 < nwarp; w2++) jt += sm.jpart[w2 * 4 + tid];
-            sm.jk[tid] = 2.0 * jt;
-        }
-        __syncthreads();
-        for (int q = warp; q < KK; q += nwarp) {
-            double acc = 0.0;
-            if (e64) {
-                const double *rat64 = reinterpret_cast<const double *>(sm.rat);
-                for (int i = lane; i < N; i += 32) acc += rat64[q * N + i];
-                acc = warp_sum(acc);
-            } else {
-                float a32 = 0.f;
-                for (int i = lane; i < N; i += 32) a32 += sm.rat[q * N + i];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) a32 += __shfl_xor_sync(0xffffffffu, a32, o);
-                acc = double(a32);
-            }
-            if (lane == 0) sm.Dm[q] = sm.jk[q / K] - A.h * acc;
-        }
-        __syncthreads();
-        if (writer) {
-            bool ok = true;
-            for (int r = 0; r < K; r++)
-                for (int cc = 0; cc < K; cc++) {
-                    double e = 0.0;
-                    for (int t = 0; t < K; t++) e = fma(sm.pinv[r * K + t], sm.Dm[t * K + cc] * sm.phi[t * K + cc], e);
-                    ok = ok && isfinite(e);
-                    A.E[s * KK + r * K + cc] = cplx{e, 0.0};
-                }
-            for (int k = 0; k < K; k++)
-                for (int kk = 0; kk < K; kk++) sm.Bm[k * K + kk] = float(sm.pinv[k * K + kk] * sm.phi[kk * K + k]);
-            if (!ok) atomicOr(A.err, kErrNonFinite);
-        }
-        for (int t = tid; t < K * NW; t += T) A.spins[s * K * NW + t] = sm.spin[t];
-        __syncthreads();
-        // the factors of the O row (code/rbm.cc:199-239 in closed form): tanh rows
-        // T[s][k][kk][j] = tanh theta_j of configuration kk under RBM k, and
-        // B[s][k][kk] = (Phi^-1)_{k,kk} Phi_{kk,k}; the signs come from the spins
-        if (A.out64) {
-            // O_{k,p} = sum_kk (Phi^-1)_{k,kk} Phi_{kk,k} d_p(configuration kk) in FP64, layout
-            // [k][a_i | b_j | w_{i*M+j}] (code/rbm.cc:199-239). The coefficients
-            // times the spin signs, bs[k][kk][i], go to the ratio space (free once
-            // Dm is formed) and the coefficients themselves to Dm (free once E is
-            // formed): K FMAs per entry.
-            const int L = N + M + N * M;
-            double *bs = reinterpret_cast<double *>(sm.rat);  // K*K*N doubles: the rat and bsig space
-            for (int e = tid; e < KK * N; e += T) {
-                const int q = e / N, i = e - q * N, k = q / K, kk = q - k * K;
-                const double b = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
-                bs[e] = down_bit(sm.spin + kk * NW, i) ? -b : b;
-            }
-            if (tid < KK) sm.Dm[tid] = sm.pinv[(tid / K) * K + tid % K] * sm.phi[(tid % K) * K + tid / K];
-            __syncthreads();
-            double *orow = A.O64 + s * size_t(A.sh.P);
-            bool split_ok = true;
-            for (int e = tid; e < K * L; e += T) {
-                const int k = e / L, p = e - k * L;
-                double v = 0.0;
-                if (p < N) {
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v += bs[(k * K + kk) * N + p];
-                } else if (p < N + M) {
-                    const int j = p - N;
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v = fma(sm.Dm[k * K + kk], sm.t64[(kk * K + k) * MP + j], v);
-                } else {
-                    const int i = (p - N - M) / M, j = (p - N - M) - i * M;
-#pragma unroll
-                    for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
-                }
-                if (A.o_split) {  // as hi + lo for the fused S·v (nqes_math.cuh: df_split)
-                    float hi, lo;
-                    split_ok &= df_split(v, hi, lo);
-                    reinterpret_cast<float2 *>(orow)[e] = make_float2(hi, lo);
-                } else {
-                    orow[e] = v;
-                }
-            }
-            if (!split_ok) atomicOr(A.err, kErrNonFinite);
-        } else {
-            const int MT = fact_mt(M);
-            float *ft = A.FT + s * size_t(KK) * MT;
-            for (int e = tid; e < KK * MT; e += T) {
-                const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
-                ft[e] = j < M ? sm.t[(kk * K + k) * MP + j] : 0.f;
-            }
-            if (tid < KK) A.FB[s * KK + tid] = sm.Bm[tid];
-        }
-        __syncthreads();
     }
+    if (overlap && warp != 0 && pending >= 0)
+        sample_phase<K_>(A, sm, size_t(pending), sm.spin_snap, tid - 32, T - 32, helper_sync);
     if (writer) {
         A.accepted[c] = nacc;
         A.exact[c] = nexact;
