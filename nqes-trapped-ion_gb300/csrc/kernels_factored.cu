@@ -592,6 +592,7 @@ cudaError_t rows_group_dispatch(int variant, const FactMember *tab, const int *f
     case 3: return rows_group<8, 16>(tab, first, n, blocks, smem, st, prepare);
     case 4: return rows_group<8, 32>(tab, first, n, blocks, smem, st, prepare);
     case 5: return rows_group<8, 64>(tab, first, n, blocks, smem, st, prepare);
+    case 6: return rows_group<4, 16, 4>(tab, first, n, blocks, smem, st, prepare);  // case 2, 4 rows a group
     default: return cudaErrorInvalidValue;
     }
 }
@@ -632,29 +633,30 @@ size_t cols_smem_of(int IB, int JB, bool sets) {
 
 }  // namespace
 
-FactGroupPlan fact_group_plan(const FactArgs &F) {
-    FactGroupPlan g{};
-    const int M = F.M;
+void fact_rows_geometry(int variant, const FactArgs &F, int *blocks, size_t *smem, int *ic) {
     int JT, JB, RB;
-    if (M <= 16) {
-        g.rows_variant = 0; JT = 4; JB = 4; RB = 32 / 4;
-    } else if (M <= 32) {
-        g.rows_variant = 1; JT = 4; JB = 8; RB = 32 / 8;
-    } else if (M <= 64) {
-        g.rows_variant = 2; JT = 4; JB = 16; RB = 2;
-    } else if (M <= 128) {
-        g.rows_variant = 3; JT = 8; JB = 16; RB = 64 / 16;
-    } else if (M <= 256) {
-        g.rows_variant = 4; JT = 8; JB = 32; RB = 64 / 32;
-    } else {
-        g.rows_variant = 5; JT = 8; JB = 64; RB = 64 / 64;
+    switch (variant) {
+    case 0: JT = 4; JB = 4; RB = 32 / 4; break;
+    case 1: JT = 4; JB = 8; RB = 32 / 8; break;
+    case 2: JT = 4; JB = 16; RB = 2; break;
+    case 3: JT = 8; JB = 16; RB = 64 / 16; break;
+    case 4: JT = 8; JB = 32; RB = 64 / 32; break;
+    case 6: JT = 4; JB = 16; RB = 4; break;
+    default: JT = 8; JB = 64; RB = 64 / 64; break;
     }
     // as rows_launch
     const int WS = JT * JB, NG = kThreads / JT;
-    g.ic = std::max(1, std::min(F.N, (48 * 1024 / 4) / WS));
-    g.rows_smem = (size_t(g.ic) * WS + ((F.N + 3) & ~3) + WS + NG * RB) * sizeof(float);
+    *ic = std::max(1, std::min(F.N, (48 * 1024 / 4) / WS));
+    *smem = (size_t(*ic) * WS + ((F.N + 3) & ~3) + WS + NG * RB) * sizeof(float);
     const int spb = (NG * RB) / F.K;
-    g.rows_blocks = (F.Ns + spb - 1) / spb;
+    *blocks = (F.Ns + spb - 1) / spb;
+}
+
+FactGroupPlan fact_group_plan(const FactArgs &F) {
+    FactGroupPlan g{};
+    const int M = F.M;
+    g.rows_variant = M <= 16 ? 0 : M <= 32 ? 1 : M <= 64 ? 2 : M <= 128 ? 3 : M <= 256 ? 4 : 5;
+    fact_rows_geometry(g.rows_variant, F, &g.rows_blocks, &g.rows_smem, &g.ic);
     // as cols_dispatch / cols_launch
     const int cjb = pick_jb(F.M), cib = pick_ib(F.N, cjb);
     g.cols_variant = 10 * cjb + cib;

@@ -1823,6 +1823,32 @@ int plan_body_groups(nqes_batch *b, const std::vector<int> &arith, BodyGroups &g
             q.smem = std::max(q.smem, pl.cols_smem);
         }
     }
+    // Rows groups of variant 2 (4 j-threads x 16 columns, 2 rows a group: the
+    // latency form of one solve) with more than two waves of blocks take 4
+    // rows a group (variant 6): the same per-row arithmetic in half the blocks.
+    for (FactGroup &r : g.rows) {
+        if (r.variant != 2 || r.blocks <= 6 * 152) continue;
+        r.variant = 6;
+        r.blocks = 0;
+        r.smem = 0;
+        r.first.assign(1, 0);
+        for (const FactMember &fm : r.mem) {
+            int blocks = 0, ic = 0;
+            size_t smem = 0;
+            fact_rows_geometry(6, fm.F, &blocks, &smem, &ic);
+            r.blocks += blocks;
+            r.first.push_back(r.blocks);
+            r.smem = std::max(r.smem, smem);
+        }
+        FactGroupPlan pl{};
+        pl.rows_variant = 6;
+        pl.cols_variant = fact_group_plan(r.mem[0].F).cols_variant;
+        const cudaError_t pe = prepare_fact_group(pl);
+        if (pe != cudaSuccess) {
+            b->err = std::string("grouped S·v kernels: ") + cudaGetErrorString(pe);
+            return NQES_ERR_CUDA;
+        }
+    }
     // one device buffer for every table
     size_t off = 0;
     auto place = [&](size_t bytes) {

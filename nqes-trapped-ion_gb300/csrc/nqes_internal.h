@@ -226,6 +226,11 @@ struct FactGroupPlan {
     size_t cols_smem;
 };
 FactGroupPlan fact_group_plan(const FactArgs &F);
+// Blocks, shared memory and staged rows (ic) of the rows pass in `variant`;
+// variant 6 is variant 2 (M <= 64) with 4 rows a thread group instead of 2
+// (fewer blocks, more work a block: the form for a large group), with the
+// same arithmetic per row.
+void fact_rows_geometry(int variant, const FactArgs &F, int *blocks, size_t *smem, int *ic);
 cudaError_t prepare_fact_group(const FactGroupPlan &g);  // outside stream capture
 cudaError_t launch_frows_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
                                cudaStream_t st);

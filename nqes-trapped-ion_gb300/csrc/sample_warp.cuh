@@ -197,9 +197,11 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
         }
     }
     __syncthreads();
-    // partial sums of A and products P over slots (kk, part): every warp takes
-    // slots, each slot a strided share of the row's hidden units
-    const int wpk = max(1, nwarp / K);
+    // sums of A and products P over slots (kk, part), max(1, 4 / K) parts per
+    // RBM, each a strided share of the row's hidden units summed by one warp
+    // (lanes, then the warp's fixed tree), the slots taken by the warps in
+    // turn: the same order, and so the same Phi, for any warps per chain
+    const int wpk = max(1, 4 / K);
     for (int v = warp; v < K * wpk; v += nwarp) {
         const int kk = v / wpk, part = v - kk * wpk, q = k * K + kk;
         double lin = 0.0, pr = 1.0;
@@ -648,31 +650,39 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
     sync();
     {
         // J(s_k) = 2 sum_{i>j} J_ij sigma_i sigma_j (code/rbm.cc:1011-1031): the
-        // N x N grid strided over the threads, partial sums per warp, then the
-        // warps' partials in order (deterministic)
-        double acc[K];
+        // N x N grid strided over 96 virtual threads (vt takes the pairs
+        // vt, vt + 96, ...), partial sums per virtual warp, then the three
+        // warps' partials in order. Physical warps take whole virtual warps in
+        // turn (the three helper warps one each), so the order, and the
+        // result, are the same for any threads.
+        for (int vw = hw; vw < 3; vw += nhw) {
+            const int vt = vw * 32 + lane;
+            double acc[K];
 #pragma unroll
-        for (int k = 0; k < K; k++) acc[k] = 0.0;
-        int i = htid / N, j = htid - (htid / N) * N;
-        const int di = HT / N, dj = HT - (HT / N) * N;
-        while (i < N) {
-            if (j < i) {
-                const double p = A.J[size_t(i) * N + j];
+            for (int k = 0; k < K; k++) acc[k] = 0.0;
+            int i = vt / N, j = vt - (vt / N) * N;
+            const int di = 96 / N, dj = 96 - (96 / N) * N;
+            while (i < N) {
+                if (j < i) {
+                    const double p = A.J[size_t(i) * N + j];
 #pragma unroll
-                for (int k = 0; k < K; k++) acc[k] += (down_bit(spin + k * NW, i) ^ down_bit(spin + k * NW, j)) ? -p : p;
+                    for (int k = 0; k < K; k++) acc[k] += (down_bit(spin + k * NW, i) ^ down_bit(spin + k * NW, j)) ? -p : p;
+                }
+                j += dj;
+                i += di;
+                if (j >= N) {
+                    j -= N;
+                    i++;
+                }
             }
-            j += dj;
-            i += di;
-            if (j >= N) {
-                j -= N;
-                i++;
+#pragma unroll
+            for (int k = 0; k < K; k++) {
+                acc[k] = warp_sum(acc[k]);
+                if (lane == 0) sm.jpart[vw * 4 + k] = acc[k];
             }
         }
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            acc[k] = warp_sum(acc[k]);
-            if (lane == 0) sm.jpart[hw * 4 + k] = acc[k];
-        }
+        sync();
+        if (htid < K) sm.jk[htid] = 2.0 * ((sm.jpart[htid] + sm.jpart[4 + htid]) + sm.jpart[8 + htid]);
     }
     if (e64 && !A.out64) {
         // MIXED: tanh of the exact theta as double-float in the t64 space
@@ -822,12 +832,6 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
             const float p = (p0 * p1) * (p2 * p3);
             sm.rat[it] = p * __ldg((down ? A.edn : A.eup) + kk * N + i);
         }
-    }
-    sync();
-    if (htid < K) {
-        double jt = 0.0;
-        for (int w2 = 0; w2 < nhw; w2++) jt += sm.jpart[w2 * 4 + htid];
-        sm.jk[htid] = 2.0 * jt;
     }
     sync();
     for (int q = hw; q < KK; q += nhw) {

@@ -95,6 +95,32 @@ def test_grouped_loop_body_equals_individual_steps(pkg):
         c.close()
 
 
+def test_large_rows_group_equals_individual_steps(pkg):
+    """A rows group of the loop body with more than six waves of blocks runs
+    the rows pass with four rows a thread group (half the blocks of the
+    one-solve form, the same arithmetic per row): five MIXED members of
+    N20 M40 K2 at 128 chains x 100 samples give each member's e_mat,
+    iterations and updated weights of nqes_sr_step on it, bit for bit."""
+    spec = [(20, 40, 2, 0.5 + 0.1 * i, 1.2, 1, True) for i in range(5)]
+    alone = [make(pkg, i, s) for i, s in enumerate(spec)]
+    mixed = [make(pkg, i, s) for i, s in enumerate(spec)]
+    batch = pkg.Batch(mixed)
+    n = len(spec)
+    seeds = [500 + 1000 * i for i in range(n)]
+    args = (seeds, [128] * n, [100] * n, [8] * n, [0.1] * n, [5.0] * n, [1e-9] * n, [2000] * n)
+    emats, infos, stats, _ = batch.sr_step(*args)
+    assert stats == [0] * n
+    for i, c in enumerate(alone):
+        e, info = c.sr_step(*[a[i] for a in args])
+        assert np.array_equal(e, emats[i]), i
+        assert info["minres_iters"] == infos[i]["minres_iters"], i
+        for x, y in zip(c.get_weights(), mixed[i].get_weights()):
+            assert np.array_equal(x, y), i
+    batch.close()
+    for c in alone + mixed:
+        c.close()
+
+
 @pytest.mark.parametrize("prec", [0, 1])
 def test_autotune_keeps_the_chains(pkg, prec):
     """The autotuner only changes launch shapes: the chains are the same and
