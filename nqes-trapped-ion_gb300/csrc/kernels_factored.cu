@@ -108,7 +108,21 @@ __device__ __forceinline__ void frows_body(const FactArgs &F, const float *__res
                 sw[t] = j < M ? vk[N + M + size_t(i0 + ii) * M + j] : 0.f;
             }
             __syncthreads();
+            // the sign of spin i0 + ii of each row at bit 31 of cur: the 32-bit
+            // word holding it, bit-reversed, shifted left by one per spin (two
+            // integer operations a spin instead of a 64-bit shift and select)
+            auto word_rev = [&](int rb, int w) -> uint32_t {
+                const uint64_t x = w < 2 ? b0[rb] : b1[rb];
+                return __brev(uint32_t((w & 1) ? (x >> 32) : x));
+            };
+            uint32_t cur[RB];
+#pragma unroll
+            for (int rb = 0; rb < RB; rb++) cur[rb] = word_rev(rb, i0 >> 5) << (i0 & 31);
             for (int ii = 0; ii < ni; ii++) {
+                if (ii > 0 && ((i0 + ii) & 31) == 0) {
+#pragma unroll
+                    for (int rb = 0; rb < RB; rb++) cur[rb] = word_rev(rb, (i0 + ii) >> 5);
+                }
                 const float4 *wr = reinterpret_cast<const float4 *>(sw + ii * WS) + tj;
                 float wv[JB];
 #pragma unroll
@@ -121,7 +135,8 @@ __device__ __forceinline__ void frows_body(const FactArgs &F, const float *__res
                 }
 #pragma unroll
                 for (int rb = 0; rb < RB; rb++) {
-                    const float sg = sgn(b0[rb], b1[rb], i0 + ii);
+                    const float sg = __uint_as_float((cur[rb] & 0x80000000u) | 0x3f800000u);  // -1: spin down
+                    cur[rb] <<= 1;
 #pragma unroll
                     for (int jb = 0; jb < JB; jb++) z[rb][jb] = fmaf(sg, wv[jb], z[rb][jb]);
                 }
