@@ -419,9 +419,11 @@ def serving_only(args):
 def precision_form(pkg, chains, samples, steps, local):
     """Config-3 style precision form: N=64, M=128, K=4, h ~ U[0.2, 1.2] (seeded),
     `chains` x `samples` per SR step in the mixed form (FP32 O resident: 16384 x 64
-    samples x 33536 parameters = 141 GB), energies compared per state with the
-    all-FP64 GPU form on the same weights and seeds at a size whose FP64 O fits
-    (the FP64 O of the full size would be 281 GB)."""
+    samples x 33536 parameters = 141 GB), the flip ratios of the local energies
+    as FP32 products (NQES_OPT_MIXED_ENERGY64 0: log-cosh ratios in FP32, as the
+    configuration states), energies compared per state with the all-FP64 GPU
+    form on the same weights and seeds at a size whose FP64 O fits (the FP64 O
+    of the full size would be 281 GB)."""
     n, m, k = 64, 128, 4
     h = float(np.random.default_rng(SEED).uniform(0.2, 1.2))
     J = pkg.synthetic_j(n)
@@ -431,6 +433,8 @@ def precision_form(pkg, chains, samples, steps, local):
         c = pkg.Context(n, m, k, J, h, device=local)
         c.set_weights(*w)
         c.set_option(pkg.OPT_PRECISION, prec)
+        if prec == pkg.PRECISION_MIXED:
+            c.set_option(pkg.OPT_MIXED_ENERGY64, 0)
         res = []
         for t in range(nsteps):
             lr, reglam = schedule(t)
@@ -450,7 +454,8 @@ def precision_form(pkg, chains, samples, steps, local):
     em = steps_of(pkg.PRECISION_MIXED, small, samples, 1)[0][0]
     ef = steps_of(pkg.PRECISION_FP64, small, samples, 1)[0][0]
     return {"shape": "N64 M128 K4", "h": h, "chains": chains, "samples_per_chain": samples, "burn_in": BURN,
-            "precision": "mixed", "ms_per_step": ms, "value": chains * samples / (ms * 1e-3), "unit": "MC samples/s",
+            "precision": "mixed", "energy_ratios": "FP32 (NQES_OPT_MIXED_ENERGY64 0)",
+            "ms_per_step": ms, "value": chains * samples / (ms * 1e-3), "unit": "MC samples/s",
             "minres_iters_mean": float(np.mean([i["minres_iters"] for _, i in full[1:]])),
             "exact_decision_rate": float(np.mean([i["exact_decisions"] / i["proposals"] for _, i in full[1:]])),
             "energies_per_site": [float(x) for x in full[-1][0]],
