@@ -77,6 +77,7 @@ __device__ __forceinline__ void frows_body(const FactArgs &F, const float *__res
     const int rows_here = min(spb, F.Ns - bid * spb) * K;
     const int rl0 = rg * RB;                       // first local row of the group
     const size_t rbase = size_t(bid) * spb * K;
+    const FastDiv dK = fast_div(unsigned(K));
     uint64_t b0[RB], b1[RB];
 #pragma unroll
     for (int rb = 0; rb < RB; rb++) {
@@ -151,13 +152,15 @@ __device__ __forceinline__ void frows_body(const FactArgs &F, const float *__res
 #pragma unroll
             for (int rb = 0; rb < RB; rb++) a[rb] = fmaf(sgn(b0[rb], b1[rb], i), va, a[rb]);
         }
-        // dot with the row's tanh values, times B
+        // dot with the row's tanh values, times B (rbase is a multiple of K: the
+        // row's sample and configuration from the local row alone)
 #pragma unroll
         for (int rb = 0; rb < RB; rb++) {
             const int rl = rl0 + rb;
             if (rl < rows_here) {
-                const size_t r = rbase + rl, s = r / K;
-                const int kk = int(r - s * K), q = k * K + kk;
+                const unsigned sl = fdiv(unsigned(rl), dK);
+                const size_t s = size_t(bid) * spb + sl;
+                const int kk = rl - int(sl) * K, q = k * K + kk;
                 const float *tr = F.T + (s * KK + q) * size_t(MT);
                 float d = a[rb];
 #pragma unroll
@@ -257,6 +260,11 @@ __device__ __forceinline__ void fcols_body(const FactArgs &F, int mode, int gn, 
     const size_t r0 = nrows * c / F.rchunks, r1 = nrows * (c + 1) / F.rchunks;
     const int nbat = int((r1 - r0 + kStage - 1) / kStage);
     const int nf = mode == 3 ? 2 : 1;
+    // row -> (sample, configuration) and piece -> (row, 16 bytes) by high
+    // multiplies while the row indices fit (uniform over the launch)
+    const FastDiv dvpr = fast_div(unsigned(vpr)), dper = fast_div(unsigned(MT / 4));
+    const bool fast = nrows < (size_t(1) << 32) / size_t(vpr);
+    auto sample_of = [&](size_t r) -> size_t { return fast ? size_t(fdiv(unsigned(r), dvpr)) : r / vpr; };
     // zero the column padding of all buffers once (copies write [0, MT) only)
     for (int t = threadIdx.x; t < 2 * 2 * kStage * WS; t += kThreads) st[t] = 0.f;
     __syncthreads();
@@ -268,8 +276,9 @@ __device__ __forceinline__ void fcols_body(const FactArgs &F, int mode, int gn, 
         const int nb = int(min(size_t(kStage), r1 - rb0));
         const int per = MT / 4;  // 16-byte pieces per row
         for (int t = threadIdx.x; t < nf * nb * per; t += kThreads) {
-            const int f = t / (nb * per), rem = t - f * nb * per, rr = rem / per, pc = rem - rr * per;
-            const size_t r = rb0 + rr, s = r / vpr;
+            const int f = t >= nb * per ? 1 : 0, rem = t - f * nb * per;
+            const int rr = int(fdiv(unsigned(rem), dper)), pc = rem - rr * per;
+            const size_t r = rb0 + rr, s = sample_of(r);
             int kk = int(r - s * vpr), kk2 = kk;
             if (mode == 3) {
                 int a = 0;
@@ -286,7 +295,7 @@ __device__ __forceinline__ void fcols_body(const FactArgs &F, int mode, int gn, 
         cp_async_commit();
         if (threadIdx.x < nb) {
             const int rr = threadIdx.x;
-            const size_t r = rb0 + rr, s = r / vpr;
+            const size_t r = rb0 + rr, s = sample_of(r);
             int kk = int(r - s * vpr), kk2 = -1;
             if (mode == 3) {
                 int a = 0;

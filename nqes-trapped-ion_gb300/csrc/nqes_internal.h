@@ -237,6 +237,22 @@ cudaError_t launch_frows_group(int variant, const FactMember *tab, const int *fi
 cudaError_t launch_fcols_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
                                cudaStream_t st);
 
+// x / d by one high multiply for 32-bit x < 2^32 / d: with m = ceil(2^32 / d)
+// and e = m d - 2^32 < d, x m / 2^32 = x / d + x e / (d 2^32) and the second
+// term stays below 1/d, so the floor is exact (d = 1: x itself). Integer
+// divisions by a run-time divisor cost tens of instructions; the index math
+// of the factored passes' staging and epilogues uses this instead.
+struct FastDiv {
+    unsigned d, m;
+};
+__host__ __device__ inline FastDiv fast_div(unsigned d) {
+    FastDiv f;
+    f.d = d;
+    f.m = d <= 1 ? 0u : unsigned((0x100000000ULL + d - 1) / d);
+    return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned x, FastDiv f) { return f.d <= 1 ? x : __umulhi(x, f.m); }
+
 // Solve m of a grouped launch owns blocks first[m] .. first[m + 1] - 1.
 __device__ __forceinline__ int group_member(const int *__restrict__ first, int n, int b) {
     int lo = 0, hi = n - 1;
