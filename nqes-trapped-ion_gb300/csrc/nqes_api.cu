@@ -371,6 +371,10 @@ MixedArgs mixed_args(nqes_ctx *ctx, int chains, int m, int burn, int tk) {
     A.bl = ctx->dbl;
     A.bnd = ctx->dbnd;
     A.etab = ctx->etab;
+    A.fdN = fast_div(unsigned(ctx->sh.N));
+    A.fdM = fast_div(unsigned(ctx->sh.M));
+    A.fdMP = fast_div(unsigned(std::max(ctx->dw_MP, 1)));
+    A.fdMT = fast_div(unsigned(fact_mt(ctx->sh.M)));
     A.G = ctx->dw_G;
     A.U = ctx->dw_U;
     A.MP = ctx->dw_MP;

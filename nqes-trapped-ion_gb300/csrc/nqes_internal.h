@@ -72,6 +72,22 @@ cudaError_t launch_eval_singular(int count, int K, const cplx *phi, const cplx *
 // Mixed-precision sampler (real weights): FP32 factors, products and accept
 // decisions with a certified error bound, FP64 shadow of theta, exact FP64
 // Phi after every sweep, exact FP64 decision when the bound is inconclusive.
+// x / d by one high multiply for 32-bit x < 2^32 / d: with m = ceil(2^32 / d)
+// and e = m d - 2^32 < d, x m / 2^32 = x / d + x e / (d 2^32) and the second
+// term stays below 1/d, so the floor is exact (d = 1: x itself). Integer
+// divisions by a run-time divisor cost tens of instructions; the index math
+// of the factored passes' staging and epilogues uses this instead.
+struct FastDiv {
+    unsigned d, m;
+};
+__host__ __device__ inline FastDiv fast_div(unsigned d) {
+    FastDiv f;
+    f.d = d;
+    f.m = d <= 1 ? 0u : unsigned((0x100000000ULL + d - 1) / d);
+    return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned x, FastDiv f) { return f.d <= 1 ? x : __umulhi(x, f.m); }
+
 struct MixedArgs {
     Shape sh;
     int chains, m, burn, tk;
@@ -94,6 +110,7 @@ struct MixedArgs {
     const float *cpl, *spl;              // the roundings' remainders: cosh(2w) - cp, sinh(2w) - spp [kk][i][MP]
     const float *bnd;                    // per (kk, i): float4 bound record, then per kk 2 max_j sum_i |w_ij|
     const double *etab;                  // e^{-n/64}, n < kExpTabN (nqes_math.cuh exp_neg_tab)
+    FastDiv fdN, fdM, fdMP, fdMT;        // the divisors N, M, MP and fact_mt(M) of the index math
     int G, U, MP;
     int stage;                           // 1: bulk-copy cp, spp, whp, wlp into shared memory first
     int stage_fault;                     // test hook (NQES_OPT_TEST_STAGE_WAIT): the staging wait runs out
@@ -236,22 +253,6 @@ cudaError_t launch_frows_group(int variant, const FactMember *tab, const int *fi
                                cudaStream_t st);
 cudaError_t launch_fcols_group(int variant, const FactMember *tab, const int *first, int n, int blocks, size_t smem,
                                cudaStream_t st);
-
-// x / d by one high multiply for 32-bit x < 2^32 / d: with m = ceil(2^32 / d)
-// and e = m d - 2^32 < d, x m / 2^32 = x / d + x e / (d 2^32) and the second
-// term stays below 1/d, so the floor is exact (d = 1: x itself). Integer
-// divisions by a run-time divisor cost tens of instructions; the index math
-// of the factored passes' staging and epilogues uses this instead.
-struct FastDiv {
-    unsigned d, m;
-};
-__host__ __device__ inline FastDiv fast_div(unsigned d) {
-    FastDiv f;
-    f.d = d;
-    f.m = d <= 1 ? 0u : unsigned((0x100000000ULL + d - 1) / d);
-    return f;
-}
-__device__ __forceinline__ unsigned fdiv(unsigned x, FastDiv f) { return f.d <= 1 ? x : __umulhi(x, f.m); }
 
 // Solve m of a grouped launch owns blocks first[m] .. first[m + 1] - 1.
 __device__ __forceinline__ int group_member(const int *__restrict__ first, int n, int b) {

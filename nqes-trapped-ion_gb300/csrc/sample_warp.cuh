@@ -172,7 +172,7 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
     // of each table per spin and four independent double-float chains, so a
     // thread has four loads and sums in flight instead of one
     for (int qd = tid; qd < K * MP / 4; qd += T) {
-        const int j0 = qd * 4 - (qd * 4 / MP) * MP, kk = qd * 4 / MP, q = k * K + kk;
+        const int kk = int(fdiv(unsigned(qd * 4), A.fdMP)), j0 = qd * 4 - kk * MP, q = k * K + kk;
         const float4 bh4 = *reinterpret_cast<const float4 *>(A.bh + kk * MP + j0);
         const float4 bl4 = *reinterpret_cast<const float4 *>(A.bl + kk * MP + j0);
         float h[4] = {bh4.x, bh4.y, bh4.z, bh4.w}, l[4] = {bl4.x, bl4.y, bl4.z, bl4.w};
@@ -634,6 +634,9 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
     const int lane = htid & 31, hw = htid >> 5, nhw = HT >> 5;
     const bool writer = htid == 0;
     const bool e64 = A.out64 || A.e64;
+    // index math by high multiplies with the launch's divisors (MixedArgs;
+    // every index below is far under 2^32 / divisor)
+    auto divN = [&](int x) { return int(fdiv(unsigned(x), A.fdN)); };
 
     // ---- sample: local energy and log-derivatives. Mixed form: FP32 flip
     // ratios combined in FP64, O as its FP32 factors. FP64 outputs: tanh of
@@ -694,7 +697,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
         // pipe, two units per packed instruction (padded units are exactly
         // 1: t = 0, c = 1, s = 0), to a few 2^-44 per factor.
         for (int e = htid; e < KK * MP; e += HT) {
-            const int q = e / MP, j = e - q * MP;
+            const int q = int(fdiv(unsigned(e), A.fdMP)), j = e - q * MP;
             float *tf = reinterpret_cast<float *>(sm.t64) + size_t(q) * 2 * MP + dfpair_hi(j);
             if (A.e64 == 2) {
                 const float t = sm.t[e];  // 0 in the padding
@@ -716,7 +719,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
             uint64_t sg;
         };
         auto rat_row = [&](int it) {
-            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const int q = divN(it), i = it - q * N, k = q / K, kk = q - k * K;
             const bool down = down_bit(spin + k * NW, i);
             const size_t o = (size_t(kk) * N + i) * MP;
             return RatRow{sm.tc + o, sm.ts + o, A.cpl + o, A.spl + o,
@@ -762,7 +765,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
             df_mul(h[0], l[0], h[1], l[1]);
             df_mul(h[2], l[2], h[3], l[3]);
             df_mul(h[0], l[0], h[2], l[2]);
-            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const int q = divN(it), i = it - q * N, k = q / K, kk = q - k * K;
             const bool down = down_bit(spin + k * NW, i);
             rat64[it] = (double(h[0]) + double(l[0])) * (down ? A.edn64 : A.eup64)[kk * N + i];
         };
@@ -786,13 +789,13 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
         }
     } else if (e64) {
         for (int e = htid; e < KK * MP; e += HT) {
-            const int j = e % MP;
+            const int j = e - int(fdiv(unsigned(e), A.fdMP)) * MP;
             sm.t64[e] = j < M ? tanh(double(sm.th_hi[e]) + double(sm.th_lo[e])) : 0.0;
         }
         sync();
         double *rat64 = reinterpret_cast<double *>(sm.rat);  // the rat and bsig space: KK*N doubles
         for (int it = htid; it < KK * N; it += HT) {
-            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const int q = divN(it), i = it - q * N, k = q / K, kk = q - k * K;
             const bool down = down_bit(spin + k * NW, i);
             // sigma t = t (spin down) or -t: the sign by an integer XOR, so that a
             // factor costs one FMA and one multiply on the FP64 pipe
@@ -811,7 +814,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
         }
     } else {
         for (int it = htid; it < KK * N; it += HT) {
-            const int q = it / N, i = it - q * N, k = q / K, kk = q - k * K;
+            const int q = divN(it), i = it - q * N, k = q / K, kk = q - k * K;
             const bool down = down_bit(spin + k * NW, i);
             const float *crow = sm.tc + (size_t(kk) * N + i) * MP;
             const float *srow = sm.ts + (size_t(kk) * N + i) * MP;
@@ -887,7 +890,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
             float2 *Dm2 = reinterpret_cast<float2 *>(sm.Dm);   // K*K
             bool ok = true;
             for (int e = htid; e < KK * N; e += HT) {
-                const int q = e / N, i = e - q * N, k = q / K, kk = q - k * K;
+                const int q = divN(e), i = e - q * N, k = q / K, kk = q - k * K;
                 const double b = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
                 float h, l;
                 ok &= df_split(down_bit(spin + kk * NW, i) ? -b : b, h, l);
@@ -906,7 +909,10 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
             sync();
             float2 *orow2 = reinterpret_cast<float2 *>(A.O64 + s * size_t(A.sh.P));
             for (int e = htid; e < K * L; e += HT) {
-                const int k = e / L, p = e - k * L;
+                int k = 0;
+#pragma unroll
+                for (int t = 1; t < K; t++) k += e >= t * L ? 1 : 0;
+                const int p = e - k * L;
                 float sh = 0.f, sl = 0.f;
                 if (p < N) {
 #pragma unroll
@@ -922,7 +928,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
                         df_fma(sh, sl, d.x, d.y, t.x, t.y);
                     }
                 } else {
-                    const int i = (p - N - M) / M, j = (p - N - M) - i * M;
+                    const int i = int(fdiv(unsigned(p - N - M), A.fdM)), j = (p - N - M) - i * M;
 #pragma unroll
                     for (int kk = 0; kk < K; kk++) {
                         const float2 b = bs2[(k * K + kk) * N + i], t = t2[(kk * K + k) * MP + j];
@@ -939,7 +945,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
         }
         double *bs = reinterpret_cast<double *>(sm.rat);  // K*K*N doubles: the rat and bsig space
         for (int e = htid; e < KK * N; e += HT) {
-            const int q = e / N, i = e - q * N, k = q / K, kk = q - k * K;
+            const int q = divN(e), i = e - q * N, k = q / K, kk = q - k * K;
             const double b = sm.pinv[k * K + kk] * sm.phi[kk * K + k];
             bs[e] = down_bit(spin + kk * NW, i) ? -b : b;
         }
@@ -948,7 +954,10 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
         double *orow = A.O64 + s * size_t(A.sh.P);
         bool split_ok = true;
         for (int e = htid; e < K * L; e += HT) {
-            const int k = e / L, p = e - k * L;
+            int k = 0;
+#pragma unroll
+            for (int t = 1; t < K; t++) k += e >= t * L ? 1 : 0;
+            const int p = e - k * L;
             double v = 0.0;
             if (p < N) {
 #pragma unroll
@@ -958,7 +967,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
 #pragma unroll
                 for (int kk = 0; kk < K; kk++) v = fma(sm.Dm[k * K + kk], sm.t64[(kk * K + k) * MP + j], v);
             } else {
-                const int i = (p - N - M) / M, j = (p - N - M) - i * M;
+                const int i = int(fdiv(unsigned(p - N - M), A.fdM)), j = (p - N - M) - i * M;
 #pragma unroll
                 for (int kk = 0; kk < K; kk++) v = fma(bs[(k * K + kk) * N + i], sm.t64[(kk * K + k) * MP + j], v);
             }
@@ -975,7 +984,7 @@ __device__ __forceinline__ void sample_phase(const MixedArgs &A, DSmem &sm, cons
         const int MT = fact_mt(M);
         float *ft = A.FT + s * size_t(KK) * MT;
         for (int e = htid; e < KK * MT; e += HT) {
-            const int q = e / MT, j = e - q * MT, k = q / K, kk = q - k * K;
+            const int q = int(fdiv(unsigned(e), A.fdMT)), j = e - q * MT, k = q / K, kk = q - k * K;
             ft[e] = j < M ? sm.t[(kk * K + k) * MP + j] : 0.f;
         }
         if (htid < KK) A.FB[s * KK + htid] = sm.Bm[htid];
