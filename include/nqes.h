@@ -84,7 +84,7 @@ extern "C" {
                                       * bound cannot decide. */
 #define NQES_OPT_SAMPLER_PLAN 12     /* launch plan of the decision-warp sampler (MIXED, CERTIFIED real):
                                       * 0 (default): planned from the chains (and the autotuner when on);
-                                      * else the warps per chain (1, 2 or 4), plus 16 to stage the step's
+                                      * else the warps per chain (1, 2, 4 or 8), plus 16 to stage the step's
                                       * tables in shared memory. Results do not depend on the plan. */
 
 /* Precision of the SR step (nqes_set_option NQES_OPT_PRECISION).

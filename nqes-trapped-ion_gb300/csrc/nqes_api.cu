@@ -444,7 +444,12 @@ void dw_plan(nqes_ctx *ctx, int chains, int *warps, int *stage) {
     if (ctx->plan_chains) chains = ctx->plan_chains;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    for (int w = 4; w >= 1; w >>= 1)
+    // the certified form's samples (FP64 tanh and flip ratios, the O row) go to
+    // the helper warps beside the sweep: seven helpers keep them off its path
+    // (128 chains at N32 M64 K2: 12.9 against 14.8 ms with three); the mixed
+    // form's lighter samples gain nothing from more than four warps
+    const int wmax = certified_dw(ctx) ? 8 : 4;
+    for (int w = wmax; w >= 1; w >>= 1)
         for (int st = 1; st >= 0; st--) {
             const size_t smem = dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1, dw_energy64(ctx));
             if (smem > 227 * 1024) continue;
@@ -886,7 +891,7 @@ template <class S> int tune_sampler(nqes_ctx *ctx, int chains, int m, int burn) 
     if (mixed && ctx->dw_U) {
         NQES_CUDA(prepare_mixed_sampler(ctx));
         int bw = 0, bs = 0;
-        for (int w = 1; w <= 4; w <<= 1)
+        for (int w = 1; w <= (certified_dw(ctx) ? 8 : 4); w <<= 1)
             for (int st = 0; st <= 1; st++) {
                 if (dw_smem_bytes(ctx->sh, ctx->dw_MP, st == 1, dw_energy64(ctx)) > 227 * 1024) continue;
                 ctx->dw_force_warps = w;
@@ -1189,8 +1194,8 @@ int nqes_set_option(nqes_ctx *ctx, int option, int64_t value) {
         return NQES_OK;
     case NQES_OPT_SAMPLER_PLAN: {
         const int w = int(value & 15);
-        if (value < 0 || value > 31 || (value != 0 && w != 1 && w != 2 && w != 4)) {
-            ctx->err = "sampler plan must be 0, or 1, 2 or 4 warps plus 16 for staged tables";
+        if (value < 0 || value > 31 || (value != 0 && w != 1 && w != 2 && w != 4 && w != 8)) {
+            ctx->err = "sampler plan must be 0, or 1, 2, 4 or 8 warps plus 16 for staged tables";
             return NQES_ERR_INVALID;
         }
         ctx->autotune = false;
