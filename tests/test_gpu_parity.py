@@ -99,16 +99,22 @@ def test_sr_step_parity(pkg, N, M, K, real):
     assert rel_err(ctx.apply_S(v), orc.apply_S(v)) < 1e-11
     # Solver: both stop on the reference's criteria; the GPU solution meets the
     # MINRES-QLP relative-residual bound when checked with the oracle's S.
+    # Iteration counts: equal or one apart where S is well sampled (72 samples
+    # for P < 2000 parameters; measured 0 or 1 apart); with 12 samples for
+    # ~9000 parameters S is the regulariser plus a rank-12 term and the count
+    # follows the operators' 1e-12 differences further (measured 421 vs 440).
     assert info["minres_flag"] == int(oinfo["flag"])
     it_g, it_o = int(info["minres_iters"]), int(oinfo["iters"])
-    assert abs(it_g - it_o) <= max(2, it_o // 10), (it_g, it_o)
+    small = ctx.P < 2000
+    assert abs(it_g - it_o) <= (1 if small else it_o // 10), (it_g, it_o)
     x = ctx.get_solution()
     r = np.linalg.norm(orc.apply_S(x) - fo)
     assert r <= 10 * 1e-9 * (info["anorm"] * np.linalg.norm(x) + np.linalg.norm(fo)), r
+    # updated weights: both solves stop at rtol 1e-9 (measured <= 6.6e-8 and 5.0e-7)
     ag, bg, wg = ctx.get_weights()
     ao, bo, wo = orc.get_weights()
     assert rel_err(np.concatenate([ag.ravel(), bg.ravel(), wg.ravel()]),
-                   np.concatenate([ao.ravel(), bo.ravel(), wo.ravel()])) < 1e-4
+                   np.concatenate([ao.ravel(), bo.ravel(), wo.ravel()])) < (1e-6 if small else 5e-6)
     ctx.close()
 
 
