@@ -417,3 +417,32 @@ def test_mixed_energies_along_the_fp64_trajectory(pkg, mode):
     assert worst <= (1e-6 if mode == 2 else 1e-10)
     f.close()
     x.close()
+
+
+@pytest.mark.parametrize("N,M,K,prec", [(32, 64, 2, 1), (32, 64, 2, 2), (12, 24, 3, 1), (20, 40, 1, 2)])
+def test_sampler_plan_does_not_change_results(pkg, N, M, K, prec):
+    """NQES_OPT_SAMPLER_PLAN: one, two, four or eight warps per chain, tables
+    staged or read from global memory, give the same bits (configurations,
+    local energies, e_mat, updated weights): the helper warps form the samples
+    in a fixed order whatever their number."""
+    J = synthetic_j(N)
+    w = helpers.random_weights(N, M, K, 0.02, 17 + N, real=True)
+    ref = None
+    for plan in (0, 1, 2, 4, 8, 17, 18, 20, 24):
+        ctx = pkg.Context(N, M, K, J, 0.595)
+        ctx.set_weights(*w)
+        ctx.set_option(pkg.OPT_PRECISION, prec)
+        ctx.set_option(pkg.OPT_SAMPLER_PLAN, plan)
+        e, info = ctx.sr_step(321, 24, 10, 6, 0.1, 5.0, 1e-9, 2000)
+        spins, eloc, E = ctx.get_samples()
+        got = dict(e=e, spins=spins, E=E, w=np.concatenate([x.ravel() for x in ctx.get_weights()]),
+                   it=info["minres_iters"])
+        ctx.close()
+        if ref is None:
+            ref = got
+            continue
+        assert np.array_equal(got["spins"], ref["spins"]), plan
+        assert np.array_equal(got["E"], ref["E"]), plan
+        assert np.array_equal(got["e"], ref["e"]), plan
+        assert got["it"] == ref["it"], plan
+        assert np.array_equal(got["w"], ref["w"]), plan
