@@ -95,6 +95,35 @@ def test_grouped_loop_body_equals_individual_steps(pkg):
         c.close()
 
 
+def test_tensor_core_members_equal_individual_steps(pkg):
+    """Members with both factored passes on the tensor cores
+    (NQES_OPT_TENSOR_CORES 2: their rows and column passes run as their own
+    launches inside the grouped loop body) beside a member in the grouped
+    CUDA-core passes: each equals nqes_sr_step on it, bit for bit."""
+    spec = [(16, 32, 2, 0.6, 1.2, 1, True), (20, 40, 3, 0.8, 1.0, 1, True), (16, 32, 2, 0.7, 1.3, 1, True)]
+    tcs = [2, 2, 1]
+    alone = [make(pkg, i, s) for i, s in enumerate(spec)]
+    mixed = [make(pkg, i, s) for i, s in enumerate(spec)]
+    for c, d, tc in zip(alone, mixed, tcs):
+        c.set_option(pkg.OPT_TENSOR_CORES, tc)
+        d.set_option(pkg.OPT_TENSOR_CORES, tc)
+    batch = pkg.Batch(mixed)
+    n = len(spec)
+    for t in range(2):
+        seeds, chains, m, burn, lr, reglam, rtol, maxit = step_args(t, n)
+        emats, infos, stats, _ = batch.sr_step(seeds, chains, m, burn, lr, reglam, rtol, maxit)
+        assert stats == [0] * n
+        for i, c in enumerate(alone):
+            e, info = c.sr_step(seeds[i], chains[i], m[i], burn[i], lr[i], reglam[i], rtol[i], maxit[i])
+            assert np.array_equal(e, emats[i]), (t, i)
+            assert info["minres_iters"] == infos[i]["minres_iters"], (t, i)
+            for x, y in zip(c.get_weights(), mixed[i].get_weights()):
+                assert np.array_equal(x, y), (t, i)
+    batch.close()
+    for c in alone + mixed:
+        c.close()
+
+
 def test_large_rows_group_equals_individual_steps(pkg):
     """A rows group of the loop body with more than six waves of blocks runs
     the rows pass with four rows a thread group (half the blocks of the
