@@ -8,7 +8,7 @@
 //
 // Here a persistent CTA per SM owns a contiguous range of rows and streams
 // them through shared memory in groups of G rows, NB groups deep (a ring of
-// buffers, each filled by a bulk copy (cp.async.bulk) on its own mbarrier,
+// buffers, each filled by bulk copies (cp.async.bulk, one per row) on its own mbarrier,
 // bounded waits), so that up to NB - 1 groups are in flight while one is
 // used. For each staged group
 //   pass 1: u_r = O_r . v, rows taken in pairs: each thread's two partial
@@ -61,10 +61,11 @@ struct FusedSvArgs {
     const int *guard;
 };
 
-// Dynamic shared memory of a launch: NB groups of G rows, the warps'
+// Dynamic shared memory of a launch: NB groups of G rows of Q >= P entries
+// (each row padded with zeros to the block's T C columns), the warps'
 // partials of the group's u (float2 [G][warps]), NB mbarriers.
-__host__ __device__ inline size_t fused_smem(int P, int G, int NB) {
-    return size_t(NB) * G * P * sizeof(double) + size_t(G) * kFsMaxWarps * sizeof(float2) +
+__host__ __device__ inline size_t fused_smem(int Q, int G, int NB) {
+    return size_t(NB) * G * Q * sizeof(double) + size_t(G) * kFsMaxWarps * sizeof(float2) +
            size_t(NB) * sizeof(uint64_t);
 }
 
@@ -84,40 +85,48 @@ __device__ __forceinline__ void warp_sum_pair(float &h, float &l, float h0, floa
         df_acc(h, l, __shfl_xor_sync(0xffffffffu, h, off), __shfl_xor_sync(0xffffffffu, l, off));
 }
 
-// Block: T = blockDim.x threads (a multiple of 32, T C >= P); thread t owns
-// columns p = t + c T (c < C), holding v's split and its partial of O^T u for
-// them in registers.
+// Block: T = blockDim.x threads (a multiple of 32, Q = T C >= P); thread t
+// owns the C consecutive columns p = t C + c (c < C), holding v's split and
+// its partial of O^T u for them in registers. Rows sit in shared memory at
+// stride Q with the columns P..Q-1 zero (v is zero there too), so the inner
+// loops carry no column test and address a thread's entries at fixed offsets
+// from its row pointer; with C odd, the 8-byte entries of a half-warp fall in
+// distinct bank pairs.
 template <int C, int MaxT, bool PRE>
 __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     extern __shared__ __align__(16) unsigned char fs_smem[];
     if (loop_guard_off(a.guard)) return;
     const int P = a.P, G = a.G, NB = a.NB, T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5,
-              nw = T >> 5;
-    if (!dyn_smem_covers(fused_smem(P, G, NB)) || nw > kFsMaxWarps || T * C < P || G > kFsMaxG || NB < 2 ||
+              nw = T >> 5, Q = T * C;
+    if (!dyn_smem_covers(fused_smem(Q, G, NB)) || nw > kFsMaxWarps || Q < P || G > kFsMaxG || NB < 2 ||
         NB > kFsMaxNB) {
         if (tid == 0) atomicOr(a.err, kErrLaunch);
         return;
     }
-    double *bufs = reinterpret_cast<double *>(fs_smem);                   // [NB][G][P]
-    float2 *red = reinterpret_cast<float2 *>(bufs + size_t(NB) * G * P);  // [G][kFsMaxWarps]
+    double *bufs = reinterpret_cast<double *>(fs_smem);                   // [NB][G][Q]
+    float2 *red = reinterpret_cast<float2 *>(bufs + size_t(NB) * G * Q);  // [G][kFsMaxWarps]
     uint64_t *mbar = reinterpret_cast<uint64_t *>(red + size_t(G) * kFsMaxWarps);  // [NB]
     const int r0 = int(int64_t(a.Ns) * blockIdx.x / gridDim.x), r1 = int(int64_t(a.Ns) * (blockIdx.x + 1) / gridDim.x);
     const int ngroups = (r1 - r0 + G - 1) / G;
+    const int p0 = tid * C;  // this thread's first column
 
     float vh[C], vl[C], yh[C], yl[C];
     bool range_ok = true;  // of the O entries (v is not checked: a solve that never starts has v = 0/0)
 #pragma unroll
     for (int c = 0; c < C; c++) {
-        const int p = tid + c * T;
         vh[c] = vl[c] = yh[c] = yl[c] = 0.f;
-        if (p < P) df_split(a.v[p], vh[c], vl[c]);
+        if (p0 + c < P) df_split(a.v[p0 + c], vh[c], vl[c]);
     }
-    auto issue = [&](int g) {  // thread 0: group g into ring slot g % NB
+    // the padding of every staged row: zero once (the copies write [0, P) only)
+    const int pad = Q - P;
+    for (int i = tid; i < NB * G * pad; i += T) bufs[size_t(i / pad) * Q + P + i % pad] = 0.0;
+    auto issue = [&](int g) {  // thread 0: group g into ring slot g % NB, one copy per row
         const int rs = r0 + g * G, nr = min(G, r1 - rs);
-        const unsigned bytes = unsigned(size_t(nr) * P * sizeof(double));
         uint64_t *mb = &mbar[g % NB];
-        mbar_expect_tx(mb, bytes);
-        bulk_g2s(bufs + size_t(g % NB) * G * P, a.O + size_t(rs) * P, bytes, mb);
+        double *dst = bufs + size_t(g % NB) * G * Q;
+        mbar_expect_tx(mb, unsigned(size_t(nr) * P * sizeof(double)));
+        for (int i = 0; i < nr; i++)
+            bulk_g2s(dst + size_t(i) * Q, a.O + size_t(rs + i) * P, unsigned(size_t(P) * sizeof(double)), mb);
     };
     if (tid == 0)
         for (int b = 0; b < NB; b++) mbar_init(&mbar[b], 1);
@@ -125,49 +134,52 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     if (tid == 0)
         for (int g = 0; g < min(NB, ngroups); g++) issue(g);
 
-    // thread's partial dot of row `row` with v (two chains over its columns);
-    // FP64 entries are split in place (each thread its own columns, read back
-    // only by itself in pass 2)
-    auto row_dot = [&](double *row, float &h, float &l) {
-        float h2 = 0.f, l2 = 0.f;
-        h = l = 0.f;
-#pragma unroll
-        for (int c = 0; c < C; c++) {
-            const int p = tid + c * T;
-            if (p < P) {
-                float oh, ol;
-                if (PRE) {  // split when it was written
-                    const float2 o = *reinterpret_cast<const float2 *>(row + p);
-                    oh = o.x;
-                    ol = o.y;
-                } else {
-                    range_ok &= df_split(row[p], oh, ol);
-                    *reinterpret_cast<float2 *>(row + p) = make_float2(oh, ol);
-                }
-                if (c & 1)
-                    df_fma(h2, l2, oh, ol, vh[c], vl[c]);
-                else
-                    df_fma(h, l, oh, ol, vh[c], vl[c]);
-            }
+    // entry c of the thread's part of a staged row as (hi, lo); FP64 entries
+    // are split in place (each thread its own columns, read back only by
+    // itself in pass 2)
+    auto entry = [&](double *row, int c, float &oh, float &ol) {
+        if (PRE) {  // split when it was written
+            const float2 o = *reinterpret_cast<const float2 *>(row + c);
+            oh = o.x;
+            ol = o.y;
+        } else {
+            range_ok &= df_split(row[c], oh, ol);
+            *reinterpret_cast<float2 *>(row + c) = make_float2(oh, ol);
         }
-        df_acc(h, l, h2, l2);
     };
 
     bool timed_out = false;
     int g = 0;
     for (; g < ngroups; g++) {
-        double *buf = bufs + size_t(g % NB) * G * P;
+        double *buf = bufs + size_t(g % NB) * G * Q;
         const int nr = min(G, r1 - (r0 + g * G));
         const bool ok = mbar_wait(&mbar[g % NB], unsigned(g / NB) & 1u);
         if (__syncthreads_or(!ok)) {
             timed_out = true;
             break;
         }
-        // pass 1: rows in pairs; the warp's sums of rows r and r + 1 to red
+        // pass 1: rows in pairs, one chain per row; the warp's sums of rows
+        // r and r + 1 to red
         for (int r = 0; r < nr; r += 2) {
-            float h0, l0, h1 = 0.f, l1 = 0.f;
-            row_dot(buf + size_t(r) * P, h0, l0);
-            if (r + 1 < nr) row_dot(buf + size_t(r + 1) * P, h1, l1);
+            double *row0 = buf + size_t(r) * Q + p0, *row1 = row0 + Q;
+            float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+            if (r + 1 < nr) {
+#pragma unroll
+                for (int c = 0; c < C; c++) {
+                    float oh, ol, qh, ql;
+                    entry(row0, c, oh, ol);
+                    entry(row1, c, qh, ql);
+                    df_fma(h0, l0, oh, ol, vh[c], vl[c]);
+                    df_fma(h1, l1, qh, ql, vh[c], vl[c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < C; c++) {
+                    float oh, ol;
+                    entry(row0, c, oh, ol);
+                    df_fma(h0, l0, oh, ol, vh[c], vl[c]);
+                }
+            }
             float h, l;
             warp_sum_pair(h, l, h0, l0, h1, l1);
             if (lane == 0) red[r * kFsMaxWarps + warp] = make_float2(h, l);
@@ -178,26 +190,28 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
         // in warp order), then y_p += O_rp u_r
         for (int r = 0; r < nr; r += 2) {
             const bool two = r + 1 < nr;
-            float2 p0 = make_float2(0.f, 0.f), p1 = make_float2(0.f, 0.f);
+            float2 s0 = make_float2(0.f, 0.f), s1 = make_float2(0.f, 0.f);
             if (lane < nw) {
-                p0 = red[r * kFsMaxWarps + lane];
-                if (two) p1 = red[(r + 1) * kFsMaxWarps + lane];
+                s0 = red[r * kFsMaxWarps + lane];
+                if (two) s1 = red[(r + 1) * kFsMaxWarps + lane];
             }
             float h, l;
-            warp_sum_pair(h, l, p0.x, p0.y, p1.x, p1.y);
+            warp_sum_pair(h, l, s0.x, s0.y, s1.x, s1.y);
             const float u0h = __shfl_sync(0xffffffffu, h, 0), u0l = __shfl_sync(0xffffffffu, l, 0);
             const float u1h = __shfl_sync(0xffffffffu, h, 16), u1l = __shfl_sync(0xffffffffu, l, 16);
-            const double *row0 = buf + size_t(r) * P, *row1 = row0 + P;
+            const float2 *row0 = reinterpret_cast<const float2 *>(buf + size_t(r) * Q + p0), *row1 = row0 + Q;
+            if (two) {
 #pragma unroll
-            for (int c = 0; c < C; c++) {
-                const int p = tid + c * T;
-                if (p < P) {
-                    const float2 o = *reinterpret_cast<const float2 *>(row0 + p);
+                for (int c = 0; c < C; c++) {
+                    const float2 o = row0[c], q = row1[c];
                     df_fma(yh[c], yl[c], o.x, o.y, u0h, u0l);
-                    if (two) {
-                        const float2 o1 = *reinterpret_cast<const float2 *>(row1 + p);
-                        df_fma(yh[c], yl[c], o1.x, o1.y, u1h, u1l);
-                    }
+                    df_fma(yh[c], yl[c], q.x, q.y, u1h, u1l);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < C; c++) {
+                    const float2 o = row0[c];
+                    df_fma(yh[c], yl[c], o.x, o.y, u0h, u0l);
                 }
             }
         }
@@ -217,17 +231,15 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
     }
     if (!range_ok) atomicOr(a.err, kErrNonFinite);
 #pragma unroll
-    for (int c = 0; c < C; c++) {
-        const int p = tid + c * T;
-        if (p < P) a.ypart[size_t(blockIdx.x) * P + p] = double(yh[c]) + double(yl[c]);
-    }
+    for (int c = 0; c < C; c++)
+        if (p0 + c < P) a.ypart[size_t(blockIdx.x) * P + p0 + c] = double(yh[c]) + double(yl[c]);
 }
 
 // Columns per thread C and threads per block T (whole warps, T C >= P): the
-// fewest columns whose block fits its register budget: C <= 6 with up to
-// 1024 threads (64 registers), 8 with up to 768, 16 with up to 512.
-constexpr int kFsShapes[8][2] = {{1, 1024}, {2, 1024}, {3, 1024}, {4, 1024},
-                                 {5, 1024}, {6, 1024}, {8, 768},  {16, 512}};
+// fewest columns whose block fits its register budget, C odd (conflict-free
+// shared-memory reads): C <= 5 with up to 1024 threads (64 registers), 7 with
+// up to 768, 9 with up to 640, 17 with up to 512.
+constexpr int kFsShapes[6][2] = {{1, 1024}, {3, 1024}, {5, 1024}, {7, 768}, {9, 640}, {17, 512}};
 bool fused_shape(int P, int *C, int *T) {
     for (const auto &sh : kFsShapes) {
         const int t = 32 * ((P + 32 * sh[0] - 1) / (32 * sh[0]));
@@ -243,13 +255,11 @@ bool fused_shape(int P, int *C, int *T) {
 template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
     switch (C) {
     case 1: return f(k_sv_fused<1, 1024, PRE>);
-    case 2: return f(k_sv_fused<2, 1024, PRE>);
     case 3: return f(k_sv_fused<3, 1024, PRE>);
-    case 4: return f(k_sv_fused<4, 1024, PRE>);
     case 5: return f(k_sv_fused<5, 1024, PRE>);
-    case 6: return f(k_sv_fused<6, 1024, PRE>);
-    case 8: return f(k_sv_fused<8, 768, PRE>);
-    default: return f(k_sv_fused<16, 512, PRE>);
+    case 7: return f(k_sv_fused<7, 768, PRE>);
+    case 9: return f(k_sv_fused<9, 640, PRE>);
+    default: return f(k_sv_fused<17, 512, PRE>);
     }
 }
 template <class F> cudaError_t fused_dispatch(int C, F &&f, bool pre = false) {
@@ -282,7 +292,7 @@ bool sv_fused_plan(int Ns, int P, int *G_out, int *NB_out, int *ctas_out) {
     int best_G = 0, best_NB = 0, best_blocks = 0, best_threads = 0, best_rows = 0;
     for (int G = 1; G <= kFsMaxG; G *= 2)
         for (int NB = 2; NB <= kFsMaxNB; NB++) {
-            const size_t smem = fused_smem(P, G, NB);
+            const size_t smem = fused_smem(C * T, G, NB);
             if (smem > size_t(optin) - 1024) continue;
             int blocks = 0;
             const cudaError_t e = fused_dispatch(C, [&](auto fn) {
@@ -308,9 +318,9 @@ bool sv_fused_plan(int Ns, int P, int *G_out, int *NB_out, int *ctas_out) {
 cudaError_t launch_sv_fused(int Ns, int P, int G, int NB, int ctas, const double *O, const double *v, double *ypart,
                             int *err, const int *guard, cudaStream_t st, bool o_split) {
     FusedSvArgs a{Ns, P, G, NB, o_split ? 1 : 0, O, v, ypart, err, guard};
-    const size_t smem = fused_smem(P, G, NB);
     int C, T;
     if (!fused_shape(P, &C, &T)) return cudaErrorInvalidValue;
+    const size_t smem = fused_smem(C * T, G, NB);
     return fused_dispatch(
         C,
         [&](auto fn) {
