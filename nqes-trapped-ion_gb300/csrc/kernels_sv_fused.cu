@@ -236,10 +236,13 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
 }
 
 // Columns per thread C and threads per block T (whole warps, T C >= P): the
-// fewest columns whose block fits its register budget, C odd (conflict-free
-// shared-memory reads): C <= 5 with up to 1024 threads (64 registers), 7 with
-// up to 768, 9 with up to 640, 17 with up to 512.
-constexpr int kFsShapes[6][2] = {{1, 1024}, {3, 1024}, {5, 1024}, {7, 768}, {9, 640}, {17, 512}};
+// fewest columns, C odd (conflict-free shared-memory reads), whose block has
+// at most the row's thread limit. Each staged row pair costs every warp two
+// butterflies whatever C is, so blocks of 500 or so threads with more columns
+// each beat full-size blocks once P passes 3000: at P = 4224 (N32 M64 K2),
+// 0.214 ms per S·v with C = 5 (864 threads), 0.193 with 7 (608), 0.180 with 9
+// (480), 0.203 with 11 (384), 0.182 with 17 (256, two blocks per SM).
+constexpr int kFsShapes[6][2] = {{1, 1024}, {3, 1024}, {5, 640}, {7, 512}, {9, 512}, {17, 512}};
 bool fused_shape(int P, int *C, int *T) {
     for (const auto &sh : kFsShapes) {
         const int t = 32 * ((P + 32 * sh[0] - 1) / (32 * sh[0]));
@@ -256,9 +259,9 @@ template <bool PRE, class F> cudaError_t fused_dispatch_p(int C, F &&f) {
     switch (C) {
     case 1: return f(k_sv_fused<1, 1024, PRE>);
     case 3: return f(k_sv_fused<3, 1024, PRE>);
-    case 5: return f(k_sv_fused<5, 1024, PRE>);
-    case 7: return f(k_sv_fused<7, 768, PRE>);
-    case 9: return f(k_sv_fused<9, 640, PRE>);
+    case 5: return f(k_sv_fused<5, 640, PRE>);
+    case 7: return f(k_sv_fused<7, 512, PRE>);
+    case 9: return f(k_sv_fused<9, 512, PRE>);
     default: return f(k_sv_fused<17, 512, PRE>);
     }
 }
