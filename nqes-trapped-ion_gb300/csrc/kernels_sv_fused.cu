@@ -239,9 +239,9 @@ __global__ void __launch_bounds__(MaxT, 1) k_sv_fused(FusedSvArgs a) {
 // fewest columns, C odd (conflict-free shared-memory reads), whose block has
 // at most the row's thread limit. Each staged row pair costs every warp two
 // butterflies whatever C is, so blocks of 500 or so threads with more columns
-// each beat full-size blocks once P passes 3000: at P = 4224 (N32 M64 K2),
-// 0.214 ms per S·v with C = 5 (864 threads), 0.193 with 7 (608), 0.180 with 9
-// (480), 0.203 with 11 (384), 0.182 with 17 (256, two blocks per SM).
+// each beat full-size blocks once P passes 3000: at P = 4288 (N32 M64 K2),
+// 0.214 ms per S·v with C = 5 (864 threads), 0.193 with 7 (640), 0.180 with 9
+// (480), 0.203 with 11 (416), 0.182 with 17 (256, two blocks per SM).
 constexpr int kFsShapes[6][2] = {{1, 1024}, {3, 1024}, {5, 640}, {7, 512}, {9, 512}, {17, 512}};
 bool fused_shape(int P, int *C, int *T) {
     for (const auto &sh : kFsShapes) {

@@ -354,7 +354,10 @@ def test_certified_matches_fp64(pkg, N, M, K, chains, m):
     assert rel_err(c["w"], f["w"]) < (1e-6 if P < 10000 else 5e-6)
 
 
-@pytest.mark.parametrize("N,M,K,prec", [(8, 16, 2, 0), (32, 64, 2, 0), (32, 64, 2, 2), (12, 20, 3, 0)])
+# P = 304, 4288, 4288, 816 and then one shape per wider thread layout of the
+# fused kernel: P = 3200 (5 columns x 640 threads), 3248 (7 x 480), 6640 (17 x 416)
+@pytest.mark.parametrize("N,M,K,prec", [(8, 16, 2, 0), (32, 64, 2, 0), (32, 64, 2, 2), (12, 20, 3, 0),
+                                        (32, 96, 1, 2), (24, 64, 2, 2), (40, 80, 2, 2)])
 def test_fused_sv_matches_two_pass(pkg, N, M, K, prec):
     """The fused S·v (one read of the FP64 O per product, double-float
     arithmetic on the FP32 pipe) against the two FP64 passes on the same
