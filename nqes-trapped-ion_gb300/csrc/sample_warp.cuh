@@ -234,7 +234,11 @@ __device__ void rebuild_row(const MixedArgs &A, DSmem &sm, int k) {
         double mx = a;
         for (int o = 1; o < 4; o <<= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         mx = __shfl_sync(0xffffffffu, mx, 0);
-        const double e = lane < K ? pp * exp(a - mx) : 0.0;
+        // e^{a - mx} from the table (a dozen FP64 instructions instead of the
+        // library exp's few dozen, each a full warp's turn on the FP64 pipe);
+        // exp itself only where an entry lies more than e^-40 below the largest
+        const double x = lane < K ? mx - a : 0.0;
+        const double e = lane < K ? pp * (x < 40.0 ? exp_neg_tab(x, A.etab) : exp(-x)) : 0.0;
         int ex = lane < K ? expo(e) : -100000;
         for (int o = 1; o < 4; o <<= 1) ex = max(ex, __shfl_xor_sync(0xffffffffu, ex, o));
         ex = __shfl_sync(0xffffffffu, ex, 0);
