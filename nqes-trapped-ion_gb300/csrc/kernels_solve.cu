@@ -18,6 +18,8 @@
 #include <cmath>
 #include <type_traits>
 
+#include <utility>
+
 #include "nqes_internal.h"
 
 namespace nqes {
@@ -427,7 +429,15 @@ template <class S> __device__ __forceinline__ void lanczos_a_body(const SolveBuf
     t = block_sum(t, sh);
     if (threadIdx.x == 0) B.part[bid] = t;
 }
+// Programmatic dependent launch: the loop body's kernels after the first on
+// each stream are launched with programmatic stream serialisation, so that
+// a kernel is scheduled while its predecessor drains; it waits here for the
+// predecessor's completion and memory before reading anything (a no-op when
+// launched without the attribute).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <class S> __global__ void __launch_bounds__(kMrColThreads) k_lanczos_a(SolveBufs<S> B) {
+    pdl_wait();
     lanczos_a_body(B, blockIdx.x);
 }
 
@@ -458,7 +468,10 @@ template <class S> __device__ __forceinline__ void lanczos_b_body(const SolveBuf
     t = block_sum(t, sh);
     if (threadIdx.x == 0) B.part[kPartStride + bid] = t;
 }
-template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) { lanczos_b_body(B, blockIdx.x); }
+template <class S> __global__ void k_lanczos_b(SolveBufs<S> B) {
+    pdl_wait();
+    lanczos_b_body(B, blockIdx.x);
+}
 
 // Lanczos part 3 of step j: beta_{j+1} = |r3|, v_{j+1} = r3 / beta_{j+1} (into
 // v, its FP32 mirror and the QLP chain's slot), o·v_{j+1} partials; the last
@@ -508,7 +521,10 @@ template <class S> __device__ __forceinline__ void lanczos_next_body(const Solve
         __threadfence();
     }
 }
-template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) { lanczos_next_body(B, blockIdx.x); }
+template <class S> __global__ void k_lanczos_next(SolveBufs<S> B) {
+    pdl_wait();
+    lanczos_next_body(B, blockIdx.x);
+}
 
 __device__ __forceinline__ double sgn(double a) { return copysign(1.0, a); }
 __device__ void givens(double a, double b, double &c, double &s, double &r) {
@@ -775,7 +791,10 @@ template <class S> __device__ __forceinline__ void qlp_vectors_body(const SolveB
         B.xl2[p] = xl2;
     }
 }
-template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) { qlp_vectors_body(B, blockIdx.x); }
+template <class S> __global__ void k_qlp_vectors(SolveBufs<S> B) {
+    pdl_wait();
+    qlp_vectors_body(B, blockIdx.x);
+}
 
 // w -= lr x in the reference layout (code/rbm.cc:699-717).
 template <class S>
@@ -911,20 +930,36 @@ template <class S> static cudaError_t launch_sv_passes(const SolveBufs<S> &B, co
     return cudaGetLastError();
 }
 
+// Launch of a kernel that may start while its predecessor on `st` drains
+// (it calls pdl_wait before reading anything).
+template <class... KArgs, class... Args>
+static cudaError_t launch_after(void (*kern)(KArgs...), int grid, int block, cudaStream_t st, Args &&...args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <class S> cudaError_t launch_lanczos_step(const SolveBufs<S> &B, cudaStream_t st) {
     const int nb = mr_blocks(B.sh.P);
-    const cudaError_t e = launch_sv_passes(B, B.v, st);
-    if (e != cudaSuccess) return e;
-    k_lanczos_a<S><<<nb, kMrColThreads, 0, st>>>(B);
-    k_lanczos_b<S><<<nb, kMrThreads, 0, st>>>(B);
-    k_lanczos_next<S><<<nb, kMrThreads, 0, st>>>(B);
-    return cudaGetLastError();
+    cudaError_t e = launch_sv_passes(B, B.v, st);
+    if (e == cudaSuccess) e = launch_after(k_lanczos_a<S>, nb, kMrColThreads, st, B);
+    if (e == cudaSuccess) e = launch_after(k_lanczos_b<S>, nb, kMrThreads, st, B);
+    if (e == cudaSuccess) e = launch_after(k_lanczos_next<S>, nb, kMrThreads, st, B);
+    return e;
 }
 
 template <class S> cudaError_t launch_qlp_step(const SolveBufs<S> &B, cudaStream_t st) {
     k_qlp_scalar<S><<<1, 32, 0, st>>>(B);
-    k_qlp_vectors<S><<<mr_blocks(B.sh.P), kMrThreads, 0, st>>>(B);
-    return cudaGetLastError();
+    const cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : launch_after(k_qlp_vectors<S>, mr_blocks(B.sh.P), kMrThreads, st, B);
 }
 
 template <class S> cudaError_t launch_sv_rows_only(const SolveBufs<S> &B, cudaStream_t st) {
